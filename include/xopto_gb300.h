@@ -1,0 +1,369 @@
+/*
+ * xopto_gb300.h - C ABI of libxopto_gb300.so, the GB300 (sm_103a) Monte Carlo
+ * photon-packet transport engine for layered (mcml) and voxelized (mcvox)
+ * turbid media.
+ *
+ * Reference interfaces replaced (paths inside the PyXOpto project):
+ *   mcgb_mcml_run      xopto/mcml/kernel/mcml.template.c:346  McKernel (mcml),
+ *                      launched by xopto/mcml/mc.py:922-953
+ *   mcgb_mcvox_run     xopto/mcvox/kernel/mcvox.template.c:548 McKernel (mcvox),
+ *                      launched by xopto/mcvox/mc.py:968
+ *   mcgb_rng_dump      xopto/mcbase/kernel/mcbase.template.c:1640 RngKernel,
+ *                      launched by xopto/mcml/mc.py:1320-1362 (Mc.rng_test)
+ *   mcgb_rng_init      xopto/src/rng/rng.cpp:64 init_RNG and
+ *                      xopto/cl/clrng.py:184 _rng_init
+ *   mcgb_rng_safeprimes xopto/src/rng/find_primes.c:40 (safe-prime multipliers,
+ *                      table xopto/data/primes/safeprimes_base32_500k.npz)
+ *   mcgb_sizeof        xopto/mcml/kernel/mcml.template.c:827 sizeof_datatypes
+ *   mcgb_fill_u64      xopto/mcbase/kernel/mcbase.template.c:1740 ScalarFillMcAccu
+ *   mcgb_batched_run   (new) batched persistent engine; replaces the sequential
+ *                      loop xopto/mcml/mcrun/helper.py:640-686
+ *   mcgb_mlp_*         (new) BF16 surrogate kernels; the reference trains its
+ *                      networks with TensorFlow (xopto/util/regression/ann.py)
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  "dev" pointers are device memory owned
+ *     by the caller (cudaMalloc or a torch tensor); the library never frees
+ *     caller memory.  "host" pointers are host memory.
+ *   - Every entry point returns 0 (MCGB_OK) on success or a negative
+ *     MCGB_E_* code.  mcgb_last_error() returns a text description of the
+ *     last failure on the calling host thread.  No C++ exception crosses the
+ *     ABI.
+ *   - Launch functions enqueue work on the caller's stream (a cudaStream_t
+ *     passed as void*, NULL = legacy default stream) and return without
+ *     waiting; the caller synchronizes before reading results, as the
+ *     reference waits on its OpenCL event (xopto/mcml/mc.py:953).
+ *   - Units are SI (m, 1/m), as in the reference (xopto/mcml/mclayer/layer.py).
+ *   - Tallies are 64-bit unsigned fixed-point integers: each deposit adds
+ *     (uint32_t)(w*K + 0.5f) with K = MCGB_ACCU_K (the reference's
+ *     MC_INT_ACCUMULATOR_K, xopto/mcbase/kernel/mcbase.template.h:237), so
+ *     totals do not depend on the order of the deposits.
+ *
+ * Packet-to-stream mapping: a run of N packets on T random-number streams
+ * gives stream t the packets t, t+T, t+2T, ... < N, each simulated to
+ * completion in order with stream t's multiply-with-carry generator.  Results
+ * are therefore bit-reproducible for a given seed table, T and math mode.
+ */
+#ifndef XOPTO_GB300_H
+#define XOPTO_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCGB_ABI_VERSION 1
+
+/* Fixed-point weight scale of the integer accumulators. */
+#define MCGB_ACCU_K 8388607
+/* Largest layer stack (including the two surrounding half-spaces). */
+#define MCGB_MAX_LAYERS 64
+/* Largest material table of a voxelized sample (voxels are uint8 indices). */
+#define MCGB_MAX_MATERIALS 256
+/* Floats in one trace event (xopto/mcbase/mctrace.py TRACE_ENTRY_LEN). */
+#define MCGB_TRACE_ENTRY_LEN 8
+
+/* ---------------------------------------------------------------- errors */
+enum {
+    MCGB_OK = 0,
+    MCGB_E_INVALID = -1,     /* invalid argument or configuration        */
+    MCGB_E_SIZE = -2,        /* buffer too small / size limit exceeded   */
+    MCGB_E_CUDA = -3,        /* CUDA runtime error                       */
+    MCGB_E_TIMEOUT = -4,     /* device deadline expired, run incomplete  */
+    MCGB_E_BAD_INDEX = -5,   /* kernel caught an out-of-range index      */
+    MCGB_E_UNSUPPORTED = -6  /* feature not built into this library      */
+};
+
+/* Status bits written by the kernels into counters[MCGB_CNT_STATUS]. */
+#define MCGB_STATUS_TIMEOUT    0x1u
+#define MCGB_STATUS_BAD_INDEX  0x2u
+#define MCGB_STATUS_STEP_LIMIT 0x4u
+#define MCGB_STATUS_ABORTED    0x8u
+
+/* Device counter block (uint64_t[MCGB_NUM_COUNTERS], caller-owned). */
+enum {
+    MCGB_CNT_PACKETS = 0,    /* packets completed                        */
+    MCGB_CNT_STEPS = 1,      /* interaction steps (loop iterations)      */
+    MCGB_CNT_STATUS = 2,     /* OR of MCGB_STATUS_* bits                 */
+    MCGB_CNT_THREADS = 3,    /* threads that simulated >= 1 packet       */
+    MCGB_CNT_ABORT = 4,      /* set nonzero by the host to stop a run    */
+    MCGB_NUM_COUNTERS = 8
+};
+
+/* ----------------------------------------------------------- enumerations */
+enum { MCGB_METHOD_ALBEDO_WEIGHT = 0,       /* MC_METHOD 0 (default)      */
+       MCGB_METHOD_ALBEDO_REJECTION = 1,    /* MC_METHOD 1                */
+       MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT = 2 };
+enum { MCGB_PF_HG = 0, MCGB_PF_GK = 1, MCGB_PF_LUT = 2 };
+enum { MCGB_SRC_LINE = 0, MCGB_SRC_GAUSSIAN_BEAM = 1 };
+enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2 };
+enum { MCGB_FLUENCE_NONE = 0, MCGB_FLUENCE_DEPOSITION = 1, MCGB_FLUENCE_RATE = 2 };
+/* Trace flags (xopto/mcbase/mctrace.py TRACE_START/END/ALL). */
+enum { MCGB_TRACE_NONE = 0, MCGB_TRACE_START = 1, MCGB_TRACE_END = 2, MCGB_TRACE_ALL = 7 };
+/* Math mode: EXACT evaluates log/sin/cos/pow/exp with the library's own
+   portable single-precision routines and IEEE +,-,*,/,sqrt without FMA
+   contraction, so GPU and CPU produce identical bits.  FAST uses the GPU's
+   special-function units (the reference's MC_USE_NATIVE_MATH). */
+enum { MCGB_MATH_EXACT = 0, MCGB_MATH_FAST = 1 };
+
+/* ------------------------------------------------------------ POD structs */
+/* Scattering phase function of one layer/material.
+   Hg:  p[0]=g                      (xopto/mcbase/mcpf/hg.py:80-95)
+   Gk:  p[0..4]=g, a, inv_a, a1, a2 (xopto/mcbase/mcpf/gk.py:102-124,153-178)
+   Lut: p[0..2]=a, b, c; lut_offset, lut_size (xopto/mcbase/mcpf/lut.py:125-155) */
+typedef struct McgbPf {
+    float p[5];
+    uint32_t lut_offset;
+    uint32_t lut_size;
+    uint32_t reserved;
+} McgbPf;                                   /* 32 bytes */
+
+/* One layer (xopto/mcml/mclayer/layer.py:40-72 ClLayer). */
+typedef struct McgbLayer {
+    float thickness, top, bottom, n;
+    float cos_critical_top, cos_critical_bottom;
+    float mus, mua, inv_mut, mua_inv_mut;
+    McgbPf pf;
+} McgbLayer;                                /* 72 bytes */
+
+/* One material of a voxelized sample (xopto/mcbase/mcmaterial.py:54-61). */
+typedef struct McgbMaterial {
+    float n, mus, mua, inv_mut, mua_inv_mut;
+    float reserved[3];
+    McgbPf pf;
+} McgbMaterial;                             /* 64 bytes */
+
+/* Photon packet source.
+   Line (xopto/mcml/mcsource/line.py:56-62,181-228): position on the sample
+     surface, direction = direction in the sample, direction_reflected,
+     reflectance = specular reflectance.
+   GaussianBeam mcml (xopto/mcml/mcsource/gaussianbeam.py:119-170,300-362):
+     transformation, position, direction (refracted), sigma, clip,
+     reflectance.
+   GaussianBeam mcvox (xopto/mcvox/mcsource/gaussianbeam.py:112-190):
+     transformation, position, direction (in the surrounding medium), sigma,
+     clip. */
+typedef struct McgbSource {
+    int32_t kind;
+    float position[3];
+    float direction[3];
+    float direction_reflected[3];
+    float reflectance;
+    float transformation[9];                /* row-major a_11 .. a_33 */
+    float sigma[2];
+    float clip;
+    float reserved[2];
+} McgbSource;                               /* 104 bytes */
+
+/* Radial or Total detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;
+   total.py:52-56,86-108). */
+typedef struct McgbDetector {
+    int32_t kind;
+    float direction[3];
+    float position[2];
+    float r_min, inv_dr, cos_min;
+    uint32_t n;
+    int32_t log_scale;
+    uint32_t reserved;
+    uint64_t offset;                        /* first accumulator */
+} McgbDetector;                             /* 56 bytes */
+
+/* Cartesian fluence (xopto/mcbase/mcfluence/fluence.py:56-62,103-143). */
+typedef struct McgbFluence {
+    int32_t kind;
+    float inv_step[3];
+    float top_left[3];
+    uint32_t shape[3];
+    int32_t k;
+    uint32_t reserved;
+    uint64_t offset;                        /* first accumulator */
+} McgbFluence;                              /* 56 bytes */
+
+/* Packet trace (xopto/mcbase/mctrace.py:541-583). */
+typedef struct McgbTrace {
+    int32_t flags;                          /* MCGB_TRACE_* */
+    uint32_t max_events;
+    uint32_t event_mask;                    /* 0 = record every event */
+    uint32_t reserved;
+    uint64_t data_offset;                   /* in the float buffer */
+    uint64_t count_offset;                  /* in the int buffer   */
+} McgbTrace;                                /* 32 bytes */
+
+/* Options shared by both media. */
+typedef struct McgbRunOptions {
+    int32_t method;                         /* MCGB_METHOD_*                   */
+    int32_t math;                           /* MCGB_MATH_*                     */
+    int32_t use_lottery;                    /* MC_USE_LOTTERY (default 1)      */
+    float packet_weight_min;                /* MC_PACKET_WEIGHT_MIN (1e-4)     */
+    float lottery_chance;                   /* MC_PACKET_LOTTERY_CHANCE (0.1)  */
+    float rmax;                             /* Mc.rmax (inf = no limit)        */
+    int32_t track_optical_pathlength;       /* MC_TRACK_OPTICAL_PATHLENGTH     */
+    uint32_t block_size;                    /* threads per block (0 = auto)    */
+    uint64_t max_steps_per_packet;          /* 0 = unlimited                   */
+    double deadline_s;                      /* device wall-clock limit, 0=300s */
+} McgbRunOptions;
+
+/* Layered medium run (the reference's McKernel arguments for mcml). */
+typedef struct McgbMcmlConfig {
+    uint64_t num_packets;
+    uint32_t num_streams;                   /* RNG streams = device threads    */
+    int32_t pf_kind;                        /* MCGB_PF_*                       */
+    uint32_t num_layers;
+    uint32_t reserved;
+    McgbRunOptions opt;
+    McgbSource source;
+    McgbDetector top, bottom, specular;
+    McgbFluence fluence;
+    McgbTrace trace;
+    McgbLayer layers[MCGB_MAX_LAYERS];
+} McgbMcmlConfig;
+
+/* Voxelized medium run (the reference's McKernel arguments for mcvox,
+   xopto/mcvox/mcgeometry/voxel.py:88-165 McVoxelConfig).  Material 0 is the
+   surrounding medium (xopto/mcvox/kernel/mcvox.template.h:772-779). */
+typedef struct McgbMcvoxConfig {
+    uint64_t num_packets;
+    uint32_t num_streams;
+    int32_t pf_kind;
+    uint32_t num_materials;
+    uint32_t reserved;
+    McgbRunOptions opt;
+    float top_left[3];
+    float bottom_right[3];
+    float voxel_size[3];
+    int32_t shape[3];
+    McgbSource source;
+    McgbDetector top, bottom, specular;
+    McgbFluence fluence;
+    McgbTrace trace;
+} McgbMcvoxConfig;
+
+/* Device buffers of one run (all caller-owned device memory). */
+typedef struct McgbBuffers {
+    uint64_t *rng_x;                /* [num_streams] mutable MWC states      */
+    const uint32_t *rng_a;          /* [num_streams] MWC multipliers         */
+    uint64_t *accumulator;          /* detector + fluence tallies            */
+    uint64_t accumulator_size;
+    float *float_buffer;            /* trace events                          */
+    uint64_t float_size;
+    int32_t *int_buffer;            /* trace event counts                    */
+    uint64_t int_size;
+    const float *fp_lut;            /* phase-function lookup tables          */
+    uint64_t fp_lut_size;
+    const uint8_t *voxels;          /* mcvox: material index per voxel,
+                                       flat index (z*ny + y)*nx + x          */
+    const McgbMaterial *materials;  /* mcvox: [num_materials]                */
+    uint64_t *counters;             /* [MCGB_NUM_COUNTERS]                   */
+} McgbBuffers;
+
+/* ------------------------------------------------------------ entry points */
+const char *mcgb_last_error(void);
+int mcgb_abi_version(void);
+/* Size of one of the POD structs above, for host/device layout checks
+   (replaces the reference's sizeof_datatypes kernel).  kind: 0 McgbLayer,
+   1 McgbSource, 2 McgbDetector, 3 McgbFluence, 4 McgbTrace, 5 McgbMaterial,
+   6 McgbMcmlConfig, 7 McgbMcvoxConfig, 8 McgbBuffers, 9 McgbRunOptions,
+   10 McgbPf.  Returns -1 for an unknown kind. */
+int mcgb_sizeof(int kind);
+
+/* Number of streams (device threads) that fills every SM of the current
+   device once for the given medium (0 = mcml, 1 = mcvox), math mode and
+   block size (0 = default). */
+int mcgb_suggest_streams(int medium, int math, uint32_t block_size, uint32_t *streams);
+
+/* Transport runs.  Validates the configuration and the buffer sizes against
+   every offset the configuration names, then launches one kernel on the
+   stream.  Returns MCGB_E_INVALID / MCGB_E_SIZE before launching anything if
+   a check fails. */
+int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *stream);
+int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *stream);
+
+/* Reads the device counter block (synchronizes the stream) and converts the
+   status bits into a return code: MCGB_OK, MCGB_E_TIMEOUT or
+   MCGB_E_BAD_INDEX.  host_counters may be NULL. */
+int mcgb_check_counters(const uint64_t *dev_counters, void *stream,
+                        uint64_t *host_counters);
+
+/* Random numbers.  mcgb_rng_safeprimes writes the first n multipliers a of
+   the safe-prime table (a*2^32-1 and a*2^31-1 both prime, scanning down
+   from 4294967118).  mcgb_rng_init expands a 64-bit initializer into n
+   (x, a) stream seeds exactly as the reference's init_RNG; returns
+   MCGB_E_INVALID for an invalid initializer. */
+int mcgb_rng_safeprimes(uint32_t *host_a, uint32_t n);
+int mcgb_rng_init(uint64_t *host_x, uint32_t *host_a, uint32_t n, uint64_t xinit);
+/* n uniform random numbers of one stream into dev_out (one device thread,
+   like RngKernel). */
+int mcgb_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *dev_out, void *stream);
+
+/* Fill a device uint64 buffer with a value (ScalarFillMcAccu). */
+int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream);
+
+/* Exact integer sum of tally arrays (the cross-replica reduction):
+   dst[i] += src[i] for i < n, host memory. */
+int mcgb_reduce_tallies(uint64_t *host_dst, const uint64_t *host_src, uint64_t n);
+
+/* --------------------------------------------------------- batched engine */
+/* One simulation of the batched engine: a semi-infinite or finite single
+   layer between two half-spaces, Hg phase function, normal Line source and
+   a radial reflectance detector (the BASELINE batched configuration). */
+typedef struct McgbBatchSim {
+    float mua, mus, g, n;               /* sample layer                      */
+    float n_above, n_below;             /* surrounding half-spaces           */
+    float thickness;                    /* inf = semi-infinite               */
+    float reserved;
+    uint64_t num_packets;
+} McgbBatchSim;                         /* 40 bytes */
+
+typedef struct McgbBatchConfig {
+    uint32_t num_sims;
+    uint32_t packets_per_chunk;         /* work item = (sim, chunk)          */
+    uint32_t block_size;                /* threads per block                 */
+    uint32_t blocks_per_sm;             /* resident blocks per SM            */
+    uint32_t num_bins;                  /* radial bins per simulation        */
+    int32_t math;                       /* MCGB_MATH_*                       */
+    float r_max;                        /* radial axis 0 .. r_max            */
+    float rmax;                         /* packet termination radius         */
+    uint64_t seed;                      /* per-chunk stream derivation       */
+    double deadline_s;
+} McgbBatchConfig;
+
+/* Runs every simulation to completion in one persistent launch.  Work items
+   are (simulation, chunk) pairs taken from a device work queue; each chunk
+   owns an RNG stream derived from (seed, sim, chunk), so the tallies do not
+   depend on which thread takes which chunk.
+   dev_sims [num_sims]; dev_tally [num_sims*num_bins] (accumulated, caller
+   zeroes); dev_work [num_sims+2] scratch (caller-owned, any contents);
+   dev_counters [MCGB_NUM_COUNTERS]. */
+int mcgb_batched_run(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
+                     uint64_t *dev_tally, uint64_t *dev_work,
+                     uint64_t *dev_counters, void *stream);
+
+/* ------------------------------------------------------ MLP surrogate */
+/* Linear layer forward: Y[M,N] = act(X[M,K] @ W[N,K]^T + b[N]) with BF16
+   X/W, FP32 accumulation, FP32 bias; Y stored as BF16 (act applied) and,
+   when dev_preact != NULL, the FP32 pre-activation for backward.
+   act: 0 = identity, 1 = GELU (tanh form).  Requires K % 16 == 0 and
+   N % 16 == 0 (pad the outer layers). */
+int mcgb_mlp_linear_fwd(const uint16_t *dev_x, const uint16_t *dev_w,
+                        const float *dev_b, uint16_t *dev_y, float *dev_preact,
+                        int m, int n, int k, int act, void *stream);
+/* Backward of the same layer given dY (BF16): dPre = dY * act'(pre);
+   dX[M,K] = dPre @ W (BF16 out, optional); dW[N,K] = dPre^T @ X (FP32,
+   accumulated); db[N] += sum_m dPre (FP32). */
+int mcgb_mlp_linear_bwd(const uint16_t *dev_x, const uint16_t *dev_w,
+                        const float *dev_preact, const uint16_t *dev_dy,
+                        uint16_t *dev_dx, float *dev_dw, float *dev_db,
+                        uint16_t *dev_dpre_scratch,
+                        int m, int n, int k, int act, void *stream);
+/* AdamW on FP32 master weights with BF16 shadow copy. */
+int mcgb_mlp_adamw(float *dev_w, uint16_t *dev_w_bf16, const float *dev_grad,
+                   float *dev_m, float *dev_v, uint64_t n, float lr,
+                   float beta1, float beta2, float eps, float weight_decay,
+                   int step, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XOPTO_GB300_H */

@@ -1,0 +1,949 @@
+/*
+ * mcoracle.c - CPU restatement of PyXOpto's Monte Carlo photon-packet
+ * transport kernel (McKernel) for layered (mcml) and voxelized (mcvox)
+ * media.
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the parity oracle.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.  The
+ * product (pyxopto_gb300) never links or calls it.
+ *
+ * Parity pin: compiled with -ffp-contract=off and run in LIBM math mode,
+ * this restatement reproduces the reference's own rendered McKernel (built
+ * for the CPU by oracle/render_ref.py) bit-for-bit on the same seeds and the
+ * same packet-to-stream mapping; tests/golden/ holds tallies produced by that
+ * reference build.  In PORTABLE math mode it evaluates log/exp/sincos/powr
+ * with pyxopto_gb300/csrc/portable_math.h, the routines of the GPU kernels'
+ * EXACT mode, so GPU and CPU tallies can be compared bit-for-bit.
+ *
+ * Packet-to-stream mapping: stream t simulates packets t, t+T, t+2T, ...
+ * (photon_index = that packet number), each to completion.  The reference
+ * takes packets from a global atomic counter instead
+ * (xopto/mcml/kernel/mcml.template.c:460,790); with one McKernel call per
+ * stream and num_packets = that stream's quota the two agree.
+ *
+ * Every function cites the reference file:line it restates.
+ */
+#define _GNU_SOURCE 1
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+
+#include "../include/xopto_gb300.h"
+#include "../pyxopto_gb300/csrc/portable_math.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+enum { MO_LIBM = 0, MO_PORTABLE = 1 };
+
+typedef struct { float x, y, z; } v3;
+typedef struct { int32_t x, y, z; } i3;
+
+/* ---------------------------------------------------------------- math */
+/* xopto/mcbase/kernel/mcbase.template.h:558-590 (standard math branch). */
+static inline float m_log(int mm, float x) { return mm ? pm_logf(x) : logf(x); }
+static inline float m_exp(int mm, float x) { return mm ? pm_expf(x) : expf(x); }
+static inline float m_pow(int mm, float x, float y) { return mm ? pm_powrf(x, y) : powf(x, y); }
+static inline void m_sincos(int mm, float x, float *s, float *c) {
+    if (mm) pm_sincosf(x, s, c); else sincosf(x, s, c);
+}
+
+/* convert_int / convert_uint with round-toward-zero and saturation, the
+   behaviour of the GPU's float-to-int conversion. */
+static inline int32_t cvt_int(float x) {
+    if (!(x == x)) return 0;
+    if (x >= 2147483647.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (-2147483647 - 1);
+    return (int32_t)x;
+}
+static inline uint32_t cvt_uint(float x) {
+    if (!(x == x) || x <= 0.0f) return 0u;
+    if (x >= 4294967295.0f) return 4294967295u;
+    return (uint32_t)x;
+}
+static inline int32_t clip_i(int32_t x, int32_t lo, int32_t hi) {
+    return x < lo ? lo : (x > hi ? hi : x);
+}
+/* mc_fsign, xopto/mcbase/kernel/mcbase.template.h:612 */
+static inline int32_t fsign(float x) { return x >= 0.0f ? 1 : -1; }
+
+/* ----------------------------------------------------------------- RNG */
+/* fp_random_single, xopto/mcbase/kernel/mcbase.template.c:1576-1594
+   (MC_USE_ENHANCED_RNG off). */
+static inline float rnd(uint64_t *x, uint32_t a) {
+    *x = (*x & 0xFFFFFFFFull) * (uint64_t)a + (*x >> 32);
+    return (float)(uint32_t)*x / (float)0xFFFFFFFFu;
+}
+
+/* ----------------------------------------------------- vector helpers */
+/* mc_dot_fpv3 (mcbase.template.c:880-882) */
+static inline float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+/* mc_normalize_fpv3 + mc_length_fpv3 (mcbase.template.c:914-916,975-981) */
+static inline v3 normalize3(v3 a) {
+    float k = 1.0f / sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+    v3 r = {a.x * k, a.y * k, a.z * k};
+    return r;
+}
+
+/* --------------------------------------------------- boundary physics */
+/* cos_critical, xopto/mcbase/kernel/mcbase.template.c:1229-1231 */
+static inline float cos_critical(float n1, float n2) {
+    return (n1 > n2) ? sqrtf(1.0f - (n2 * n2) / (n1 * n1)) : 0.0f;
+}
+
+/* reflectance, xopto/mcbase/kernel/mcbase.template.c:1244-1289 */
+static float reflectance(float n1, float n2, float cos1, float cc) {
+    float Rp, Rs, R = 1.0f, n1_d_n2, sin1, sin2, cos2, n_cos1, n_cos2;
+    cos1 = fabsf(cos1);
+    if (n1 == n2) return 0.0f;
+    if (cos1 > cc) {
+        n1_d_n2 = n1 / n2;
+        sin1 = sqrtf(1.0f - cos1 * cos1);
+        if (cos1 >= 1.0f) sin1 = 0.0f;
+        sin2 = fminf(1.0f, n1_d_n2 * sin1);
+        cos2 = sqrtf(1.0f - sin2 * sin2);
+        n_cos1 = n1_d_n2 * cos1;
+        n_cos2 = n1_d_n2 * cos2;
+        Rs = (n_cos1 - cos2) / (n_cos1 + cos2);
+        Rs *= Rs;
+        Rp = (n_cos2 - cos1) / (n_cos2 + cos1);
+        Rp *= Rp;
+        R = 0.5f * (Rp + Rs);
+        if (cos1 <= 0.0f || sin2 == 1.0f) return 1.0f;
+    }
+    return R;
+}
+
+/* reflect, xopto/mcbase/kernel/mcbase.template.c:1361-1369 */
+static inline v3 reflect3(v3 p, v3 n) {
+    float p_n_2 = 2.0f * dot3(p, n);
+    v3 r = {p.x - n.x * p_n_2, p.y - n.y * p_n_2, p.z - n.z * p_n_2};
+    return r;
+}
+
+/* refract, xopto/mcbase/kernel/mcbase.template.c:1424-1440 */
+static inline v3 refract3(v3 p, v3 n, float n1, float n2) {
+    float cos1 = dot3(p, n);
+    float n1_d_n2 = n1 / n2;
+    float sin2_squared = n1_d_n2 * n1_d_n2 * (1.0f - cos1 * cos1);
+    float k = (float)fsign(cos1) * (n1_d_n2 * fabsf(cos1) - sqrtf(1.0f - sin2_squared));
+    v3 r = {n1_d_n2 * p.x - k * n.x, n1_d_n2 * p.y - k * n.y, n1_d_n2 * p.z - k * n.z};
+    return r;
+}
+
+/* refract_safe, xopto/mcbase/kernel/mcbase.template.c:1466-1487 */
+static inline int refract_safe3(v3 p, v3 n, float n1, float n2, v3 *r) {
+    float cos1 = dot3(p, n);
+    float n1_d_n2 = n1 / n2;
+    float sin2_squared = n1_d_n2 * n1_d_n2 * (1.0f - cos1 * cos1);
+    if (sin2_squared > 1.0f) return 1;
+    float k = (float)fsign(cos1) * (n1_d_n2 * fabsf(cos1) - sqrtf(1.0f - sin2_squared));
+    r->x = n1_d_n2 * p.x - k * n.x;
+    r->y = n1_d_n2 * p.y - k * n.y;
+    r->z = n1_d_n2 * p.z - k * n.z;
+    return 0;
+}
+
+/* scatter_direction, xopto/mcbase/kernel/mcbase.template.c:1522-1555 */
+static void scatter_direction(int mm, v3 *dir, float cos_theta, float fi) {
+    float sin_fi, cos_fi, sin_theta, px, k, stcf, stsf;
+    sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+    m_sincos(mm, fi, &sin_fi, &cos_fi);
+    stcf = sin_theta * cos_fi;
+    stsf = sin_theta * sin_fi;
+    px = dir->x;
+    if (fabsf(dir->z) >= 1.0f) {
+        dir->x = stcf;
+        dir->y = stsf;
+        dir->z = copysignf(cos_theta, dir->z * cos_theta);
+    } else {
+        k = sqrtf(1.0f - dir->z * dir->z);
+        dir->x = (stcf * px * dir->z - stsf * dir->y) / k + px * cos_theta;
+        dir->y = (stcf * dir->y * dir->z + stsf * px) / k + dir->y * cos_theta;
+        dir->z = (-stcf) * k + dir->z * cos_theta;
+    }
+    *dir = normalize3(*dir);
+}
+
+/* -------------------------------------------------- phase functions */
+/* Returns cos(theta) and the azimuth; draws in the reference's order.
+   Hg: xopto/mcbase/mcpf/hg.py:80-95
+   Gk: xopto/mcbase/mcpf/gk.py:102-124
+   Lut: xopto/mcbase/mcpf/lut.py:125-155 */
+static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
+                       uint64_t *x, uint32_t a, float *azimuth) {
+    float cos_theta;
+    if (kind == MCGB_PF_HG) {
+        float g = pf->p[0];
+        *azimuth = 6.28318548f * rnd(x, a);
+        float k = (1.0f - g * g) / (1.0f + g * (2.0f * rnd(x, a) - 1.0f));
+        cos_theta = (1.0f + g * g - k * k) / (2.0f * g);
+        if (g == 0.0f) cos_theta = 1.0f - 2.0f * rnd(x, a);
+        return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+    } else if (kind == MCGB_PF_GK) {
+        float g = pf->p[0], ga = pf->p[1], inv_a = pf->p[2], a1 = pf->p[3], a2 = pf->p[4];
+        float tmp;
+        *azimuth = 6.28318548f * rnd(x, a);
+        if (g == 0.0f) {
+            cos_theta = 1.0f - 2.0f * rnd(x, a);
+        } else if (ga == 0.0f) {
+            cos_theta = a1 + m_pow(mm, (1.0f - g) / (1.0f + g), 2.0f * rnd(x, a)) * a2;
+        } else {
+            tmp = a1 * rnd(x, a) + a2;
+            tmp = 1.0f + g * g - m_pow(mm, tmp, -inv_a);
+            cos_theta = tmp / (2.0f * g);
+        }
+        /* mc_fclip = clamp = min(max(x, lo), hi) */
+        return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
+    } else {
+        float la = pf->p[0], lb = pf->p[1], lc = pf->p[2];
+        uint32_t offset = pf->lut_offset;
+        uint32_t lut_size = pf->lut_size - 1u;
+        *azimuth = 6.28318548f * rnd(x, a);
+        float fp_index = (la / (rnd(x, a) - lc) - lb + 1.0f) * (float)lut_size * 0.5f;
+        float fp_index_floor = floorf(fp_index);
+        float d = fp_index - fp_index_floor;
+        int32_t index = cvt_int(fp_index_floor);
+        int32_t i1 = index + 1 < (int32_t)lut_size ? index + 1 : (int32_t)lut_size;
+        return lut[offset + (uint32_t)index] * (1.0f - d) + lut[offset + (uint32_t)i1] * d;
+    }
+}
+
+/* ------------------------------------------------------------ tallies */
+static inline uint32_t weight_to_u32(float w, float accept) {
+    /* weight_to_int(w)*(accept), xopto/mcml/kernel/mcml.template.h:606 */
+    return (uint32_t)((w * (float)MCGB_ACCU_K + 0.5f) * accept);
+}
+
+/* Radial / Total detector deposit:
+   xopto/mcml/mcdetector/radial.py:117-150, total.py:86-108 */
+static void detector_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir,
+                             float weight, uint64_t *accu) {
+    if (det->kind == MCGB_DET_NONE) return;
+    v3 ddir = {det->direction[0], det->direction[1], det->direction[2]};
+    float accept = (float)(det->cos_min <= fabsf(dot3(dir, ddir)));
+    uint64_t index = 0;
+    if (det->kind == MCGB_DET_RADIAL) {
+        float dx = pos.x - det->position[0];
+        float dy = pos.y - det->position[1];
+        float r = sqrtf(dx * dx + dy * dy);
+        if (det->log_scale) r = m_log(mm, fmaxf(r, 1e-12f));
+        int32_t r_index = cvt_int((r - det->r_min) * det->inv_dr);
+        index = (uint64_t)clip_i(r_index, 0, (int32_t)det->n - 1);
+    }
+    uint32_t w = weight_to_u32(weight, accept);
+    if (w > 0) accu[det->offset + index] += w;
+}
+
+/* Fluence deposit, xopto/mcbase/mcfluence/fluence.py:103-143 */
+static void fluence_deposit(const McgbFluence *fl, v3 pos, float weight, float mua,
+                            uint64_t *accu) {
+    float ix = (pos.x - fl->top_left[0]) * fl->inv_step[0];
+    float iy = (pos.y - fl->top_left[1]) * fl->inv_step[1];
+    float iz = (pos.z - fl->top_left[2]) * fl->inv_step[2];
+    if (ix >= 0 && iy >= 0 && iz >= 0 && ix < (float)fl->shape[0] &&
+        iy < (float)fl->shape[1] && iz < (float)fl->shape[2]) {
+        uint32_t jx = cvt_uint(ix), jy = cvt_uint(iy), jz = cvt_uint(iz);
+        uint64_t index = ((uint64_t)jz * fl->shape[1] + jy) * fl->shape[0] + jx;
+        if (fl->kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? 1.0f / mua : 0.0f;
+        uint32_t w = (uint32_t)(weight * (float)fl->k + 0.5f);
+        accu[fl->offset + index] += w;
+    }
+}
+
+/* Trace event, xopto/mcbase/mctrace.py:541-583 */
+typedef struct {
+    v3 pos, dir;
+    float w, opl;
+    uint64_t photon_index;
+    uint32_t trace_count;
+    uint32_t events;
+} TraceState;
+
+static void trace_event(const McgbTrace *tr, TraceState *s, float *fbuf) {
+    if (tr->event_mask && !(tr->event_mask & s->events)) return;
+    uint32_t ev = s->trace_count < tr->max_events - 1 ? s->trace_count : tr->max_events - 1;
+    uint64_t pos = (uint64_t)ev * MCGB_TRACE_ENTRY_LEN +
+                   s->photon_index * tr->max_events * MCGB_TRACE_ENTRY_LEN + tr->data_offset;
+    fbuf[pos++] = s->pos.x; fbuf[pos++] = s->pos.y; fbuf[pos++] = s->pos.z;
+    fbuf[pos++] = s->dir.x; fbuf[pos++] = s->dir.y; fbuf[pos++] = s->dir.z;
+    fbuf[pos++] = s->w;
+    fbuf[pos++] = s->opl;
+    s->trace_count++;
+}
+
+/* Event bits, xopto/mcbase/kernel/mcbase.template.h:640-660 */
+#define EV_REFLECTION 1u
+#define EV_REFRACTION 2u
+#define EV_BOUNDARY_HIT 4u
+#define EV_LAUNCH 8u
+#define EV_ABSORPTION 16u
+#define EV_SCATTERING 32u
+#define EV_TERMINATED 64u
+#define EV_ESCAPED 128u
+
+/* ================================================================ mcml */
+typedef struct {
+    v3 pos, dir;
+    float w;
+    int32_t layer;
+    float opl;
+} MlState;
+
+/* Line.mcsim_launch (xopto/mcml/mcsource/line.py:95-108) and
+   GaussianBeam.mcsim_launch (xopto/mcml/mcsource/gaussianbeam.py:119-170). */
+static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x,
+                        uint32_t a, uint64_t *accu) {
+    const McgbSource *src = &c->source;
+    if (src->kind == MCGB_SRC_LINE) {
+        s->w = 1.0f - src->reflectance;
+        s->pos.x = src->position[0]; s->pos.y = src->position[1]; s->pos.z = src->position[2];
+        s->dir.x = src->direction[0]; s->dir.y = src->direction[1]; s->dir.z = src->direction[2];
+        if (c->specular.kind != MCGB_DET_NONE) {
+            v3 d = {src->direction_reflected[0], src->direction_reflected[1],
+                    src->direction_reflected[2]};
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+        }
+        s->layer = 1;
+    } else {
+        float cos_fi, sin_fi, r;
+        v3 pt_src, pt_mc;
+        r = sqrtf(-2.0f * m_log(mm, 1.0f - rnd(x, a)));
+        r = fminf(r, src->clip);
+        m_sincos(mm, 6.28318548f * rnd(x, a), &sin_fi, &cos_fi);
+        pt_src.x = r * cos_fi * src->sigma[0];
+        pt_src.y = r * sin_fi * src->sigma[1];
+        pt_src.z = 0.0f;
+        const float *T = src->transformation;
+        /* mc_transform_fpv3, xopto/mcbase/kernel/mcbase.template.c:380-386 */
+        pt_mc.x = T[0] * pt_src.x + T[1] * pt_src.y + T[2] * pt_src.z;
+        pt_mc.y = T[3] * pt_src.x + T[4] * pt_src.y + T[5] * pt_src.z;
+        pt_mc.z = T[6] * pt_src.x + T[7] * pt_src.y + T[8] * pt_src.z;
+        float k = (0.0f - pt_mc.z) / src->direction[2];
+        pt_mc.x += k * src->direction[0];
+        pt_mc.y += k * src->direction[1];
+        pt_mc.z = 0.0f;
+        s->pos.x = src->position[0] + pt_mc.x;
+        s->pos.y = src->position[1] + pt_mc.y;
+        s->pos.z = 0.0f;
+        s->dir.x = src->direction[0]; s->dir.y = src->direction[1]; s->dir.z = src->direction[2];
+        s->layer = 1;
+        s->w = 1.0f - src->reflectance;
+        if (c->specular.kind != MCGB_DET_NONE) {
+            v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
+            v3 normal = {0.0f, 0.0f, -1.0f};
+            v3 d = refract3(dir_in, normal, c->layers[1].n, c->layers[0].n);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+        }
+    }
+}
+
+/* mcsim_boundary (mcml), xopto/mcml/kernel/mcml.template.c:80-203 */
+static uint32_t mcml_boundary(const McgbMcmlConfig *c, MlState *s, int32_t next,
+                              uint64_t *x, uint32_t a) {
+    float cc, cos1, sin1, cos2, sin2, n_cos1, n_cos2, n2, n1_d_n2, R, Rs, Rp;
+    const McgbLayer *cur = &c->layers[s->layer];
+    const McgbLayer *nxt = &c->layers[s->layer + fsign(s->dir.z)];
+    cc = (s->dir.z < 0.0f) ? cur->cos_critical_top : cur->cos_critical_bottom;
+    n2 = nxt->n;
+    if (cur->n == n2) {
+        s->layer = next;
+        return EV_REFRACTION;
+    }
+    s->dir.z = -s->dir.z;
+    cos1 = fabsf(s->dir.z);
+    if (cos1 > cc) {
+        if (cos1 > 1.0f) {
+            R = (cur->n - n2) / (cur->n + n2);
+            if (R * R < rnd(x, a)) {
+                s->layer = next;
+                s->dir.z = -s->dir.z;
+                return EV_REFRACTION;
+            }
+            return EV_REFLECTION;
+        }
+        n1_d_n2 = cur->n / n2;
+        sin1 = sqrtf(1.0f - cos1 * cos1);
+        if (cos1 >= 1.0f) sin1 = 0.0f;
+        sin2 = fminf(1.0f, n1_d_n2 * sin1);
+        cos2 = sqrtf(1.0f - sin2 * sin2);
+        n_cos1 = n1_d_n2 * cos1;
+        n_cos2 = n1_d_n2 * cos2;
+        Rs = (n_cos1 - cos2) / (n_cos1 + cos2);
+        Rs *= Rs;
+        Rp = (n_cos2 - cos1) / (n_cos2 + cos1);
+        Rp *= Rp;
+        R = 0.5f * (Rs + Rp);
+        if (cos1 <= 0.0f || sin2 == 1.0f) R = 1.0f;
+        if (R < rnd(x, a)) {
+            s->layer = next;
+            s->dir.x *= n1_d_n2;
+            s->dir.y *= n1_d_n2;
+            s->dir.z = -copysignf(cos2, s->dir.z);
+            return EV_REFRACTION;
+        }
+    }
+    return EV_REFLECTION;
+}
+
+/* Simulates the packets of one stream: McKernel (mcml),
+   xopto/mcml/kernel/mcml.template.c:346-824.  Returns the number of
+   interaction steps. */
+static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
+                            uint64_t *rng_x, uint32_t a, uint64_t first,
+                            uint64_t stride, uint64_t *accu, float *fbuf,
+                            int32_t *ibuf) {
+    const McgbRunOptions *o = &c->opt;
+    uint64_t x = *rng_x, steps = 0;
+    v3 src_pos = {c->source.position[0], c->source.position[1], c->source.position[2]};
+    float rmax2 = o->rmax * o->rmax;
+    int use_trace = c->trace.flags != MCGB_TRACE_NONE;
+    for (uint64_t p = first; p < c->num_packets; p += stride) {
+        MlState s;
+        TraceState ts;
+        memset(&s, 0, sizeof(s));
+        ts.photon_index = p; ts.trace_count = 0; ts.events = 0;
+        mcml_launch(mm, c, &s, &x, a, accu);
+        uint32_t events = EV_LAUNCH;
+#define MO_TRACE_SNAPSHOT() do { ts.pos = s.pos; ts.dir = s.dir; ts.w = s.w; ts.opl = s.opl; \
+                                 ts.events = events; } while (0)
+        if (use_trace && (c->trace.flags & MCGB_TRACE_START)) {
+            MO_TRACE_SNAPSHOT();
+            trace_event(&c->trace, &ts, fbuf);
+        }
+        int done = 0;
+        uint64_t packet_steps = 0;
+        while (!done) {
+            const McgbLayer *L = &c->layers[s.layer];
+            float step, deposit;
+            ++steps;
+            if (o->method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
+                step = -m_log(mm, rnd(&x, a)) / L->mus;
+            else
+                step = -m_log(mm, rnd(&x, a)) * L->inv_mut;
+            step = fminf(step, FLT_MAX);
+            int32_t next = s.layer;
+            if (s.pos.z + step * s.dir.z < L->top) {
+                --next;
+                if (fabsf(s.dir.z) != 0.0f) step = (L->top - s.pos.z) / s.dir.z;
+            }
+            if (s.pos.z + step * s.dir.z >= L->bottom) {
+                ++next;
+                if (fabsf(s.dir.z) != 0.0f) step = (L->bottom - s.pos.z) / s.dir.z;
+            }
+            s.pos.x = s.pos.x + s.dir.x * step;
+            s.pos.y = s.pos.y + s.dir.y * step;
+            s.pos.z = s.pos.z + s.dir.z * step;
+            if (o->track_optical_pathlength) s.opl += L->n * step;
+            if (s.layer < next) s.pos.z = L->bottom;
+            if (s.layer > next) s.pos.z = L->top;
+
+            if (o->method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
+                /* mcml.template.c:584-666 */
+                float mua = L->mua;
+                float fraction = 1.0f - m_exp(mm, -mua * step);
+                deposit = fraction * s.w;
+                s.w -= deposit;
+                events |= EV_ABSORPTION;
+                if (c->fluence.kind != MCGB_FLUENCE_NONE) {
+                    float step_back = (mua != 0.0f)
+                        ? step - (-m_log(mm, 1.0f - rnd(&x, a) * fraction)) / mua : 0.0f;
+                    v3 dp = {s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
+                             s.pos.z - step_back * s.dir.z};
+                    fluence_deposit(&c->fluence, dp, deposit, L->mua, accu);
+                }
+                if (next != s.layer) {
+                    events |= mcml_boundary(c, &s, next, &x, a) | EV_BOUNDARY_HIT;
+                    if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
+                        if (s.layer <= 0)
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                        else if (s.layer >= (int32_t)c->num_layers - 1)
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                        done = 1;
+                    }
+                } else {
+                    float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az);
+                    scatter_direction(mm, &s.dir, ct, az);
+                    events |= EV_SCATTERING;
+                }
+                if (s.w < o->packet_weight_min) {
+                    if (o->use_lottery) {
+                        if (rnd(&x, a) > o->lottery_chance) done = 1;
+                        else s.w = s.w / o->lottery_chance;
+                    } else {
+                        done = 1;
+                    }
+                }
+            } else {
+                if (next != s.layer) {
+                    events |= mcml_boundary(c, &s, next, &x, a) | EV_BOUNDARY_HIT;
+                    if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
+                        if (s.layer <= 0)
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                        else if (s.layer >= (int32_t)c->num_layers - 1)
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                        done = 1;
+                    }
+                } else if (o->method == MCGB_METHOD_ALBEDO_REJECTION) {
+                    /* mcml.template.c:705-721 */
+                    if (rnd(&x, a) < L->mua_inv_mut) {
+                        deposit = s.w;
+                        done = 1;
+                        s.w -= deposit;
+                        events |= EV_ABSORPTION;
+                        if (c->fluence.kind != MCGB_FLUENCE_NONE)
+                            fluence_deposit(&c->fluence, s.pos, deposit, L->mua, accu);
+                    } else {
+                        float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az);
+                        scatter_direction(mm, &s.dir, ct, az);
+                        events |= EV_SCATTERING;
+                    }
+                } else {
+                    /* albedo weight, mcml.template.c:722-753 */
+                    deposit = s.w * L->mua_inv_mut;
+                    s.w -= deposit;
+                    events |= EV_ABSORPTION;
+                    if (c->fluence.kind != MCGB_FLUENCE_NONE)
+                        fluence_deposit(&c->fluence, s.pos, deposit, L->mua, accu);
+                    float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az);
+                    scatter_direction(mm, &s.dir, ct, az);
+                    events |= EV_SCATTERING;
+                    if (s.w < o->packet_weight_min) {
+                        if (o->use_lottery) {
+                            if (rnd(&x, a) > o->lottery_chance) done = 1;
+                            else s.w = s.w / o->lottery_chance;
+                        } else {
+                            done = 1;
+                        }
+                    }
+                }
+            }
+            /* rmax, mcml.template.c:759-763 */
+            v3 d = {s.pos.x - src_pos.x, s.pos.y - src_pos.y, s.pos.z - src_pos.z};
+            if (dot3(d, d) > rmax2) {
+                done = 1;
+                events |= EV_ESCAPED;
+            }
+            if (done) events |= EV_TERMINATED;
+            if (use_trace) {
+                if (c->trace.flags == MCGB_TRACE_ALL ||
+                    ((c->trace.flags & MCGB_TRACE_END) && done)) {
+                    MO_TRACE_SNAPSHOT();
+                    trace_event(&c->trace, &ts, fbuf);
+                }
+            }
+            events = 0;
+            if (!done && o->max_steps_per_packet && ++packet_steps >= o->max_steps_per_packet)
+                done = 1;
+        }
+        if (use_trace)
+            ibuf[c->trace.count_offset + p] = (int32_t)ts.trace_count;
+#undef MO_TRACE_SNAPSHOT
+    }
+    *rng_x = x;
+    return steps;
+}
+
+/* ================================================================ mcvox */
+typedef struct {
+    v3 pos, dir;
+    i3 vox;
+    int32_t mat;
+    float w, opl;
+} MvState;
+
+static inline int mv_valid(const McgbMcvoxConfig *c, i3 i) {
+    return i.x >= 0 && i.x < c->shape[0] && i.y >= 0 && i.y < c->shape[1] &&
+           i.z >= 0 && i.z < c->shape[2];
+}
+/* mcsim_flat_voxel_index, xopto/mcvox/kernel/mcvox.template.h:786-804 */
+static inline int32_t mv_material_at(const McgbMcvoxConfig *c, const uint8_t *vox, i3 i) {
+    uint64_t flat = ((uint64_t)i.z * (uint64_t)c->shape[1] + (uint64_t)i.y) *
+                    (uint64_t)c->shape[0] + (uint64_t)i.x;
+    return vox[flat];
+}
+/* mcsim_position_to_voxel_index, xopto/mcvox/kernel/mcvox.template.c:206-220 */
+static inline i3 mv_index(const McgbMcvoxConfig *c, v3 p) {
+    i3 r;
+    r.x = cvt_int((p.x - c->top_left[0]) / c->voxel_size[0]);
+    r.y = cvt_int((p.y - c->top_left[1]) / c->voxel_size[1]);
+    r.z = cvt_int((p.z - c->top_left[2]) / c->voxel_size[2]);
+    return r;
+}
+
+/* mcsim_sample_box_intersect, xopto/mcvox/kernel/mcvox.template.c:94-162 */
+static int mv_box_intersect(const McgbMcvoxConfig *c, v3 pos, v3 dir, v3 *isec, v3 *normal) {
+    float ix = (dir.x != 0.0f) ? 1.0f / dir.x : INFINITY;
+    float iy = (dir.y != 0.0f) ? 1.0f / dir.y : INFINITY;
+    float iz = (dir.z != 0.0f) ? 1.0f / dir.z : INFINITY;
+    float t1 = (c->top_left[0] - pos.x) * ix;
+    float t2 = (c->bottom_right[0] - pos.x) * ix;
+    float t3 = (c->top_left[1] - pos.y) * iy;
+    float t4 = (c->bottom_right[1] - pos.y) * iy;
+    float t5 = (c->top_left[2] - pos.z) * iz;
+    float t6 = (c->bottom_right[2] - pos.z) * iz;
+    float txmin = fminf(t1, t2), txmax = fmaxf(t1, t2);
+    float tymin = fminf(t3, t4), tymax = fmaxf(t3, t4);
+    float tzmin = fminf(t5, t6), tzmax = fmaxf(t5, t6);
+    float tmin = fmaxf(fmaxf(txmin, tymin), tzmin);
+    float tmax = fminf(fminf(txmax, tymax), tzmax);
+    if (tmin > tmax) return 0;
+    normal->x = (float)(txmin >= tymin && txmin >= tzmin);
+    normal->y = (float)((normal->x == 0.0f) && tymin >= tzmin);
+    normal->z = (float)(normal->x == 0.0f && normal->y == 0.0f);
+    normal->x *= (float)fsign(dir.x);
+    normal->y *= (float)fsign(dir.y);
+    normal->z *= (float)fsign(dir.z);
+    float t = (tmin > 0.0f) ? tmin : tmax;
+    isec->x = pos.x + t * dir.x;
+    isec->y = pos.y + t * dir.y;
+    isec->z = pos.z + t * dir.z;
+    isec->x = fminf(fmaxf(isec->x, c->top_left[0]), c->bottom_right[0] - 1.1920929e-07f);
+    isec->y = fminf(fmaxf(isec->y, c->top_left[1]), c->bottom_right[1] - 1.1920929e-07f);
+    isec->z = fminf(fmaxf(isec->z, c->top_left[2]), c->bottom_right[2] - 1.1920929e-07f);
+    return tmax >= tmin && tmax >= 0.0f;
+}
+
+/* GaussianBeam.mcsim_launch (mcvox), xopto/mcvox/mcsource/gaussianbeam.py:112-190,
+   Line.mcsim_launch (mcvox), xopto/mcvox/mcsource/line.py, followed by
+   mcsim_set_voxel_index_from_position (mcvox.template.c:240-262). */
+static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *mats,
+                         const uint8_t *vox, MvState *s, uint64_t *x, uint32_t a,
+                         uint64_t *accu) {
+    const McgbSource *src = &c->source;
+    if (src->kind == MCGB_SRC_LINE) {
+        /* xopto/mcvox/mcsource/line.py: position and directions are
+           precomputed on the host by Line.cl_pack */
+        s->w = 1.0f - src->reflectance;
+        s->pos.x = src->position[0]; s->pos.y = src->position[1]; s->pos.z = src->position[2];
+        s->dir.x = src->direction[0]; s->dir.y = src->direction[1]; s->dir.z = src->direction[2];
+        if (c->specular.kind != MCGB_DET_NONE) {
+            v3 d = {src->direction_reflected[0], src->direction_reflected[1],
+                    src->direction_reflected[2]};
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+        }
+    } else {
+        float specular_r = 0.0f;
+        float cos_fi, sin_fi, r;
+        v3 pt_src, pt_mc;
+        r = sqrtf(-2.0f * m_log(mm, 1.0f - rnd(x, a)));
+        r = fminf(r, src->clip);
+        m_sincos(mm, 6.28318548f * rnd(x, a), &sin_fi, &cos_fi);
+        pt_src.x = r * cos_fi * src->sigma[0];
+        pt_src.y = r * sin_fi * src->sigma[1];
+        pt_src.z = 0.0f;
+        const float *T = src->transformation;
+        pt_mc.x = T[0] * pt_src.x + T[1] * pt_src.y + T[2] * pt_src.z;
+        pt_mc.y = T[3] * pt_src.x + T[4] * pt_src.y + T[5] * pt_src.z;
+        pt_mc.z = T[6] * pt_src.x + T[7] * pt_src.y + T[8] * pt_src.z;
+        pt_mc.x += src->position[0];
+        pt_mc.y += src->position[1];
+        pt_mc.z += src->position[2];
+        v3 direction = {src->direction[0], src->direction[1], src->direction[2]};
+        /* mcsim_sample_box_contains, xopto/mcvox/kernel/mcvox.template.h:1227-1235 */
+        if (pt_mc.x >= c->top_left[0] && pt_mc.x < c->bottom_right[0] &&
+            pt_mc.y >= c->top_left[1] && pt_mc.y < c->bottom_right[1] &&
+            pt_mc.z >= c->top_left[2] && pt_mc.z < c->bottom_right[2]) {
+            direction.x = -direction.x; direction.y = -direction.y; direction.z = -direction.z;
+        }
+        v3 isec, normal;
+        if (mv_box_intersect(c, pt_mc, direction, &isec, &normal)) {
+            s->pos = isec;
+            direction.x = -direction.x; direction.y = -direction.y; direction.z = -direction.z;
+            normal.x = -normal.x; normal.y = -normal.y; normal.z = -normal.z;
+            float n_outside = mats[0].n;
+            i3 vi = mv_index(c, s->pos);
+            vi.x = clip_i(vi.x, 0, c->shape[0] - 1);
+            vi.y = clip_i(vi.y, 0, c->shape[1] - 1);
+            vi.z = clip_i(vi.z, 0, c->shape[2] - 1);
+            int32_t mi = mv_material_at(c, vox, vi);
+            float n_inside = mats[mi].n;
+            v3 refracted = direction;
+            refract_safe3(direction, normal, n_outside, n_inside, &refracted);
+            s->dir = refracted;
+            specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
+                                     cos_critical(n_outside, n_inside));
+            if (c->specular.kind != MCGB_DET_NONE)
+                detector_deposit(mm, &c->specular, s->pos, direction, specular_r, accu);
+        } else {
+            s->pos.x = c->top_left[0]; s->pos.y = c->top_left[1]; s->pos.z = c->top_left[2];
+            s->dir.x = 0.0f; s->dir.y = 0.0f; s->dir.z = 1.0f;
+            specular_r = 1.0f;
+        }
+        s->w = 1.0f - specular_r;
+    }
+    s->vox = mv_index(c, s->pos);
+    s->mat = mv_valid(c, s->vox) ? mv_material_at(c, vox, s->vox) : 0;
+}
+
+/* mcsim_intersect, xopto/mcvox/kernel/mcvox.template.c:173-196 */
+static float mv_intersect(const McgbMcvoxConfig *c, const MvState *s, v3 *d) {
+    d->x = c->top_left[0] + (float)((s->dir.x >= 0.0f) + s->vox.x) * c->voxel_size[0] - s->pos.x;
+    d->y = c->top_left[1] + (float)((s->dir.y >= 0.0f) + s->vox.y) * c->voxel_size[1] - s->pos.y;
+    d->z = c->top_left[2] + (float)((s->dir.z >= 0.0f) + s->vox.z) * c->voxel_size[2] - s->pos.z;
+    d->x = (s->dir.x != 0.0f) ? d->x / s->dir.x : INFINITY;
+    d->y = (s->dir.y != 0.0f) ? d->y / s->dir.y : INFINITY;
+    d->z = (s->dir.z != 0.0f) ? d->z / s->dir.z : INFINITY;
+    return fminf(d->x, fminf(d->y, d->z));
+}
+
+/* mcsim_boundary (mcvox), xopto/mcvox/kernel/mcvox.template.c:275-388 */
+static uint32_t mv_boundary(const McgbMcvoxConfig *c, const McgbMaterial *mats,
+                            const uint8_t *vox, MvState *s, v3 dist, uint64_t *x, uint32_t a) {
+    i3 nrm, nv;
+    nrm.x = (dist.x <= dist.y) && (dist.x <= dist.z);
+    nrm.y = nrm.x ? 0 : ((dist.y <= dist.x) && (dist.y <= dist.z));
+    nrm.z = !(nrm.x + nrm.y);
+    nrm.x = s->dir.x < 0.0f ? -nrm.x : nrm.x;
+    nrm.y = s->dir.y < 0.0f ? -nrm.y : nrm.y;
+    nrm.z = s->dir.z < 0.0f ? -nrm.z : nrm.z;
+    nv.x = s->vox.x + nrm.x; nv.y = s->vox.y + nrm.y; nv.z = s->vox.z + nrm.z;
+    int escaping = !mv_valid(c, nv);
+    int32_t next_mat = !escaping ? mv_material_at(c, vox, nv) : 0;
+    if (s->mat == next_mat && !escaping) {
+        s->vox = nv;
+        return EV_REFRACTION;
+    }
+    float n1 = mats[s->mat].n, n2 = mats[next_mat].n;
+    if (n1 == n2) {
+        s->vox = nv;
+        s->mat = next_mat;
+        return EV_REFRACTION;
+    }
+    float cc = cos_critical(n1, n2);
+    float cos1 = (float)nrm.x * s->dir.x + (float)nrm.y * s->dir.y + (float)nrm.z * s->dir.z;
+    v3 fn = {(float)nrm.x, (float)nrm.y, (float)nrm.z};
+    if (cos1 > cc) {
+        float R = reflectance(n1, n2, cos1, cc);
+        if (R < rnd(x, a)) {
+            s->dir = refract3(s->dir, fn, n1, n2);
+            s->vox = nv;
+            s->mat = next_mat;
+            return EV_REFRACTION;
+        }
+    }
+    s->dir = reflect3(s->dir, fn);
+    return EV_REFLECTION;
+}
+
+/* McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:548-1048 */
+static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMaterial *mats,
+                             const uint8_t *vox, const float *lut, uint64_t *rng_x,
+                             uint32_t a, uint64_t first, uint64_t stride,
+                             uint64_t *accu, float *fbuf, int32_t *ibuf) {
+    const McgbRunOptions *o = &c->opt;
+    uint64_t x = *rng_x, steps = 0;
+    v3 src_pos = {c->source.position[0], c->source.position[1], c->source.position[2]};
+    float rmax2 = o->rmax * o->rmax;
+    int use_trace = c->trace.flags != MCGB_TRACE_NONE;
+    for (uint64_t p = first; p < c->num_packets; p += stride) {
+        MvState s;
+        TraceState ts;
+        memset(&s, 0, sizeof(s));
+        ts.photon_index = p; ts.trace_count = 0; ts.events = 0;
+        mcvox_launch(mm, c, mats, vox, &s, &x, a, accu);
+        uint32_t events = EV_LAUNCH;
+#define MV_TRACE_SNAPSHOT() do { ts.pos = s.pos; ts.dir = s.dir; ts.w = s.w; ts.opl = s.opl; \
+                                 ts.events = events; } while (0)
+        if (use_trace && (c->trace.flags & MCGB_TRACE_START)) {
+            MV_TRACE_SNAPSHOT();
+            trace_event(&c->trace, &ts, fbuf);
+        }
+        int done = 0;
+        uint64_t packet_steps = 0;
+        while (!done) {
+            const McgbMaterial *M = &mats[s.mat];
+            float step, deposit, d, d_ok;
+            v3 dist;
+            ++steps;
+            if (o->method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
+                step = -m_log(mm, rnd(&x, a)) / M->mus;
+            else
+                step = -m_log(mm, rnd(&x, a)) * M->inv_mut;
+            step = fminf(step, FLT_MAX);
+            d = mv_intersect(c, &s, &dist);
+            d_ok = fminf(d, step);
+            s.pos.x = s.pos.x + d_ok * s.dir.x;
+            s.pos.y = s.pos.y + d_ok * s.dir.y;
+            s.pos.z = s.pos.z + d_ok * s.dir.z;
+            if (o->track_optical_pathlength) s.opl += M->n * d_ok;
+            if (o->method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
+                float mua = M->mua;
+                float fraction = 1.0f - m_exp(mm, -mua * d_ok);
+                deposit = fraction * s.w;
+                s.w -= deposit;
+                events |= EV_ABSORPTION;
+                if (c->fluence.kind != MCGB_FLUENCE_NONE) {
+                    float step_back = (mua != 0.0f)
+                        ? d_ok - (-m_log(mm, 1.0f - rnd(&x, a) * fraction)) / mua : 0.0f;
+                    v3 dp = {s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
+                             s.pos.z - step_back * s.dir.z};
+                    fluence_deposit(&c->fluence, dp, deposit, M->mua, accu);
+                }
+                if (d < step) {
+                    events |= mv_boundary(c, mats, vox, &s, dist, &x, a) | EV_BOUNDARY_HIT;
+                    if (!mv_valid(c, s.vox)) {
+                        if (s.vox.z < 0)
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                        else if (s.vox.z >= c->shape[2])
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                        done = 1;
+                    }
+                } else {
+                    float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az);
+                    scatter_direction(mm, &s.dir, ct, az);
+                    events |= EV_SCATTERING;
+                }
+                if (s.w < o->packet_weight_min) {
+                    if (o->use_lottery) {
+                        if (rnd(&x, a) > o->lottery_chance) done = 1;
+                        else s.w = s.w / o->lottery_chance;
+                    } else {
+                        done = 1;
+                    }
+                }
+            } else {
+                if (d < step) {
+                    events |= mv_boundary(c, mats, vox, &s, dist, &x, a) | EV_BOUNDARY_HIT;
+                    if (!mv_valid(c, s.vox)) {
+                        if (s.vox.z < 0)
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                        else if (s.vox.z >= c->shape[2])
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                        done = 1;
+                    }
+                } else if (o->method == MCGB_METHOD_ALBEDO_REJECTION) {
+                    if (rnd(&x, a) < M->mua_inv_mut) {
+                        deposit = s.w;
+                        s.w -= deposit;
+                        events |= EV_ABSORPTION;
+                        done = 1;
+                        if (c->fluence.kind != MCGB_FLUENCE_NONE)
+                            fluence_deposit(&c->fluence, s.pos, deposit, M->mua, accu);
+                    } else {
+                        float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az);
+                        scatter_direction(mm, &s.dir, ct, az);
+                        events |= EV_SCATTERING;
+                    }
+                } else {
+                    deposit = s.w * M->mua_inv_mut;
+                    s.w -= deposit;
+                    events |= EV_ABSORPTION;
+                    if (c->fluence.kind != MCGB_FLUENCE_NONE)
+                        fluence_deposit(&c->fluence, s.pos, deposit, M->mua, accu);
+                    float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az);
+                    scatter_direction(mm, &s.dir, ct, az);
+                    events |= EV_SCATTERING;
+                    if (s.w < o->packet_weight_min) {
+                        if (o->use_lottery) {
+                            if (rnd(&x, a) > o->lottery_chance) done = 1;
+                            else s.w = s.w / o->lottery_chance;
+                        } else {
+                            done = 1;
+                        }
+                    }
+                }
+            }
+            /* mcvox.template.c:1004-1008 */
+            v3 dd = {s.pos.x - src_pos.x, s.pos.y - src_pos.y, s.pos.z - src_pos.z};
+            if (dot3(dd, dd) > rmax2 || s.w <= 0.0f) {
+                done = 1;
+                events |= EV_ESCAPED;
+            }
+            if (done) events |= EV_TERMINATED;
+            if (use_trace) {
+                if (c->trace.flags == MCGB_TRACE_ALL ||
+                    ((c->trace.flags & MCGB_TRACE_END) && done)) {
+                    MV_TRACE_SNAPSHOT();
+                    trace_event(&c->trace, &ts, fbuf);
+                }
+            }
+            events = 0;
+            if (!done && o->max_steps_per_packet && ++packet_steps >= o->max_steps_per_packet)
+                done = 1;
+        }
+        if (use_trace)
+            ibuf[c->trace.count_offset + p] = (int32_t)ts.trace_count;
+#undef MV_TRACE_SNAPSHOT
+    }
+    *rng_x = x;
+    return steps;
+}
+
+/* ====================================================== exported API */
+/* Runs every stream t < num_streams with the static packet mapping.  With
+   nthreads > 1 the streams run on an OpenMP pool, each thread tallying into
+   a private copy of the accumulator that is summed at the end (integer sums,
+   so the result equals the serial run).  Returns the interaction steps. */
+#define MO_RUN_BODY(STREAM_CALL)                                                    \
+    uint64_t steps = 0;                                                             \
+    int64_t T = cfg->num_streams;                                                   \
+    if (nthreads <= 1) {                                                            \
+        for (int64_t t = 0; t < T; ++t) {                                           \
+            uint64_t *acc = accu;                                                   \
+            steps += STREAM_CALL;                                                   \
+        }                                                                           \
+        return steps;                                                               \
+    }                                                                               \
+    int failed = 0;                                                                 \
+    _Pragma("omp parallel num_threads(nthreads) reduction(+:steps)")               \
+    {                                                                               \
+        uint64_t *acc = (uint64_t *)calloc(accu_size ? accu_size : 1, 8);           \
+        if (!acc) {                                                                 \
+            _Pragma("omp atomic write") failed = 1;                                 \
+        } else {                                                                    \
+            _Pragma("omp for schedule(dynamic, 4)")                                 \
+            for (int64_t t = 0; t < T; ++t) steps += STREAM_CALL;                   \
+            _Pragma("omp critical")                                                 \
+            for (uint64_t i = 0; i < accu_size; ++i) accu[i] += acc[i];             \
+            free(acc);                                                              \
+        }                                                                           \
+    }                                                                               \
+    return failed ? 0 : steps;
+
+uint64_t mco_mcml_run(int math_mode, const McgbMcmlConfig *cfg, const float *lut,
+                      uint64_t *rng_x, const uint32_t *rng_a, uint64_t *accu,
+                      uint64_t accu_size, float *fbuf, int32_t *ibuf, int nthreads) {
+    MO_RUN_BODY(mcml_stream(math_mode, cfg, lut, &rng_x[t], rng_a[t], (uint64_t)t,
+                            (uint64_t)T, acc, fbuf, ibuf))
+}
+
+uint64_t mco_mcvox_run(int math_mode, const McgbMcvoxConfig *cfg,
+                       const McgbMaterial *materials, const uint8_t *voxels,
+                       const float *lut, uint64_t *rng_x, const uint32_t *rng_a,
+                       uint64_t *accu, uint64_t accu_size, float *fbuf, int32_t *ibuf,
+                       int nthreads) {
+    MO_RUN_BODY(mcvox_stream(math_mode, cfg, materials, voxels, lut, &rng_x[t], rng_a[t],
+                             (uint64_t)t, (uint64_t)T, acc, fbuf, ibuf))
+}
+
+/* Stream of uniform random numbers (RngKernel, mcbase.template.c:1640-1646). */
+void mco_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *out) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = rnd(&x, a);
+}
+
+/* Elementary functions for accuracy tests of the portable math. */
+float mco_pm_log(float x) { return pm_logf(x); }
+float mco_pm_exp(float x) { return pm_expf(x); }
+float mco_pm_pow(float x, float y) { return pm_powrf(x, y); }
+void mco_pm_sincos(float x, float *s, float *c) { pm_sincosf(x, s, c); }
+
+int mco_sizeof(int kind) {
+    switch (kind) {
+        case 0: return (int)sizeof(McgbLayer);
+        case 1: return (int)sizeof(McgbSource);
+        case 2: return (int)sizeof(McgbDetector);
+        case 3: return (int)sizeof(McgbFluence);
+        case 4: return (int)sizeof(McgbTrace);
+        case 5: return (int)sizeof(McgbMaterial);
+        case 6: return (int)sizeof(McgbMcmlConfig);
+        case 7: return (int)sizeof(McgbMcvoxConfig);
+        case 8: return (int)sizeof(McgbBuffers);
+        case 9: return (int)sizeof(McgbRunOptions);
+        case 10: return (int)sizeof(McgbPf);
+        default: return -1;
+    }
+}

@@ -1,0 +1,200 @@
+"""Run machinery shared by the layered and voxelized simulators: buffer
+allocators with the reference's method names (xopto/mcbase/mcworker.py
+ClWorker / ClWorkerStandardBufferLutMixin / ClWorkerRngMixin), persistent
+random-number streams on the device, and the launch / download cycle of
+``Mc.run`` (xopto/mcml/mc.py:730-1018).
+
+Device memory and streams come from PyTorch; the compute is the C-ABI
+library.  Nothing here runs the simulation on the CPU.
+"""
+import ctypes as C
+import time
+from typing import Dict, List, Tuple
+
+import numpy as np
+
+from . import _abi, _lib
+from .mcbase import mcoptions
+from .rng import Random
+
+
+class _Pool:
+    """Linear allocator of one device buffer (accumulator, float or int)."""
+
+    def __init__(self):
+        self.size = 0
+        self.items = []        # (owner, offset, count)
+
+    def clear(self):
+        self.size = 0
+        self.items = []
+
+    def allocate(self, owner, shape) -> int:
+        count = int(np.prod(shape)) if len(shape) else 1
+        # keep allocations 16-byte aligned for vectorized trace stores
+        offset = (self.size + 3) // 4 * 4
+        self.items.append((owner, offset, count))
+        self.size = offset + count
+        return offset
+
+    def find(self, owner) -> Tuple[int, int]:
+        for o, off, n in self.items:
+            if o is owner:
+                return off, n
+        raise KeyError(owner)
+
+
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError('A CUDA device is required to run the GB300 simulator '
+                           '(there is no CPU fallback).')
+    return torch
+
+
+class McEngine:
+    """Base class of mcml.Mc and mcvox.Mc."""
+    MEDIUM = 0
+
+    def __init__(self, options=None, rnginit=None, types=None):
+        from .mcbase import mctypes
+        self._types = mctypes.check(types)
+        self._mc_options = list(options or [])
+        self._rnginit = rnginit
+        self._rmax = float('inf')
+        self._acc = _Pool()
+        self._flt = _Pool()
+        self._int = _Pool()
+        self._luts: List[np.ndarray] = []
+        self._lut_size = 0
+        self._dev = {}                # persistent device tensors
+        self._num_streams = None
+        self._run_report = {'upload': None, 'download': None, 'execution': None,
+                            'threads': None, 'items': None, 'steps': None}
+        self._block_size = 0
+
+    # ------------------------------------------------ reference worker API
+    def cl_allocate_rw_accumulator_buffer(self, owner, shape) -> int:
+        return self._acc.allocate(owner, shape)
+
+    def cl_allocate_rw_float_buffer(self, owner, shape) -> int:
+        return self._flt.allocate(owner, shape)
+
+    def cl_allocate_rw_int_buffer(self, owner, shape) -> int:
+        return self._int.allocate(owner, shape)
+
+    def append_r_lut(self, data) -> int:
+        data = np.asarray(data, dtype=np.float32).ravel()
+        offset = self._lut_size
+        self._luts.append(data)
+        self._lut_size += data.size
+        return offset
+
+    def clear_r_luts(self):
+        self._luts = []
+        self._lut_size = 0
+
+    def _clear_allocators(self):
+        self._acc.clear()
+        self._flt.clear()
+        self._int.clear()
+        self.clear_r_luts()
+
+    types = property(lambda self: self._types)
+    options = property(lambda self: self._mc_options)
+    run_report = property(lambda self: dict(self._run_report), None, None,
+                          'Timing of the latest run: upload, execution, download (s), '
+                          'threads, items (packets) and steps.')
+
+    def _get_rmax(self):
+        return self._rmax
+
+    def _set_rmax(self, v):
+        self._rmax = float(v)
+
+    rmax = property(_get_rmax, _set_rmax, None, 'Radius beyond which packets are terminated (m).')
+
+    def _resolved_options(self) -> Dict:
+        return mcoptions.resolve(self._mc_options)
+
+    def _run_options(self, track_opl: bool) -> _abi.McgbRunOptions:
+        res = self._resolved_options()
+        o = _abi.default_options()
+        o.method = int(res.get('MC_METHOD', 0))
+        fast = bool(res.get('MC_USE_NATIVE_MATH', False) or res.get('MC_USE_HALF_MATH', False))
+        o.math = _abi.MATH_FAST if fast else _abi.MATH_EXACT
+        o.use_lottery = int(bool(res.get('MC_USE_LOTTERY', True)))
+        o.packet_weight_min = float(res.get('MC_PACKET_WEIGHT_MIN', 1e-4))
+        o.lottery_chance = float(res.get('MC_PACKET_LOTTERY_CHANCE', 0.1))
+        o.rmax = self._rmax
+        o.track_optical_pathlength = int(bool(track_opl))
+        o.block_size = self._block_size
+        return o
+
+    def _lut_array(self) -> np.ndarray:
+        if not self._luts:
+            return np.zeros((0,), dtype=np.float32)
+        return np.concatenate(self._luts).astype(np.float32)
+
+    # ------------------------------------------------------------- streams
+    def suggested_streams(self, math: int) -> int:
+        lib = _lib.load()
+        torch_cuda()
+        n = C.c_uint32(0)
+        _lib.check(lib.mcgb_suggest_streams(self.MEDIUM, int(math), self._block_size, C.byref(n)))
+        return int(n.value)
+
+    def host_seeds(self, n: int):
+        """(x, a) of the first n streams for this simulator's initializer."""
+        if self._rnginit is None:
+            self._rnginit = Random().initializer()
+        return Random().seeds(n, self._rnginit)
+
+    def _ensure_streams(self, torch, n: int, device):
+        """Allocates and seeds n device streams once; their x states persist
+        across runs so successive runs continue the streams (the reference
+        keeps rng_seeds_x in device memory, xopto/mcml/mc.py:829-845)."""
+        if self._num_streams == n and 'rng_x' in self._dev:
+            return
+        x, a = self.host_seeds(n)
+        self._dev['rng_x'] = torch.from_numpy(x.view(np.int64)).to(device)
+        self._dev['rng_a'] = torch.from_numpy(a.view(np.int32)).to(device)
+        self._num_streams = n
+
+    def rng_states(self) -> np.ndarray:
+        """Current x states of the device streams (copyseeds)."""
+        if 'rng_x' not in self._dev:
+            return None
+        return self._dev['rng_x'].cpu().numpy().view(np.uint64).copy()
+
+    # ----------------------------------------------------------- run cycle
+    def _device_buffers(self, torch, device, lut: np.ndarray, extra: dict) -> _abi.McgbBuffers:
+        d = self._dev
+        d['accu'] = torch.zeros((max(self._acc.size, 1),), dtype=torch.int64, device=device)
+        d['flt'] = torch.zeros((max(self._flt.size, 4),), dtype=torch.float32, device=device)
+        d['int'] = torch.zeros((max(self._int.size, 1),), dtype=torch.int32, device=device)
+        d['lut'] = torch.from_numpy(lut if lut.size else np.zeros((1,), np.float32)).to(device)
+        d['counters'] = torch.zeros((_abi.NUM_COUNTERS,), dtype=torch.int64, device=device)
+        b = _abi.McgbBuffers()
+        b.rng_x = d['rng_x'].data_ptr()
+        b.rng_a = d['rng_a'].data_ptr()
+        b.accumulator = d['accu'].data_ptr()
+        b.accumulator_size = self._acc.size
+        b.float_buffer = d['flt'].data_ptr()
+        b.float_size = self._flt.size
+        b.int_buffer = d['int'].data_ptr()
+        b.int_size = self._int.size
+        b.fp_lut = d['lut'].data_ptr() if lut.size else None
+        b.fp_lut_size = int(lut.size)
+        for k, v in extra.items():
+            setattr(b, k, v)
+        b.counters = d['counters'].data_ptr()
+        return b
+
+    def _launch(self, lib_fn, cfg, buffers, torch):
+        stream = torch.cuda.current_stream().cuda_stream
+        _lib.check(lib_fn(C.byref(cfg), C.byref(buffers), C.c_void_p(stream)))
+        counters = (C.c_uint64 * _abi.NUM_COUNTERS)()
+        code = _lib.load().mcgb_check_counters(C.c_void_p(self._dev['counters'].data_ptr()),
+                                               C.c_void_p(stream), counters)
+        return code, [int(v) for v in counters]

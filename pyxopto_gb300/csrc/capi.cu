@@ -1,0 +1,279 @@
+/*
+ * capi.cu - the C ABI of libxopto_gb300.so (declared in
+ * include/xopto_gb300.h): argument validation, launch shapes, status
+ * checks, and the small utility kernels (random-number dump, buffer fill).
+ *
+ * Host-side checks mirror the reference's failure detection: struct-size
+ * handshake (xopto/mcml/mc.py:674-728), packet-count limit (mc.py:813-818),
+ * LUT/option consistency (mc.py:887-898).  Every offset a configuration names
+ * is checked against the buffer sizes before a kernel is launched, so the
+ * kernels index only memory the caller handed over.
+ */
+#include <cuda_runtime.h>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include "../../include/xopto_gb300.h"
+#include "launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(MCGB_E_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+bool range_ok(uint64_t offset, uint64_t count, uint64_t size) {
+    return offset <= size && count <= size - offset;
+}
+
+int check_pf(int kind, const McgbPf &pf, const McgbBuffers *b, const char *who, unsigned idx) {
+    if (kind == MCGB_PF_LUT) {
+        if (!b->fp_lut) return fail(MCGB_E_INVALID, "%s %u: Lut phase function without a LUT buffer", who, idx);
+        if (pf.lut_size < 2) return fail(MCGB_E_INVALID, "%s %u: Lut size %u < 2", who, idx, pf.lut_size);
+        if (!range_ok(pf.lut_offset, pf.lut_size, b->fp_lut_size))
+            return fail(MCGB_E_SIZE, "%s %u: LUT [%u, +%u) beyond the LUT buffer (%llu floats)", who, idx,
+                        pf.lut_offset, pf.lut_size, (unsigned long long)b->fp_lut_size);
+    }
+    return MCGB_OK;
+}
+
+int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uint32_t num_streams,
+                 const McgbSource &src, const McgbDetector *dets, const McgbFluence &fl,
+                 const McgbTrace &tr, const McgbBuffers *b) {
+    if (!b) return fail(MCGB_E_INVALID, "buffers is NULL");
+    if (num_streams == 0) return fail(MCGB_E_INVALID, "num_streams must be positive");
+    if (num_streams > (1u << 24)) return fail(MCGB_E_SIZE, "num_streams %u exceeds 2^24", num_streams);
+    if (!b->rng_x || !b->rng_a) return fail(MCGB_E_INVALID, "RNG state buffers are NULL");
+    if (!b->counters) return fail(MCGB_E_INVALID, "counters buffer is NULL");
+    if (o.method < 0 || o.method > 2) return fail(MCGB_E_INVALID, "unknown method %d", o.method);
+    if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
+        return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
+    if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
+    if (src.kind != MCGB_SRC_LINE && src.kind != MCGB_SRC_GAUSSIAN_BEAM)
+        return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
+    if (!(o.lottery_chance > 0.0f && o.lottery_chance <= 1.0f))
+        return fail(MCGB_E_INVALID, "lottery chance %g outside (0, 1]", (double)o.lottery_chance);
+    if (!(o.packet_weight_min > 0.0f && o.packet_weight_min <= 1.0f))
+        return fail(MCGB_E_INVALID, "minimum packet weight %g outside (0, 1]", (double)o.packet_weight_min);
+    if (num_packets > 0 && num_packets > UINT64_MAX - num_streams)
+        return fail(MCGB_E_SIZE, "packet count overflows the packet index");
+    const char *names[3] = {"top", "bottom", "specular"};
+    for (int i = 0; i < 3; ++i) {
+        const McgbDetector &d = dets[i];
+        if (d.kind == MCGB_DET_NONE) continue;
+        if (d.kind != MCGB_DET_TOTAL && d.kind != MCGB_DET_RADIAL)
+            return fail(MCGB_E_INVALID, "%s detector: unknown kind %d", names[i], d.kind);
+        uint64_t n = d.kind == MCGB_DET_RADIAL ? d.n : 1;
+        if (n == 0) return fail(MCGB_E_INVALID, "%s detector has no bins", names[i]);
+        if (!b->accumulator || !range_ok(d.offset, n, b->accumulator_size))
+            return fail(MCGB_E_SIZE, "%s detector [%llu, +%llu) beyond the accumulator (%llu)", names[i],
+                        (unsigned long long)d.offset, (unsigned long long)n,
+                        (unsigned long long)b->accumulator_size);
+    }
+    if (fl.kind != MCGB_FLUENCE_NONE) {
+        if (fl.kind != MCGB_FLUENCE_DEPOSITION && fl.kind != MCGB_FLUENCE_RATE)
+            return fail(MCGB_E_INVALID, "unknown fluence kind %d", fl.kind);
+        if (fl.shape[0] == 0 || fl.shape[1] == 0 || fl.shape[2] == 0)
+            return fail(MCGB_E_INVALID, "fluence grid has an empty axis");
+        uint64_t n = (uint64_t)fl.shape[0] * fl.shape[1] * fl.shape[2];
+        if (!b->accumulator || !range_ok(fl.offset, n, b->accumulator_size))
+            return fail(MCGB_E_SIZE, "fluence [%llu, +%llu) beyond the accumulator (%llu)",
+                        (unsigned long long)fl.offset, (unsigned long long)n,
+                        (unsigned long long)b->accumulator_size);
+        if (fl.k <= 0) return fail(MCGB_E_INVALID, "fluence k must be positive");
+    }
+    if (tr.flags != MCGB_TRACE_NONE) {
+        if (tr.max_events == 0) return fail(MCGB_E_INVALID, "trace max_events must be positive");
+        if (num_packets > (UINT64_MAX / MCGB_TRACE_ENTRY_LEN) / tr.max_events)
+            return fail(MCGB_E_SIZE, "trace size overflows");
+        uint64_t nf = num_packets * tr.max_events * MCGB_TRACE_ENTRY_LEN;
+        if (!b->float_buffer || !range_ok(tr.data_offset, nf, b->float_size))
+            return fail(MCGB_E_SIZE, "trace events beyond the float buffer");
+        if (!b->int_buffer || !range_ok(tr.count_offset, num_packets, b->int_size))
+            return fail(MCGB_E_SIZE, "trace counts beyond the int buffer");
+    }
+    return MCGB_OK;
+}
+
+int device_sm_count(int *sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    return MCGB_OK;
+}
+
+int make_shape(int medium, int math, uint32_t block_size, uint32_t num_streams, const McgbBuffers *b,
+               double deadline_s, LaunchShape *s) {
+    s->block = block_size ? block_size : 128;
+    if (s->block > 256 || (s->block % 32) != 0)
+        return fail(MCGB_E_INVALID, "block size %u must be a multiple of 32 and <= 256", s->block);
+    s->grid = (num_streams + s->block - 1) / s->block;
+    s->lut_in_smem = (b->fp_lut && b->fp_lut_size > 0 && b->fp_lut_size <= 24576) ? 1 : 0;
+    s->dyn_smem = s->lut_in_smem ? (size_t)b->fp_lut_size * sizeof(float) : 0;
+    double d = deadline_s > 0.0 ? deadline_s : 300.0;
+    s->deadline_ns = (uint64_t)(d * 1e9);
+    (void)medium;
+    (void)math;
+    return MCGB_OK;
+}
+
+/* One device thread dumps n random numbers of one stream (RngKernel,
+   xopto/mcbase/kernel/mcbase.template.c:1640-1646). */
+__global__ void rng_dump_kernel(uint64_t x, uint32_t a, uint64_t n, float *out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (uint64_t i = 0; i < n; ++i) {
+        x = (uint64_t)(uint32_t)x * (uint64_t)a + (x >> 32);
+        out[i] = __uint2float_rn((uint32_t)x) * 2.3283064365386963e-10f;
+    }
+}
+
+/* ScalarFillMcAccu (xopto/mcbase/kernel/mcbase.template.c:1740-1748) */
+__global__ void fill_u64_kernel(uint64_t *p, uint64_t n, uint64_t v) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mcgb_last_error(void) { return g_last_error.c_str(); }
+
+int mcgb_abi_version(void) { return MCGB_ABI_VERSION; }
+
+int mcgb_sizeof(int kind) {
+    switch (kind) {
+        case 0: return (int)sizeof(McgbLayer);
+        case 1: return (int)sizeof(McgbSource);
+        case 2: return (int)sizeof(McgbDetector);
+        case 3: return (int)sizeof(McgbFluence);
+        case 4: return (int)sizeof(McgbTrace);
+        case 5: return (int)sizeof(McgbMaterial);
+        case 6: return (int)sizeof(McgbMcmlConfig);
+        case 7: return (int)sizeof(McgbMcvoxConfig);
+        case 8: return (int)sizeof(McgbBuffers);
+        case 9: return (int)sizeof(McgbRunOptions);
+        case 10: return (int)sizeof(McgbPf);
+        default: return -1;
+    }
+}
+
+int mcgb_suggest_streams(int medium, int math, uint32_t block_size, uint32_t *streams) {
+    if (!streams) return fail(MCGB_E_INVALID, "streams is NULL");
+    int sms = 0, r = device_sm_count(&sms);
+    if (r) return r;
+    int bps = 0;
+    unsigned block = block_size ? block_size : 128;
+    cudaError_t e = (math == MCGB_MATH_FAST) ? mcgb_fast::occupancy(medium, (int)block, 0, &bps)
+                                             : mcgb_exact::occupancy(medium, (int)block, 0, &bps);
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy");
+    *streams = (uint32_t)sms * (uint32_t)bps * block;
+    return MCGB_OK;
+}
+
+int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *stream) {
+    if (!cfg) return fail(MCGB_E_INVALID, "cfg is NULL");
+    if (cfg->num_layers < 3 || cfg->num_layers > MCGB_MAX_LAYERS)
+        return fail(MCGB_E_INVALID, "num_layers %u outside [3, %d]", cfg->num_layers, MCGB_MAX_LAYERS);
+    McgbDetector dets[3] = {cfg->top, cfg->bottom, cfg->specular};
+    int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
+                         cfg->fluence, cfg->trace, buf);
+    if (r) return r;
+    for (uint32_t i = 0; i < cfg->num_layers; ++i) {
+        r = check_pf(cfg->pf_kind, cfg->layers[i].pf, buf, "layer", i);
+        if (r) return r;
+    }
+    if (cfg->num_packets == 0) return MCGB_OK;
+    LaunchShape s;
+    r = make_shape(0, cfg->opt.math, cfg->opt.block_size, cfg->num_streams, buf, cfg->opt.deadline_s, &s);
+    if (r) return r;
+    cudaError_t e = (cfg->opt.math == MCGB_MATH_FAST)
+                        ? mcgb_fast::launch_mcml(*cfg, *buf, (cudaStream_t)stream, s)
+                        : mcgb_exact::launch_mcml(*cfg, *buf, (cudaStream_t)stream, s);
+    if (e != cudaSuccess) return cuda_fail(e, "mcml launch");
+    return MCGB_OK;
+}
+
+int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *stream) {
+    if (!cfg) return fail(MCGB_E_INVALID, "cfg is NULL");
+    if (cfg->num_materials < 2 || cfg->num_materials > MCGB_MAX_MATERIALS)
+        return fail(MCGB_E_INVALID, "num_materials %u outside [2, %d]", cfg->num_materials,
+                    MCGB_MAX_MATERIALS);
+    for (int k = 0; k < 3; ++k) {
+        if (cfg->shape[k] <= 0) return fail(MCGB_E_INVALID, "voxel shape must be positive");
+        if (!(cfg->voxel_size[k] > 0.0f)) return fail(MCGB_E_INVALID, "voxel size must be positive");
+    }
+    McgbDetector dets[3] = {cfg->top, cfg->bottom, cfg->specular};
+    int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
+                         cfg->fluence, cfg->trace, buf);
+    if (r) return r;
+    if (!buf->voxels || !buf->materials) return fail(MCGB_E_INVALID, "voxel or material buffer is NULL");
+    /* Voxel material indices are validated by the caller (uint8 < num_materials):
+       the host wrapper checks the array before upload. */
+    if (cfg->num_packets == 0) return MCGB_OK;
+    LaunchShape s;
+    r = make_shape(1, cfg->opt.math, cfg->opt.block_size, cfg->num_streams, buf, cfg->opt.deadline_s, &s);
+    if (r) return r;
+    cudaError_t e = (cfg->opt.math == MCGB_MATH_FAST)
+                        ? mcgb_fast::launch_mcvox(*cfg, *buf, (cudaStream_t)stream, s)
+                        : mcgb_exact::launch_mcvox(*cfg, *buf, (cudaStream_t)stream, s);
+    if (e != cudaSuccess) return cuda_fail(e, "mcvox launch");
+    return MCGB_OK;
+}
+
+int mcgb_check_counters(const uint64_t *dev_counters, void *stream, uint64_t *host_counters) {
+    if (!dev_counters) return fail(MCGB_E_INVALID, "counters is NULL");
+    uint64_t h[MCGB_NUM_COUNTERS];
+    cudaError_t e = cudaMemcpyAsync(h, dev_counters, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "reading counters");
+    if (host_counters) memcpy(host_counters, h, sizeof(h));
+    uint64_t st = h[MCGB_CNT_STATUS];
+    if (st & MCGB_STATUS_BAD_INDEX) return fail(MCGB_E_BAD_INDEX, "kernel reported an out-of-range index");
+    if (st & MCGB_STATUS_TIMEOUT) return fail(MCGB_E_TIMEOUT, "run deadline expired before all packets finished");
+    if (st & MCGB_STATUS_ABORTED) return fail(MCGB_E_TIMEOUT, "run aborted by the host");
+    return MCGB_OK;
+}
+
+int mcgb_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *dev_out, void *stream) {
+    if (!dev_out && n) return fail(MCGB_E_INVALID, "output is NULL");
+    if (n == 0) return MCGB_OK;
+    rng_dump_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(x, a, n, dev_out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? MCGB_OK : cuda_fail(e, "rng dump launch");
+}
+
+int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream) {
+    if (n == 0) return MCGB_OK;
+    if (!dev) return fail(MCGB_E_INVALID, "buffer is NULL");
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    fill_u64_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(dev, n, value);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? MCGB_OK : cuda_fail(e, "fill launch");
+}
+
+int mcgb_reduce_tallies(uint64_t *host_dst, const uint64_t *host_src, uint64_t n) {
+    if (n && (!host_dst || !host_src)) return fail(MCGB_E_INVALID, "NULL tally array");
+    for (uint64_t i = 0; i < n; ++i) host_dst[i] += host_src[i];
+    return MCGB_OK;
+}
+
+}  // extern "C"

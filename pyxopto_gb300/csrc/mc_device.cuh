@@ -1,0 +1,295 @@
+/*
+ * mc_device.cuh - device functions shared by the layered (mcml) and
+ * voxelized (mcvox) transport kernels: random numbers, boundary optics,
+ * direction sampling, phase functions and integer tallies.
+ *
+ * Included by exactly one translation unit per math mode:
+ *   transport_exact.cu  MCGB_FAST_MATH == 0, compiled with -fmad=false:
+ *                       IEEE +,-,*,/,sqrt and the portable log/exp/sincos/powr
+ *                       routines, bit-identical to a CPU evaluation.
+ *   transport_fast.cu   MCGB_FAST_MATH == 1, compiled with -use_fast_math:
+ *                       special-function-unit log2/sin/cos/ex2, approximate
+ *                       division and square root (the reference's
+ *                       MC_USE_NATIVE_MATH, xopto/mcbase/kernel/mcbase.template.h:522-556).
+ * Each unit wraps the kernels in its own namespace (mcgb_exact / mcgb_fast).
+ *
+ * The algorithms follow PyXOpto's OpenCL device library; each function cites
+ * the reference lines it implements.
+ */
+#pragma once
+#include <cstdint>
+#include <cfloat>
+#include "../../include/xopto_gb300.h"
+#include "portable_math.h"
+
+#ifndef MCGB_FAST_MATH
+#error "MCGB_FAST_MATH must be defined to 0 or 1"
+#endif
+
+#define MCGB_DEV static __device__ __forceinline__
+
+#if MCGB_FAST_MATH
+MCGB_DEV float mc_log(float x) { return __logf(x); }
+MCGB_DEV float mc_exp(float x) { return __expf(x); }
+MCGB_DEV float mc_pow(float x, float y) { return __powf(x, y); }
+MCGB_DEV void mc_sincos(float x, float *s, float *c) { __sincosf(x, s, c); }
+MCGB_DEV float mc_div(float a, float b) { return __fdividef(a, b); }
+MCGB_DEV float mc_sqrt(float x) { return sqrtf(x); }
+MCGB_DEV float mc_rcp_length(float x2) { return rsqrtf(x2); }
+#else
+MCGB_DEV float mc_log(float x) { return pm_logf(x); }
+MCGB_DEV float mc_exp(float x) { return pm_expf(x); }
+MCGB_DEV float mc_pow(float x, float y) { return pm_powrf(x, y); }
+MCGB_DEV void mc_sincos(float x, float *s, float *c) { pm_sincosf(x, s, c); }
+MCGB_DEV float mc_div(float a, float b) { return a / b; }
+MCGB_DEV float mc_sqrt(float x) { return sqrtf(x); }
+/* mc_normalize_fpv3: k = 1/length (xopto/mcbase/kernel/mcbase.template.c:975-981) */
+MCGB_DEV float mc_rcp_length(float x2) { return 1.0f / sqrtf(x2); }
+#endif
+
+struct f3 { float x, y, z; };
+struct i3 { int x, y, z; };
+
+/* Float-to-int conversions round toward zero and saturate (the reference's
+   convert_int / convert_uint). */
+MCGB_DEV int cvt_int(float x) { return __float2int_rz(x); }
+MCGB_DEV unsigned cvt_uint(float x) { return __float2uint_rz(x); }
+MCGB_DEV int fsign(float x) { return x >= 0.0f ? 1 : -1; }
+MCGB_DEV int clip_i(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+/* Marsaglia multiply-with-carry step and its uniform float:
+   fp_random_single, xopto/mcbase/kernel/mcbase.template.c:1576-1594.
+   x = lo32(x)*a + hi32(x) is one 32x32->64 multiply-add; the float is
+   (uint32)x / 2^32 (an exact scaling). */
+struct Rng {
+    uint64_t x;
+    uint32_t a;
+    __device__ __forceinline__ float next() {
+        x = (uint64_t)(uint32_t)x * (uint64_t)a + (x >> 32);
+        return __uint2float_rn((uint32_t)x) * 2.3283064365386963e-10f;
+    }
+};
+
+MCGB_DEV float dot3(const f3 &a, const f3 &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+/* cos_critical, xopto/mcbase/kernel/mcbase.template.c:1229-1231 */
+MCGB_DEV float cos_critical(float n1, float n2) {
+    return (n1 > n2) ? mc_sqrt(1.0f - mc_div(n2 * n2, n1 * n1)) : 0.0f;
+}
+
+/* reflectance, xopto/mcbase/kernel/mcbase.template.c:1244-1289 */
+MCGB_DEV float reflectance(float n1, float n2, float cos1, float cc) {
+    float R = 1.0f;
+    cos1 = fabsf(cos1);
+    if (n1 == n2) return 0.0f;
+    if (cos1 > cc) {
+        float n1_d_n2 = mc_div(n1, n2);
+        float sin1 = mc_sqrt(1.0f - cos1 * cos1);
+        if (cos1 >= 1.0f) sin1 = 0.0f;
+        float sin2 = fminf(1.0f, n1_d_n2 * sin1);
+        float cos2 = mc_sqrt(1.0f - sin2 * sin2);
+        float n_cos1 = n1_d_n2 * cos1;
+        float n_cos2 = n1_d_n2 * cos2;
+        float Rs = mc_div(n_cos1 - cos2, n_cos1 + cos2);
+        Rs *= Rs;
+        float Rp = mc_div(n_cos2 - cos1, n_cos2 + cos1);
+        Rp *= Rp;
+        R = 0.5f * (Rp + Rs);
+        if (cos1 <= 0.0f || sin2 == 1.0f) return 1.0f;
+    }
+    return R;
+}
+
+/* reflect, xopto/mcbase/kernel/mcbase.template.c:1361-1369 */
+MCGB_DEV f3 reflect3(const f3 &p, const f3 &n) {
+    float p_n_2 = 2.0f * dot3(p, n);
+    return f3{p.x - n.x * p_n_2, p.y - n.y * p_n_2, p.z - n.z * p_n_2};
+}
+
+/* refract, xopto/mcbase/kernel/mcbase.template.c:1424-1440 */
+MCGB_DEV f3 refract3(const f3 &p, const f3 &n, float n1, float n2) {
+    float cos1 = dot3(p, n);
+    float n1_d_n2 = mc_div(n1, n2);
+    float sin2_squared = n1_d_n2 * n1_d_n2 * (1.0f - cos1 * cos1);
+    float k = (float)fsign(cos1) * (n1_d_n2 * fabsf(cos1) - mc_sqrt(1.0f - sin2_squared));
+    return f3{n1_d_n2 * p.x - k * n.x, n1_d_n2 * p.y - k * n.y, n1_d_n2 * p.z - k * n.z};
+}
+
+/* refract_safe, xopto/mcbase/kernel/mcbase.template.c:1466-1487 */
+MCGB_DEV int refract_safe3(const f3 &p, const f3 &n, float n1, float n2, f3 *r) {
+    float cos1 = dot3(p, n);
+    float n1_d_n2 = mc_div(n1, n2);
+    float sin2_squared = n1_d_n2 * n1_d_n2 * (1.0f - cos1 * cos1);
+    if (sin2_squared > 1.0f) return 1;
+    float k = (float)fsign(cos1) * (n1_d_n2 * fabsf(cos1) - mc_sqrt(1.0f - sin2_squared));
+    r->x = n1_d_n2 * p.x - k * n.x;
+    r->y = n1_d_n2 * p.y - k * n.y;
+    r->z = n1_d_n2 * p.z - k * n.z;
+    return 0;
+}
+
+/* scatter_direction + unconditional renormalisation,
+   xopto/mcbase/kernel/mcbase.template.c:1522-1555 */
+MCGB_DEV void scatter_direction(f3 &dir, float cos_theta, float fi) {
+    float sin_fi, cos_fi;
+    float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+    mc_sincos(fi, &sin_fi, &cos_fi);
+    float stcf = sin_theta * cos_fi;
+    float stsf = sin_theta * sin_fi;
+    float px = dir.x;
+    if (fabsf(dir.z) >= 1.0f) {
+        dir.x = stcf;
+        dir.y = stsf;
+        dir.z = copysignf(cos_theta, dir.z * cos_theta);
+    } else {
+        float k = mc_sqrt(1.0f - dir.z * dir.z);
+        dir.x = mc_div(stcf * px * dir.z - stsf * dir.y, k) + px * cos_theta;
+        dir.y = mc_div(stcf * dir.y * dir.z + stsf * px, k) + dir.y * cos_theta;
+        dir.z = (-stcf) * k + dir.z * cos_theta;
+    }
+    float k = mc_rcp_length(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
+    dir.x = dir.x * k;
+    dir.y = dir.y * k;
+    dir.z = dir.z * k;
+}
+
+/* Phase-function sampling.  Returns cos(theta); the azimuth is drawn first,
+   as in the reference.
+   Hg:  xopto/mcbase/mcpf/hg.py:80-95
+   Gk:  xopto/mcbase/mcpf/gk.py:102-124
+   Lut: xopto/mcbase/mcpf/lut.py:125-155 */
+MCGB_DEV float pf_sample(int kind, const McgbPf &pf, const float *lut, Rng &rng, float *azimuth) {
+    *azimuth = 6.28318548f * rng.next();
+    if (kind == MCGB_PF_HG) {
+        float g = pf.p[0];
+        float k = mc_div(1.0f - g * g, 1.0f + g * (2.0f * rng.next() - 1.0f));
+        float cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
+        if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
+        return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+    } else if (kind == MCGB_PF_GK) {
+        float g = pf.p[0], ga = pf.p[1], inv_a = pf.p[2], a1 = pf.p[3], a2 = pf.p[4];
+        float cos_theta;
+        if (g == 0.0f) {
+            cos_theta = 1.0f - 2.0f * rng.next();
+        } else if (ga == 0.0f) {
+            cos_theta = a1 + mc_pow(mc_div(1.0f - g, 1.0f + g), 2.0f * rng.next()) * a2;
+        } else {
+            float tmp = a1 * rng.next() + a2;
+            tmp = 1.0f + g * g - mc_pow(tmp, -inv_a);
+            cos_theta = mc_div(tmp, 2.0f * g);
+        }
+        return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
+    } else {
+        uint32_t lut_size = pf.lut_size - 1u;
+        float fp_index = (mc_div(pf.p[0], rng.next() - pf.p[2]) - pf.p[1] + 1.0f) *
+                         (float)lut_size * 0.5f;
+        float fp_index_floor = floorf(fp_index);
+        float d = fp_index - fp_index_floor;
+        int index = cvt_int(fp_index_floor);
+        int i1 = index + 1 < (int)lut_size ? index + 1 : (int)lut_size;
+        return lut[pf.lut_offset + (uint32_t)index] * (1.0f - d) +
+               lut[pf.lut_offset + (uint32_t)i1] * d;
+    }
+}
+
+/* weight_to_int(w)*accept (xopto/mcml/kernel/mcml.template.h:606) */
+MCGB_DEV uint32_t weight_to_u32(float w, float accept) {
+    return (uint32_t)((w * (float)MCGB_ACCU_K + 0.5f) * accept);
+}
+
+MCGB_DEV void accu_add(uint64_t *accu, uint64_t index, uint32_t w) {
+    atomicAdd((unsigned long long *)(accu + index), (unsigned long long)w);
+}
+
+/* Radial / Total detector deposit:
+   xopto/mcml/mcdetector/radial.py:117-150, total.py:86-108 */
+MCGB_DEV void detector_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir,
+                               float weight, uint64_t *accu) {
+    if (det.kind == MCGB_DET_NONE) return;
+    f3 ddir{det.direction[0], det.direction[1], det.direction[2]};
+    float accept = (float)(det.cos_min <= fabsf(dot3(dir, ddir)));
+    uint64_t index = 0;
+    if (det.kind == MCGB_DET_RADIAL) {
+        float dx = pos.x - det.position[0];
+        float dy = pos.y - det.position[1];
+        float r = mc_sqrt(dx * dx + dy * dy);
+        if (det.log_scale) r = mc_log(fmaxf(r, 1e-12f));
+        int r_index = cvt_int((r - det.r_min) * det.inv_dr);
+        index = (uint64_t)clip_i(r_index, 0, (int)det.n - 1);
+    }
+    uint32_t w = weight_to_u32(weight, accept);
+    if (w > 0) accu_add(accu, det.offset + index, w);
+}
+
+/* Fluence deposit (xopto/mcbase/mcfluence/fluence.py:103-143) through a
+   one-entry per-thread cache: consecutive deposits into the same voxel are
+   summed in a register and flushed with one 64-bit atomic when the voxel
+   changes (integer sums, so the tally is unchanged). */
+struct FluenceCache {
+    uint64_t index;
+    uint64_t sum;
+    __device__ __forceinline__ void flush(uint64_t *accu) {
+        if (sum) atomicAdd((unsigned long long *)(accu + index), (unsigned long long)sum);
+        sum = 0;
+    }
+    __device__ __forceinline__ void add(uint64_t *accu, uint64_t i, uint32_t w) {
+        if (i != index) {
+            flush(accu);
+            index = i;
+        }
+        sum += w;
+    }
+};
+
+MCGB_DEV void fluence_deposit(const McgbFluence &fl, const f3 &pos, float weight, float mua,
+                              uint64_t *accu, FluenceCache &cache) {
+    float ix = (pos.x - fl.top_left[0]) * fl.inv_step[0];
+    float iy = (pos.y - fl.top_left[1]) * fl.inv_step[1];
+    float iz = (pos.z - fl.top_left[2]) * fl.inv_step[2];
+    if (ix >= 0.0f && iy >= 0.0f && iz >= 0.0f && ix < (float)fl.shape[0] &&
+        iy < (float)fl.shape[1] && iz < (float)fl.shape[2]) {
+        uint32_t jx = cvt_uint(ix), jy = cvt_uint(iy), jz = cvt_uint(iz);
+        uint64_t index = ((uint64_t)jz * fl.shape[1] + jy) * fl.shape[0] + jx;
+        if (fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
+        uint32_t w = (uint32_t)(weight * (float)fl.k + 0.5f);
+        cache.add(accu, fl.offset + index, w);
+    }
+}
+
+/* Event bits, xopto/mcbase/kernel/mcbase.template.h:640-660 */
+#define MCGB_EV_REFLECTION 1u
+#define MCGB_EV_REFRACTION 2u
+#define MCGB_EV_BOUNDARY_HIT 4u
+#define MCGB_EV_LAUNCH 8u
+#define MCGB_EV_ABSORPTION 16u
+#define MCGB_EV_SCATTERING 32u
+#define MCGB_EV_TERMINATED 64u
+#define MCGB_EV_ESCAPED 128u
+
+/* Trace event (xopto/mcbase/mctrace.py:541-583): 8 floats per event, the
+   last slot is overwritten when the trace is full. */
+MCGB_DEV void trace_event(const McgbTrace &tr, uint64_t photon_index, uint32_t &count,
+                          uint32_t events, const f3 &pos, const f3 &dir, float w, float opl,
+                          float *fbuf) {
+    if (tr.event_mask && !(tr.event_mask & events)) return;
+    uint32_t ev = count < tr.max_events - 1 ? count : tr.max_events - 1;
+    uint64_t p = (uint64_t)ev * MCGB_TRACE_ENTRY_LEN +
+                 photon_index * tr.max_events * MCGB_TRACE_ENTRY_LEN + tr.data_offset;
+    float4 *dst = reinterpret_cast<float4 *>(fbuf + p);
+    if ((p & 3u) == 0) {
+        dst[0] = make_float4(pos.x, pos.y, pos.z, dir.x);
+        dst[1] = make_float4(dir.y, dir.z, w, opl);
+    } else {
+        fbuf[p + 0] = pos.x; fbuf[p + 1] = pos.y; fbuf[p + 2] = pos.z;
+        fbuf[p + 3] = dir.x; fbuf[p + 4] = dir.y; fbuf[p + 5] = dir.z;
+        fbuf[p + 6] = w; fbuf[p + 7] = opl;
+    }
+    ++count;
+}
+
+/* Device wall clock (ns) for the run deadline. */
+MCGB_DEV uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}

@@ -1,0 +1,230 @@
+"""Surface detectors: Total and Radial, grouped by Detectors into the top,
+bottom and specular slots (xopto/mcml/mcdetector/base.py, total.py,
+radial.py; the mcvox package uses the same classes).
+
+Tallies come back from the device as uint64 fixed-point integers and are
+converted with the reference's rule raw += accumulator/K
+(xopto/mcml/mcdetector/base.py:269-292).
+"""
+from typing import Tuple
+import numpy as np
+
+from .. import _abi
+from .mcutil import Axis, RadialAxis
+
+
+class Detector:
+    kind = _abi.DET_NONE
+
+    def __init__(self, raw_data: np.ndarray, nphotons: int):
+        self._raw_data = raw_data
+        self._nphotons = int(nphotons)
+
+    raw = property(lambda self: self._raw_data, None, None, 'Raw accumulator data.')
+    nphotons = property(lambda self: self._nphotons)
+    shape = property(lambda self: self._raw_data.shape)
+    total = property(lambda self: self._raw_data.sum())
+
+    def set_raw_data(self, data, nphotons):
+        self._raw_data[:] = np.asarray(data, dtype=self._raw_data.dtype)
+        self._nphotons = int(nphotons)
+
+    def update_data(self, mc, accumulators, nphotons: int, **kwargs):
+        new_data = np.reshape(accumulators[0], self.shape)
+        self._raw_data += new_data * (1.0 / _abi.ACCU_K)
+        self._nphotons += int(nphotons)
+
+    def pack(self, mc, target: _abi.McgbDetector):
+        target.kind = _abi.DET_NONE
+        return target
+
+    def copy(self):
+        raise NotImplementedError
+
+
+class DetectorDefault(Detector):
+    """Empty detector slot (xopto/mcml/mcdetector/base.py:140-200)."""
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(np.zeros((0,)), 0)
+
+    def copy(self):
+        return DetectorDefault()
+
+    def __str__(self):
+        return 'DetectorDefault()'
+
+
+class Total(Detector):
+    """Total reflectance/transmittance (xopto/mcml/mcdetector/total.py:32-239)."""
+    kind = _abi.DET_TOTAL
+
+    def __init__(self, cosmin=0.0, direction=(0.0, 0.0, 1.0)):
+        if isinstance(cosmin, Total):
+            other = cosmin
+            super().__init__(np.copy(other.raw), other.nphotons)
+            cosmin, direction = other.cosmin, other.direction
+        else:
+            super().__init__(np.zeros((1,)), 0)
+        self._cosmin = 0.0
+        self._direction = np.zeros((3,))
+        self.cosmin = cosmin
+        self.direction = direction
+
+    def _set_cosmin(self, v):
+        self._cosmin = min(max(float(v), 0.0), 1.0)
+
+    cosmin = property(lambda self: self._cosmin, _set_cosmin)
+
+    def _set_direction(self, d):
+        self._direction[:] = d
+        n = np.linalg.norm(self._direction)
+        if n == 0.0:
+            raise ValueError('Direction vector norm/length must not be 0!')
+        self._direction *= 1.0 / n
+
+    direction = property(lambda self: self._direction, _set_direction)
+
+    def _get_normalized(self):
+        return self.raw * (1.0 / max(self.nphotons, 1.0))
+
+    normalized = property(_get_normalized)
+    reflectance = property(_get_normalized)
+    transmittance = property(_get_normalized)
+
+    def pack(self, mc, target):
+        target.kind = _abi.DET_TOTAL
+        target.offset = mc.cl_allocate_rw_accumulator_buffer(self, self.shape)
+        target.cos_min = self._cosmin
+        target.direction[:] = [float(v) for v in self._direction]
+        return target
+
+    def copy(self):
+        return Total(self)
+
+    def todict(self):
+        return {'type': 'Total', 'cosmin': self._cosmin, 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'Total(cosmin={}, direction=({}, {}, {}))'.format(self._cosmin, *self._direction)
+
+
+class Radial(Detector):
+    """Radial (concentric ring) detector; radii beyond the axis are clipped
+    into the last bin (xopto/mcml/mcdetector/radial.py:32-337)."""
+    kind = _abi.DET_RADIAL
+
+    def __init__(self, raxis, position=(0.0, 0.0), cosmin=0.0, direction=(0.0, 0.0, 1.0)):
+        if isinstance(raxis, Radial):
+            other = raxis
+            super().__init__(np.copy(other.raw), other.nphotons)
+            position, cosmin, direction = other.position, other.cosmin, other.direction
+            raxis = type(other.raxis)(other.raxis)
+        else:
+            super().__init__(np.zeros((raxis.n,)), 0)
+        self._r_axis = raxis
+        self._position = np.zeros((2,))
+        self._direction = np.zeros((3,))
+        self._cosmin = 0.0
+        self.position = position
+        self.cosmin = cosmin
+        self.direction = direction
+        e = self._r_axis.edges
+        self._inv_accumulators_area = 1.0 / (np.pi * (e[1:] ** 2 - e[:-1] ** 2))
+
+    raxis = property(lambda self: self._r_axis)
+
+    def _set_position(self, v):
+        self._position[:] = v
+
+    position = property(lambda self: self._position, _set_position)
+
+    def _set_cosmin(self, v):
+        self._cosmin = min(max(float(v), 0.0), 1.0)
+
+    cosmin = property(lambda self: self._cosmin, _set_cosmin)
+
+    def _set_direction(self, d):
+        self._direction[:] = d
+        n = np.linalg.norm(self._direction)
+        if n == 0.0:
+            raise ValueError('Direction vector norm/length must not be 0!')
+        self._direction *= 1.0 / n
+
+    direction = property(lambda self: self._direction, _set_direction)
+    r = property(lambda self: self._r_axis.centers)
+    edges = property(lambda self: self._r_axis.edges)
+    n = property(lambda self: self._r_axis.n)
+    logscale = property(lambda self: self._r_axis.logscale)
+
+    def _get_normalized(self):
+        return self.raw * self._inv_accumulators_area * (1.0 / max(self.nphotons, 1))
+
+    normalized = property(_get_normalized)
+    reflectance = property(_get_normalized)
+    transmittance = property(_get_normalized)
+
+    def pack(self, mc, target):
+        target.kind = _abi.DET_RADIAL
+        target.offset = mc.cl_allocate_rw_accumulator_buffer(self, self.shape)
+        target.position[:] = [float(v) for v in self._position]
+        target.r_min = self._r_axis.scaled_start
+        target.inv_dr = 1.0 / self._r_axis.step if self._r_axis.step != 0.0 else 0.0
+        target.log_scale = int(self._r_axis.logscale)
+        target.n = self._r_axis.n
+        target.cos_min = self._cosmin
+        target.direction[:] = [float(v) for v in self._direction]
+        return target
+
+    def copy(self):
+        return Radial(self)
+
+    def todict(self):
+        return {'type': 'Radial', 'r_axis': self._r_axis.todict(),
+                'position': self._position.tolist(), 'cosmin': self._cosmin,
+                'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'Radial(raxis={}, position=({}, {}), cosmin={})'.format(
+            self._r_axis, *self._position, self._cosmin)
+
+
+class Detectors:
+    """Top, bottom and specular detectors
+    (xopto/mcml/mcdetector/base.py:295-568)."""
+
+    def __init__(self, top=None, bottom=None, specular=None):
+        if isinstance(top, Detectors):
+            other = top
+            top, bottom, specular = other.top.copy(), other.bottom.copy(), other.specular.copy()
+        self._top = top if top is not None else DetectorDefault()
+        self._bottom = bottom if bottom is not None else DetectorDefault()
+        self._specular = specular if specular is not None else DetectorDefault()
+
+    top = property(lambda self: self._top)
+    bottom = property(lambda self: self._bottom)
+    specular = property(lambda self: self._specular)
+
+    def types(self):
+        return type(self._top), type(self._bottom), type(self._specular)
+
+    def __iter__(self):
+        return iter([d for d in (self._top, self._bottom, self._specular)
+                     if not isinstance(d, DetectorDefault)])
+
+    def pack(self, mc, cfg):
+        self._top.pack(mc, cfg.top)
+        self._bottom.pack(mc, cfg.bottom)
+        self._specular.pack(mc, cfg.specular)
+
+    def slots(self):
+        return (('top', self._top), ('bottom', self._bottom), ('specular', self._specular))
+
+    def __str__(self):
+        return 'Detectors(top={}, bottom={}, specular={})'.format(
+            self._top, self._bottom, self._specular)
+
+    __repr__ = __str__
+
+
+__all__ = ['Axis', 'RadialAxis', 'Detector', 'DetectorDefault', 'Total', 'Radial', 'Detectors']

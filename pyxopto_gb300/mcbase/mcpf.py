@@ -1,0 +1,156 @@
+"""Scattering phase functions: Henyey-Greenstein, Gegenbauer kernel and
+lookup table, with the reference's names and parameters
+(xopto/mcbase/mcpf/hg.py, gk.py, lut.py).
+
+Each object packs itself into the ``McgbPf`` struct that the GB300 kernels
+read from their shared-memory layer/material table.
+"""
+import numpy as np
+
+from .. import _abi
+
+
+class PfBase:
+    kind = None
+
+    def pack(self, mc, target: _abi.McgbPf):
+        raise NotImplementedError
+
+    def todict(self) -> dict:
+        raise NotImplementedError
+
+    @classmethod
+    def fromdict(cls, data: dict):
+        data = dict(data)
+        data.pop('type', None)
+        return cls(**data)
+
+    def __repr__(self):
+        return str(self)
+
+
+class Hg(PfBase):
+    """Henyey-Greenstein phase function (xopto/mcbase/mcpf/hg.py:25-167)."""
+    kind = _abi.PF_HG
+
+    def __init__(self, g: float):
+        self._g = 0.0
+        self.g = g
+
+    def _get_g(self):
+        return self._g
+
+    def _set_g(self, g):
+        self._g = min(max(float(g), -1.0), 1.0)
+
+    g = property(_get_g, _set_g, None, 'Anisotropy factor.')
+
+    def pack(self, mc, target):
+        target.p[0] = self._g
+        return target
+
+    def todict(self):
+        return {'g': self._g, 'type': 'Hg'}
+
+    def __str__(self):
+        return 'Hg(g={})'.format(self._g)
+
+
+class Gk(PfBase):
+    """Gegenbauer kernel phase function (xopto/mcbase/mcpf/gk.py:30-243).
+    The sampling constants inv_a, a1, a2 are precomputed on the host as in
+    gk.py:153-178."""
+    kind = _abi.PF_GK
+
+    def __init__(self, g: float, a: float):
+        self._g = min(max(float(g), -1.0), 1.0)
+        self._a = max(float(a), -0.5)
+        self._recalculate()
+
+    def _recalculate(self):
+        g, a = self._g, self._a
+        if g == 0:
+            inv_a = a1 = a2 = 0.0
+        elif a == 0:
+            a1 = (1 + g ** 2) / (2 * g)
+            a2 = (1 + 2 * g + g ** 2) / (2 * g)
+            inv_a = 0.0
+        else:
+            temp = a * g * (1.0 - g * g) ** (2.0 * a)
+            temp = temp / (np.pi * ((1.0 + g) ** (2.0 * a) - (1.0 - g) ** (2.0 * a)))
+            a1 = 2.0 * a * g / (2.0 * np.pi * temp)
+            a2 = (1 + g) ** (-2.0 * a)
+            inv_a = 1.0 / a
+        self._precalculated = [inv_a, a1, a2]
+
+    def _get_g(self):
+        return self._g
+
+    def _set_g(self, g):
+        self._g = min(max(float(g), -1.0), 1.0)
+        self._recalculate()
+
+    g = property(_get_g, _set_g, None, 'Anisotropy factor when a=0.5.')
+
+    def _get_a(self):
+        return self._a
+
+    def _set_a(self, a):
+        self._a = max(float(a), -0.5)
+        self._recalculate()
+
+    a = property(_get_a, _set_a, None, 'Parameter alpha.')
+
+    def pack(self, mc, target):
+        target.p[0] = self._g
+        target.p[1] = self._a
+        target.p[2] = self._precalculated[0]
+        target.p[3] = self._precalculated[1]
+        target.p[4] = self._precalculated[2]
+        return target
+
+    def todict(self):
+        return {'g': self._g, 'a': self._a, 'type': 'Gk'}
+
+    def __str__(self):
+        return 'Gk(g={}, a={})'.format(self._g, self._a)
+
+
+class Lut(PfBase):
+    """Lookup-table phase function with the nonlinear index transform
+    index = (a/(xi - c) - b + 1)*(N - 1)/2 (xopto/mcbase/mcpf/lut.py:31-260).
+    The table is appended to the simulator's floating-point LUT buffer."""
+    kind = _abi.PF_LUT
+
+    def __init__(self, params, lut):
+        self._params = np.zeros((3,))
+        self._params[:] = params
+        self._lut = np.asarray(lut, dtype=np.float64).ravel()
+        if self._lut.size < 2:
+            raise ValueError('A lookup table needs at least two entries!')
+        self._offset = 0
+
+    params = property(lambda self: self._params)
+    lut = property(lambda self: self._lut)
+    size = property(lambda self: self._lut.size)
+    offset = property(lambda self: self._offset)
+
+    def pack(self, mc, target):
+        self._offset = mc.append_r_lut(self._lut)
+        target.p[0] = self._params[0]
+        target.p[1] = self._params[1]
+        target.p[2] = self._params[2]
+        target.lut_offset = self._offset
+        target.lut_size = self._lut.size
+        return target
+
+    def todict(self):
+        return {'params': list(self._params), 'lut': self._lut.tolist(), 'type': 'Lut'}
+
+    def __str__(self):
+        return 'Lut(params=({}, {}, {}), size={})'.format(*self._params, self._lut.size)
+
+
+def pf_fromdict(data: dict) -> PfBase:
+    kinds = {'Hg': Hg, 'Gk': Gk, 'Lut': Lut}
+    return kinds[data['type']].fromdict(data)

@@ -1,0 +1,217 @@
+"""Parity scenarios shared by the golden-vector generator and the tests.
+
+Each scenario is a plain dict (SI units).  ``build_mc`` turns it into a
+pyxopto_gb300 simulator; ``make_golden.py`` turns the same dict into the
+reference's own simulator objects.  Sizes are small enough for the CPU oracle
+to finish in seconds.
+"""
+import math
+
+import numpy as np
+
+INF = float('inf')
+
+
+def _air(pf):
+    return dict(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=pf)
+
+
+def lut_table(n=256, g=0.8):
+    """A lookup table (params, cos theta values) for the Lut phase function:
+    HG quantiles at the uniform numbers that the index transform
+    (a/(u - c) - b + 1)*(N - 1)/2 maps onto each entry, with a=-4, b=-3, c=-1."""
+    a, b, c = -4.0, -3.0, -1.0
+    i = np.arange(n)
+    u = a / (2.0 * i / (n - 1) + b - 1.0) + c
+    u = np.clip(u, 0.0, 1.0)
+    k = (1 - g * g) / (1 + g * (2 * u - 1))
+    cos_t = np.clip((1 + g * g - k * k) / (2 * g), -1.0, 1.0)
+    return [a, b, c], cos_t
+
+
+SCENARIOS = {
+    # BASELINE config 1 (10 mm slab, HG 0.8, Line, radial 0-5 mm / 50 bins)
+    'c1_line_hg_radial': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]), dict(d=0.010, n=1.33, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 5e-3, 50]), specular=dict(type='Total')),
+        nphotons=6000, streams=48, rnginit=1),
+    # BASELINE config 2 stack (Gk, three layers) with a Cartesian fluence grid
+    'c2_gk_fluence': dict(
+        medium='mcml',
+        layers=[_air(['Gk', 0.0, 0.5]),
+                dict(d=1e-4, n=1.45, mua=500.0, mus=4e4, pf=['Gk', 0.9, 0.5]),
+                dict(d=1.5e-3, n=1.40, mua=50.0, mus=2.5e4, pf=['Gk', 0.85, 0.5]),
+                dict(d=8e-3, n=1.40, mua=20.0, mus=2e4, pf=['Gk', 0.8, 0.5]),
+                _air(['Gk', 0.0, 0.5])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-5e-3, 5e-3, 20], y=[-5e-3, 5e-3, 20], z=[0.0, 10e-3, 20],
+                     mode='deposition'),
+        nphotons=1500, streams=32, rnginit=7),
+    'gk_alpha_1p2_rejection': dict(
+        medium='mcml',
+        layers=[_air(['Gk', 0.0, 1.2]), dict(d=2e-3, n=1.4, mua=300.0, mus=6e3, pf=['Gk', 0.7, 1.2]),
+                dict(d=INF, n=1.0, mua=0.0, mus=0.0, pf=['Gk', 0.0, 1.2])],
+        source=dict(type='Line'), method=1,
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), bottom=dict(type='Total')),
+        nphotons=4000, streams=40, rnginit=11),
+    'hg_mbl_gaussian_fluence': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]), dict(d=3e-3, n=1.37, mua=80.0, mus=8e3, pf=['Hg', 0.9]),
+                dict(d=4e-3, n=1.45, mua=20.0, mus=1e4, pf=['Hg', 0.75]), _air(['Hg', 0.0])],
+        source=dict(type='GaussianBeam', sigma=2e-4, clip=5.0), method=2,
+        detectors=dict(top=dict(type='Radial', axis=[1e-5, 5e-3, 25], logscale=True, cosmin=0.3),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-2e-3, 2e-3, 8], y=[-2e-3, 2e-3, 8], z=[0.0, 7e-3, 14], mode='deposition'),
+        nphotons=2000, streams=32, rnginit=3),
+    'lut_rmax_oblique': dict(
+        medium='mcml',
+        layers=[dict(d=0.0, n=1.33, mua=0.0, mus=0.0, pf=['Lut']),
+                dict(d=5e-3, n=1.5, mua=50.0, mus=5e3, pf=['Lut']),
+                dict(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=['Lut'])],
+        source=dict(type='Line', position=[-1e-3, 0.0, -1e-3], direction=[0.3, 0.1, 1.0]),
+        rmax=4e-3,
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 4e-3, 40], position=[0.5e-3, 0.0]),
+                       bottom=dict(type='Radial', axis=[0.0, 4e-3, 40]),
+                       specular=dict(type='Total', cosmin=0.5)),
+        nphotons=3000, streams=24, rnginit=5),
+    # BASELINE config 4 sample: semi-infinite, one draw of the batched ranges
+    'semiinf_hg': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]), dict(d=INF, n=1.42, mua=30.0, mus=8000.0, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30])),
+        nphotons=1500, streams=16, rnginit=2, no_lottery=False),
+    # BASELINE config 3 shape (two layers + absorbing cylinder) on a 24^3 grid
+    'c3_vox_cylinder': dict(
+        medium='mcvox',
+        grid=dict(x=[-1.2e-3, 1.2e-3, 24], y=[-1.2e-3, 1.2e-3, 24], z=[0.0, 2.4e-3, 24]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.40, mua=20.0, mus=1.5e4, pf=['Hg', 0.9]),
+                   dict(n=1.40, mua=150.0, mus=2e4, pf=['Hg', 0.9]),
+                   dict(n=1.33, mua=2000.0, mus=1.5e4, pf=['Hg', 0.9])],
+        layout=dict(kind='skin_vessel', epidermis=1e-4, vessel_depth=1.0e-3, vessel_radius=4e-4),
+        source=dict(type='GaussianBeam', sigma=3e-4, clip=5.0),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1.2e-3, 12]), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-1.2e-3, 1.2e-3, 24], y=[-1.2e-3, 1.2e-3, 24], z=[0.0, 2.4e-3, 24],
+                     mode='deposition'),
+        nphotons=1500, streams=32, rnginit=9),
+    'vox_line_gk_oblique': dict(
+        medium='mcvox',
+        grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Gk', 0.0, 0.5]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Gk', 0.85, 0.5]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Gk', 0.6, 0.5])],
+        layout=dict(kind='checker'),
+        source=dict(type='Line', position=[0.0, 0.0, -1e-3], direction=[0.2, -0.1, 1.0]),
+        method=1,
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Radial', axis=[0.0, 1e-3, 10]),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='fluence'),
+        nphotons=2000, streams=20, rnginit=13),
+}
+
+
+def voxel_layout(grid, layout):
+    """(nz, ny, nx) uint8 material indices of a scenario layout."""
+    nx, ny, nz = grid['x'][2], grid['y'][2], grid['z'][2]
+    xe = np.linspace(*grid['x'][:2], nx + 1)
+    ye = np.linspace(*grid['y'][:2], ny + 1)
+    ze = np.linspace(*grid['z'][:2], nz + 1)
+    xc, yc, zc = 0.5 * (xe[1:] + xe[:-1]), 0.5 * (ye[1:] + ye[:-1]), 0.5 * (ze[1:] + ze[:-1])
+    Z, Y, X = np.meshgrid(zc, yc, xc, indexing='ij')
+    m = np.ones((nz, ny, nx), dtype=np.uint8)
+    if layout['kind'] == 'skin_vessel':
+        m[Z < layout['epidermis']] = 2
+        r2 = X ** 2 + (Z - layout['vessel_depth']) ** 2
+        m[r2 <= layout['vessel_radius'] ** 2] = 3
+    elif layout['kind'] == 'checker':
+        ix = np.arange(nx)[None, None, :]
+        iy = np.arange(ny)[None, :, None]
+        iz = np.arange(nz)[:, None, None]
+        m = (1 + ((ix // 2 + iy // 3 + iz // 2) % 2)).astype(np.uint8)
+        m = np.broadcast_to(m, (nz, ny, nx)).copy()
+    return m
+
+
+def _pf(pkg, spec):
+    if spec[0] == 'Hg':
+        return pkg.mcpf.Hg(spec[1])
+    if spec[0] == 'Gk':
+        return pkg.mcpf.Gk(spec[1], spec[2])
+    params, table = lut_table()
+    return pkg.mcpf.Lut(params, table)
+
+
+def _axis(pkg, d):
+    lo, hi, n = d['axis']
+    return pkg.mcdetector.Axis(lo, hi, n, logscale=d.get('logscale', False))
+
+
+def _detectors(pkg, spec):
+    if not spec:
+        return None
+    slots = {}
+    for slot in ('top', 'bottom', 'specular'):
+        d = spec.get(slot)
+        if d is None:
+            continue
+        if d['type'] == 'Total':
+            slots[slot] = pkg.mcdetector.Total(cosmin=d.get('cosmin', 0.0))
+        else:
+            slots[slot] = pkg.mcdetector.Radial(_axis(pkg, d), position=d.get('position', (0.0, 0.0)),
+                                                cosmin=d.get('cosmin', 0.0))
+    return pkg.mcdetector.Detectors(**slots)
+
+
+def _fluence(pkg, spec):
+    if not spec:
+        return None
+    A = pkg.mcfluence.Axis
+    return pkg.mcfluence.Fluence(A(*spec['x']), A(*spec['y']), A(*spec['z']), mode=spec['mode'])
+
+
+def _source(src_mod, spec):
+    kw = {k: v for k, v in spec.items() if k != 'type'}
+    return getattr(src_mod, spec['type'])(**kw)
+
+
+def options(pkg, scenario, fast=False):
+    opts = [pkg.mcoptions.McMethod(scenario.get('method', 0))]
+    if fast:
+        opts.append(pkg.mcoptions.McUseNativeMath(True))
+    return opts
+
+
+def build_mc(name_or_spec, fast=False, package='pyxopto_gb300'):
+    """A pyxopto_gb300 simulator for a scenario."""
+    import importlib
+    s = SCENARIOS[name_or_spec] if isinstance(name_or_spec, str) else name_or_spec
+    if s['medium'] == 'mcml':
+        mc = importlib.import_module(package + '.mcml.mc')
+        layers = mc.mclayer.Layers([
+            mc.mclayer.Layer(d=l['d'], n=l['n'], mua=l['mua'], mus=l['mus'], pf=_pf(mc, l['pf']))
+            for l in s['layers']])
+        obj = mc.Mc(layers, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
+                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast),
+                    rnginit=s['rnginit'])
+    else:
+        mc = importlib.import_module(package + '.mcvox.mc')
+        g = s['grid']
+        A = mc.mcdetector.Axis
+        vox = mc.mcgeometry.Voxels(A(*g['x']), A(*g['y']), A(*g['z']))
+        vox.material = voxel_layout(g, s['layout'])
+        mats = [mc.mcmaterial.Material(n=m['n'], mua=m['mua'], mus=m['mus'], pf=_pf(mc, m['pf']))
+                for m in s['materials']]
+        obj = mc.Mc(vox, mats, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
+                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast),
+                    rnginit=s['rnginit'])
+    if 'rmax' in s:
+        obj.rmax = s['rmax']
+    return obj
