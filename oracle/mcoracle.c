@@ -206,7 +206,9 @@ static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
         float fp_index = (la / (rnd(x, a) - lc) - lb + 1.0f) * (float)lut_size * 0.5f;
         float fp_index_floor = floorf(fp_index);
         float d = fp_index - fp_index_floor;
-        int32_t index = cvt_int(fp_index_floor);
+        /* clamped to the table (the GPU kernel does the same; in-range
+           indices are unchanged) */
+        int32_t index = clip_i(cvt_int(fp_index_floor), 0, (int32_t)lut_size);
         int32_t i1 = index + 1 < (int32_t)lut_size ? index + 1 : (int32_t)lut_size;
         return lut[offset + (uint32_t)index] * (1.0f - d) + lut[offset + (uint32_t)i1] * d;
     }

@@ -87,7 +87,7 @@ def _install_stubs():
 def reference_mc(name):
     """The reference simulator object for a scenario."""
     _install_stubs()
-    s = scenarios.SCENARIOS[name]
+    s = scenarios.ALL[name]
     if s['medium'] == 'mcml':
         from xopto.mcml import mc
         layers = mc.mclayer.Layers([
@@ -178,7 +178,7 @@ def _blob(obj, min_size=8):
 def render(name, nphotons=None):
     """Renders, saves and compiles the reference build of one scenario.
     Returns the path of the compiled library."""
-    s = scenarios.SCENARIOS[name]
+    s = scenarios.ALL[name]
     m = reference_mc(name)
     nphotons = int(nphotons or s['nphotons'])
     m._pack(nphotons)

@@ -185,7 +185,9 @@ MCGB_DEV float pf_sample(int kind, const McgbPf &pf, const float *lut, Rng &rng,
                          (float)lut_size * 0.5f;
         float fp_index_floor = floorf(fp_index);
         float d = fp_index - fp_index_floor;
-        int index = cvt_int(fp_index_floor);
+        /* clamped to the table: parameters that map a uniform number
+           outside [0, N-1] would read past the table in the reference */
+        int index = clip_i(cvt_int(fp_index_floor), 0, (int)lut_size);
         int i1 = index + 1 < (int)lut_size ? index + 1 : (int)lut_size;
         return lut[pf.lut_offset + (uint32_t)index] * (1.0f - d) +
                lut[pf.lut_offset + (uint32_t)i1] * d;

@@ -112,12 +112,16 @@ struct PrimeTable {
                     }
                 }
             }
-            for (uint64_t v = hi; v >= lo && a.size() < n; --v) {
+            /* scan the window downwards; a request that is satisfied in the
+               middle of the window resumes from the next candidate */
+            uint64_t v = hi;
+            for (; v >= lo; --v) {
+                if (a.size() >= n) break;
                 if (bad[v - lo]) continue;
                 uint64_t p = (v << 32) - 1;
                 if (is_prime_u64(p) && is_prime_u64((p - 1) >> 1)) a.push_back((uint32_t)v);
             }
-            next = lo - 1;
+            next = v;   /* == lo - 1 after a full window */
         }
         return true;
     }

@@ -1,0 +1,100 @@
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+Run where the PyXOpto sources are importable (default /root/reference,
+override with XOPTO_REFERENCE):
+
+    python tests/golden/make_golden.py
+
+Writes
+  golden_<scenario>.npz  for every scenario in scenarios.py: the stream seeds
+                         produced by the reference's clrng.Random().seeds,
+                         and the tallies plus final RNG states of the
+                         reference's own McKernel, rendered by its plugins
+                         and compiled for the CPU (oracle/render_ref.py),
+                         run with one McKernel call per stream.
+  rng_tables.npz         samples of the reference's safe-prime multiplier
+                         table and of its seed expansion for several
+                         initializers.
+  cuda_mcml_radial.npz   the CUDA-MCML radial reflectance profile that the
+                         reference's validation suite compares against
+                         (xopto/mcml/test/reference/cuda_singlelayer_linesource_radial.pkl,
+                         test xopto/mcml/test/validate.py:219-345).
+"""
+import os
+import pickle
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [HERE, os.path.join(REPO, 'oracle')]
+
+import scenarios  # noqa: E402
+import render_ref  # noqa: E402
+
+
+def reference_seeds(n, xinit):
+    render_ref._install_stubs()
+    from xopto.cl import clrng
+    return clrng.Random().seeds(n, xinit=xinit)
+
+
+def make_scenario(name):
+    s = scenarios.SCENARIOS[name]
+    render_ref.render(name)
+    x, a = reference_seeds(s['streams'], s['rnginit'])
+    out = render_ref.run_ref(name, s['nphotons'], s['streams'], (x, a))
+    data = {'seeds_x': x, 'seeds_a': a, 'rng_x_final': out['rng_x'],
+            'nphotons': np.array([s['nphotons']]), 'streams': np.array([s['streams']])}
+    for k, v in out.items():
+        if k not in ('accu', 'rng_x'):
+            data['tally_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'golden_{}.npz'.format(name)), **data)
+    print(name, {k: int(v.sum()) for k, v in data.items() if k.startswith('tally_')})
+
+
+def make_rng_tables():
+    render_ref._install_stubs()
+    from xopto.cl import clrng
+    r = clrng.Random()
+    a_table = np.asarray(r._primes[:, 0], dtype=np.uint64)
+    idx = np.unique(np.concatenate([np.arange(2000), np.arange(2000, a_table.size, 997),
+                                    np.arange(a_table.size - 20, a_table.size)]))
+    data = {'primes_index': idx, 'primes_a': a_table[idx], 'primes_count': np.array([a_table.size])}
+    for xinit in (1, 12345678901, 0x00000000FFFFFFFE):
+        x, a = r.seeds(3000, xinit=xinit)
+        data['seeds_x_{}'.format(xinit)] = x
+        data['seeds_a_{}'.format(xinit)] = a
+    np.savez_compressed(os.path.join(HERE, 'rng_tables.npz'), **data)
+    print('rng_tables', idx.size)
+
+
+def make_cuda_mcml():
+    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference',
+                        'cuda_singlelayer_linesource_radial.pkl')
+    with open(path, 'rb') as f:
+        d = pickle.load(f)
+    layers = d['layers']
+    np.savez_compressed(
+        os.path.join(HERE, 'cuda_mcml_radial.npz'),
+        reflectance=np.asarray(d['reflectance'], dtype=np.float64),
+        n=np.array([l['basic']['n'] for l in layers]),
+        d=np.array([l['basic']['d'] for l in layers]),
+        mua=np.array([l['basic']['mua'] for l in layers]),
+        mus=np.array([l['basic']['mus'] for l in layers]),
+        g=np.array([l['pf']['pfparams'][0] for l in layers]),
+        axis=np.array([d['detector']['axis']['start'], d['detector']['axis']['stop'],
+                       d['detector']['axis']['n']]),
+        cosmin=np.array([d['detector']['cosmin']]),
+        rmax=np.array([d['mc']['rmax']]))
+    print('cuda_mcml_radial', len(d['reflectance']))
+
+
+if __name__ == '__main__':
+    names = sys.argv[1:] or list(scenarios.SCENARIOS)
+    for n in names:
+        make_scenario(n)
+    if not sys.argv[1:]:
+        make_rng_tables()
+        make_cuda_mcml()

@@ -117,6 +117,35 @@ SCENARIOS = {
         nphotons=2000, streams=20, rnginit=13),
 }
 
+# Bench workloads (not golden-tested at these sizes): the layered
+# configuration of the headline metric, and config 1 at full size.
+BENCH = {
+    # 3-layer skin-like stack, Gegenbauer phase function (alpha 0.5), Line
+    # source, Cartesian fluence 100x100x100 over 10x10x10 mm, 1e8 packets
+    'c2_skin_gk_fluence': dict(
+        medium='mcml',
+        layers=[_air(['Gk', 0.0, 0.5]),
+                dict(d=1e-4, n=1.45, mua=500.0, mus=4e4, pf=['Gk', 0.9, 0.5]),
+                dict(d=1.5e-3, n=1.40, mua=50.0, mus=2.5e4, pf=['Gk', 0.85, 0.5]),
+                dict(d=8e-3, n=1.40, mua=20.0, mus=2e4, pf=['Gk', 0.8, 0.5]),
+                _air(['Gk', 0.0, 0.5])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-5e-3, 5e-3, 100], y=[-5e-3, 5e-3, 100], z=[0.0, 10e-3, 100],
+                     mode='deposition'),
+        nphotons=100_000_000, streams=0, rnginit=1),
+    # 10 mm slab, HG 0.8, radial 0-5 mm / 50 bins, 1e6 packets
+    'c1_slab_hg_radial': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]), dict(d=0.010, n=1.33, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 5e-3, 50]), specular=dict(type='Total')),
+        nphotons=1_000_000, streams=0, rnginit=1),
+}
+ALL = dict(SCENARIOS, **BENCH)
+
 
 def voxel_layout(grid, layout):
     """(nz, ny, nx) uint8 material indices of a scenario layout."""
@@ -192,7 +221,7 @@ def options(pkg, scenario, fast=False):
 def build_mc(name_or_spec, fast=False, package='pyxopto_gb300'):
     """A pyxopto_gb300 simulator for a scenario."""
     import importlib
-    s = SCENARIOS[name_or_spec] if isinstance(name_or_spec, str) else name_or_spec
+    s = ALL[name_or_spec] if isinstance(name_or_spec, str) else name_or_spec
     if s['medium'] == 'mcml':
         mc = importlib.import_module(package + '.mcml.mc')
         layers = mc.mclayer.Layers([

@@ -1,0 +1,164 @@
+"""GPU parity: the CUDA kernels against the CPU oracle, through the C ABI.
+
+EXACT math mode must reproduce the oracle's PORTABLE-mode tallies and final
+RNG states bit-for-bit (integer tallies, identical IEEE operations).  FAST
+math mode (special-function units) is checked statistically: per-bin
+differences within the Monte Carlo error (|z| < 4.5 on every populated bin,
+chi-square of z consistent) and total reflectance within 0.5 % relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import scenarios
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+K = 8388607.0
+
+
+def gpu_run(mc, nphotons, streams, torch):
+    trace, fluence, dets = mc.run(nphotons, maxthreads=streams)
+    accu = mc._dev['accu'].cpu().numpy().view(np.uint64).copy()
+    return accu, mc.rng_states(), mc.run_report
+
+
+@pytest.mark.parametrize('name', sorted(scenarios.SCENARIOS))
+def test_exact_mode_bit_identical_to_oracle(cuda, lib, oracle, name):
+    s = scenarios.SCENARIOS[name]
+    n, t = s['nphotons'], s['streams']
+    mc = scenarios.build_mc(name)
+    ref = oracle.run(mc, n, t, oracle.PORTABLE)
+    accu, rng_x, report = gpu_run(mc, n, t, cuda)
+    got = oracle.tallies(mc, accu)
+    assert set(got) == set(k for k in ref if k in got)
+    for k in got:
+        assert np.array_equal(got[k], ref[k]), (k, int(got[k].sum()), int(ref[k].sum()))
+    assert np.array_equal(rng_x, ref['rng_x'])
+    assert report['steps'] == ref['steps']
+    assert report['threads'] == min(t, n)
+
+
+def test_exact_mode_many_streams_bit_identical(cuda, lib, oracle):
+    """Full-occupancy launch (many blocks) on config 2's stack."""
+    mc = scenarios.build_mc('c2_gk_fluence')
+    n, t = 20000, 4096
+    ref = oracle.run(mc, n, t, oracle.PORTABLE, nthreads=8)
+    accu, rng_x, _ = gpu_run(mc, n, t, cuda)
+    assert np.array_equal(accu[:ref['accu'].size], ref['accu'])
+    assert np.array_equal(rng_x, ref['rng_x'])
+
+
+def test_runs_continue_streams(cuda, lib, oracle):
+    """Two runs on the same simulator continue the RNG streams (the seed
+    state stays on the device), like the reference's persistent
+    rng_seeds_x buffer; the oracle chained on the returned states agrees."""
+    mc = scenarios.build_mc('semiinf_hg')
+    n, t = 600, 16
+    a1, x1, _ = gpu_run(mc, n, t, cuda)
+    a2, x2, _ = gpu_run(mc, n, t, cuda)
+    seeds = mc.host_seeds(t)
+    r1 = oracle.run(mc, n, t, oracle.PORTABLE, seeds=seeds)
+    r2 = oracle.run(mc, n, t, oracle.PORTABLE, seeds=(r1['rng_x'], seeds[1]))
+    assert np.array_equal(a1[:r1['accu'].size], r1['accu'])
+    assert np.array_equal(a2[:r2['accu'].size], r2['accu'])
+
+
+def test_fast_mode_deterministic(cuda, lib):
+    a = scenarios.build_mc('c3_vox_cylinder', fast=True)
+    b = scenarios.build_mc('c3_vox_cylinder', fast=True)
+    ra, _, _ = gpu_run(a, 20000, 2048, cuda)
+    rb, _, _ = gpu_run(b, 20000, 2048, cuda)
+    assert np.array_equal(ra, rb)
+
+
+def _batched(mc, nphotons, streams, batches):
+    """Per-batch normalized tallies (batches continue the RNG streams)."""
+    rows = []
+    for _ in range(batches):
+        _, _, dets = mc.run(nphotons, maxthreads=streams)
+        rows.append(np.asarray(dets.top.raw, dtype=np.float64) / nphotons)
+    return np.array(rows)
+
+
+def _z(a, b):
+    ma, mb = a.mean(0), b.mean(0)
+    se = np.sqrt(a.var(0, ddof=1) / len(a) + b.var(0, ddof=1) / len(b))
+    ok = se > 0
+    return (ma[ok] - mb[ok]) / se[ok]
+
+
+@pytest.mark.parametrize('name', ['c1_line_hg_radial', 'gk_alpha_1p2_rejection', 'c3_vox_cylinder'])
+def test_fast_mode_statistically_equal_to_exact(cuda, lib, name):
+    fast = scenarios.build_mc(name, fast=True)
+    exact = scenarios.build_mc(name)
+    exact._rnginit = 424242
+    a = _batched(fast, 200000, 65536, 10)
+    b = _batched(exact, 200000, 65536, 10)
+    z = _z(a, b)
+    assert np.max(np.abs(z)) < 4.5, z
+    # chi-square of the z scores: mean of z^2 near 1
+    assert np.mean(z ** 2) < 2.0
+    ta, tb = a.sum(1).mean(), b.sum(1).mean()
+    assert abs(ta - tb) / tb < 5e-3
+
+
+def test_config1_total_reflectance_1e8(cuda, lib):
+    """Spec bar: total diffuse reflectance within 0.5 % relative at 1e8
+    packets, fast math against exact math (the exact mode is bit-identical to
+    the oracle, which is bit-identical to the reference kernel)."""
+    fast = scenarios.build_mc('c1_line_hg_radial', fast=True)
+    exact = scenarios.build_mc('c1_line_hg_radial')
+    exact._rnginit = 99
+    _, _, d1 = fast.run(100_000_000)
+    _, _, d2 = exact.run(100_000_000)
+    r1, r2 = d1.top.raw.sum() / 1e8, d2.top.raw.sum() / 1e8
+    assert abs(r1 - r2) / r2 < 5e-3
+    # the specular reflectance is deterministic
+    assert abs(d1.specular.raw.sum() / 1e8 - ((0.33 / 2.33) ** 2)) < 1e-6
+
+
+@pytest.mark.parametrize('fast', [False, True])
+def test_cuda_mcml_golden_profile(cuda, lib, fast):
+    """The reference's validation test SingleLayerLineSourceRadialProfile
+    (xopto/mcml/test/validate.py:219-345): radial reflectance against the
+    CUDA-MCML profile, pass if |mean relative error| < 0.5 %."""
+    from pyxopto_gb300.mcml import mc
+    g = np.load(os.path.join(GOLD, 'cuda_mcml_radial.npz'))
+    layers = mc.mclayer.Layers([
+        mc.mclayer.Layer(d=float(g['d'][i]), n=float(g['n'][i]), mua=float(g['mua'][i]),
+                         mus=float(g['mus'][i]), pf=mc.mcpf.Hg(float(g['g'][i]))) for i in range(3)])
+    start, stop, nb = g['axis']
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(
+        mc.mcdetector.RadialAxis(float(start), float(stop), int(nb)), cosmin=float(g['cosmin'][0])))
+    opts = [mc.mcoptions.McUseNativeMath(True)] if fast else []
+    sim = mc.Mc(layers, mc.mcsource.Line(), det, options=opts, rnginit=5)
+    sim.rmax = float(g['rmax'][0])
+    _, _, res = sim.run(10_000_000)
+    rel = (res.top.reflectance - g['reflectance']) / g['reflectance'] * 100.0
+    assert abs(np.mean(rel)) < 0.5, np.mean(rel)
+
+
+def test_rng_dump_matches_oracle(cuda, lib, oracle):
+    from pyxopto_gb300.mcml import mc
+    sim = scenarios.build_mc('c1_line_hg_radial')
+    out = sim.rng_test(5000, 18446741578333584324, 4294966893)
+    assert np.array_equal(out, oracle.rng_dump(18446741578333584324, 4294966893, 5000))
+
+
+def test_trace_bit_identical_to_oracle(cuda, lib, oracle):
+    from pyxopto_gb300.mcml import mc
+    spec = dict(scenarios.SCENARIOS['c1_line_hg_radial'])
+    sim = scenarios.build_mc(spec)
+    sim._trace = mc.mctrace.Trace(maxlen=64, options=mc.mctrace.Trace.TRACE_ALL)
+    n, t = 300, 32
+    ref = oracle.run(sim, n, t, oracle.PORTABLE)
+    tr, _, _ = sim.run(n, maxthreads=t)
+    off, cnt = sim._flt.find(sim._trace)
+    ioff, icnt = sim._int.find(sim._trace)
+    assert np.array_equal(tr.n, ref['int'][ioff:ioff + icnt])
+    got = np.ascontiguousarray(tr.data).view(np.float32).reshape(-1)
+    assert np.array_equal(got, ref['float'][off:off + cnt])
+    assert tr.n.min() >= 1
