@@ -164,7 +164,7 @@ def gpu_bench(args, rank, world, local_rank):
     dev = torch.device('cuda', local_rank)
     lib = _lib.load()
     spec = scenarios.ALL[args.workload]
-    nphotons = int(spec['nphotons'])
+    nphotons = int(args.packets or spec['nphotons'])
     fast = args.math == 'fast'
     mc = scenarios.build_mc(args.workload, fast=fast)
     mc._rnginit = 1 + 7919 * rank
@@ -259,11 +259,14 @@ def main():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--packets', type=int, default=None,
+                    help='override the packets per step (small profiling cases only; '
+                         'a headline number uses the workload size)')
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     import scenarios
     spec = scenarios.ALL[args.workload]
-    config = {'workload': args.workload, 'packets_per_step': int(spec['nphotons']),
+    config = {'workload': args.workload, 'packets_per_step': int(args.packets or spec['nphotons']),
               'medium': spec['medium'], 'math': args.math,
               'l2': 'flushed between steps (256 MB write); fluence tally 8 MB fits L2'}
 
