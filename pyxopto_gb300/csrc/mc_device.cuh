@@ -153,44 +153,67 @@ MCGB_DEV void scatter_direction(f3 &dir, float cos_theta, float fi) {
     dir.z = dir.z * k;
 }
 
+/* Phase-function constants of one layer/material, precomputed once per
+   kernel with the same float operations the per-step formulas use, so the
+   sampled values are bit-identical to evaluating the reference formulas in
+   place:
+     Hg:  pf0 = (g, 1 - g*g, 1 + g*g, 2*g)
+     Gk:  pf0 = (g, a, -inv_a, a1), pf1 = (a2, 1 + g*g, 2*g, (1 - g)/(1 + g))
+     Lut: pf0 = (a, b, c, (float)(N - 1)), pf1 = (offset, N - 1) as int bits */
+MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
+    if (kind == MCGB_PF_HG) {
+        float g = pf.p[0];
+        pf0 = make_float4(g, 1.0f - g * g, 1.0f + g * g, 2.0f * g);
+        pf1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    } else if (kind == MCGB_PF_GK) {
+        float g = pf.p[0];
+        pf0 = make_float4(g, pf.p[1], -pf.p[2], pf.p[3]);
+        pf1 = make_float4(pf.p[4], 1.0f + g * g, 2.0f * g, mc_div(1.0f - g, 1.0f + g));
+    } else {
+        uint32_t n1 = pf.lut_size - 1u;
+        pf0 = make_float4(pf.p[0], pf.p[1], pf.p[2], (float)n1);
+        pf1 = make_float4(__int_as_float((int)pf.lut_offset), __int_as_float((int)n1), 0.0f, 0.0f);
+    }
+}
+
 /* Phase-function sampling.  Returns cos(theta); the azimuth is drawn first,
    as in the reference.
    Hg:  xopto/mcbase/mcpf/hg.py:80-95
    Gk:  xopto/mcbase/mcpf/gk.py:102-124
    Lut: xopto/mcbase/mcpf/lut.py:125-155 */
-MCGB_DEV float pf_sample(int kind, const McgbPf &pf, const float *lut, Rng &rng, float *azimuth) {
+template <int PF>
+MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut, Rng &rng,
+                         float *azimuth) {
     *azimuth = 6.28318548f * rng.next();
-    if (kind == MCGB_PF_HG) {
-        float g = pf.p[0];
-        float k = mc_div(1.0f - g * g, 1.0f + g * (2.0f * rng.next() - 1.0f));
-        float cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
+    if (PF == MCGB_PF_HG) {
+        float g = pf0.x;
+        float k = mc_div(pf0.y, 1.0f + g * (2.0f * rng.next() - 1.0f));
+        float cos_theta = mc_div(pf0.z - k * k, pf0.w);
         if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
         return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
-    } else if (kind == MCGB_PF_GK) {
-        float g = pf.p[0], ga = pf.p[1], inv_a = pf.p[2], a1 = pf.p[3], a2 = pf.p[4];
+    } else if (PF == MCGB_PF_GK) {
         float cos_theta;
-        if (g == 0.0f) {
+        if (pf0.x == 0.0f) {
             cos_theta = 1.0f - 2.0f * rng.next();
-        } else if (ga == 0.0f) {
-            cos_theta = a1 + mc_pow(mc_div(1.0f - g, 1.0f + g), 2.0f * rng.next()) * a2;
+        } else if (pf0.y == 0.0f) {
+            cos_theta = pf0.w + mc_pow(pf1.w, 2.0f * rng.next()) * pf1.x;
         } else {
-            float tmp = a1 * rng.next() + a2;
-            tmp = 1.0f + g * g - mc_pow(tmp, -inv_a);
-            cos_theta = mc_div(tmp, 2.0f * g);
+            float tmp = pf0.w * rng.next() + pf1.x;
+            tmp = pf1.y - mc_pow(tmp, pf0.z);
+            cos_theta = mc_div(tmp, pf1.z);
         }
         return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
     } else {
-        uint32_t lut_size = pf.lut_size - 1u;
-        float fp_index = (mc_div(pf.p[0], rng.next() - pf.p[2]) - pf.p[1] + 1.0f) *
-                         (float)lut_size * 0.5f;
+        int offset = __float_as_int(pf1.x);
+        int n1 = __float_as_int(pf1.y);
+        float fp_index = (mc_div(pf0.x, rng.next() - pf0.z) - pf0.y + 1.0f) * pf0.w * 0.5f;
         float fp_index_floor = floorf(fp_index);
         float d = fp_index - fp_index_floor;
         /* clamped to the table: parameters that map a uniform number
            outside [0, N-1] would read past the table in the reference */
-        int index = clip_i(cvt_int(fp_index_floor), 0, (int)lut_size);
-        int i1 = index + 1 < (int)lut_size ? index + 1 : (int)lut_size;
-        return lut[pf.lut_offset + (uint32_t)index] * (1.0f - d) +
-               lut[pf.lut_offset + (uint32_t)i1] * d;
+        int index = clip_i(cvt_int(fp_index_floor), 0, n1);
+        int i1 = index + 1 < n1 ? index + 1 : n1;
+        return lut[offset + index] * (1.0f - d) + lut[offset + i1] * d;
     }
 }
 
@@ -248,13 +271,16 @@ MCGB_DEV void fluence_deposit(const McgbFluence &fl, const f3 &pos, float weight
     float ix = (pos.x - fl.top_left[0]) * fl.inv_step[0];
     float iy = (pos.y - fl.top_left[1]) * fl.inv_step[1];
     float iz = (pos.z - fl.top_left[2]) * fl.inv_step[2];
-    if (ix >= 0.0f && iy >= 0.0f && iz >= 0.0f && ix < (float)fl.shape[0] &&
-        iy < (float)fl.shape[1] && iz < (float)fl.shape[2]) {
+    /* indexf < (float)shape  <=>  trunc(indexf) < shape for indexf >= 0, so
+       the bounds test runs on the truncated integer indices */
+    if (ix >= 0.0f && iy >= 0.0f && iz >= 0.0f) {
         uint32_t jx = cvt_uint(ix), jy = cvt_uint(iy), jz = cvt_uint(iz);
-        uint64_t index = ((uint64_t)jz * fl.shape[1] + jy) * fl.shape[0] + jx;
-        if (fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
-        uint32_t w = (uint32_t)(weight * (float)fl.k + 0.5f);
-        cache.add(accu, fl.offset + index, w);
+        if (jx < fl.shape[0] && jy < fl.shape[1] && jz < fl.shape[2]) {
+            uint64_t index = ((uint64_t)jz * fl.shape[1] + jy) * fl.shape[0] + jx;
+            if (fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
+            uint32_t w = (uint32_t)(weight * (float)fl.k + 0.5f);
+            cache.add(accu, fl.offset + index, w);
+        }
     }
 }
 

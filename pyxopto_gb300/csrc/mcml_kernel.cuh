@@ -5,16 +5,20 @@
  * One thread = one random-number stream.  Thread t simulates packets
  * t, t+T, t+2T, ... < N (T = num_streams); when a packet terminates the thread
  * launches its next packet inside the same loop iteration, so a warp keeps
- * all lanes busy until the lanes run out of packets.  The layer table is
- * copied into shared memory (divergent per-lane layer indices hit distinct
- * shared-memory words instead of serialising on the constant cache), and so
- * is the phase-function lookup table when it fits.
+ * all lanes busy until the lanes run out of packets.
+ *
+ * The layer table is rebuilt in shared memory as 16-byte records read with
+ * vector loads (divergent per-lane layer indices hit distinct shared-memory
+ * words instead of serialising on the constant cache); phase-function
+ * constants are precomputed there once.  The kernel is specialised at compile
+ * time on the phase function, the stepping method and whether a fluence grid
+ * is tallied; traces and optical path length stay run-time options.
  *
  * Tallies are 64-bit integer atomics (detectors: one per escaping packet;
  * fluence: one per change of voxel through a per-thread cache).
  *
  * Run control: every 1024 loop iterations a thread compares %globaltimer with
- * the run deadline and polls the host abort word; on expiry it sets a status
+ * its deadline and polls the host abort word; on expiry it sets a status
  * bit, stores its RNG state and leaves.  The kernel never waits on anything.
  */
 #pragma once
@@ -22,13 +26,22 @@
 
 namespace MCGB_NS {
 
+/* Shared-memory record of one layer. */
+struct __align__(16) MlLayer {
+    float4 g0;    /* top, bottom, inv_mut, mua_inv_mut */
+    float4 g1;    /* n, mua, mus, cos_critical_top */
+    float4 pf0;   /* phase-function constants (pf_prepare) */
+    float4 pf1;
+    float4 g2;    /* cos_critical_bottom, -, -, - */
+};
+
 struct MlSmem {
-    McgbLayer layers[MCGB_MAX_LAYERS];
+    MlLayer layers[MCGB_MAX_LAYERS];
 };
 
 /* Line / GaussianBeam launch (xopto/mcml/mcsource/line.py:95-108,
    gaussianbeam.py:119-170). */
-static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const McgbLayer *L,
+static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
                                                    Rng &rng, f3 &pos, f3 &dir, float &w,
                                                    int &layer, uint64_t *accu) {
     const McgbSource &src = c.source;
@@ -61,19 +74,18 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
         if (c.specular.kind != MCGB_DET_NONE) {
             f3 dir_in{dir.x, dir.y, -dir.z};
             f3 normal{0.0f, 0.0f, -1.0f};
-            f3 d = refract3(dir_in, normal, L[1].n, L[0].n);
+            f3 d = refract3(dir_in, normal, L[1].g1.x, L[0].g1.x);
             detector_deposit(c.specular, pos, d, src.reflectance, accu);
         }
     }
 }
 
 /* mcsim_boundary (mcml), xopto/mcml/kernel/mcml.template.c:80-203 */
-static __device__ __forceinline__ uint32_t mcml_boundary(const McgbLayer *L, int &layer, int next,
+static __device__ __forceinline__ uint32_t mcml_boundary(const MlLayer *L, int &layer, int next,
                                                          f3 &dir, Rng &rng) {
-    const McgbLayer &cur = L[layer];
-    float cc = (dir.z < 0.0f) ? cur.cos_critical_top : cur.cos_critical_bottom;
-    float n1 = cur.n;
-    float n2 = L[layer + fsign(dir.z)].n;
+    float cc = (dir.z < 0.0f) ? L[layer].g1.w : L[layer].g2.x;
+    float n1 = L[layer].g1.x;
+    float n2 = L[layer + fsign(dir.z)].g1.x;
     if (n1 == n2) {
         layer = next;
         return MCGB_EV_REFRACTION;
@@ -114,18 +126,26 @@ static __device__ __forceinline__ uint32_t mcml_boundary(const McgbLayer *L, int
     return MCGB_EV_REFLECTION;
 }
 
+template <int PF, int METHOD, bool FLU>
 __global__ void __launch_bounds__(256)
 mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
                       uint64_t deadline_ns, int lut_in_smem) {
     __shared__ MlSmem sm;
     extern __shared__ float s_lut[];
-    for (uint32_t i = threadIdx.x; i < c.num_layers * (sizeof(McgbLayer) / 4); i += blockDim.x)
-        reinterpret_cast<float *>(sm.layers)[i] = reinterpret_cast<const float *>(c.layers)[i];
+    for (uint32_t i = threadIdx.x; i < c.num_layers; i += blockDim.x) {
+        const McgbLayer &l = c.layers[i];
+        MlLayer h;
+        h.g0 = make_float4(l.top, l.bottom, l.inv_mut, l.mua_inv_mut);
+        h.g1 = make_float4(l.n, l.mua, l.mus, l.cos_critical_top);
+        h.g2 = make_float4(l.cos_critical_bottom, 0.0f, 0.0f, 0.0f);
+        pf_prepare(PF, l.pf, h.pf0, h.pf1);
+        sm.layers[i] = h;
+    }
     if (lut_in_smem)
         for (uint64_t i = threadIdx.x; i < b.fp_lut_size; i += blockDim.x) s_lut[i] = b.fp_lut[i];
     __syncthreads();
     const float *lut = lut_in_smem ? s_lut : b.fp_lut;
-    const McgbLayer *L = sm.layers;
+    const MlLayer *L = sm.layers;
 
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= c.num_streams || t >= c.num_packets) return;
@@ -133,19 +153,19 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
 
     const McgbRunOptions &o = c.opt;
     const uint64_t T = c.num_streams;
-    const int method = o.method;
-    const int pf_kind = c.pf_kind;
-    const bool use_fluence = c.fluence.kind != MCGB_FLUENCE_NONE;
     const bool use_trace = c.trace.flags != MCGB_TRACE_NONE;
     const bool track_opl = o.track_optical_pathlength != 0;
     const float rmax2 = o.rmax * o.rmax;
+    /* dist2 > inf is never true: skip the test for an infinite rmax */
+    const bool use_rmax = rmax2 < __int_as_float(0x7f800000);
     const int last_layer = (int)c.num_layers - 1;
     const f3 src_pos{c.source.position[0], c.source.position[1], c.source.position[2]};
     uint64_t *accu = b.accumulator;
 
     Rng rng{b.rng_x[t], b.rng_a[t]};
     FluenceCache fcache{~0ull, 0};
-    uint64_t steps = 0, packets = 0, packet_steps = 0;
+    uint64_t steps = 0, packets = 0;
+    uint32_t packet_steps = 0, iter = 0;
     uint32_t status = 0;
 
     uint64_t p = t;
@@ -158,39 +178,41 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
         trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
 
     for (;;) {
-        const McgbLayer &cl = L[layer];
-        ++steps;
+        const float4 g0 = L[layer].g0;   /* top, bottom, inv_mut, mua_inv_mut */
         ++packet_steps;
+        ++iter;
         float u = rng.next();
-        float step = (method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
-                         ? mc_div(-mc_log(u), cl.mus)
-                         : -mc_log(u) * cl.inv_mut;
+        float step;
+        if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
+            step = mc_div(-mc_log(u), L[layer].g1.z);
+        else
+            step = -mc_log(u) * g0.z;
         step = fminf(step, FLT_MAX);
         int next = layer;
-        if (pos.z + step * dir.z < cl.top) {
+        if (pos.z + step * dir.z < g0.x) {
             --next;
-            if (fabsf(dir.z) != 0.0f) step = mc_div(cl.top - pos.z, dir.z);
+            if (fabsf(dir.z) != 0.0f) step = mc_div(g0.x - pos.z, dir.z);
         }
-        if (pos.z + step * dir.z >= cl.bottom) {
+        if (pos.z + step * dir.z >= g0.y) {
             ++next;
-            if (fabsf(dir.z) != 0.0f) step = mc_div(cl.bottom - pos.z, dir.z);
+            if (fabsf(dir.z) != 0.0f) step = mc_div(g0.y - pos.z, dir.z);
         }
         pos.x = pos.x + dir.x * step;
         pos.y = pos.y + dir.y * step;
         pos.z = pos.z + dir.z * step;
-        if (track_opl) opl += cl.n * step;
-        if (layer < next) pos.z = cl.bottom;
-        if (layer > next) pos.z = cl.top;
+        if (track_opl) opl += L[layer].g1.x * step;
+        if (layer < next) pos.z = g0.y;
+        if (layer > next) pos.z = g0.x;
 
         bool done = false;
-        if (method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
+        if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
             /* mcml.template.c:584-666 */
-            float mua = cl.mua;
+            float mua = L[layer].g1.y;
             float fraction = 1.0f - mc_exp(-mua * step);
             float deposit = fraction * w;
             w -= deposit;
             events |= MCGB_EV_ABSORPTION;
-            if (use_fluence) {
+            if (FLU) {
                 float step_back = (mua != 0.0f)
                                       ? step - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
                                       : 0.0f;
@@ -205,7 +227,8 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
                     done = true;
                 }
             } else {
-                float az, ct = pf_sample(pf_kind, cl.pf, lut, rng, &az);
+                const MlLayer &cl = L[layer];
+                float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, lut, rng, &az);
                 scatter_direction(dir, ct, az);
                 events |= MCGB_EV_SCATTERING;
             }
@@ -224,26 +247,28 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
                 else detector_deposit(c.bottom, pos, dir, w, accu);
                 done = true;
             }
-        } else if (method == MCGB_METHOD_ALBEDO_REJECTION) {
+        } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
             /* mcml.template.c:705-721 */
-            if (rng.next() < cl.mua_inv_mut) {
+            if (rng.next() < g0.w) {
                 float deposit = w;
                 done = true;
                 w -= deposit;
                 events |= MCGB_EV_ABSORPTION;
-                if (use_fluence) fluence_deposit(c.fluence, pos, deposit, cl.mua, accu, fcache);
+                if (FLU) fluence_deposit(c.fluence, pos, deposit, L[layer].g1.y, accu, fcache);
             } else {
-                float az, ct = pf_sample(pf_kind, cl.pf, lut, rng, &az);
+                const MlLayer &cl = L[layer];
+                float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, lut, rng, &az);
                 scatter_direction(dir, ct, az);
                 events |= MCGB_EV_SCATTERING;
             }
         } else {
             /* albedo weight, mcml.template.c:722-753 */
-            float deposit = w * cl.mua_inv_mut;
+            float deposit = w * g0.w;
             w -= deposit;
             events |= MCGB_EV_ABSORPTION;
-            if (use_fluence) fluence_deposit(c.fluence, pos, deposit, cl.mua, accu, fcache);
-            float az, ct = pf_sample(pf_kind, cl.pf, lut, rng, &az);
+            if (FLU) fluence_deposit(c.fluence, pos, deposit, L[layer].g1.y, accu, fcache);
+            const MlLayer &cl = L[layer];
+            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, lut, rng, &az);
             scatter_direction(dir, ct, az);
             events |= MCGB_EV_SCATTERING;
             if (w < o.packet_weight_min) {
@@ -256,15 +281,19 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
             }
         }
         /* rmax, mcml.template.c:759-763 */
-        f3 d{pos.x - src_pos.x, pos.y - src_pos.y, pos.z - src_pos.z};
-        if (dot3(d, d) > rmax2) {
-            done = true;
-            events |= MCGB_EV_ESCAPED;
+        if (use_rmax) {
+            f3 d{pos.x - src_pos.x, pos.y - src_pos.y, pos.z - src_pos.z};
+            if (dot3(d, d) > rmax2) {
+                done = true;
+                events |= MCGB_EV_ESCAPED;
+            }
         }
-        if (done) events |= MCGB_EV_TERMINATED;
-        if (use_trace && (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done)))
-            trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
-        events = 0;
+        if (use_trace) {
+            if (done) events |= MCGB_EV_TERMINATED;
+            if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
+                trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
+            events = 0;
+        }
         if (!done && o.max_steps_per_packet && packet_steps >= o.max_steps_per_packet) {
             done = true;
             status |= MCGB_STATUS_STEP_LIMIT;
@@ -272,23 +301,25 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
 
         if (done) {
             ++packets;
+            steps += packet_steps;
+            packet_steps = 0;
             if (use_trace) b.int_buffer[c.trace.count_offset + p] = (int32_t)trace_count;
             p += T;
             if (p >= c.num_packets) break;
             trace_count = 0;
             opl = 0.0f;
-            packet_steps = 0;
             events = MCGB_EV_LAUNCH;
             mcml_launch(c, L, rng, pos, dir, w, layer, accu);
             if (use_trace && (c.trace.flags & MCGB_TRACE_START))
                 trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
         }
-        if ((steps & 1023u) == 0) {
+        if ((iter & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
             if (*(volatile uint64_t *)(b.counters + MCGB_CNT_ABORT)) { status |= MCGB_STATUS_ABORTED; break; }
         }
     }
-    if (use_fluence) fcache.flush(accu);
+    steps += packet_steps;
+    if (FLU) fcache.flush(accu);
     b.rng_x[t] = rng.x;
     atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_STEPS), (unsigned long long)steps);
     atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_PACKETS), (unsigned long long)packets);

@@ -13,8 +13,16 @@
 
 namespace MCGB_NS {
 
+/* Shared-memory record of one material. */
+struct __align__(16) MvMaterial {
+    float4 g0;    /* mus, mua, inv_mut, mua_inv_mut */
+    float4 g1;    /* n, -, -, - */
+    float4 pf0;   /* phase-function constants (pf_prepare) */
+    float4 pf1;
+};
+
 struct MvSmem {
-    McgbMaterial materials[MCGB_MAX_MATERIALS];
+    MvMaterial materials[MCGB_MAX_MATERIALS];
 };
 
 struct MvGeom {
@@ -71,7 +79,7 @@ static __device__ __forceinline__ int mv_box_intersect(const MvGeom &g, const f3
    (xopto/mcvox/mcsource/gaussianbeam.py:112-190), then the voxel index of
    the launch position (mcvox.template.c:240-262). */
 static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, const MvGeom &g,
-                                                    const McgbMaterial *M, const uint8_t *vox,
+                                                    const MvMaterial *M, const uint8_t *vox,
                                                     Rng &rng, f3 &pos, f3 &dir, float &w, i3 &vi,
                                                     int &mat, uint64_t *accu) {
     const McgbSource &src = c.source;
@@ -106,12 +114,12 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
             pos = isec;
             direction = f3{-direction.x, -direction.y, -direction.z};
             normal = f3{-normal.x, -normal.y, -normal.z};
-            float n_outside = M[0].n;
+            float n_outside = M[0].g1.x;
             i3 li = mv_index(g, pos);
             li.x = clip_i(li.x, 0, g.sh[0] - 1);
             li.y = clip_i(li.y, 0, g.sh[1] - 1);
             li.z = clip_i(li.z, 0, g.sh[2] - 1);
-            float n_inside = M[mv_material_at(g, vox, li)].n;
+            float n_inside = M[mv_material_at(g, vox, li)].g1.x;
             f3 refracted = direction;
             refract_safe3(direction, normal, n_outside, n_inside, &refracted);
             dir = refracted;
@@ -131,7 +139,7 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
 }
 
 /* mcsim_boundary (mcvox), mcvox.template.c:275-388 */
-static __device__ __forceinline__ uint32_t mv_boundary(const MvGeom &g, const McgbMaterial *M,
+static __device__ __forceinline__ uint32_t mv_boundary(const MvGeom &g, const MvMaterial *M,
                                                        const uint8_t *vox, f3 &dir, i3 &vi,
                                                        int &mat, const f3 &dist, Rng &rng) {
     i3 nrm;
@@ -148,7 +156,7 @@ static __device__ __forceinline__ uint32_t mv_boundary(const MvGeom &g, const Mc
         vi = nv;
         return MCGB_EV_REFRACTION;
     }
-    float n1 = M[mat].n, n2 = M[next_mat].n;
+    float n1 = M[mat].g1.x, n2 = M[next_mat].g1.x;
     if (n1 == n2) {
         vi = nv;
         mat = next_mat;
@@ -170,18 +178,25 @@ static __device__ __forceinline__ uint32_t mv_boundary(const MvGeom &g, const Mc
     return MCGB_EV_REFLECTION;
 }
 
+template <int PF, int METHOD, bool FLU>
 __global__ void __launch_bounds__(256)
 mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
                        uint64_t deadline_ns, int lut_in_smem) {
     __shared__ MvSmem sm;
     extern __shared__ float s_lut[];
-    for (uint32_t i = threadIdx.x; i < c.num_materials * (sizeof(McgbMaterial) / 4); i += blockDim.x)
-        reinterpret_cast<float *>(sm.materials)[i] = reinterpret_cast<const float *>(b.materials)[i];
+    for (uint32_t i = threadIdx.x; i < c.num_materials; i += blockDim.x) {
+        const McgbMaterial &m = b.materials[i];
+        MvMaterial h;
+        h.g0 = make_float4(m.mus, m.mua, m.inv_mut, m.mua_inv_mut);
+        h.g1 = make_float4(m.n, 0.0f, 0.0f, 0.0f);
+        pf_prepare(PF, m.pf, h.pf0, h.pf1);
+        sm.materials[i] = h;
+    }
     if (lut_in_smem)
         for (uint64_t i = threadIdx.x; i < b.fp_lut_size; i += blockDim.x) s_lut[i] = b.fp_lut[i];
     __syncthreads();
     const float *lut = lut_in_smem ? s_lut : b.fp_lut;
-    const McgbMaterial *M = sm.materials;
+    const MvMaterial *M = sm.materials;
 
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= c.num_streams || t >= c.num_packets) return;
@@ -194,19 +209,18 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
     }
     const McgbRunOptions &o = c.opt;
     const uint64_t T = c.num_streams;
-    const int method = o.method;
-    const int pf_kind = c.pf_kind;
-    const bool use_fluence = c.fluence.kind != MCGB_FLUENCE_NONE;
     const bool use_trace = c.trace.flags != MCGB_TRACE_NONE;
     const bool track_opl = o.track_optical_pathlength != 0;
     const float rmax2 = o.rmax * o.rmax;
+    const bool use_rmax = rmax2 < __int_as_float(0x7f800000);
     const f3 src_pos{c.source.position[0], c.source.position[1], c.source.position[2]};
     const uint8_t *vox = b.voxels;
     uint64_t *accu = b.accumulator;
 
     Rng rng{b.rng_x[t], b.rng_a[t]};
     FluenceCache fcache{~0ull, 0};
-    uint64_t steps = 0, packets = 0, packet_steps = 0;
+    uint64_t steps = 0, packets = 0;
+    uint32_t packet_steps = 0, iter = 0;
     uint32_t status = 0;
 
     uint64_t p = t;
@@ -220,13 +234,13 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
         trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
 
     for (;;) {
-        const McgbMaterial &cm = M[mat];
-        ++steps;
+        const float4 g0 = M[mat].g0;   /* mus, mua, inv_mut, mua_inv_mut */
         ++packet_steps;
+        ++iter;
         float u = rng.next();
-        float step = (method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
-                         ? mc_div(-mc_log(u), cm.mus)
-                         : -mc_log(u) * cm.inv_mut;
+        float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
+                         ? mc_div(-mc_log(u), g0.x)
+                         : -mc_log(u) * g0.z;
         step = fminf(step, FLT_MAX);
         /* mcsim_intersect, mcvox.template.c:173-196 */
         f3 dist;
@@ -241,16 +255,16 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
         pos.x = pos.x + d_ok * dir.x;
         pos.y = pos.y + d_ok * dir.y;
         pos.z = pos.z + d_ok * dir.z;
-        if (track_opl) opl += cm.n * d_ok;
+        if (track_opl) opl += M[mat].g1.x * d_ok;
 
         bool done = false;
-        if (method == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
-            float mua = cm.mua;
+        if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
+            float mua = g0.y;
             float fraction = 1.0f - mc_exp(-mua * d_ok);
             float deposit = fraction * w;
             w -= deposit;
             events |= MCGB_EV_ABSORPTION;
-            if (use_fluence) {
+            if (FLU) {
                 float step_back = (mua != 0.0f)
                                       ? d_ok - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
                                       : 0.0f;
@@ -265,7 +279,8 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
                     done = true;
                 }
             } else {
-                float az, ct = pf_sample(pf_kind, cm.pf, lut, rng, &az);
+                const MvMaterial &cm = M[mat];
+                float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, lut, rng, &az);
                 scatter_direction(dir, ct, az);
                 events |= MCGB_EV_SCATTERING;
             }
@@ -284,24 +299,26 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
                 else if (vi.z >= g.sh[2]) detector_deposit(c.bottom, pos, dir, w, accu);
                 done = true;
             }
-        } else if (method == MCGB_METHOD_ALBEDO_REJECTION) {
-            if (rng.next() < cm.mua_inv_mut) {
+        } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
+            if (rng.next() < g0.w) {
                 float deposit = w;
                 w -= deposit;
                 events |= MCGB_EV_ABSORPTION;
                 done = true;
-                if (use_fluence) fluence_deposit(c.fluence, pos, deposit, cm.mua, accu, fcache);
+                if (FLU) fluence_deposit(c.fluence, pos, deposit, g0.y, accu, fcache);
             } else {
-                float az, ct = pf_sample(pf_kind, cm.pf, lut, rng, &az);
+                const MvMaterial &cm = M[mat];
+                float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, lut, rng, &az);
                 scatter_direction(dir, ct, az);
                 events |= MCGB_EV_SCATTERING;
             }
         } else {
-            float deposit = w * cm.mua_inv_mut;
+            float deposit = w * g0.w;
             w -= deposit;
             events |= MCGB_EV_ABSORPTION;
-            if (use_fluence) fluence_deposit(c.fluence, pos, deposit, cm.mua, accu, fcache);
-            float az, ct = pf_sample(pf_kind, cm.pf, lut, rng, &az);
+            if (FLU) fluence_deposit(c.fluence, pos, deposit, g0.y, accu, fcache);
+            const MvMaterial &cm = M[mat];
+            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, lut, rng, &az);
             scatter_direction(dir, ct, az);
             events |= MCGB_EV_SCATTERING;
             if (w < o.packet_weight_min) {
@@ -314,38 +331,46 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
             }
         }
         /* mcvox.template.c:1004-1008 */
-        f3 dd{pos.x - src_pos.x, pos.y - src_pos.y, pos.z - src_pos.z};
-        if (dot3(dd, dd) > rmax2 || w <= 0.0f) {
+        bool escaped = w <= 0.0f;
+        if (use_rmax) {
+            f3 dd{pos.x - src_pos.x, pos.y - src_pos.y, pos.z - src_pos.z};
+            escaped = escaped || dot3(dd, dd) > rmax2;
+        }
+        if (escaped) {
             done = true;
             events |= MCGB_EV_ESCAPED;
         }
-        if (done) events |= MCGB_EV_TERMINATED;
-        if (use_trace && (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done)))
-            trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
-        events = 0;
+        if (use_trace) {
+            if (done) events |= MCGB_EV_TERMINATED;
+            if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
+                trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
+            events = 0;
+        }
         if (!done && o.max_steps_per_packet && packet_steps >= o.max_steps_per_packet) {
             done = true;
             status |= MCGB_STATUS_STEP_LIMIT;
         }
         if (done) {
             ++packets;
+            steps += packet_steps;
+            packet_steps = 0;
             if (use_trace) b.int_buffer[c.trace.count_offset + p] = (int32_t)trace_count;
             p += T;
             if (p >= c.num_packets) break;
             trace_count = 0;
             opl = 0.0f;
-            packet_steps = 0;
             events = MCGB_EV_LAUNCH;
             mcvox_launch(c, g, M, vox, rng, pos, dir, w, vi, mat, accu);
             if (use_trace && (c.trace.flags & MCGB_TRACE_START))
                 trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
         }
-        if ((steps & 1023u) == 0) {
+        if ((iter & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
             if (*(volatile uint64_t *)(b.counters + MCGB_CNT_ABORT)) { status |= MCGB_STATUS_ABORTED; break; }
         }
     }
-    if (use_fluence) fcache.flush(accu);
+    steps += packet_steps;
+    if (FLU) fcache.flush(accu);
     b.rng_x[t] = rng.x;
     atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_STEPS), (unsigned long long)steps);
     atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_PACKETS), (unsigned long long)packets);

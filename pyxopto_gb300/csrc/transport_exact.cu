@@ -13,32 +13,61 @@
 
 namespace mcgb_exact {
 
+/* Kernel variants specialised on phase function x method x fluence. */
+#define MCGB_V(K, PF, M) {(const void *)K<PF, M, false>, (const void *)K<PF, M, true>}
+#define MCGB_METHODS(K, PF) {MCGB_V(K, PF, 0), MCGB_V(K, PF, 1), MCGB_V(K, PF, 2)}
+#define MCGB_TABLE(K) {MCGB_METHODS(K, 0), MCGB_METHODS(K, 1), MCGB_METHODS(K, 2)}
+
+static const void *const kMcml[3][3][2] = MCGB_TABLE(mcml_transport_kernel);
+static const void *const kMcvox[3][3][2] = MCGB_TABLE(mcvox_transport_kernel);
+
+static const void *select(int medium, int pf, int method, bool fluence) {
+    if (pf < 0 || pf > 2 || method < 0 || method > 2) return nullptr;
+    return medium == 0 ? kMcml[pf][method][fluence ? 1 : 0] : kMcvox[pf][method][fluence ? 1 : 0];
+}
+
+template <class Cfg>
+static cudaError_t launch(int medium, const Cfg &cfg, const McgbBuffers &buf, cudaStream_t stream,
+                          const LaunchShape &shape) {
+    const void *k = select(medium, cfg.pf_kind, cfg.opt.method, cfg.fluence.kind != MCGB_FLUENCE_NONE);
+    if (!k) return cudaErrorInvalidValue;
+    if (shape.dyn_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)shape.dyn_smem);
+        if (e != cudaSuccess) return e;
+    }
+    McgbBuffers b = buf;
+    uint64_t deadline = shape.deadline_ns;
+    int lut = shape.lut_in_smem;
+    void *args[] = {(void *)&cfg, (void *)&b, (void *)&deadline, (void *)&lut};
+    return cudaLaunchKernel(k, dim3(shape.grid), dim3(shape.block), args, shape.dyn_smem, stream);
+}
+
 cudaError_t launch_mcml(const McgbMcmlConfig &cfg, const McgbBuffers &buf, cudaStream_t stream,
                         const LaunchShape &shape) {
-    if (shape.dyn_smem > 48 * 1024)
-        cudaFuncSetAttribute(mcml_transport_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)shape.dyn_smem);
-    mcml_transport_kernel<<<shape.grid, shape.block, shape.dyn_smem, stream>>>(
-        cfg, buf, shape.deadline_ns, shape.lut_in_smem);
-    return cudaGetLastError();
+    return launch(0, cfg, buf, stream, shape);
 }
 
 cudaError_t launch_mcvox(const McgbMcvoxConfig &cfg, const McgbBuffers &buf, cudaStream_t stream,
                          const LaunchShape &shape) {
-    if (shape.dyn_smem > 48 * 1024)
-        cudaFuncSetAttribute(mcvox_transport_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)shape.dyn_smem);
-    mcvox_transport_kernel<<<shape.grid, shape.block, shape.dyn_smem, stream>>>(
-        cfg, buf, shape.deadline_ns, shape.lut_in_smem);
-    return cudaGetLastError();
+    return launch(1, cfg, buf, stream, shape);
 }
 
 cudaError_t occupancy(int medium, int block, size_t dyn_smem, int *blocks_per_sm) {
-    if (medium == 0)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mcml_transport_kernel,
-                                                             block, dyn_smem);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mcvox_transport_kernel,
-                                                         block, dyn_smem);
+    /* the smallest residency over every variant of the medium, so that one
+       wave of the suggested stream count fits whichever variant runs */
+    int best = 1 << 30;
+    for (int pf = 0; pf < 3; ++pf)
+        for (int m = 0; m < 3; ++m)
+            for (int fl = 0; fl < 2; ++fl) {
+                int n = 0;
+                cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &n, select(medium, pf, m, fl != 0), block, dyn_smem);
+                if (e != cudaSuccess) return e;
+                best = n < best ? n : best;
+            }
+    *blocks_per_sm = best;
+    return cudaSuccess;
 }
 
 }  // namespace mcgb_exact
