@@ -305,40 +305,57 @@ int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream);
 int mcgb_reduce_tallies(uint64_t *host_dst, const uint64_t *host_src, uint64_t n);
 
 /* --------------------------------------------------------- batched engine */
-/* One simulation of the batched engine: a semi-infinite or finite single
-   layer between two half-spaces, Hg phase function, normal Line source and
-   a radial reflectance detector (the BASELINE batched configuration). */
+/* One simulation of the batched engine: a single layer (finite or
+   semi-infinite) between two half-spaces, Henyey-Greenstein phase function,
+   normally incident Line source, albedo-weight stepping and a radial
+   reflectance detector at the top surface (the batched configuration of
+   the benchmark suite; each simulation matches an mcml run of that shape). */
 typedef struct McgbBatchSim {
-    float mua, mus, g, n;               /* sample layer                      */
+    float mua, mus, g, n;               /* sample layer (1/m, 1/m, -, -)     */
     float n_above, n_below;             /* surrounding half-spaces           */
-    float thickness;                    /* inf = semi-infinite               */
+    float thickness;                    /* m; inf = semi-infinite            */
     float reserved;
     uint64_t num_packets;
 } McgbBatchSim;                         /* 40 bytes */
 
 typedef struct McgbBatchConfig {
     uint32_t num_sims;
-    uint32_t packets_per_chunk;         /* work item = (sim, chunk)          */
-    uint32_t block_size;                /* threads per block                 */
-    uint32_t blocks_per_sm;             /* resident blocks per SM            */
+    uint32_t packets_per_item;          /* work item size, multiple of 32    */
+    uint32_t block_size;                /* threads per block (multiple of 32)*/
+    uint32_t blocks_per_sm;             /* 0 = as many as fit                */
     uint32_t num_bins;                  /* radial bins per simulation        */
     int32_t math;                       /* MCGB_MATH_*                       */
-    float r_max;                        /* radial axis 0 .. r_max            */
-    float rmax;                         /* packet termination radius         */
-    uint64_t seed;                      /* per-chunk stream derivation       */
-    double deadline_s;
+    float inv_dr;                       /* 1/bin width: bins cover
+                                           [0, num_bins/inv_dr); radii beyond
+                                           land in the last bin (1/m)        */
+    float rmax;                         /* packet termination radius (m)     */
+    uint64_t seed;                      /* per-packet stream derivation      */
+    double deadline_s;                  /* device wall-clock limit, 0 = 300s */
+    uint32_t num_multipliers;           /* entries of dev_multipliers        */
+    uint32_t reserved;
 } McgbBatchConfig;
 
-/* Runs every simulation to completion in one persistent launch.  Work items
-   are (simulation, chunk) pairs taken from a device work queue; each chunk
-   owns an RNG stream derived from (seed, sim, chunk), so the tallies do not
-   depend on which thread takes which chunk.
-   dev_sims [num_sims]; dev_tally [num_sims*num_bins] (accumulated, caller
-   zeroes); dev_work [num_sims+2] scratch (caller-owned, any contents);
-   dev_counters [MCGB_NUM_COUNTERS]. */
+/* Bytes of scratch that mcgb_batched_run needs for num_sims simulations
+   (work-queue counter, packet prefix sums, per-simulation layer tables). */
+int mcgb_batched_work_size(uint32_t num_sims, uint64_t *bytes);
+
+/* Runs every simulation to completion in one persistent launch (plus a
+   small preparation kernel).  Warps take work items of packets_per_item
+   consecutive packets from a device queue and refill idle lanes packet by
+   packet; packet k of simulation s uses the MWC stream derived from
+   (seed, s, k), so the tallies do not depend on the scheduling.
+   dev_sims [num_sims]; dev_multipliers [num_multipliers] safe-prime
+   multipliers; dev_tally [num_sims*num_bins] uint64 radial tallies
+   (accumulated: the caller zeroes them); dev_work scratch of
+   mcgb_batched_work_size bytes (any contents, caller-owned);
+   dev_counters [MCGB_NUM_COUNTERS] (zeroed by the caller).  Launches only
+   (no synchronisation), so the call can be captured in a CUDA graph. */
 int mcgb_batched_run(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
-                     uint64_t *dev_tally, uint64_t *dev_work,
-                     uint64_t *dev_counters, void *stream);
+                     const uint32_t *dev_multipliers, uint64_t *dev_tally,
+                     void *dev_work, uint64_t *dev_counters, void *stream);
+
+/* Resident blocks per SM of the batched kernel for a block size. */
+int mcgb_batched_occupancy(uint32_t block_size, int math, uint32_t *blocks_per_sm);
 
 /* ------------------------------------------------------ MLP surrogate */
 /* Linear layer forward: Y[M,N] = act(X[M,K] @ W[N,K]^T + b[N]) with BF16

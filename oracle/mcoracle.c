@@ -32,6 +32,7 @@
 
 #include "../include/xopto_gb300.h"
 #include "../pyxopto_gb300/csrc/portable_math.h"
+#include "../pyxopto_gb300/csrc/batch_rng.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -948,4 +949,84 @@ int mco_sizeof(int kind) {
         case 10: return (int)sizeof(McgbPf);
         default: return -1;
     }
+}
+
+/* ===================================================== batched engine */
+/* Per-simulation configuration of the batched engine as an mcml run:
+   three layers (above, sample, below), Henyey-Greenstein phase function,
+   normally incident Line source, radial top detector at offset
+   sim*num_bins.  Layer fields follow the layered packing
+   (xopto/mcml/mclayer/layer.py:304-354,944-1007) evaluated in double from
+   the float simulation parameters. */
+static double cc_d(double n1, double n2) { return n1 > n2 ? sqrt(1.0 - (n2 / n1) * (n2 / n1)) : 0.0; }
+
+static void batch_sim_config(const McgbBatchConfig *bc, const McgbBatchSim *m, uint32_t sim,
+                             McgbMcmlConfig *c) {
+    memset(c, 0, sizeof(*c));
+    c->num_packets = 1;
+    c->num_streams = 1;
+    c->pf_kind = MCGB_PF_HG;
+    c->num_layers = 3;
+    c->opt.method = MCGB_METHOD_ALBEDO_WEIGHT;
+    c->opt.use_lottery = 1;
+    c->opt.packet_weight_min = 1e-4f;
+    c->opt.lottery_chance = 0.1f;
+    c->opt.rmax = bc->rmax;
+    double mua = m->mua, mus = m->mus, mut = mua + mus;
+    McgbLayer *L = c->layers;
+    L[0].top = -INFINITY; L[0].bottom = 0.0f; L[0].thickness = INFINITY;
+    L[0].n = m->n_above; L[0].inv_mut = INFINITY; L[0].mua_inv_mut = 1.0f;
+    L[0].cos_critical_bottom = (float)cc_d(m->n_above, m->n);
+    L[1].top = 0.0f; L[1].bottom = m->thickness; L[1].thickness = m->thickness;
+    L[1].n = m->n; L[1].mua = m->mua; L[1].mus = m->mus;
+    L[1].inv_mut = mut > 0.0 ? (float)(1.0 / mut) : INFINITY;
+    L[1].mua_inv_mut = mus == 0.0 ? 1.0f : (float)(mua * (mut > 0.0 ? 1.0 / mut : 0.0));
+    L[1].cos_critical_top = (float)cc_d(m->n, m->n_above);
+    L[1].cos_critical_bottom = (float)cc_d(m->n, m->n_below);
+    L[1].pf.p[0] = m->g;
+    L[2].top = m->thickness; L[2].bottom = INFINITY; L[2].thickness = INFINITY;
+    L[2].n = m->n_below; L[2].inv_mut = INFINITY; L[2].mua_inv_mut = 1.0f;
+    L[2].cos_critical_top = (float)cc_d(m->n_below, m->n);
+    double r = ((double)m->n_above - m->n) / ((double)m->n_above + m->n);
+    c->source.kind = MCGB_SRC_LINE;
+    c->source.direction[2] = 1.0f;
+    c->source.direction_reflected[2] = -1.0f;
+    c->source.reflectance = (float)(r * r);
+    c->top.kind = MCGB_DET_RADIAL;
+    c->top.direction[2] = 1.0f;
+    c->top.r_min = 0.0f;
+    c->top.inv_dr = bc->inv_dr;
+    c->top.cos_min = 0.0f;
+    c->top.n = bc->num_bins;
+    c->top.offset = (uint64_t)sim * bc->num_bins;
+}
+
+/* Every packet k of simulation s on its own stream (batch_rng.h); returns
+   the interaction steps.  tally has num_sims*num_bins entries. */
+uint64_t mco_batched_run(int math_mode, const McgbBatchConfig *bc, const McgbBatchSim *sims,
+                         const uint32_t *mult, uint64_t *tally, int nthreads) {
+    uint64_t steps = 0;
+    int64_t S = bc->num_sims;
+    uint64_t nt = (uint64_t)bc->num_sims * bc->num_bins;
+    (void)nt;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1) reduction(+:steps)
+    {
+        uint64_t *acc = (uint64_t *)calloc(nt ? nt : 1, 8);
+        McgbMcmlConfig *c = (McgbMcmlConfig *)malloc(sizeof(McgbMcmlConfig));
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t s = 0; s < S; ++s) {
+            batch_sim_config(bc, &sims[s], (uint32_t)s, c);
+            for (uint64_t k = 0; k < sims[s].num_packets; ++k) {
+                uint64_t x;
+                uint32_t a;
+                br_packet_stream(bc->seed, (uint32_t)s, k, mult, bc->num_multipliers, &x, &a);
+                steps += mcml_stream(math_mode, c, NULL, &x, a, 0, 1, acc, NULL, NULL);
+            }
+        }
+#pragma omp critical
+        for (uint64_t i = 0; i < nt; ++i) tally[i] += acc[i];
+        free(acc);
+        free(c);
+    }
+    return steps;
 }

@@ -44,6 +44,8 @@ def load():
         lib.mco_pm_pow.argtypes = [C.c_float, C.c_float]
         lib.mco_pm_sincos.argtypes = [C.c_float, vp, vp]
         lib.mco_sizeof.argtypes = [C.c_int]
+        lib.mco_batched_run.restype = C.c_uint64
+        lib.mco_batched_run.argtypes = [C.c_int, vp, vp, vp, vp, C.c_int]
         _lib = lib
     return _lib
 
@@ -105,3 +107,14 @@ def rng_dump(x: int, a: int, n: int) -> np.ndarray:
     out = np.zeros((int(n),), dtype=np.float32)
     load().mco_rng_dump(int(x), int(a), int(n), out.ctypes.data)
     return out
+
+
+def batched_run(bmc, math: int = PORTABLE, nthreads: int = 1, **shape):
+    """CPU restatement of a BatchedMc run: returns (tallies (S, bins), steps)."""
+    lib = load()
+    cfg = bmc.config(**shape)
+    mult = np.ascontiguousarray(bmc.multipliers(cfg.num_multipliers), dtype=np.uint32)
+    tally = np.zeros((bmc.num_sims * bmc.raxis.n,), dtype=np.uint64)
+    steps = lib.mco_batched_run(int(math), C.addressof(cfg), C.addressof(bmc._sims),
+                                mult.ctypes.data, tally.ctypes.data, int(nthreads))
+    return tally.reshape(bmc.num_sims, bmc.raxis.n), int(steps)

@@ -110,14 +110,15 @@ class McgbBatchSim(C.Structure):
 
 
 class McgbBatchConfig(C.Structure):
-    _fields_ = [('num_sims', u32), ('packets_per_chunk', u32), ('block_size', u32),
+    _fields_ = [('num_sims', u32), ('packets_per_item', u32), ('block_size', u32),
                 ('blocks_per_sm', u32), ('num_bins', u32), ('math', i32),
-                ('r_max', f32), ('rmax', f32), ('seed', u64), ('deadline_s', C.c_double)]
+                ('inv_dr', f32), ('rmax', f32), ('seed', u64), ('deadline_s', C.c_double),
+                ('num_multipliers', u32), ('reserved', u32)]
 
 
 SIZEOF_KINDS = [McgbLayer, McgbSource, McgbDetector, McgbFluence, McgbTrace,
                 McgbMaterial, McgbMcmlConfig, McgbMcvoxConfig, McgbBuffers,
-                McgbRunOptions, McgbPf]
+                McgbRunOptions, McgbPf, McgbBatchSim, McgbBatchConfig]
 
 
 def check_layout(sizeof_fn):

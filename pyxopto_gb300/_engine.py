@@ -72,6 +72,9 @@ class McEngine:
         self._run_report = {'upload': None, 'download': None, 'execution': None,
                             'threads': None, 'items': None, 'steps': None}
         self._block_size = 0
+        self._deadline = 0.0
+        self._max_steps = 0
+        self._shard = (0, 1)
 
     # ------------------------------------------------ reference worker API
     def cl_allocate_rw_accumulator_buffer(self, owner, shape) -> int:
@@ -114,6 +117,32 @@ class McEngine:
 
     rmax = property(_get_rmax, _set_rmax, None, 'Radius beyond which packets are terminated (m).')
 
+    def _set_deadline(self, seconds):
+        self._deadline = max(0.0, float(seconds or 0.0))
+
+    deadline = property(lambda self: self._deadline, _set_deadline, None,
+                        'Device wall-clock limit of one run in seconds (0 = 300 s).  A run '
+                        'that reaches it stops, keeps its RNG states and raises McgbError '
+                        'with code E_TIMEOUT; the device stays usable.')
+
+    def _set_max_steps(self, n):
+        self._max_steps = max(0, int(n or 0))
+
+    max_steps_per_packet = property(lambda self: self._max_steps, _set_max_steps, None,
+                                    'Terminate a packet after this many steps (0 = no limit).')
+
+    def shard(self, rank: int, world: int):
+        """Use slice ``rank`` of a stream table ``world`` times larger than
+        one run needs: replicas on different GPUs then simulate disjoint
+        streams, and the sum of their integer tallies equals one run with
+        world x the streams (for packet counts divisible by the total
+        stream count)."""
+        if not (0 <= int(rank) < int(world)):
+            raise ValueError('rank must be in [0, world)')
+        self._shard = (int(rank), int(world))
+        self._num_streams = None
+        self._dev.pop('rng_x', None)
+
     def _resolved_options(self) -> Dict:
         return mcoptions.resolve(self._mc_options)
 
@@ -129,6 +158,8 @@ class McEngine:
         o.rmax = self._rmax
         o.track_optical_pathlength = int(bool(track_opl))
         o.block_size = self._block_size
+        o.deadline_s = self._deadline
+        o.max_steps_per_packet = self._max_steps
         return o
 
     def _lut_array(self) -> np.ndarray:
@@ -148,7 +179,11 @@ class McEngine:
         """(x, a) of the first n streams for this simulator's initializer."""
         if self._rnginit is None:
             self._rnginit = Random().initializer()
-        return Random().seeds(n, self._rnginit)
+        rank, world = self._shard
+        if world == 1:
+            return Random().seeds(n, self._rnginit)
+        x, a = Random().seeds(n * world, self._rnginit)
+        return x[rank * n:(rank + 1) * n].copy(), a[rank * n:(rank + 1) * n].copy()
 
     def _ensure_streams(self, torch, n: int, device):
         """Allocates and seeds n device streams once; their x states persist

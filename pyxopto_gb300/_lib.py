@@ -31,8 +31,9 @@ _SIGNATURES = {
     'mcgb_reduce_tallies': (C.c_int, [_vp, _vp, C.c_uint64]),
 }
 _OPTIONAL = {
-    'mcgb_batched_run': (C.c_int, [C.POINTER(_abi.McgbBatchConfig), _vp, _vp, _vp, _vp, _vp]),
+    'mcgb_batched_run': (C.c_int, [C.POINTER(_abi.McgbBatchConfig), _vp, _vp, _vp, _vp, _vp, _vp]),
     'mcgb_batched_occupancy': (C.c_int, [C.c_uint32, C.c_int, C.POINTER(C.c_uint32)]),
+    'mcgb_batched_work_size': (C.c_int, [C.c_uint32, C.POINTER(C.c_uint64)]),
     'mcgb_mlp_linear_fwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_linear_bwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                       C.c_int, C.c_int, C.c_int, C.c_int, _vp]),

@@ -1,0 +1,239 @@
+/*
+ * batched_kernel.cuh - thousands of independent single-layer simulations in
+ * one persistent, work-stealing launch.
+ *
+ * The packets of all simulations are numbered consecutively (simulation s
+ * owns [prefix[s], prefix[s+1])).  A work item is packets_per_item
+ * consecutive packets; a warp takes items from a device-wide counter and
+ * hands packets to its lanes one at a time: whenever lanes finish a packet,
+ * a warp ballot gives them the next packets of the current item, taking a
+ * new item when it runs out.  Lanes therefore stay busy until the last items
+ * are gone, whatever the spread of packet lengths between simulations.
+ *
+ * Each packet owns the MWC stream derived from (seed, s, k) (batch_rng.h),
+ * so the integer tallies are independent of the scheduling.  The physics of
+ * a packet is the layered kernel's albedo-weight loop (mcml_boundary,
+ * pf_sample, scatter_direction) on the simulation's three-layer table, with
+ * a normally incident Line source and a radial reflectance tally at the top
+ * surface; every simulation is statistically an mcml run of that shape.
+ */
+#pragma once
+#include "mc_device.cuh"
+#include "batch_rng.h"
+#include "mcml_kernel.cuh"
+
+namespace MCGB_NS {
+
+/* Per-simulation table in the scratch buffer. */
+struct __align__(16) BatchPrep {
+    MlLayer L[3];
+    float reflectance;      /* specular reflectance of the Line source */
+    float pad[3];
+};
+
+/* cos_critical / Fresnel at normal incidence in double precision, as the
+   host-side packing of the layered simulator computes them
+   (xopto/mcml/mclayer/layer.py:944-1007, mcutil/boundary.py:25-71). */
+static __device__ __forceinline__ double cc_d(double n1, double n2) {
+    return n1 > n2 ? sqrt(1.0 - (n2 / n1) * (n2 / n1)) : 0.0;
+}
+
+/* One block: packet prefix sums and the per-simulation layer tables. */
+__global__ void batch_prep_kernel(const McgbBatchSim *sims, uint32_t S, uint64_t *prefix,
+                                  BatchPrep *prep, unsigned long long *queue) {
+    __shared__ uint64_t part[1024];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t per = (S + nt - 1) / nt;
+    const uint32_t lo = tid * per, hi = min(S, lo + per);
+    uint64_t sum = 0;
+    for (uint32_t s = lo; s < hi; ++s) sum += sims[s].num_packets;
+    part[tid] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < nt; ++i) {
+            uint64_t v = part[i];
+            part[i] = run;
+            run += v;
+        }
+        prefix[S] = run;
+        *queue = 0ull;
+    }
+    __syncthreads();
+    uint64_t run = part[tid];
+    for (uint32_t s = lo; s < hi; ++s) {
+        prefix[s] = run;
+        run += sims[s].num_packets;
+    }
+    for (uint32_t s = tid; s < S; s += nt) {
+        const McgbBatchSim m = sims[s];
+        double mua = m.mua, mus = m.mus;
+        double mut = mua + mus;
+        float inv_mut = mut > 0.0 ? (float)(1.0 / mut) : __int_as_float(0x7f800000);
+        float mua_inv_mut = mus == 0.0 ? 1.0f : (float)(mua * (mut > 0.0 ? 1.0 / mut : 0.0));
+        float inf = __int_as_float(0x7f800000);
+        BatchPrep p;
+        McgbPf hg0 = {{0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, 0u, 0u, 0u};
+        McgbPf hg1 = {{m.g, 0.0f, 0.0f, 0.0f, 0.0f}, 0u, 0u, 0u};
+        p.L[0].g0 = make_float4(-inf, 0.0f, inf, 1.0f);
+        p.L[0].g1 = make_float4(m.n_above, 0.0f, 0.0f, 0.0f);
+        p.L[0].g2 = make_float4((float)cc_d(m.n_above, m.n), 0.0f, 0.0f, 0.0f);
+        pf_prepare(MCGB_PF_HG, hg0, p.L[0].pf0, p.L[0].pf1);
+        p.L[1].g0 = make_float4(0.0f, m.thickness, inv_mut, mua_inv_mut);
+        p.L[1].g1 = make_float4(m.n, m.mua, m.mus, (float)cc_d(m.n, m.n_above));
+        p.L[1].g2 = make_float4((float)cc_d(m.n, m.n_below), 0.0f, 0.0f, 0.0f);
+        pf_prepare(MCGB_PF_HG, hg1, p.L[1].pf0, p.L[1].pf1);
+        p.L[2].g0 = make_float4(m.thickness, inf, inf, 1.0f);
+        p.L[2].g1 = make_float4(m.n_below, 0.0f, 0.0f, (float)cc_d(m.n_below, m.n));
+        p.L[2].g2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        pf_prepare(MCGB_PF_HG, hg0, p.L[2].pf0, p.L[2].pf1);
+        double r = ((double)m.n_above - m.n) / ((double)m.n_above + m.n);
+        p.reflectance = (float)(r * r);
+        p.pad[0] = p.pad[1] = p.pad[2] = 0.0f;
+        prep[s] = p;
+    }
+}
+
+#define MCGB_FULL 0xffffffffu
+
+template <bool RMAX>
+__global__ void __launch_bounds__(256)
+batched_kernel(const McgbBatchConfig cfg, const uint32_t *__restrict__ mult,
+               const uint64_t *__restrict__ prefix, const BatchPrep *__restrict__ prep,
+               unsigned long long *queue, uint64_t *tally, uint64_t *counters, uint64_t deadline_ns) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t S = cfg.num_sims;
+    const uint64_t total = prefix[S];
+    const uint64_t B = cfg.packets_per_item;
+    const float inv_dr = cfg.inv_dr;
+    const int last_bin = (int)cfg.num_bins - 1;
+    const float rmax2 = cfg.rmax * cfg.rmax;
+    const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
+
+    uint64_t item_next = 0, item_end = 0;   /* warp-uniform */
+    bool more = true;                         /* warp-uniform */
+    bool active = false;
+    f3 pos{0.0f, 0.0f, 0.0f}, dir{0.0f, 0.0f, 1.0f};
+    float w = 0.0f;
+    int layer = 1;
+    uint32_t sim = 0;
+    Rng rng{0ull, 0u};
+    const MlLayer *L = prep[0].L;
+    uint64_t steps = 0, packets = 0;
+    uint32_t iter = 0, status = 0;
+
+    for (;;) {
+        /* refill idle lanes with the next packets of the warp's item */
+        uint32_t need = __ballot_sync(MCGB_FULL, !active);
+        while (need && more) {
+            if (item_next >= item_end) {
+                unsigned long long item = 0;
+                if (lane == 0) item = atomicAdd(queue, 1ull);
+                item = __shfl_sync(MCGB_FULL, item, 0);
+                item_next = (uint64_t)item * B;
+                if (item_next >= total) {
+                    more = false;
+                    break;
+                }
+                item_end = min(item_next + B, total);
+            }
+            uint32_t avail = (uint32_t)min(item_end - item_next, (uint64_t)32);
+            uint32_t rank = __popc(need & ((1u << lane) - 1u));
+            bool mine = ((need >> lane) & 1u) && rank < avail;
+            if (mine) {
+                uint64_t g = item_next + rank;
+                /* largest s with prefix[s] <= g (skips empty simulations) */
+                uint32_t lo = 0, hi = S;
+                while (lo < hi) {
+                    uint32_t mid = (lo + hi + 1u) >> 1;
+                    if (prefix[mid] <= g) lo = mid;
+                    else hi = mid - 1u;
+                }
+                sim = lo;
+                uint64_t x;
+                uint32_t a;
+                br_packet_stream(cfg.seed, sim, g - prefix[sim], mult, cfg.num_multipliers, &x, &a);
+                rng = Rng{x, a};
+                L = prep[sim].L;
+                /* Line source at normal incidence (xopto/mcml/mcsource/line.py:95-108) */
+                w = 1.0f - prep[sim].reflectance;
+                pos = f3{0.0f, 0.0f, 0.0f};
+                dir = f3{0.0f, 0.0f, 1.0f};
+                layer = 1;
+                active = true;
+            }
+            uint32_t taken = __ballot_sync(MCGB_FULL, mine);
+            item_next += __popc(taken);
+            need &= ~taken;
+        }
+        if (!__any_sync(MCGB_FULL, active)) break;
+
+        if (active) {
+            const float4 g0 = L[layer].g0;
+            ++steps;
+            float step = -mc_log(rng.next()) * g0.z;
+            step = fminf(step, FLT_MAX);
+            int next = layer;
+            if (pos.z + step * dir.z < g0.x) {
+                --next;
+                if (fabsf(dir.z) != 0.0f) step = mc_div(g0.x - pos.z, dir.z);
+            }
+            if (pos.z + step * dir.z >= g0.y) {
+                ++next;
+                if (fabsf(dir.z) != 0.0f) step = mc_div(g0.y - pos.z, dir.z);
+            }
+            pos.x = pos.x + dir.x * step;
+            pos.y = pos.y + dir.y * step;
+            pos.z = pos.z + dir.z * step;
+            if (layer < next) pos.z = g0.y;
+            if (layer > next) pos.z = g0.x;
+            bool done = false;
+            if (next != layer) {
+                mcml_boundary(L, layer, next, dir, rng);
+                if (!(layer > 0 && layer < 2)) {
+                    if (layer <= 0) {
+                        /* Radial detector, xopto/mcml/mcdetector/radial.py:117-150 */
+                        float r = mc_sqrt(pos.x * pos.x + pos.y * pos.y);
+                        int idx = clip_i(cvt_int(r * inv_dr), 0, last_bin);
+                        uint32_t wi = weight_to_u32(w, 1.0f);
+                        if (wi > 0) accu_add(tally, (uint64_t)sim * cfg.num_bins + idx, wi);
+                    }
+                    done = true;
+                }
+            } else {
+                float deposit = w * g0.w;
+                w -= deposit;
+                float az, ct = pf_sample<MCGB_PF_HG>(L[layer].pf0, L[layer].pf1, nullptr, rng, &az);
+                scatter_direction(dir, ct, az);
+                if (w < 1e-4f) {
+                    if (rng.next() > 0.1f) done = true;
+                    else w = mc_div(w, 0.1f);
+                }
+            }
+            if (RMAX && dot3(pos, pos) > rmax2) done = true;
+            if (done) {
+                active = false;
+                ++packets;
+            }
+        }
+        if (((++iter) & 1023u) == 0) {
+            uint32_t stop = 0;
+            if (lane == 0) {
+                if (globaltimer_ns() > t_deadline) stop = MCGB_STATUS_TIMEOUT;
+                else if (*(volatile uint64_t *)(counters + MCGB_CNT_ABORT)) stop = MCGB_STATUS_ABORTED;
+            }
+            stop = __shfl_sync(MCGB_FULL, stop, 0);
+            if (stop) {
+                status |= stop;
+                break;
+            }
+        }
+    }
+    atomicAdd((unsigned long long *)(counters + MCGB_CNT_STEPS), (unsigned long long)steps);
+    atomicAdd((unsigned long long *)(counters + MCGB_CNT_PACKETS), (unsigned long long)packets);
+    if (lane == 0) atomicAdd((unsigned long long *)(counters + MCGB_CNT_THREADS), 32ull);
+    if (status && lane == 0)
+        atomicOr((unsigned long long *)(counters + MCGB_CNT_STATUS), (unsigned long long)status);
+}
+
+}  // namespace MCGB_NS

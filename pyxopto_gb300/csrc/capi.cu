@@ -17,6 +17,7 @@
 #include <string>
 #include "../../include/xopto_gb300.h"
 #include "launch.h"
+#include "batch_launch.h"
 
 namespace {
 
@@ -171,6 +172,8 @@ int mcgb_sizeof(int kind) {
         case 8: return (int)sizeof(McgbBuffers);
         case 9: return (int)sizeof(McgbRunOptions);
         case 10: return (int)sizeof(McgbPf);
+        case 11: return (int)sizeof(McgbBatchSim);
+        case 12: return (int)sizeof(McgbBatchConfig);
         default: return -1;
     }
 }
@@ -268,6 +271,59 @@ int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream) {
     fill_u64_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(dev, n, value);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? MCGB_OK : cuda_fail(e, "fill launch");
+}
+
+int mcgb_batched_work_size(uint32_t num_sims, uint64_t *bytes) {
+    if (!bytes) return fail(MCGB_E_INVALID, "bytes is NULL");
+    *bytes = batch_work_bytes(num_sims);
+    return MCGB_OK;
+}
+
+int mcgb_batched_occupancy(uint32_t block_size, int math, uint32_t *blocks_per_sm) {
+    if (!blocks_per_sm) return fail(MCGB_E_INVALID, "blocks_per_sm is NULL");
+    int n = 0;
+    cudaError_t e = (math == MCGB_MATH_FAST) ? mcgb_fast_batch::batched_occupancy((int)block_size, &n)
+                                             : mcgb_exact_batch::batched_occupancy((int)block_size, &n);
+    if (e != cudaSuccess) return cuda_fail(e, "batched occupancy");
+    *blocks_per_sm = (uint32_t)n;
+    return MCGB_OK;
+}
+
+int mcgb_batched_run(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
+                     const uint32_t *dev_multipliers, uint64_t *dev_tally, void *dev_work,
+                     uint64_t *dev_counters, void *stream) {
+    if (!cfg) return fail(MCGB_E_INVALID, "cfg is NULL");
+    if (cfg->num_sims == 0) return MCGB_OK;
+    if (cfg->num_sims > (1u << 24)) return fail(MCGB_E_SIZE, "at most 2^24 simulations per batch");
+    if (!dev_sims || !dev_multipliers || !dev_tally || !dev_work || !dev_counters)
+        return fail(MCGB_E_INVALID, "NULL device buffer");
+    if (cfg->num_bins == 0) return fail(MCGB_E_INVALID, "num_bins must be positive");
+    if (cfg->num_multipliers < 1) return fail(MCGB_E_INVALID, "no RNG multipliers");
+    if (cfg->packets_per_item < 32) return fail(MCGB_E_INVALID, "packets_per_item must be >= 32");
+    if (cfg->math != MCGB_MATH_EXACT && cfg->math != MCGB_MATH_FAST)
+        return fail(MCGB_E_INVALID, "unknown math mode %d", cfg->math);
+    if (!(cfg->inv_dr >= 0.0f)) return fail(MCGB_E_INVALID, "inv_dr must be non-negative");
+    unsigned block = cfg->block_size ? cfg->block_size : 128;
+    if (block > 256 || block % 32) return fail(MCGB_E_INVALID, "block size must be a multiple of 32, <= 256");
+    if (((uintptr_t)dev_work) % 16) return fail(MCGB_E_INVALID, "work buffer must be 16-byte aligned");
+    int sms = 0, r = device_sm_count(&sms);
+    if (r) return r;
+    uint32_t bps = cfg->blocks_per_sm;
+    if (!bps) {
+        r = mcgb_batched_occupancy(block, cfg->math, &bps);
+        if (r) return r;
+        if (!bps) return fail(MCGB_E_INVALID, "block size %u does not fit an SM", block);
+    }
+    unsigned grid = (unsigned)sms * bps;
+    double d = cfg->deadline_s > 0.0 ? cfg->deadline_s : 300.0;
+    uint64_t deadline = (uint64_t)(d * 1e9);
+    cudaError_t e = (cfg->math == MCGB_MATH_FAST)
+        ? mcgb_fast_batch::launch_batched(*cfg, dev_sims, dev_multipliers, dev_tally, dev_work,
+                                          dev_counters, (cudaStream_t)stream, grid, block, deadline)
+        : mcgb_exact_batch::launch_batched(*cfg, dev_sims, dev_multipliers, dev_tally, dev_work,
+                                           dev_counters, (cudaStream_t)stream, grid, block, deadline);
+    if (e != cudaSuccess) return cuda_fail(e, "batched launch");
+    return MCGB_OK;
 }
 
 int mcgb_reduce_tallies(uint64_t *host_dst, const uint64_t *host_src, uint64_t n) {

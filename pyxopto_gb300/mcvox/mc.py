@@ -120,12 +120,15 @@ class Mc(McEngine):
         t1 = time.perf_counter()
         code, counters = self._launch(lib.mcgb_mcvox_run, cfg, buffers, torch)
         t2 = time.perf_counter()
+        self._run_report.update(status=counters[_abi.CNT_STATUS],
+                                packets_done=counters[_abi.CNT_PACKETS])
         _lib.check(code)
         results = self._download(nphotons, out)
         t3 = time.perf_counter()
         self._run_report.update(upload=t1 - t0, execution=t2 - t1, download=t3 - t2,
                                 threads=counters[_abi.CNT_THREADS], items=nphotons,
-                                steps=counters[_abi.CNT_STEPS])
+                                steps=counters[_abi.CNT_STEPS], status=counters[_abi.CNT_STATUS],
+                                packets_done=counters[_abi.CNT_PACKETS])
         if verbose:
             print('McKernel processed {:,d} packets in {:,d} threads in {:.3f} ms'.format(
                 nphotons, counters[_abi.CNT_THREADS], (t2 - t1) * 1e3))
