@@ -358,27 +358,51 @@ int mcgb_batched_run(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
 int mcgb_batched_occupancy(uint32_t block_size, int math, uint32_t *blocks_per_sm);
 
 /* ------------------------------------------------------ MLP surrogate */
-/* Linear layer forward: Y[M,N] = act(X[M,K] @ W[N,K]^T + b[N]) with BF16
-   X/W, FP32 accumulation, FP32 bias; Y stored as BF16 (act applied) and,
-   when dev_preact != NULL, the FP32 pre-activation for backward.
-   act: 0 = identity, 1 = GELU (tanh form).  Requires K % 16 == 0 and
-   N % 16 == 0 (pad the outer layers). */
-int mcgb_mlp_linear_fwd(const uint16_t *dev_x, const uint16_t *dev_w,
-                        const float *dev_b, uint16_t *dev_y, float *dev_preact,
-                        int m, int n, int k, int act, void *stream);
-/* Backward of the same layer given dY (BF16): dPre = dY * act'(pre);
-   dX[M,K] = dPre @ W (BF16 out, optional); dW[N,K] = dPre^T @ X (FP32,
-   accumulated); db[N] += sum_m dPre (FP32). */
-int mcgb_mlp_linear_bwd(const uint16_t *dev_x, const uint16_t *dev_w,
-                        const float *dev_preact, const uint16_t *dev_dy,
-                        uint16_t *dev_dx, float *dev_dw, float *dev_db,
-                        uint16_t *dev_dpre_scratch,
-                        int m, int n, int k, int act, void *stream);
-/* AdamW on FP32 master weights with BF16 shadow copy. */
-int mcgb_mlp_adamw(float *dev_w, uint16_t *dev_w_bf16, const float *dev_grad,
-                   float *dev_m, float *dev_v, uint64_t n, float lr,
-                   float beta1, float beta2, float eps, float weight_decay,
-                   int step, void *stream);
+/* Kernels of the radial-reflectance surrogate (a small MLP).  Matrices are
+   row-major; bf16 values are passed as uint16_t bit patterns; every GEMM
+   accumulates in FP32 on the tensor cores.  Requirements: M % 8 == 0,
+   N % 16 == 0, K % 16 == 0 (pad the narrow input and output layers).
+   act: 0 = identity, 1 = GELU (tanh form). */
+
+/* Y[M,N] = act(X[M,K] W[N,K]^T + b[N]) stored as bf16; when pre != NULL the
+   FP32 pre-activation is stored as well (for the backward pass). */
+int mcgb_mlp_linear_fwd(const uint16_t *dev_x, const uint16_t *dev_w, const float *dev_b,
+                        uint16_t *dev_y, float *dev_pre, int m, int n, int k, int act,
+                        void *stream);
+
+/* dPre[M,N] = dY[M,N] * act'(pre) (bf16) and db[N] = sum over rows of dPre
+   (FP32, overwritten, summed in a fixed order through dev_scratch of
+   mcgb_mlp_act_bwd_scratch(m, n) floats). */
+int mcgb_mlp_act_bwd(const uint16_t *dev_dy, const float *dev_pre, uint16_t *dev_dpre,
+                     float *dev_db, float *dev_scratch, int m, int n, int act, void *stream);
+uint64_t mcgb_mlp_act_bwd_scratch(int m, int n);
+
+/* dX[M,K] = dPre[M,N] W[N,K], with the weight given transposed as
+   Wt[K,N] (the optimizer keeps both copies). */
+int mcgb_mlp_linear_bwd_input(const uint16_t *dev_dpre, const uint16_t *dev_wt,
+                              uint16_t *dev_dx, int m, int n, int k, void *stream);
+
+/* dW[N,K] = dPre[M,N]^T X[M,K] (FP32, overwritten).  The rows are split
+   into fixed slices whose partial sums go to dev_scratch and are added in
+   a fixed order, so the result is deterministic; dev_scratch holds
+   mcgb_mlp_bwd_weight_scratch(m, n, k) floats. */
+int mcgb_mlp_linear_bwd_weight(const uint16_t *dev_dpre, const uint16_t *dev_x, float *dev_dw,
+                               float *dev_scratch, int m, int n, int k, void *stream);
+uint64_t mcgb_mlp_bwd_weight_scratch(int m, int n, int k);
+
+/* Mean-squared-error gradient on the first n_valid of N columns:
+   dY = 2*(Y - T)/(M*n_valid) (bf16), other columns 0; the per-block loss
+   partial sums go to dev_loss[ceil(M/256)]. */
+int mcgb_mlp_mse_grad(const uint16_t *dev_y, const float *dev_t, uint16_t *dev_dy,
+                      float *dev_loss, int m, int n, int n_valid, void *stream);
+
+/* AdamW on FP32 master weights w[rows*cols] (decoupled weight decay); also
+   writes the bf16 copy w_bf16[rows,cols] and, when wt_bf16 != NULL, the
+   transposed bf16 copy wt_bf16[cols,rows].  step counts from 1. */
+int mcgb_mlp_adamw(float *dev_w, uint16_t *dev_w_bf16, uint16_t *dev_wt_bf16,
+                   const float *dev_grad, float *dev_m, float *dev_v, int rows, int cols,
+                   float lr, float beta1, float beta2, float eps, float weight_decay, int step,
+                   void *stream);
 
 #ifdef __cplusplus
 }

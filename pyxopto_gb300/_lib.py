@@ -35,10 +35,14 @@ _OPTIONAL = {
     'mcgb_batched_occupancy': (C.c_int, [C.c_uint32, C.c_int, C.POINTER(C.c_uint32)]),
     'mcgb_batched_work_size': (C.c_int, [C.c_uint32, C.POINTER(C.c_uint64)]),
     'mcgb_mlp_linear_fwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
-    'mcgb_mlp_linear_bwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                      C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
-    'mcgb_mlp_adamw': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_uint64, C.c_float, C.c_float,
-                                 C.c_float, C.c_float, C.c_float, C.c_int, _vp]),
+    'mcgb_mlp_act_bwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    'mcgb_mlp_act_bwd_scratch': (C.c_uint64, [C.c_int, C.c_int]),
+    'mcgb_mlp_linear_bwd_input': (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    'mcgb_mlp_linear_bwd_weight': (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    'mcgb_mlp_bwd_weight_scratch': (C.c_uint64, [C.c_int, C.c_int, C.c_int]),
+    'mcgb_mlp_mse_grad': (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    'mcgb_mlp_adamw': (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_float,
+                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, _vp]),
     'mcgb_mcml_run_noalloc': (C.c_int, [C.POINTER(_abi.McgbMcmlConfig), C.POINTER(_abi.McgbBuffers), _vp]),
 }
 

@@ -17,6 +17,7 @@
 #include <string>
 #include "../../include/xopto_gb300.h"
 #include "launch.h"
+#include "errors.h"
 #include "batch_launch.h"
 
 namespace {
@@ -152,6 +153,13 @@ __global__ void fill_u64_kernel(uint64_t *p, uint64_t n, uint64_t v) {
 }
 
 }  // namespace
+
+namespace mcgb_internal {
+int set_error(int code, const char *msg) {
+    g_last_error = msg;
+    return code;
+}
+}  // namespace mcgb_internal
 
 extern "C" {
 

@@ -1,0 +1,350 @@
+/*
+ * mlp.cu - training and inference kernels of the radial-reflectance MLP
+ * surrogate: BF16 tensor-core GEMMs with FP32 accumulation and fused
+ * epilogues (bias + GELU forward; input and weight gradients), the GELU
+ * backward with a deterministic bias-gradient reduction, the MSE gradient
+ * and AdamW.
+ *
+ * GEMM: C[R, Cc] = sum_l A(r, l) B(c, l) on 64x64 output tiles, 4 warps of
+ * 32x32, k-steps of 16 through mma.sync m16n8k16 (bf16 x bf16 -> f32).
+ * Operands are staged in shared memory with the reduction index contiguous;
+ * transposed operands (activations in the weight gradient) are transposed
+ * while staging.  The weight gradient splits the batch rows into fixed
+ * slices and adds the slice results in a fixed order (deterministic).
+ *
+ * The layers of the surrogate are 256 wide and its batches 64k rows, small
+ * GEMMs whose time is dominated by launch and epilogue work; the warp-level
+ * mma.sync path keeps them simple.
+ */
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdarg>
+#include <string>
+#include "../../include/xopto_gb300.h"
+#include "errors.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int BM = 64, BN = 64, BK = 16, PAD = 8, NT = 128;
+
+enum { EPI_FWD = 0, EPI_BF16 = 1, EPI_F32 = 2 };
+
+__device__ __forceinline__ float gelu(float x) {
+    const float c = 0.7978845608028654f;   /* sqrt(2/pi) */
+    float t = tanhf(c * (x + 0.044715f * x * x * x));
+    return 0.5f * x * (1.0f + t);
+}
+
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float c = 0.7978845608028654f;
+    float u = c * (x + 0.044715f * x * x * x);
+    float t = tanhf(u);
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * 0.044715f * x * x);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+/* Stage a 64 x 16 tile of op(X) (rows r0.., reduction l0..) into S[row][l].
+   X(r, l) = TR ? X[l*ld + r] : X[r*ld + l].  Rows >= R are zero. */
+template <bool TR>
+__device__ __forceinline__ void stage(bf16 (*S)[BK + PAD], const bf16 *X, int ld, int R, int L,
+                                      int r0, int l0) {
+    const int t = threadIdx.x;
+    if (!TR) {
+        int row = t >> 1, col = (t & 1) * 8;
+        int r = r0 + row;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (r < R && l0 + col + 8 <= L) v = *reinterpret_cast<const uint4 *>(X + (size_t)r * ld + l0 + col);
+        *reinterpret_cast<uint4 *>(&S[row][col]) = v;
+    } else {
+        int l = t >> 3, rc = (t & 7) * 8;
+        int r = r0 + rc;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (r + 8 <= R && l0 + l < L) v = *reinterpret_cast<const uint4 *>(X + (size_t)(l0 + l) * ld + r);
+        const bf16 *e = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) S[rc + i][l] = e[i];
+    }
+}
+
+/* C = op(A) op(B)^T over the reduction range of blockIdx.z's slice. */
+template <bool TA, bool TB, int EPI>
+__global__ void __launch_bounds__(NT)
+gemm_bf16(const bf16 *__restrict__ A, int lda, const bf16 *__restrict__ B, int ldb, int R, int Cc,
+          int L, int l_slice, const float *__restrict__ bias, int act, bf16 *Cb, float *Cf,
+          float *pre, int ldc) {
+    __shared__ __align__(16) bf16 As[BM][BK + PAD];
+    __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
+    const int r0 = blockIdx.y * BM, c0 = blockIdx.x * BN;
+    const int lb = blockIdx.z * l_slice;
+    const int le = min(L, lb + l_slice);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, tig = lane & 3;
+    const int wr = (warp >> 1) * 32, wc = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0f;
+
+    for (int l0 = lb; l0 < le; l0 += BK) {
+        stage<TA>(As, A, lda, R, le, r0, l0);
+        stage<TB>(Bs, B, ldb, Cc, le, c0, l0);
+        __syncthreads();
+        uint32_t a[2][4], b[4][2];
+#pragma unroll
+        for (int mi = 0; mi < 2; ++mi) {
+            int rb = wr + mi * 16;
+            a[mi][0] = *reinterpret_cast<const uint32_t *>(&As[rb + g][tig * 2]);
+            a[mi][1] = *reinterpret_cast<const uint32_t *>(&As[rb + g + 8][tig * 2]);
+            a[mi][2] = *reinterpret_cast<const uint32_t *>(&As[rb + g][tig * 2 + 8]);
+            a[mi][3] = *reinterpret_cast<const uint32_t *>(&As[rb + g + 8][tig * 2 + 8]);
+        }
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) {
+            int cb = wc + ni * 8;
+            b[ni][0] = *reinterpret_cast<const uint32_t *>(&Bs[cb + g][tig * 2]);
+            b[ni][1] = *reinterpret_cast<const uint32_t *>(&Bs[cb + g][tig * 2 + 8]);
+        }
+#pragma unroll
+        for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], a[mi], b[ni]);
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int r = r0 + wr + mi * 16 + g + (q >> 1) * 8;
+                int c = c0 + wc + ni * 8 + tig * 2 + (q & 1);
+                if (r >= R || c >= Cc) continue;
+                float v = acc[mi][ni][q];
+                size_t o = (size_t)r * ldc + c;
+                if (EPI == EPI_FWD) {
+                    v += bias ? bias[c] : 0.0f;
+                    if (pre) pre[o] = v;
+                    Cb[o] = __float2bfloat16_rn(act ? gelu(v) : v);
+                } else if (EPI == EPI_BF16) {
+                    Cb[o] = __float2bfloat16_rn(v);
+                } else {
+                    Cf[(size_t)blockIdx.z * R * ldc + o] = v;
+                }
+            }
+}
+
+/* dW = sum of the slice partials in slice order. */
+__global__ void sum_slices(const float *__restrict__ part, float *out, int slices, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int z = 0; z < slices; ++z) s += part[(size_t)z * n + i];
+        out[i] = s;
+    }
+}
+
+/* dPre = dY * act'(pre); column partial sums of dPre over row chunks of 256. */
+__global__ void act_bwd_kernel(const bf16 *__restrict__ dy, const float *__restrict__ pre, bf16 *dpre,
+                               float *part, int M, int N, int act) {
+    const int c = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int rbeg = blockIdx.y * 256;
+    const int rend = min(M, rbeg + 256);
+    __shared__ float red[8][33];
+    float s = 0.0f;
+    if (c < N) {
+        for (int r = rbeg + (threadIdx.x >> 5); r < rend; r += 8) {
+            size_t o = (size_t)r * N + c;
+            float v = __bfloat162float(dy[o]);
+            if (act) v *= gelu_grad(pre[o]);
+            dpre[o] = __float2bfloat16_rn(v);
+            s += v;
+        }
+    }
+    red[threadIdx.x >> 5][threadIdx.x & 31] = s;
+    __syncthreads();
+    if (threadIdx.x < 32 && c < N) {
+        float t = 0.0f;
+        for (int i = 0; i < 8; ++i) t += red[i][threadIdx.x];
+        part[(size_t)blockIdx.y * N + c] = t;
+    }
+}
+
+__global__ void mse_grad_kernel(const bf16 *__restrict__ y, const float *__restrict__ tgt, bf16 *dy,
+                                float *loss, int M, int N, int nv) {
+    __shared__ float red[256];
+    const float scale = 1.0f / ((float)M * (float)nv);
+    float s = 0.0f;
+    size_t base = (size_t)blockIdx.x * 256;
+    for (int i = threadIdx.x; i < 256 * N; i += blockDim.x) {
+        size_t r = base + i / N;
+        int c = i % N;
+        if (r >= (size_t)M) continue;
+        size_t o = r * N + c;
+        float d = 0.0f;
+        if (c < nv) {
+            d = __bfloat162float(y[o]) - tgt[o];
+            s += d * d * scale;
+        }
+        dy[o] = __float2bfloat16_rn(2.0f * d * scale);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) loss[blockIdx.x] = red[0];
+}
+
+__global__ void adamw_kernel(float *w, bf16 *wb, bf16 *wt, const float *__restrict__ gr, float *m, float *v,
+                             int rows, int cols, float lr, float b1, float b2, float eps, float wd,
+                             float c1, float c2) {
+    size_t n = (size_t)rows * cols;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float g = gr[i];
+        float mi = b1 * m[i] + (1.0f - b1) * g;
+        float vi = b2 * v[i] + (1.0f - b2) * g * g;
+        m[i] = mi;
+        v[i] = vi;
+        float upd = (mi / c1) / (sqrtf(vi / c2) + eps);
+        float wi = w[i] - lr * (upd + wd * w[i]);
+        w[i] = wi;
+        bf16 h = __float2bfloat16_rn(wi);
+        wb[i] = h;
+        if (wt) {
+            size_t r = i / cols, c = i % cols;
+            wt[c * rows + r] = h;
+        }
+    }
+}
+
+int fail(int code, const char *fmt, ...) {
+    char buf[256];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    return mcgb_internal::set_error(code, buf);
+}
+
+int check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(MCGB_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return MCGB_OK;
+}
+
+int shape_ok(int m, int n, int k) {
+    if (m <= 0 || n <= 0 || k <= 0) return fail(MCGB_E_INVALID, "MLP shapes must be positive");
+    if (m % 8 || n % 16 || k % 16) return fail(MCGB_E_INVALID, "MLP shapes need M%%8, N%%16, K%%16 == 0");
+    return MCGB_OK;
+}
+
+int weight_slices(int m) {
+    int s = (m + 2047) / 2048;
+    return s < 1 ? 1 : (s > 32 ? 32 : s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcgb_mlp_linear_fwd(const uint16_t *x, const uint16_t *w, const float *b, uint16_t *y, float *pre,
+                        int m, int n, int k, int act, void *stream) {
+    int r = shape_ok(m, n, k);
+    if (r) return r;
+    if (!x || !w || !y) return fail(MCGB_E_INVALID, "NULL operand");
+    dim3 grid((n + BN - 1) / BN, (m + BM - 1) / BM, 1);
+    gemm_bf16<false, false, EPI_FWD><<<grid, NT, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)x, k, (const bf16 *)w, k, m, n, k, k, b, act, (bf16 *)y, nullptr, pre, n);
+    return check_launch("mlp forward");
+}
+
+uint64_t mcgb_mlp_bwd_weight_scratch(int m, int n, int k) {
+    return (uint64_t)weight_slices(m) * (uint64_t)n * (uint64_t)k;
+}
+
+int mcgb_mlp_linear_bwd_input(const uint16_t *dpre, const uint16_t *wt, uint16_t *dx, int m, int n, int k,
+                              void *stream) {
+    int r = shape_ok(m, n, k);
+    if (r) return r;
+    if (!dpre || !wt || !dx) return fail(MCGB_E_INVALID, "NULL operand");
+    /* dX[m,k] = sum_n dPre[m,n] Wt[k,n] */
+    dim3 grid((k + BN - 1) / BN, (m + BM - 1) / BM, 1);
+    gemm_bf16<false, false, EPI_BF16><<<grid, NT, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)dpre, n, (const bf16 *)wt, n, m, k, n, n, nullptr, 0, (bf16 *)dx, nullptr, nullptr, k);
+    return check_launch("mlp backward input");
+}
+
+int mcgb_mlp_linear_bwd_weight(const uint16_t *dpre, const uint16_t *x, float *dw, float *scratch,
+                               int m, int n, int k, void *stream) {
+    int r = shape_ok(m, n, k);
+    if (r) return r;
+    if (!dpre || !x || !dw || !scratch) return fail(MCGB_E_INVALID, "NULL operand");
+    /* dW[n,k] = sum_m dPre[m,n] X[m,k]: R = n, Cc = k, reduction over m */
+    int slices = weight_slices(m);
+    int per = ((m + slices - 1) / slices + BK - 1) / BK * BK;
+    slices = (m + per - 1) / per;
+    dim3 grid((k + BN - 1) / BN, (n + BM - 1) / BM, slices);
+    gemm_bf16<true, true, EPI_F32><<<grid, NT, 0, (cudaStream_t)stream>>>(
+        (const bf16 *)dpre, n, (const bf16 *)x, k, n, k, m, per, nullptr, 0, nullptr, scratch, nullptr, k);
+    r = check_launch("mlp backward weight");
+    if (r) return r;
+    size_t total = (size_t)n * k;
+    unsigned blocks = (unsigned)((total + 255) / 256);
+    sum_slices<<<blocks, 256, 0, (cudaStream_t)stream>>>(scratch, dw, slices, total);
+    return check_launch("mlp weight slice sum");
+}
+
+uint64_t mcgb_mlp_act_bwd_scratch(int m, int n) { return (uint64_t)((m + 255) / 256) * (uint64_t)n; }
+
+int mcgb_mlp_act_bwd(const uint16_t *dy, const float *pre, uint16_t *dpre, float *db, float *scratch,
+                      int m, int n, int act, void *stream) {
+    if (m <= 0 || n <= 0 || !dy || !dpre || !db || !scratch || (act && !pre))
+        return fail(MCGB_E_INVALID, "bad act_bwd arguments");
+    dim3 grid((n + 31) / 32, (m + 255) / 256);
+    act_bwd_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const bf16 *)dy, pre, (bf16 *)dpre, scratch,
+                                                          m, n, act);
+    int r = check_launch("mlp activation backward");
+    if (r) return r;
+    int chunks = (m + 255) / 256;
+    sum_slices<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(scratch, db, chunks, (size_t)n);
+    return check_launch("mlp bias gradient");
+}
+
+int mcgb_mlp_mse_grad(const uint16_t *y, const float *t, uint16_t *dy, float *loss, int m, int n, int nv,
+                      void *stream) {
+    if (m <= 0 || n <= 0 || nv <= 0 || nv > n || !y || !t || !dy || !loss)
+        return fail(MCGB_E_INVALID, "bad mse_grad arguments");
+    mse_grad_kernel<<<(m + 255) / 256, 256, 0, (cudaStream_t)stream>>>((const bf16 *)y, t, (bf16 *)dy, loss,
+                                                                      m, n, nv);
+    return check_launch("mlp mse gradient");
+}
+
+int mcgb_mlp_adamw(float *w, uint16_t *wb, uint16_t *wt, const float *g, float *m, float *v, int rows,
+                   int cols, float lr, float b1, float b2, float eps, float wd, int step, void *stream) {
+    if (!w || !wb || !g || !m || !v || rows <= 0 || cols <= 0 || step < 1)
+        return fail(MCGB_E_INVALID, "bad adamw arguments");
+    float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    size_t n = (size_t)rows * cols;
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    adamw_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(w, (bf16 *)wb, (bf16 *)wt, g, m, v, rows, cols, lr,
+                                                           b1, b2, eps, wd, c1, c2);
+    return check_launch("mlp adamw");
+}
+
+}  // extern "C"

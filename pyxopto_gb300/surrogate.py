@@ -1,0 +1,281 @@
+"""Learned surrogate of radial reflectance profiles, trained on the GPU by
+the library's own BF16 kernels, with Monte Carlo kept as judge and
+fallback.
+
+Network: (log mua, log mus', g, n) -> 256 -> 256 -> 256 -> 30 bins of
+log10 radial reflectance, GELU activations, BF16 weights and activations,
+FP32 accumulation and FP32 master weights updated by AdamW.  The narrow input
+and output layers are zero-padded to 16 and 32 columns for the tensor-core
+tiles.  Training profiles come from the batched engine (BatchedMc).
+
+Serving: a batch of queries is answered by the network; a fixed fraction of
+the queries (1 % by default) is re-simulated with the batched engine as the
+judge, and every judged query whose relative RMS error exceeds the tolerance
+is replaced by its Monte Carlo profile.  If more than ``max_fail`` of the
+judged queries fail, the whole batch falls back to Monte Carlo.
+"""
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib
+from .batched import BatchedMc
+from .mcbase.mcutil import Axis
+
+RANGES = {'log_mua': (np.log(1.0), np.log(1000.0)), 'log_musr': (np.log(500.0), np.log(5000.0)),
+          'g': (0.6, 0.95), 'n': (1.33, 1.5)}
+IN_PAD, OUT_PAD = 16, 32
+
+
+def features(mua, musr, g, n):
+    """Normalised network input [M, 16] (4 used columns, zero padding)."""
+    cols = [np.log(np.asarray(mua, np.float64)), np.log(np.asarray(musr, np.float64)),
+            np.asarray(g, np.float64), np.asarray(n, np.float64)]
+    keys = ['log_mua', 'log_musr', 'g', 'n']
+    x = np.zeros((len(cols[0]), IN_PAD), dtype=np.float32)
+    for i, (c, k) in enumerate(zip(cols, keys)):
+        lo, hi = RANGES[k]
+        x[:, i] = (c - lo) / (hi - lo) * 2.0 - 1.0
+    return x
+
+
+class Mlp:
+    """Parameters and buffers of the MLP on the GPU (torch memory, library
+    kernels)."""
+
+    def __init__(self, sizes=(4, 256, 256, 256, 30), seed=0, batch=4096):
+        import torch
+        self.torch = torch
+        self.lib = _lib.load()
+        self.sizes = list(sizes)
+        self.pads = [IN_PAD] + list(sizes[1:-1]) + [OUT_PAD]
+        self.acts = [1] * (len(sizes) - 2) + [0]
+        rng = np.random.default_rng(seed)
+        dev = 'cuda'
+        self.w, self.b, self.wb, self.wt, self.m, self.v, self.mb, self.vb = ([] for _ in range(8))
+        self.bb = []
+        for i in range(len(sizes) - 1):
+            k, n = self.pads[i], self.pads[i + 1]
+            w = np.zeros((n, k), np.float32)
+            lim = np.sqrt(6.0 / (sizes[i] + sizes[i + 1]))
+            w[:sizes[i + 1], :sizes[i]] = rng.uniform(-lim, lim, (sizes[i + 1], sizes[i]))
+            self.w.append(torch.from_numpy(w).to(dev))
+            self.b.append(torch.zeros((n,), dtype=torch.float32, device=dev))
+            self.wb.append(torch.empty((n, k), dtype=torch.bfloat16, device=dev))
+            self.wt.append(torch.empty((k, n), dtype=torch.bfloat16, device=dev))
+            self.m.append(torch.zeros_like(self.w[-1]))
+            self.v.append(torch.zeros_like(self.w[-1]))
+            self.mb.append(torch.zeros_like(self.b[-1]))
+            self.vb.append(torch.zeros_like(self.b[-1]))
+            self.bb.append(torch.empty((n,), dtype=torch.bfloat16, device=dev))
+        self.step_count = 0
+        self.sync_copies()
+        self._alloc(batch)
+
+    def sync_copies(self):
+        for i in range(len(self.w)):
+            self.wb[i].copy_(self.w[i].to(self.torch.bfloat16))
+            self.wt[i].copy_(self.w[i].t().contiguous().to(self.torch.bfloat16))
+
+    def _alloc(self, batch):
+        torch = self.torch
+        self.batch = batch
+        self.h = [torch.empty((batch, p), dtype=torch.bfloat16, device='cuda') for p in self.pads]
+        self.pre = [torch.empty((batch, p), dtype=torch.float32, device='cuda') for p in self.pads[1:]]
+        self.grad_h = [torch.empty((batch, p), dtype=torch.bfloat16, device='cuda') for p in self.pads]
+        self.dpre = [torch.empty((batch, p), dtype=torch.bfloat16, device='cuda') for p in self.pads[1:]]
+        self.dw = [torch.empty_like(w) for w in self.w]
+        self.db = [torch.empty_like(b) for b in self.b]
+        nscr = 0
+        for i in range(len(self.w)):
+            nscr = max(nscr, int(self.lib.mcgb_mlp_bwd_weight_scratch(batch, self.pads[i + 1], self.pads[i])),
+                       int(self.lib.mcgb_mlp_act_bwd_scratch(batch, self.pads[i + 1])))
+        self.scratch = torch.empty((max(nscr, 1),), dtype=torch.float32, device='cuda')
+        self.loss_part = torch.empty(((batch + 255) // 256,), dtype=torch.float32, device='cuda')
+
+    @staticmethod
+    def _p(t):
+        return C.c_void_p(t.data_ptr()) if t is not None else None
+
+    def _stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def forward(self, x_bf16, store=True):
+        """x_bf16: [M, 16] bf16 tensor with M <= batch.  Returns the bf16
+        output view [M, 32]."""
+        m = x_bf16.shape[0]
+        if m > self.batch:
+            self._alloc(m)
+        self.h[0][:m].copy_(x_bf16)
+        for i in range(len(self.w)):
+            k, n = self.pads[i], self.pads[i + 1]
+            _lib.check(self.lib.mcgb_mlp_linear_fwd(
+                self._p(self.h[i]), self._p(self.wb[i]), self._p(self.b[i]), self._p(self.h[i + 1]),
+                self._p(self.pre[i]) if store else None, m, n, k, self.acts[i], self._stream()))
+        return self.h[-1][:m]
+
+    def backward(self, dy_bf16, m):
+        """Gradients of every layer for the last forward pass of m rows."""
+        g = dy_bf16
+        for i in range(len(self.w) - 1, -1, -1):
+            k, n = self.pads[i], self.pads[i + 1]
+            _lib.check(self.lib.mcgb_mlp_act_bwd(self._p(g), self._p(self.pre[i]), self._p(self.dpre[i]),
+                                                 self._p(self.db[i]), self._p(self.scratch), m, n,
+                                                 self.acts[i], self._stream()))
+            _lib.check(self.lib.mcgb_mlp_linear_bwd_weight(self._p(self.dpre[i]), self._p(self.h[i]),
+                                                           self._p(self.dw[i]), self._p(self.scratch),
+                                                           m, n, k, self._stream()))
+            if i > 0:
+                _lib.check(self.lib.mcgb_mlp_linear_bwd_input(self._p(self.dpre[i]), self._p(self.wt[i]),
+                                                              self._p(self.grad_h[i]), m, n, k,
+                                                              self._stream()))
+                g = self.grad_h[i]
+        return self.dw, self.db
+
+    def mse_grad(self, y, t_f32, m, n_valid):
+        dy = self.grad_h[-1]
+        _lib.check(self.lib.mcgb_mlp_mse_grad(self._p(y), self._p(t_f32), self._p(dy), self._p(self.loss_part),
+                                              m, self.pads[-1], n_valid, self._stream()))
+        return dy
+
+    def adamw(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        self.step_count += 1
+        for i in range(len(self.w)):
+            n, k = self.w[i].shape
+            _lib.check(self.lib.mcgb_mlp_adamw(self._p(self.w[i]), self._p(self.wb[i]), self._p(self.wt[i]),
+                                               self._p(self.dw[i]), self._p(self.m[i]), self._p(self.v[i]),
+                                               n, k, lr, b1, b2, eps, wd, self.step_count, self._stream()))
+            _lib.check(self.lib.mcgb_mlp_adamw(self._p(self.b[i]), self._p(self.bb[i]), None,
+                                               self._p(self.db[i]), self._p(self.mb[i]), self._p(self.vb[i]),
+                                               1, n, lr, b1, b2, eps, 0.0, self.step_count, self._stream()))
+
+    def train_step(self, x_bf16, t_f32, n_valid, lr):
+        m = x_bf16.shape[0]
+        y = self.forward(x_bf16, store=True)
+        dy = self.mse_grad(y, t_f32, m, n_valid)
+        self.backward(dy, m)
+        self.adamw(lr=lr)
+        return self.loss_part[:(m + 255) // 256]
+
+
+class Surrogate:
+    """Radial reflectance surrogate for the batched single-layer family."""
+
+    def __init__(self, raxis: Axis = None, floor: float = 1e-2, seed: int = 0):
+        self.raxis = raxis if raxis is not None else Axis(0.0, 3e-3, 30)
+        self.floor = float(floor)
+        self.seed = seed
+        self.mlp = None
+        self.mu = self.sd = None
+        self.report = {}
+
+    # -------------------------------------------------------- data
+    def simulate(self, sims, fast=True, seed=1):
+        """Monte Carlo reflectance profiles of a dict of simulations."""
+        b = BatchedMc(sims, raxis=self.raxis, fast=fast, seed=seed)
+        return b.run()
+
+    def targets(self, refl):
+        return np.log10(np.maximum(refl, 0.0) + self.floor)
+
+    def fit(self, sims, refl, epochs=40, batch=4096, lr=2e-3, lr_min=5e-5, verbose=False):
+        """Trains the network on (sims, reflectance) for ``epochs`` passes."""
+        import torch
+        x = features(sims['mua'], sims['mus'] * (1.0 - np.asarray(sims['g'])), sims['g'], sims['n'])
+        y = self.targets(refl)
+        self.mu, self.sd = y.mean(0), y.std(0) + 1e-6
+        t = np.zeros((len(x), OUT_PAD), np.float32)
+        t[:, :y.shape[1]] = (y - self.mu) / self.sd
+        nb = self.raxis.n
+        if self.mlp is None:
+            self.mlp = Mlp(sizes=(4, 256, 256, 256, nb), seed=self.seed, batch=batch)
+        xd = torch.from_numpy(x).cuda().to(torch.bfloat16)
+        td = torch.from_numpy(t).cuda()
+        n = (len(x) // 8) * 8
+        rng = np.random.default_rng(self.seed)
+        steps = epochs * max(1, n // batch)
+        hist = []
+        t0 = time.perf_counter()
+        k = 0
+        for ep in range(epochs):
+            perm = torch.from_numpy(rng.permutation(len(x))[:n]).cuda()
+            for s in range(0, n - batch + 1, batch):
+                idx = perm[s:s + batch]
+                lr_k = lr_min + 0.5 * (lr - lr_min) * (1 + np.cos(np.pi * k / steps))
+                lp = self.mlp.train_step(xd[idx], td[idx], nb, lr_k)
+                k += 1
+            hist.append(float(lp.sum().item()))
+            if verbose:
+                print('epoch', ep, hist[-1])
+        torch.cuda.synchronize()
+        self.report['train_seconds'] = time.perf_counter() - t0
+        self.report['train_steps'] = k
+        self.report['loss'] = hist
+        return hist
+
+    def predict(self, mua, musr, g, n):
+        """Reflectance profiles [M, bins] for the given optical properties."""
+        import torch
+        x = features(mua, musr, g, n)
+        m = len(x)
+        mp = (m + 7) // 8 * 8
+        xp = np.zeros((mp, IN_PAD), np.float32)
+        xp[:m] = x
+        xd = torch.from_numpy(xp).cuda().to(torch.bfloat16)
+        out = []
+        for s in range(0, mp, self.mlp.batch):
+            y = self.mlp.forward(xd[s:s + self.mlp.batch], store=False)
+            out.append(y[:, :self.raxis.n].float().cpu().numpy())
+        y = np.concatenate(out)[:m] * self.sd + self.mu
+        return np.maximum(10.0 ** y - self.floor, 0.0)
+
+    @staticmethod
+    def rms_rel(pred, ref, mask=None):
+        rel = (pred - ref) / np.where(ref > 0, ref, 1.0)
+        if mask is not None:
+            rel = np.where(mask, rel, 0.0)
+            return np.sqrt((rel ** 2).sum(1) / np.maximum(mask.sum(1), 1))
+        return np.sqrt((rel ** 2).mean(1))
+
+    def serve(self, sims, judge_fraction=0.01, judge_packets=1_000_000, tol=0.01, max_fail=0.1,
+              seed=7, rel_floor=None):
+        """Answers a batch of queries: network prediction for all, Monte Carlo
+        judge on a fraction, MC fallback where the judge disagrees by more
+        than ``tol`` (relative RMS over the bins above ``rel_floor`` of the
+        profile peak).  Returns (profiles, report)."""
+        import torch
+        m = len(sims['mua'])
+        t0 = time.perf_counter()
+        musr = np.asarray(sims['mus']) * (1.0 - np.asarray(sims['g']))
+        pred = self.predict(sims['mua'], musr, sims['g'], sims['n'])
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        rng = np.random.default_rng(seed)
+        nj = max(1, int(round(judge_fraction * m)))
+        jidx = np.sort(rng.choice(m, nj, replace=False))
+        jsims = {k: np.asarray(v)[jidx] for k, v in sims.items()}
+        jsims['num_packets'] = np.full(nj, judge_packets, dtype=np.uint64)
+        mc = self.simulate(jsims, seed=seed)
+        t2 = time.perf_counter()
+        mask = None
+        if rel_floor is not None:
+            mask = mc >= rel_floor * mc.max(1, keepdims=True)
+        err = self.rms_rel(pred[jidx], mc, mask)
+        fail = err > tol
+        out = pred.copy()
+        out[jidx[fail]] = mc[fail]
+        fallback = bool(fail.mean() > max_fail)
+        t3 = t2
+        if fallback:
+            all_sims = dict(sims)
+            all_sims['num_packets'] = np.full(m, judge_packets, dtype=np.uint64)
+            out = self.simulate(all_sims, seed=seed + 1)
+            t3 = time.perf_counter()
+        rep = {'queries': m, 'judged': nj, 'judge_rms_rel_mean': float(err.mean()),
+               'judge_rms_rel_median': float(np.median(err)), 'judge_fail_fraction': float(fail.mean()),
+               'fallback_all': fallback, 'infer_seconds': t1 - t0, 'judge_seconds': t2 - t1,
+               'fallback_seconds': t3 - t2, 'seconds': (t3 if fallback else t2) - t0}
+        rep['profiles_per_s'] = m / rep['seconds']
+        self.report.update(serve=rep)
+        return out, rep
