@@ -43,7 +43,6 @@ _OPTIONAL = {
     'mcgb_mlp_mse_grad': (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_adamw': (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_float,
                                  C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, _vp]),
-    'mcgb_mcml_run_noalloc': (C.c_int, [C.POINTER(_abi.McgbMcmlConfig), C.POINTER(_abi.McgbBuffers), _vp]),
 }
 
 
