@@ -357,6 +357,23 @@ int mcgb_batched_run(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
 /* Resident blocks per SM of the batched kernel for a block size. */
 int mcgb_batched_occupancy(uint32_t block_size, int math, uint32_t *blocks_per_sm);
 
+/* No counterpart in the reference (it has no batched engine).
+   mcgb_batched_run for callers that cannot allocate device memory (code in
+   another framework's memory pool or a real-time loop that forbids
+   cudaMalloc, or a plugin host that hands over only input and output
+   buffers): the scratch lives in a fixed device array inside the library,
+   sized for at most MCGB_NOALLOC_MAX_SIMS simulations (about 2.2 MB, held by
+   every GPU that loads the library until exit).  Larger batches return
+   MCGB_E_SIZE.  The caller still passes every input and output.  The first
+   call on a device looks up the array's device address; make that call
+   before any stream capture.  All calls share the array: calls that overlap
+   on the GPU race and must be serialized by the caller.  No device memory is
+   allocated or freed. */
+#define MCGB_NOALLOC_MAX_SIMS 8192u
+int mcgb_batched_run_noalloc(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
+                             const uint32_t *dev_multipliers, uint64_t *dev_tally,
+                             uint64_t *dev_counters, void *stream);
+
 /* ------------------------------------------------------ MLP surrogate */
 /* Kernels of the radial-reflectance surrogate (a small MLP).  Matrices are
    row-major; bf16 values are passed as uint16_t bit patterns; every GEMM

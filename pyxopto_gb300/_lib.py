@@ -34,6 +34,7 @@ _OPTIONAL = {
     'mcgb_batched_run': (C.c_int, [C.POINTER(_abi.McgbBatchConfig), _vp, _vp, _vp, _vp, _vp, _vp]),
     'mcgb_batched_occupancy': (C.c_int, [C.c_uint32, C.c_int, C.POINTER(C.c_uint32)]),
     'mcgb_batched_work_size': (C.c_int, [C.c_uint32, C.POINTER(C.c_uint64)]),
+    'mcgb_batched_run_noalloc': (C.c_int, [C.POINTER(_abi.McgbBatchConfig), _vp, _vp, _vp, _vp, _vp]),
     'mcgb_mlp_linear_fwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_act_bwd': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_act_bwd_scratch': (C.c_uint64, [C.c_int, C.c_int]),

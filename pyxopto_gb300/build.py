@@ -27,6 +27,7 @@ UNITS = [
     ('batched.cu', ['-use_fast_math']),
     ('batched_exact.cu', ['-fmad=false']),
     ('mlp.cu', []),
+    ('noalloc.cu', []),
     ('rng_host.cpp', None),
 ]
 
