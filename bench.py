@@ -166,13 +166,10 @@ def gpu_bench(args, rank, world, local_rank):
     spec = scenarios.ALL[args.workload]
     nphotons = int(args.packets or spec['nphotons'])
     fast = args.math == 'fast'
-    mc = scenarios.build_mc(args.workload, fast=fast)
+    mc = scenarios.build_mc(args.workload, fast=fast, scheduling=args.scheduling)
     mc._rnginit = 1 + 7919 * rank
-    math = _abi.MATH_FAST if fast else _abi.MATH_EXACT
-    streams = mc.suggested_streams(math)
-    cfg = mc.pack(nphotons, streams)
-    mc._ensure_streams(torch, streams, dev)
-    bufs = mc._device_buffers(torch, dev, mc._lut_array(), {})
+    run_fn, cfg, bufs = mc._prepare(nphotons)
+    streams = cfg.num_streams
     stream = torch.cuda.current_stream()
     sptr = C.c_void_p(stream.cuda_stream)
     flush = torch.empty((L2_FLUSH_BYTES // 4,), dtype=torch.float32, device=dev)
@@ -183,7 +180,7 @@ def gpu_bench(args, rank, world, local_rank):
     def step():
         accu.zero_()
         counters.zero_()
-        _lib.check(lib.mcgb_mcml_run(C.byref(cfg), C.byref(bufs), sptr))
+        _lib.check(run_fn(C.byref(cfg), C.byref(bufs), sptr))
 
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
 
@@ -208,7 +205,7 @@ def gpu_bench(args, rank, world, local_rank):
         accu.zero_()
         counters.zero_()
         ev[k][0].record(stream)
-        _lib.check(lib.mcgb_mcml_run(C.byref(cfg), C.byref(bufs), sptr))
+        _lib.check(run_fn(C.byref(cfg), C.byref(bufs), sptr))
         ev[k][1].record(stream)
     t_end.record(stream)
     torch.cuda.synchronize()
@@ -227,7 +224,7 @@ def gpu_bench(args, rank, world, local_rank):
     # ---- end-to-end through the public API (host buffers, copies inside)
     e2e = None
     if not args.no_e2e:
-        api = scenarios.build_mc(args.workload, fast=fast)
+        api = scenarios.build_mc(args.workload, fast=fast, scheduling=args.scheduling)
         api._rnginit = 2 + 7919 * rank
         api.run(nphotons, maxthreads=streams)        # warm-up (seeds, buffers)
         torch.cuda.synchronize()
@@ -236,7 +233,11 @@ def gpu_bench(args, rank, world, local_rank):
             api.run(nphotons, maxthreads=streams)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        h2d = C.sizeof(_abi.McgbMcmlConfig) + 4 * int(api._lut_size)
+        h2d = C.sizeof(cfg) + 4 * int(api._lut_size)
+        if spec['medium'] == 'mcvox':
+            # the voxel grid stays on the device between runs; the material
+            # table is uploaded with every run
+            h2d += C.sizeof(_abi.McgbMaterial) * len(api.materials)
         d2h = 8 * int(api._acc.size) + 4 * int(api._flt.size) + 4 * int(api._int.size) + \
             8 * _abi.NUM_COUNTERS
         e2e = {'value': nphotons * args.e2e_steps * world / dt, 'unit': 'packets/s',
@@ -247,6 +248,109 @@ def gpu_bench(args, rank, world, local_rank):
                 packets_done=int(host_counters[_abi.CNT_PACKETS]))
 
 
+def batched_bench(args):
+    """4096 single-layer simulations (the batched benchmark ranges) in one
+    persistent launch replayed from a CUDA graph; metric profiles/s."""
+    import torch
+    from pyxopto_gb300.batched import BatchedMc
+    sims = BatchedMc.sample_sims(4096, seed=1)
+    b = BatchedMc(sims, fast=args.math == 'fast')
+    tune = b.autotune()
+    for _ in range(args.warmup):
+        b.run_raw(graph=True)
+    stream = torch.cuda.current_stream()
+    sampler = ClockSampler(0)
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sampler.start()
+    t0e.record(stream)
+    for _ in range(args.steps):
+        b._graph.replay()
+    t1e.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    dev_s = t0e.elapsed_time(t1e) / 1e3 / args.steps
+    npk = int(b.packets.sum())
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        b.run(graph=True)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    steps = b.last_report['steps']
+    return {'metric': 'profiles/s (batched MC, 4096 single-layer simulations)',
+            'value': 4096 / dev_s, 'unit': 'profiles/s', 'ms_per_step': dev_s * 1e3,
+            'packets_per_s': npk / dev_s, 'steps_per_s': steps / dev_s,
+            'config': {'workload': 'batched_4096', 'sims': 4096, 'packets_total': npk,
+                       'radial_bins': 30, 'r_max_m': 3e-3, 'autotuned': {
+                           k: tune[k] for k in ('block_size', 'packets_per_item')},
+                       'graph': True},
+            'clocks': clocks, 'gpu_launches': 2 * args.steps,
+            'e2e': {'value': 4096 / e2e_s, 'unit': 'profiles/s',
+                    'h2d_bytes_per_step': 40 * 4096, 'd2h_bytes_per_step': 8 * 30 * 4096 + 64,
+                    'path': 'pyxopto_gb300.batched.BatchedMc.run(graph=True)'}}
+
+
+def surrogate_bench(args):
+    """MLP surrogate + 1 % Monte Carlo judge on 65536 queries, against
+    sequential plain Mc.run calls at the packet count that reaches 1 % RMS
+    relative error (1e6 packets); metric profiles/s."""
+    import torch
+    from pyxopto_gb300.batched import BatchedMc
+    from pyxopto_gb300.surrogate import Surrogate
+    from pyxopto_gb300.mcml import mc
+    t_setup = time.perf_counter()
+    sur = Surrogate()
+    train = BatchedMc.sample_sims(args.train_sims, seed=21,
+                                  packets=(args.train_packets, args.train_packets + 1))
+    refl = sur.simulate(train)
+    t_gen = time.perf_counter() - t_setup
+    sur.fit(train, refl, epochs=args.train_epochs, batch=4096, lr=3e-3)
+    t_fit = sur.report['train_seconds']
+    # accuracy against high-accuracy Monte Carlo (independent of the judge)
+    test = BatchedMc.sample_sims(128, seed=99, packets=(4_000_000, 4_000_001))
+    ref = sur.simulate(test, seed=77)
+    pred = sur.predict(test['mua'], test['mus'] * (1 - test['g']), test['g'], test['n'])
+    err = Surrogate.rms_rel(pred, ref)
+    queries = BatchedMc.sample_sims(65536, seed=5, packets=(1, 2))
+    for _ in range(args.warmup):
+        sur.serve(queries, judge_fraction=0.01, judge_packets=1_000_000, tol=0.01, max_fail=1.0)
+    reps = []
+    for k in range(args.steps):
+        _, rep = sur.serve(queries, judge_fraction=0.01, judge_packets=1_000_000, tol=0.01,
+                           max_fail=1.0, seed=7 + k)
+        reps.append(rep)
+    sec = float(np.mean([r['seconds'] for r in reps]))
+    # sequential plain Monte Carlo: one Mc.run of 1e6 packets per profile
+    seq = BatchedMc.sample_sims(args.seq_profiles, seed=31, packets=(1, 2))
+    t0 = time.perf_counter()
+    for i in range(args.seq_profiles):
+        layers = mc.mclayer.Layers([
+            mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0)),
+            mc.mclayer.Layer(d=np.inf, n=float(seq['n'][i]), mua=float(seq['mua'][i]),
+                             mus=float(seq['mus'][i]), pf=mc.mcpf.Hg(float(seq['g'][i]))),
+            mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0))])
+        det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(mc.mcdetector.Axis(0.0, 3e-3, 30)))
+        m = mc.Mc(layers, mc.mcsource.Line(), det, options=[mc.mcoptions.McUseNativeMath(True)],
+                  rnginit=1 + i)
+        m.run(1_000_000)
+    seq_rate = args.seq_profiles / (time.perf_counter() - t0)
+    value = 65536 / sec
+    return {'metric': 'profiles/s (surrogate + 1% MC judge, 65536 queries)', 'value': value,
+            'unit': 'profiles/s', 'ms_per_step': sec * 1e3,
+            'sequential_plain_mc_profiles_per_s': seq_rate,
+            'gain_vs_sequential_plain_mc': value / seq_rate,
+            'surrogate_rms_rel_vs_4e6_mc': {'median': float(np.median(err)), 'mean': float(err.mean()),
+                                            'p90': float(np.percentile(err, 90))},
+            'judge': {k: float(np.mean([r[k] for r in reps]))
+                      for k in ('judge_rms_rel_mean', 'judge_rms_rel_median', 'judge_fail_fraction',
+                                'infer_seconds', 'judge_seconds')},
+            'config': {'workload': 'surrogate', 'mlp': '4-256-256-256-30 GELU bf16/fp32',
+                       'train_profiles': args.train_sims, 'train_packets': args.train_packets,
+                       'train_epochs': args.train_epochs, 'train_gen_s': t_gen, 'train_fit_s': t_fit,
+                       'judge_fraction': 0.01, 'judge_packets': 1_000_000, 'tol': 0.01,
+                       'sequential_profiles_timed': args.seq_profiles},
+            'gpu_launches': None}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -255,19 +359,34 @@ def main():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--workload', default='c2_skin_gk_fluence')
     ap.add_argument('--math', default='fast', choices=['fast', 'exact'])
+    ap.add_argument('--scheduling', default='dynamic', choices=['dynamic', 'static'])
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--train-sims', type=int, default=1 << 16)
+    ap.add_argument('--train-packets', type=int, default=100_000)
+    ap.add_argument('--train-epochs', type=int, default=150)
+    ap.add_argument('--seq-profiles', type=int, default=8)
     ap.add_argument('--packets', type=int, default=None,
                     help='override the packets per step (small profiling cases only; '
                          'a headline number uses the workload size)')
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
+    if args.workload in ('batched_4096', 'surrogate') and args.impl == 'gb300':
+        import torch
+        torch.cuda.set_device(local_rank)
+        res = batched_bench(args) if args.workload == 'batched_4096' else surrogate_bench(args)
+        line = dict({'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
+                     'scaling': 'none', 'vs_baseline': None, 'dtype': 'f32',
+                     'data': 'synthetic (seeded parameter draws and RNG streams)'}, **res)
+        if rank == 0:
+            print(json.dumps(line))
+        return
     import scenarios
     spec = scenarios.ALL[args.workload]
     config = {'workload': args.workload, 'packets_per_step': int(args.packets or spec['nphotons']),
-              'medium': spec['medium'], 'math': args.math,
+              'medium': spec['medium'], 'math': args.math, 'scheduling': args.scheduling,
               'l2': 'flushed between steps (256 MB write); fluence tally 8 MB fits L2'}
 
     if args.impl == 'reference':

@@ -89,6 +89,7 @@ enum {
     MCGB_CNT_STATUS = 2,     /* OR of MCGB_STATUS_* bits                 */
     MCGB_CNT_THREADS = 3,    /* threads that simulated >= 1 packet       */
     MCGB_CNT_ABORT = 4,      /* set nonzero by the host to stop a run    */
+    MCGB_CNT_QUEUE = 5,      /* work queue of dynamic scheduling (zero it) */
     MCGB_NUM_COUNTERS = 8
 };
 
@@ -107,6 +108,16 @@ enum { MCGB_TRACE_NONE = 0, MCGB_TRACE_START = 1, MCGB_TRACE_END = 2, MCGB_TRACE
    contraction, so GPU and CPU produce identical bits.  FAST uses the GPU's
    special-function units (the reference's MC_USE_NATIVE_MATH). */
 enum { MCGB_MATH_EXACT = 0, MCGB_MATH_FAST = 1 };
+/* Packet scheduling.  STATIC: thread t owns random-number stream t (state
+   rng_x[t], multiplier rng_a[t]) and simulates packets t, t+T, t+2T, ...
+   (the reference's per-thread streams).  DYNAMIC: persistent warps take
+   packets from a device work queue (counters[MCGB_CNT_QUEUE], zeroed by the
+   caller) and refill idle lanes packet by packet; packet p simulates on
+   its own MWC stream derived from (seed, packet_offset + p) with a
+   multiplier from rng_a[0 .. num_streams) (batch_rng.h); rng_x is unused.
+   Both are bit-reproducible; DYNAMIC keeps every lane busy until the last
+   packets. */
+enum { MCGB_SCHED_STATIC = 0, MCGB_SCHED_DYNAMIC = 1 };
 
 /* ------------------------------------------------------------ POD structs */
 /* Scattering phase function of one layer/material.
@@ -203,6 +214,10 @@ typedef struct McgbRunOptions {
     uint32_t block_size;                    /* threads per block (0 = auto)    */
     uint64_t max_steps_per_packet;          /* 0 = unlimited                   */
     double deadline_s;                      /* device wall-clock limit, 0=300s */
+    int32_t scheduling;                     /* MCGB_SCHED_*                    */
+    uint32_t reserved;
+    uint64_t seed;                          /* DYNAMIC: stream derivation seed */
+    uint64_t packet_offset;                 /* DYNAMIC: index of packet 0      */
 } McgbRunOptions;
 
 /* Layered medium run (the reference's McKernel arguments for mcml). */

@@ -907,9 +907,35 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
     }                                                                               \
     return failed ? 0 : steps;
 
+/* DYNAMIC scheduling: packet p on the stream of (seed, packet_offset + p)
+   with the multipliers rng_a[0 .. num_streams); rng_x is unused. */
+#define MO_DYNAMIC_BODY(PACKET_CALL)                                                 \
+    uint64_t steps = 0;                                                              \
+    int64_t N = (int64_t)cfg->num_packets;                                           \
+    _Pragma("omp parallel num_threads(nthreads > 0 ? nthreads : 1) reduction(+:steps)") \
+    {                                                                                \
+        uint64_t *acc = (uint64_t *)calloc(accu_size ? accu_size : 1, 8);            \
+        _Pragma("omp for schedule(dynamic, 16)")                                     \
+        for (int64_t p = 0; p < N; ++p) {                                            \
+            uint64_t x;                                                              \
+            uint32_t a;                                                              \
+            br_packet_stream(cfg->opt.seed, 0u, cfg->opt.packet_offset + (uint64_t)p, \
+                             rng_a, cfg->num_streams, &x, &a);                       \
+            steps += PACKET_CALL;                                                    \
+        }                                                                            \
+        _Pragma("omp critical")                                                      \
+        for (uint64_t i = 0; i < accu_size; ++i) accu[i] += acc[i];                  \
+        free(acc);                                                                   \
+    }                                                                                \
+    return steps;
+
 uint64_t mco_mcml_run(int math_mode, const McgbMcmlConfig *cfg, const float *lut,
                       uint64_t *rng_x, const uint32_t *rng_a, uint64_t *accu,
                       uint64_t accu_size, float *fbuf, int32_t *ibuf, int nthreads) {
+    if (cfg->opt.scheduling == MCGB_SCHED_DYNAMIC) {
+        MO_DYNAMIC_BODY(mcml_stream(math_mode, cfg, lut, &x, a, (uint64_t)p, (uint64_t)N, acc,
+                                    fbuf, ibuf))
+    }
     MO_RUN_BODY(mcml_stream(math_mode, cfg, lut, &rng_x[t], rng_a[t], (uint64_t)t,
                             (uint64_t)T, acc, fbuf, ibuf))
 }
@@ -919,6 +945,10 @@ uint64_t mco_mcvox_run(int math_mode, const McgbMcvoxConfig *cfg,
                        const float *lut, uint64_t *rng_x, const uint32_t *rng_a,
                        uint64_t *accu, uint64_t accu_size, float *fbuf, int32_t *ibuf,
                        int nthreads) {
+    if (cfg->opt.scheduling == MCGB_SCHED_DYNAMIC) {
+        MO_DYNAMIC_BODY(mcvox_stream(math_mode, cfg, materials, voxels, lut, &x, a, (uint64_t)p,
+                                     (uint64_t)N, acc, fbuf, ibuf))
+    }
     MO_RUN_BODY(mcvox_stream(math_mode, cfg, materials, voxels, lut, &rng_x[t], rng_a[t],
                              (uint64_t)t, (uint64_t)T, acc, fbuf, ibuf))
 }

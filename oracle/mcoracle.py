@@ -62,7 +62,12 @@ def run(mc, nphotons: int, streams: int, math: int = LIBM, nthreads: int = 1, se
         mats = None
     else:
         cfg, mats = mc.pack(nphotons, streams)
-    if seeds is None:
+    from pyxopto_gb300 import _abi
+    if cfg.opt.scheduling == _abi.SCHED_DYNAMIC:
+        a = mc.dynamic_multipliers()
+        x = np.zeros((1,), dtype=np.uint64)
+        cfg.num_streams = a.size
+    elif seeds is None:
         x, a = mc.host_seeds(streams)
     else:
         x, a = seeds

@@ -14,7 +14,8 @@ TRACE_ENTRY_LEN = 8
 OK, E_INVALID, E_SIZE, E_CUDA, E_TIMEOUT, E_BAD_INDEX, E_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
 
 STATUS_TIMEOUT, STATUS_BAD_INDEX, STATUS_STEP_LIMIT, STATUS_ABORTED = 1, 2, 4, 8
-CNT_PACKETS, CNT_STEPS, CNT_STATUS, CNT_THREADS, CNT_ABORT, NUM_COUNTERS = 0, 1, 2, 3, 4, 8
+CNT_PACKETS, CNT_STEPS, CNT_STATUS, CNT_THREADS, CNT_ABORT, CNT_QUEUE, NUM_COUNTERS = 0, 1, 2, 3, 4, 5, 8
+SCHED_STATIC, SCHED_DYNAMIC = 0, 1
 
 METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT = 0, 1, 2
 PF_HG, PF_GK, PF_LUT = 0, 1, 2
@@ -73,7 +74,8 @@ class McgbRunOptions(C.Structure):
     _fields_ = [('method', i32), ('math', i32), ('use_lottery', i32),
                 ('packet_weight_min', f32), ('lottery_chance', f32), ('rmax', f32),
                 ('track_optical_pathlength', i32), ('block_size', u32),
-                ('max_steps_per_packet', u64), ('deadline_s', C.c_double)]
+                ('max_steps_per_packet', u64), ('deadline_s', C.c_double),
+                ('scheduling', i32), ('reserved', u32), ('seed', u64), ('packet_offset', u64)]
 
 
 class McgbMcmlConfig(C.Structure):
@@ -142,4 +144,7 @@ def default_options():
     o.block_size = 0
     o.max_steps_per_packet = 0
     o.deadline_s = 0.0
+    o.scheduling = SCHED_STATIC
+    o.seed = 0
+    o.packet_offset = 0
     return o

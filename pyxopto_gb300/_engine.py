@@ -75,6 +75,7 @@ class McEngine:
         self._deadline = 0.0
         self._max_steps = 0
         self._shard = (0, 1)
+        self._packets_total = 0          # packets simulated so far (dynamic streams)
 
     # ------------------------------------------------ reference worker API
     def cl_allocate_rw_accumulator_buffer(self, owner, shape) -> int:
@@ -160,7 +161,23 @@ class McEngine:
         o.block_size = self._block_size
         o.deadline_s = self._deadline
         o.max_steps_per_packet = self._max_steps
+        if res.get('MCGB_SCHEDULING', 'dynamic') == 'dynamic':
+            o.scheduling = _abi.SCHED_DYNAMIC
+            if self._rnginit is None:
+                self._rnginit = Random().initializer()
+            rank, world = self._shard
+            o.seed = (int(self._rnginit) + 0x9E3779B97F4A7C15 * rank) & 0xFFFFFFFFFFFFFFFF
+            o.packet_offset = self._packets_total
+        else:
+            o.scheduling = _abi.SCHED_STATIC
         return o
+
+    DYNAMIC_MULTIPLIERS = 4096
+
+    def dynamic_multipliers(self) -> np.ndarray:
+        """Multipliers of the per-packet streams (dynamic scheduling): the
+        first entries of the safe-prime table."""
+        return Random().multipliers(self.DYNAMIC_MULTIPLIERS)
 
     def _lut_array(self) -> np.ndarray:
         if not self._luts:
@@ -184,6 +201,13 @@ class McEngine:
             return Random().seeds(n, self._rnginit)
         x, a = Random().seeds(n * world, self._rnginit)
         return x[rank * n:(rank + 1) * n].copy(), a[rank * n:(rank + 1) * n].copy()
+
+    def _ensure_dynamic_streams(self, torch, device):
+        if self._dev.get('dyn_mult') is None:
+            a = self.dynamic_multipliers()
+            self._dev['dyn_mult'] = torch.from_numpy(a.view(np.int32)).to(device)
+            self._dev['dyn_x'] = torch.zeros((1,), dtype=torch.int64, device=device)
+        return self.DYNAMIC_MULTIPLIERS
 
     def _ensure_streams(self, torch, n: int, device):
         """Allocates and seeds n device streams once; their x states persist
@@ -211,8 +235,12 @@ class McEngine:
         d['lut'] = torch.from_numpy(lut if lut.size else np.zeros((1,), np.float32)).to(device)
         d['counters'] = torch.zeros((_abi.NUM_COUNTERS,), dtype=torch.int64, device=device)
         b = _abi.McgbBuffers()
-        b.rng_x = d['rng_x'].data_ptr()
-        b.rng_a = d['rng_a'].data_ptr()
+        if 'dyn_mult' in d and extra.pop('_dynamic', False):
+            b.rng_x = d['dyn_x'].data_ptr()
+            b.rng_a = d['dyn_mult'].data_ptr()
+        else:
+            b.rng_x = d['rng_x'].data_ptr()
+            b.rng_a = d['rng_a'].data_ptr()
         b.accumulator = d['accu'].data_ptr()
         b.accumulator_size = self._acc.size
         b.float_buffer = d['flt'].data_ptr()

@@ -59,7 +59,11 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (!b) return fail(MCGB_E_INVALID, "buffers is NULL");
     if (num_streams == 0) return fail(MCGB_E_INVALID, "num_streams must be positive");
     if (num_streams > (1u << 24)) return fail(MCGB_E_SIZE, "num_streams %u exceeds 2^24", num_streams);
-    if (!b->rng_x || !b->rng_a) return fail(MCGB_E_INVALID, "RNG state buffers are NULL");
+    if (o.scheduling != MCGB_SCHED_STATIC && o.scheduling != MCGB_SCHED_DYNAMIC)
+        return fail(MCGB_E_INVALID, "unknown scheduling %d", o.scheduling);
+    if (!b->rng_a) return fail(MCGB_E_INVALID, "RNG multiplier buffer is NULL");
+    if (o.scheduling == MCGB_SCHED_STATIC && !b->rng_x)
+        return fail(MCGB_E_INVALID, "RNG state buffer is NULL");
     if (!b->counters) return fail(MCGB_E_INVALID, "counters buffer is NULL");
     if (o.method < 0 || o.method > 2) return fail(MCGB_E_INVALID, "unknown method %d", o.method);
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)

@@ -23,6 +23,7 @@
  */
 #pragma once
 #include "mc_device.cuh"
+#include "batch_rng.h"
 
 namespace MCGB_NS {
 
@@ -126,12 +127,194 @@ static __device__ __forceinline__ uint32_t mcml_boundary(const MlLayer *L, int &
     return MCGB_EV_REFLECTION;
 }
 
+/* Per-thread constants of a run. */
+struct MlCtx {
+    const MlLayer *L;
+    const float *lut;
+    float rmax2;
+    bool use_rmax, use_trace, track_opl;
+    int last_layer;
+    f3 src_pos;
+};
+
+/* State of the packet a thread is simulating. */
+struct MlPacket {
+    f3 pos, dir;
+    float w, opl;
+    int layer;
+    uint32_t trace_count, events, steps;
+    uint64_t p;          /* packet number (trace slot) */
+};
+
+static __device__ __forceinline__ MlCtx mcml_ctx(const McgbMcmlConfig &c, const MlLayer *L,
+                                                 const float *lut) {
+    MlCtx x;
+    x.L = L;
+    x.lut = lut;
+    x.rmax2 = c.opt.rmax * c.opt.rmax;
+    /* dist2 > inf is never true: skip the test for an infinite rmax */
+    x.use_rmax = x.rmax2 < __int_as_float(0x7f800000);
+    x.use_trace = c.trace.flags != MCGB_TRACE_NONE;
+    x.track_opl = c.opt.track_optical_pathlength != 0;
+    x.last_layer = (int)c.num_layers - 1;
+    x.src_pos = f3{c.source.position[0], c.source.position[1], c.source.position[2]};
+    return x;
+}
+
+static __device__ __forceinline__ void mcml_begin(const McgbMcmlConfig &c, const McgbBuffers &b,
+                                                  const MlCtx &x, MlPacket &s, Rng &rng, uint64_t p) {
+    s.p = p;
+    s.opl = 0.0f;
+    s.trace_count = 0;
+    s.steps = 0;
+    s.events = MCGB_EV_LAUNCH;
+    mcml_launch(c, x.L, rng, s.pos, s.dir, s.w, s.layer, b.accumulator);
+    if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
+        trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
+}
+
+static __device__ __forceinline__ void mcml_end(const McgbMcmlConfig &c, const McgbBuffers &b,
+                                                const MlCtx &x, const MlPacket &s) {
+    if (x.use_trace) b.int_buffer[c.trace.count_offset + s.p] = (int32_t)s.trace_count;
+}
+
+/* One interaction step of a packet (the body of McKernel's while(!done)
+   loop, xopto/mcml/kernel/mcml.template.c:525-814).  Returns true when the
+   packet terminated. */
 template <int PF, int METHOD, bool FLU>
-__global__ void __launch_bounds__(256)
-mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
-                      uint64_t deadline_ns, int lut_in_smem) {
-    __shared__ MlSmem sm;
-    extern __shared__ float s_lut[];
+static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const McgbBuffers &b,
+                                                 const MlCtx &x, MlPacket &s, Rng &rng,
+                                                 FluenceCache &fcache, uint32_t &status) {
+    const MlLayer *L = x.L;
+    const McgbRunOptions &o = c.opt;
+    uint64_t *accu = b.accumulator;
+    const float4 g0 = L[s.layer].g0;   /* top, bottom, inv_mut, mua_inv_mut */
+    ++s.steps;
+    float u = rng.next();
+    float step;
+    if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
+        step = mc_div(-mc_log(u), L[s.layer].g1.z);
+    else
+        step = -mc_log(u) * g0.z;
+    step = fminf(step, FLT_MAX);
+    int next = s.layer;
+    if (s.pos.z + step * s.dir.z < g0.x) {
+        --next;
+        if (fabsf(s.dir.z) != 0.0f) step = mc_div(g0.x - s.pos.z, s.dir.z);
+    }
+    if (s.pos.z + step * s.dir.z >= g0.y) {
+        ++next;
+        if (fabsf(s.dir.z) != 0.0f) step = mc_div(g0.y - s.pos.z, s.dir.z);
+    }
+    s.pos.x = s.pos.x + s.dir.x * step;
+    s.pos.y = s.pos.y + s.dir.y * step;
+    s.pos.z = s.pos.z + s.dir.z * step;
+    if (x.track_opl) s.opl += L[s.layer].g1.x * step;
+    if (s.layer < next) s.pos.z = g0.y;
+    if (s.layer > next) s.pos.z = g0.x;
+
+    bool done = false;
+    if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
+        /* mcml.template.c:584-666 */
+        float mua = L[s.layer].g1.y;
+        float fraction = 1.0f - mc_exp(-mua * step);
+        float deposit = fraction * s.w;
+        s.w -= deposit;
+        s.events |= MCGB_EV_ABSORPTION;
+        if (FLU) {
+            float step_back = (mua != 0.0f)
+                                  ? step - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
+                                  : 0.0f;
+            f3 dp{s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
+                  s.pos.z - step_back * s.dir.z};
+            fluence_deposit(c.fluence, dp, deposit, mua, accu, fcache);
+        }
+        if (next != s.layer) {
+            s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
+            if (!(s.layer > 0 && s.layer < x.last_layer)) {
+                if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
+                else detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+                done = true;
+            }
+        } else {
+            const MlLayer &cl = L[s.layer];
+            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
+            scatter_direction(s.dir, ct, az);
+            s.events |= MCGB_EV_SCATTERING;
+        }
+        if (s.w < o.packet_weight_min) {
+            if (o.use_lottery) {
+                if (rng.next() > o.lottery_chance) done = true;
+                else s.w = mc_div(s.w, o.lottery_chance);
+            } else {
+                done = true;
+            }
+        }
+    } else if (next != s.layer) {
+        s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
+        if (!(s.layer > 0 && s.layer < x.last_layer)) {
+            if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
+            else detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+            done = true;
+        }
+    } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
+        /* mcml.template.c:705-721 */
+        if (rng.next() < g0.w) {
+            float deposit = s.w;
+            done = true;
+            s.w -= deposit;
+            s.events |= MCGB_EV_ABSORPTION;
+            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, accu, fcache);
+        } else {
+            const MlLayer &cl = L[s.layer];
+            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
+            scatter_direction(s.dir, ct, az);
+            s.events |= MCGB_EV_SCATTERING;
+        }
+    } else {
+        /* albedo weight, mcml.template.c:722-753 */
+        float deposit = s.w * g0.w;
+        s.w -= deposit;
+        s.events |= MCGB_EV_ABSORPTION;
+        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, accu, fcache);
+        const MlLayer &cl = L[s.layer];
+        float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
+        scatter_direction(s.dir, ct, az);
+        s.events |= MCGB_EV_SCATTERING;
+        if (s.w < o.packet_weight_min) {
+            if (o.use_lottery) {
+                if (rng.next() > o.lottery_chance) done = true;
+                else s.w = mc_div(s.w, o.lottery_chance);
+            } else {
+                done = true;
+            }
+        }
+    }
+    /* rmax, mcml.template.c:759-763 */
+    if (x.use_rmax) {
+        f3 d{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
+        if (dot3(d, d) > x.rmax2) {
+            done = true;
+            s.events |= MCGB_EV_ESCAPED;
+        }
+    }
+    if (x.use_trace) {
+        if (done) s.events |= MCGB_EV_TERMINATED;
+        if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
+            trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
+        s.events = 0;
+    }
+    if (!done && o.max_steps_per_packet && s.steps >= o.max_steps_per_packet) {
+        done = true;
+        status |= MCGB_STATUS_STEP_LIMIT;
+    }
+    return done;
+}
+
+/* Shared-memory tables of one block. */
+template <int PF>
+static __device__ __forceinline__ const float *mcml_stage(const McgbMcmlConfig &c, const McgbBuffers &b,
+                                                          MlSmem &sm, float *s_lut, int lut_in_smem) {
     for (uint32_t i = threadIdx.x; i < c.num_layers; i += blockDim.x) {
         const McgbLayer &l = c.layers[i];
         MlLayer h;
@@ -144,187 +327,139 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
     if (lut_in_smem)
         for (uint64_t i = threadIdx.x; i < b.fp_lut_size; i += blockDim.x) s_lut[i] = b.fp_lut[i];
     __syncthreads();
-    const float *lut = lut_in_smem ? s_lut : b.fp_lut;
-    const MlLayer *L = sm.layers;
+    return lut_in_smem ? s_lut : b.fp_lut;
+}
 
+static __device__ __forceinline__ void mc_finish(const McgbBuffers &b, uint64_t steps, uint64_t packets,
+                                                 uint32_t status, bool count_thread) {
+    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_STEPS), (unsigned long long)steps);
+    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_PACKETS), (unsigned long long)packets);
+    if (count_thread) atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_THREADS), 1ull);
+    if (status) atomicOr((unsigned long long *)(b.counters + MCGB_CNT_STATUS), (unsigned long long)status);
+}
+
+/* STATIC scheduling: thread t owns stream t and packets t, t+T, ... */
+template <int PF, int METHOD, bool FLU>
+__global__ void __launch_bounds__(256)
+mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
+                      uint64_t deadline_ns, int lut_in_smem) {
+    __shared__ MlSmem sm;
+    extern __shared__ float s_lut[];
+    const float *lut = mcml_stage<PF>(c, b, sm, s_lut, lut_in_smem);
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= c.num_streams || t >= c.num_packets) return;
     const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
-
-    const McgbRunOptions &o = c.opt;
+    const MlCtx x = mcml_ctx(c, sm.layers, lut);
     const uint64_t T = c.num_streams;
-    const bool use_trace = c.trace.flags != MCGB_TRACE_NONE;
-    const bool track_opl = o.track_optical_pathlength != 0;
-    const float rmax2 = o.rmax * o.rmax;
-    /* dist2 > inf is never true: skip the test for an infinite rmax */
-    const bool use_rmax = rmax2 < __int_as_float(0x7f800000);
-    const int last_layer = (int)c.num_layers - 1;
-    const f3 src_pos{c.source.position[0], c.source.position[1], c.source.position[2]};
-    uint64_t *accu = b.accumulator;
-
     Rng rng{b.rng_x[t], b.rng_a[t]};
     FluenceCache fcache{~0ull, 0};
     uint64_t steps = 0, packets = 0;
-    uint32_t packet_steps = 0, iter = 0;
-    uint32_t status = 0;
-
-    uint64_t p = t;
-    f3 pos, dir;
-    float w, opl = 0.0f;
-    int layer;
-    uint32_t trace_count = 0, events = MCGB_EV_LAUNCH;
-    mcml_launch(c, L, rng, pos, dir, w, layer, accu);
-    if (use_trace && (c.trace.flags & MCGB_TRACE_START))
-        trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
-
+    uint32_t iter = 0, status = 0;
+    MlPacket s;
+    mcml_begin(c, b, x, s, rng, t);
     for (;;) {
-        const float4 g0 = L[layer].g0;   /* top, bottom, inv_mut, mua_inv_mut */
-        ++packet_steps;
-        ++iter;
-        float u = rng.next();
-        float step;
-        if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
-            step = mc_div(-mc_log(u), L[layer].g1.z);
-        else
-            step = -mc_log(u) * g0.z;
-        step = fminf(step, FLT_MAX);
-        int next = layer;
-        if (pos.z + step * dir.z < g0.x) {
-            --next;
-            if (fabsf(dir.z) != 0.0f) step = mc_div(g0.x - pos.z, dir.z);
-        }
-        if (pos.z + step * dir.z >= g0.y) {
-            ++next;
-            if (fabsf(dir.z) != 0.0f) step = mc_div(g0.y - pos.z, dir.z);
-        }
-        pos.x = pos.x + dir.x * step;
-        pos.y = pos.y + dir.y * step;
-        pos.z = pos.z + dir.z * step;
-        if (track_opl) opl += L[layer].g1.x * step;
-        if (layer < next) pos.z = g0.y;
-        if (layer > next) pos.z = g0.x;
-
-        bool done = false;
-        if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
-            /* mcml.template.c:584-666 */
-            float mua = L[layer].g1.y;
-            float fraction = 1.0f - mc_exp(-mua * step);
-            float deposit = fraction * w;
-            w -= deposit;
-            events |= MCGB_EV_ABSORPTION;
-            if (FLU) {
-                float step_back = (mua != 0.0f)
-                                      ? step - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
-                                      : 0.0f;
-                f3 dp{pos.x - step_back * dir.x, pos.y - step_back * dir.y, pos.z - step_back * dir.z};
-                fluence_deposit(c.fluence, dp, deposit, mua, accu, fcache);
-            }
-            if (next != layer) {
-                events |= mcml_boundary(L, layer, next, dir, rng) | MCGB_EV_BOUNDARY_HIT;
-                if (!(layer > 0 && layer < last_layer)) {
-                    if (layer <= 0) detector_deposit(c.top, pos, dir, w, accu);
-                    else detector_deposit(c.bottom, pos, dir, w, accu);
-                    done = true;
-                }
-            } else {
-                const MlLayer &cl = L[layer];
-                float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, lut, rng, &az);
-                scatter_direction(dir, ct, az);
-                events |= MCGB_EV_SCATTERING;
-            }
-            if (w < o.packet_weight_min) {
-                if (o.use_lottery) {
-                    if (rng.next() > o.lottery_chance) done = true;
-                    else w = mc_div(w, o.lottery_chance);
-                } else {
-                    done = true;
-                }
-            }
-        } else if (next != layer) {
-            events |= mcml_boundary(L, layer, next, dir, rng) | MCGB_EV_BOUNDARY_HIT;
-            if (!(layer > 0 && layer < last_layer)) {
-                if (layer <= 0) detector_deposit(c.top, pos, dir, w, accu);
-                else detector_deposit(c.bottom, pos, dir, w, accu);
-                done = true;
-            }
-        } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
-            /* mcml.template.c:705-721 */
-            if (rng.next() < g0.w) {
-                float deposit = w;
-                done = true;
-                w -= deposit;
-                events |= MCGB_EV_ABSORPTION;
-                if (FLU) fluence_deposit(c.fluence, pos, deposit, L[layer].g1.y, accu, fcache);
-            } else {
-                const MlLayer &cl = L[layer];
-                float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, lut, rng, &az);
-                scatter_direction(dir, ct, az);
-                events |= MCGB_EV_SCATTERING;
-            }
-        } else {
-            /* albedo weight, mcml.template.c:722-753 */
-            float deposit = w * g0.w;
-            w -= deposit;
-            events |= MCGB_EV_ABSORPTION;
-            if (FLU) fluence_deposit(c.fluence, pos, deposit, L[layer].g1.y, accu, fcache);
-            const MlLayer &cl = L[layer];
-            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, lut, rng, &az);
-            scatter_direction(dir, ct, az);
-            events |= MCGB_EV_SCATTERING;
-            if (w < o.packet_weight_min) {
-                if (o.use_lottery) {
-                    if (rng.next() > o.lottery_chance) done = true;
-                    else w = mc_div(w, o.lottery_chance);
-                } else {
-                    done = true;
-                }
-            }
-        }
-        /* rmax, mcml.template.c:759-763 */
-        if (use_rmax) {
-            f3 d{pos.x - src_pos.x, pos.y - src_pos.y, pos.z - src_pos.z};
-            if (dot3(d, d) > rmax2) {
-                done = true;
-                events |= MCGB_EV_ESCAPED;
-            }
-        }
-        if (use_trace) {
-            if (done) events |= MCGB_EV_TERMINATED;
-            if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
-                trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
-            events = 0;
-        }
-        if (!done && o.max_steps_per_packet && packet_steps >= o.max_steps_per_packet) {
-            done = true;
-            status |= MCGB_STATUS_STEP_LIMIT;
-        }
-
-        if (done) {
+        if (mcml_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
             ++packets;
-            steps += packet_steps;
-            packet_steps = 0;
-            if (use_trace) b.int_buffer[c.trace.count_offset + p] = (int32_t)trace_count;
-            p += T;
-            if (p >= c.num_packets) break;
-            trace_count = 0;
-            opl = 0.0f;
-            events = MCGB_EV_LAUNCH;
-            mcml_launch(c, L, rng, pos, dir, w, layer, accu);
-            if (use_trace && (c.trace.flags & MCGB_TRACE_START))
-                trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
+            steps += s.steps;
+            mcml_end(c, b, x, s);
+            uint64_t p = s.p + T;
+            if (p >= c.num_packets) {
+                s.steps = 0;
+                break;
+            }
+            mcml_begin(c, b, x, s, rng, p);
         }
-        if ((iter & 1023u) == 0) {
+        if (((++iter) & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
             if (*(volatile uint64_t *)(b.counters + MCGB_CNT_ABORT)) { status |= MCGB_STATUS_ABORTED; break; }
         }
     }
-    steps += packet_steps;
-    if (FLU) fcache.flush(accu);
+    steps += s.steps;
+    if (FLU) fcache.flush(b.accumulator);
     b.rng_x[t] = rng.x;
-    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_STEPS), (unsigned long long)steps);
-    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_PACKETS), (unsigned long long)packets);
-    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_THREADS), 1ull);
-    if (status) atomicOr((unsigned long long *)(b.counters + MCGB_CNT_STATUS), (unsigned long long)status);
+    mc_finish(b, steps, packets, status, true);
+}
+
+#define MCGB_FULL_MASK 0xffffffffu
+
+/* DYNAMIC scheduling: persistent warps refill idle lanes packet by packet
+   from the queue counters[MCGB_CNT_QUEUE]; packet p runs on the stream of
+   (seed, packet_offset + p). */
+template <int PF, int METHOD, bool FLU>
+__global__ void __launch_bounds__(256)
+mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
+                    uint64_t deadline_ns, int lut_in_smem) {
+    __shared__ MlSmem sm;
+    extern __shared__ float s_lut[];
+    const float *lut = mcml_stage<PF>(c, b, sm, s_lut, lut_in_smem);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
+    const MlCtx x = mcml_ctx(c, sm.layers, lut);
+    const uint64_t N = c.num_packets;
+    const uint64_t B = 128;
+    unsigned long long *queue = (unsigned long long *)(b.counters + MCGB_CNT_QUEUE);
+    uint64_t item_next = 0, item_end = 0;   /* warp-uniform */
+    bool more = true, active = false;
+    Rng rng{0ull, 1u};
+    FluenceCache fcache{~0ull, 0};
+    uint64_t steps = 0, packets = 0;
+    uint32_t iter = 0, status = 0;
+    MlPacket s;
+    s.steps = 0;
+    for (;;) {
+        uint32_t need = __ballot_sync(MCGB_FULL_MASK, !active);
+        while (need && more) {
+            if (item_next >= item_end) {
+                unsigned long long item = 0;
+                if (lane == 0) item = atomicAdd(queue, 1ull);
+                item = __shfl_sync(MCGB_FULL_MASK, item, 0);
+                item_next = (uint64_t)item * B;
+                if (item_next >= N) {
+                    more = false;
+                    break;
+                }
+                item_end = min(item_next + B, N);
+            }
+            uint32_t avail = (uint32_t)min(item_end - item_next, (uint64_t)32);
+            uint32_t rank = __popc(need & ((1u << lane) - 1u));
+            bool mine = ((need >> lane) & 1u) && rank < avail;
+            if (mine) {
+                uint64_t p = item_next + rank;
+                uint64_t xs;
+                uint32_t as;
+                br_packet_stream(c.opt.seed, 0u, c.opt.packet_offset + p, b.rng_a, c.num_streams, &xs, &as);
+                rng = Rng{xs, as};
+                mcml_begin(c, b, x, s, rng, p);
+                active = true;
+            }
+            uint32_t taken = __ballot_sync(MCGB_FULL_MASK, mine);
+            item_next += __popc(taken);
+            need &= ~taken;
+        }
+        if (!__any_sync(MCGB_FULL_MASK, active)) break;
+        if (active && mcml_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
+            ++packets;
+            steps += s.steps;
+            s.steps = 0;
+            mcml_end(c, b, x, s);
+            active = false;
+        }
+        if (((++iter) & 1023u) == 0) {
+            uint32_t stop = 0;
+            if (lane == 0) {
+                if (globaltimer_ns() > t_deadline) stop = MCGB_STATUS_TIMEOUT;
+                else if (*(volatile uint64_t *)(b.counters + MCGB_CNT_ABORT)) stop = MCGB_STATUS_ABORTED;
+            }
+            stop = __shfl_sync(MCGB_FULL_MASK, stop, 0);
+            if (stop) {
+                status |= stop;
+                break;
+            }
+        }
+    }
+    steps += s.steps;
+    if (FLU) fcache.flush(b.accumulator);
+    mc_finish(b, steps, packets, status, packets > 0);
 }
 
 }  // namespace MCGB_NS

@@ -10,6 +10,7 @@
  */
 #pragma once
 #include "mc_device.cuh"
+#include "batch_rng.h"
 
 namespace MCGB_NS {
 
@@ -178,12 +179,192 @@ static __device__ __forceinline__ uint32_t mv_boundary(const MvGeom &g, const Mv
     return MCGB_EV_REFLECTION;
 }
 
+struct MvCtx {
+    const MvMaterial *M;
+    const float *lut;
+    const uint8_t *vox;
+    MvGeom g;
+    float rmax2;
+    bool use_rmax, use_trace, track_opl;
+    f3 src_pos;
+};
+
+struct MvPacket {
+    f3 pos, dir;
+    i3 vi;
+    int mat;
+    float w, opl;
+    uint32_t trace_count, events, steps;
+    uint64_t p;
+};
+
+static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, const McgbBuffers &b,
+                                                  const MvMaterial *M, const float *lut) {
+    MvCtx x;
+    x.M = M;
+    x.lut = lut;
+    x.vox = b.voxels;
+    for (int k = 0; k < 3; ++k) {
+        x.g.tl[k] = c.top_left[k];
+        x.g.br[k] = c.bottom_right[k];
+        x.g.vs[k] = c.voxel_size[k];
+        x.g.sh[k] = c.shape[k];
+    }
+    x.rmax2 = c.opt.rmax * c.opt.rmax;
+    x.use_rmax = x.rmax2 < __int_as_float(0x7f800000);
+    x.use_trace = c.trace.flags != MCGB_TRACE_NONE;
+    x.track_opl = c.opt.track_optical_pathlength != 0;
+    x.src_pos = f3{c.source.position[0], c.source.position[1], c.source.position[2]};
+    return x;
+}
+
+static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, const McgbBuffers &b,
+                                                   const MvCtx &x, MvPacket &s, Rng &rng, uint64_t p) {
+    s.p = p;
+    s.opl = 0.0f;
+    s.trace_count = 0;
+    s.steps = 0;
+    s.events = MCGB_EV_LAUNCH;
+    mcvox_launch(c, x.g, x.M, x.vox, rng, s.pos, s.dir, s.w, s.vi, s.mat, b.accumulator);
+    if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
+        trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
+}
+
+static __device__ __forceinline__ void mcvox_end(const McgbMcvoxConfig &c, const McgbBuffers &b,
+                                                 const MvCtx &x, const MvPacket &s) {
+    if (x.use_trace) b.int_buffer[c.trace.count_offset + s.p] = (int32_t)s.trace_count;
+}
+
+/* One step of McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:760-1038. */
 template <int PF, int METHOD, bool FLU>
-__global__ void __launch_bounds__(256)
-mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
-                       uint64_t deadline_ns, int lut_in_smem) {
-    __shared__ MvSmem sm;
-    extern __shared__ float s_lut[];
+static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
+                                                  const MvCtx &x, MvPacket &s, Rng &rng,
+                                                  FluenceCache &fcache, uint32_t &status) {
+    const MvMaterial *M = x.M;
+    const MvGeom &g = x.g;
+    const McgbRunOptions &o = c.opt;
+    uint64_t *accu = b.accumulator;
+    const float4 g0 = M[s.mat].g0;   /* mus, mua, inv_mut, mua_inv_mut */
+    ++s.steps;
+    float u = rng.next();
+    float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) ? mc_div(-mc_log(u), g0.x)
+                                                                   : -mc_log(u) * g0.z;
+    step = fminf(step, FLT_MAX);
+    /* mcsim_intersect, mcvox.template.c:173-196 */
+    f3 dist;
+    dist.x = g.tl[0] + (float)((s.dir.x >= 0.0f) + s.vi.x) * g.vs[0] - s.pos.x;
+    dist.y = g.tl[1] + (float)((s.dir.y >= 0.0f) + s.vi.y) * g.vs[1] - s.pos.y;
+    dist.z = g.tl[2] + (float)((s.dir.z >= 0.0f) + s.vi.z) * g.vs[2] - s.pos.z;
+    dist.x = (s.dir.x != 0.0f) ? mc_div(dist.x, s.dir.x) : __int_as_float(0x7f800000);
+    dist.y = (s.dir.y != 0.0f) ? mc_div(dist.y, s.dir.y) : __int_as_float(0x7f800000);
+    dist.z = (s.dir.z != 0.0f) ? mc_div(dist.z, s.dir.z) : __int_as_float(0x7f800000);
+    float d = fminf(dist.x, fminf(dist.y, dist.z));
+    float d_ok = fminf(d, step);
+    s.pos.x = s.pos.x + d_ok * s.dir.x;
+    s.pos.y = s.pos.y + d_ok * s.dir.y;
+    s.pos.z = s.pos.z + d_ok * s.dir.z;
+    if (x.track_opl) s.opl += M[s.mat].g1.x * d_ok;
+
+    bool done = false;
+    if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
+        float mua = g0.y;
+        float fraction = 1.0f - mc_exp(-mua * d_ok);
+        float deposit = fraction * s.w;
+        s.w -= deposit;
+        s.events |= MCGB_EV_ABSORPTION;
+        if (FLU) {
+            float step_back = (mua != 0.0f)
+                                  ? d_ok - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
+                                  : 0.0f;
+            f3 dp{s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
+                  s.pos.z - step_back * s.dir.z};
+            fluence_deposit(c.fluence, dp, deposit, mua, accu, fcache);
+        }
+        if (d < step) {
+            s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
+            if (!mv_valid(g, s.vi)) {
+                if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
+                else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+                done = true;
+            }
+        } else {
+            const MvMaterial &cm = M[s.mat];
+            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
+            scatter_direction(s.dir, ct, az);
+            s.events |= MCGB_EV_SCATTERING;
+        }
+        if (s.w < o.packet_weight_min) {
+            if (o.use_lottery) {
+                if (rng.next() > o.lottery_chance) done = true;
+                else s.w = mc_div(s.w, o.lottery_chance);
+            } else {
+                done = true;
+            }
+        }
+    } else if (d < step) {
+        s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
+        if (!mv_valid(g, s.vi)) {
+            if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
+            else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+            done = true;
+        }
+    } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
+        if (rng.next() < g0.w) {
+            float deposit = s.w;
+            s.w -= deposit;
+            s.events |= MCGB_EV_ABSORPTION;
+            done = true;
+            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, accu, fcache);
+        } else {
+            const MvMaterial &cm = M[s.mat];
+            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
+            scatter_direction(s.dir, ct, az);
+            s.events |= MCGB_EV_SCATTERING;
+        }
+    } else {
+        float deposit = s.w * g0.w;
+        s.w -= deposit;
+        s.events |= MCGB_EV_ABSORPTION;
+        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, accu, fcache);
+        const MvMaterial &cm = M[s.mat];
+        float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
+        scatter_direction(s.dir, ct, az);
+        s.events |= MCGB_EV_SCATTERING;
+        if (s.w < o.packet_weight_min) {
+            if (o.use_lottery) {
+                if (rng.next() > o.lottery_chance) done = true;
+                else s.w = mc_div(s.w, o.lottery_chance);
+            } else {
+                done = true;
+            }
+        }
+    }
+    /* mcvox.template.c:1004-1008 */
+    bool escaped = s.w <= 0.0f;
+    if (x.use_rmax) {
+        f3 dd{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
+        escaped = escaped || dot3(dd, dd) > x.rmax2;
+    }
+    if (escaped) {
+        done = true;
+        s.events |= MCGB_EV_ESCAPED;
+    }
+    if (x.use_trace) {
+        if (done) s.events |= MCGB_EV_TERMINATED;
+        if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
+            trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
+        s.events = 0;
+    }
+    if (!done && o.max_steps_per_packet && s.steps >= o.max_steps_per_packet) {
+        done = true;
+        status |= MCGB_STATUS_STEP_LIMIT;
+    }
+    return done;
+}
+
+template <int PF>
+static __device__ __forceinline__ const float *mcvox_stage(const McgbMcvoxConfig &c, const McgbBuffers &b,
+                                                           MvSmem &sm, float *s_lut, int lut_in_smem) {
     for (uint32_t i = threadIdx.x; i < c.num_materials; i += blockDim.x) {
         const McgbMaterial &m = b.materials[i];
         MvMaterial h;
@@ -195,187 +376,135 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
     if (lut_in_smem)
         for (uint64_t i = threadIdx.x; i < b.fp_lut_size; i += blockDim.x) s_lut[i] = b.fp_lut[i];
     __syncthreads();
-    const float *lut = lut_in_smem ? s_lut : b.fp_lut;
-    const MvMaterial *M = sm.materials;
+    return lut_in_smem ? s_lut : b.fp_lut;
+}
 
+static __device__ __forceinline__ void mv_finish(const McgbBuffers &b, uint64_t steps, uint64_t packets,
+                                                 uint32_t status, bool count_thread) {
+    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_STEPS), (unsigned long long)steps);
+    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_PACKETS), (unsigned long long)packets);
+    if (count_thread) atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_THREADS), 1ull);
+    if (status) atomicOr((unsigned long long *)(b.counters + MCGB_CNT_STATUS), (unsigned long long)status);
+}
+
+/* STATIC scheduling (thread t owns stream t). */
+template <int PF, int METHOD, bool FLU>
+__global__ void __launch_bounds__(256)
+mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
+                       uint64_t deadline_ns, int lut_in_smem) {
+    __shared__ MvSmem sm;
+    extern __shared__ float s_lut[];
+    const float *lut = mcvox_stage<PF>(c, b, sm, s_lut, lut_in_smem);
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= c.num_streams || t >= c.num_packets) return;
     const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
-
-    MvGeom g;
-    for (int k = 0; k < 3; ++k) {
-        g.tl[k] = c.top_left[k]; g.br[k] = c.bottom_right[k];
-        g.vs[k] = c.voxel_size[k]; g.sh[k] = c.shape[k];
-    }
-    const McgbRunOptions &o = c.opt;
+    const MvCtx x = mcvox_ctx(c, b, sm.materials, lut);
     const uint64_t T = c.num_streams;
-    const bool use_trace = c.trace.flags != MCGB_TRACE_NONE;
-    const bool track_opl = o.track_optical_pathlength != 0;
-    const float rmax2 = o.rmax * o.rmax;
-    const bool use_rmax = rmax2 < __int_as_float(0x7f800000);
-    const f3 src_pos{c.source.position[0], c.source.position[1], c.source.position[2]};
-    const uint8_t *vox = b.voxels;
-    uint64_t *accu = b.accumulator;
-
     Rng rng{b.rng_x[t], b.rng_a[t]};
     FluenceCache fcache{~0ull, 0};
     uint64_t steps = 0, packets = 0;
-    uint32_t packet_steps = 0, iter = 0;
-    uint32_t status = 0;
-
-    uint64_t p = t;
-    f3 pos, dir;
-    i3 vi;
-    int mat;
-    float w, opl = 0.0f;
-    uint32_t trace_count = 0, events = MCGB_EV_LAUNCH;
-    mcvox_launch(c, g, M, vox, rng, pos, dir, w, vi, mat, accu);
-    if (use_trace && (c.trace.flags & MCGB_TRACE_START))
-        trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
-
+    uint32_t iter = 0, status = 0;
+    MvPacket s;
+    mcvox_begin(c, b, x, s, rng, t);
     for (;;) {
-        const float4 g0 = M[mat].g0;   /* mus, mua, inv_mut, mua_inv_mut */
-        ++packet_steps;
-        ++iter;
-        float u = rng.next();
-        float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
-                         ? mc_div(-mc_log(u), g0.x)
-                         : -mc_log(u) * g0.z;
-        step = fminf(step, FLT_MAX);
-        /* mcsim_intersect, mcvox.template.c:173-196 */
-        f3 dist;
-        dist.x = g.tl[0] + (float)((dir.x >= 0.0f) + vi.x) * g.vs[0] - pos.x;
-        dist.y = g.tl[1] + (float)((dir.y >= 0.0f) + vi.y) * g.vs[1] - pos.y;
-        dist.z = g.tl[2] + (float)((dir.z >= 0.0f) + vi.z) * g.vs[2] - pos.z;
-        dist.x = (dir.x != 0.0f) ? mc_div(dist.x, dir.x) : __int_as_float(0x7f800000);
-        dist.y = (dir.y != 0.0f) ? mc_div(dist.y, dir.y) : __int_as_float(0x7f800000);
-        dist.z = (dir.z != 0.0f) ? mc_div(dist.z, dir.z) : __int_as_float(0x7f800000);
-        float d = fminf(dist.x, fminf(dist.y, dist.z));
-        float d_ok = fminf(d, step);
-        pos.x = pos.x + d_ok * dir.x;
-        pos.y = pos.y + d_ok * dir.y;
-        pos.z = pos.z + d_ok * dir.z;
-        if (track_opl) opl += M[mat].g1.x * d_ok;
-
-        bool done = false;
-        if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
-            float mua = g0.y;
-            float fraction = 1.0f - mc_exp(-mua * d_ok);
-            float deposit = fraction * w;
-            w -= deposit;
-            events |= MCGB_EV_ABSORPTION;
-            if (FLU) {
-                float step_back = (mua != 0.0f)
-                                      ? d_ok - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
-                                      : 0.0f;
-                f3 dp{pos.x - step_back * dir.x, pos.y - step_back * dir.y, pos.z - step_back * dir.z};
-                fluence_deposit(c.fluence, dp, deposit, mua, accu, fcache);
-            }
-            if (d < step) {
-                events |= mv_boundary(g, M, vox, dir, vi, mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
-                if (!mv_valid(g, vi)) {
-                    if (vi.z < 0) detector_deposit(c.top, pos, dir, w, accu);
-                    else if (vi.z >= g.sh[2]) detector_deposit(c.bottom, pos, dir, w, accu);
-                    done = true;
-                }
-            } else {
-                const MvMaterial &cm = M[mat];
-                float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, lut, rng, &az);
-                scatter_direction(dir, ct, az);
-                events |= MCGB_EV_SCATTERING;
-            }
-            if (w < o.packet_weight_min) {
-                if (o.use_lottery) {
-                    if (rng.next() > o.lottery_chance) done = true;
-                    else w = mc_div(w, o.lottery_chance);
-                } else {
-                    done = true;
-                }
-            }
-        } else if (d < step) {
-            events |= mv_boundary(g, M, vox, dir, vi, mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
-            if (!mv_valid(g, vi)) {
-                if (vi.z < 0) detector_deposit(c.top, pos, dir, w, accu);
-                else if (vi.z >= g.sh[2]) detector_deposit(c.bottom, pos, dir, w, accu);
-                done = true;
-            }
-        } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
-            if (rng.next() < g0.w) {
-                float deposit = w;
-                w -= deposit;
-                events |= MCGB_EV_ABSORPTION;
-                done = true;
-                if (FLU) fluence_deposit(c.fluence, pos, deposit, g0.y, accu, fcache);
-            } else {
-                const MvMaterial &cm = M[mat];
-                float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, lut, rng, &az);
-                scatter_direction(dir, ct, az);
-                events |= MCGB_EV_SCATTERING;
-            }
-        } else {
-            float deposit = w * g0.w;
-            w -= deposit;
-            events |= MCGB_EV_ABSORPTION;
-            if (FLU) fluence_deposit(c.fluence, pos, deposit, g0.y, accu, fcache);
-            const MvMaterial &cm = M[mat];
-            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, lut, rng, &az);
-            scatter_direction(dir, ct, az);
-            events |= MCGB_EV_SCATTERING;
-            if (w < o.packet_weight_min) {
-                if (o.use_lottery) {
-                    if (rng.next() > o.lottery_chance) done = true;
-                    else w = mc_div(w, o.lottery_chance);
-                } else {
-                    done = true;
-                }
-            }
-        }
-        /* mcvox.template.c:1004-1008 */
-        bool escaped = w <= 0.0f;
-        if (use_rmax) {
-            f3 dd{pos.x - src_pos.x, pos.y - src_pos.y, pos.z - src_pos.z};
-            escaped = escaped || dot3(dd, dd) > rmax2;
-        }
-        if (escaped) {
-            done = true;
-            events |= MCGB_EV_ESCAPED;
-        }
-        if (use_trace) {
-            if (done) events |= MCGB_EV_TERMINATED;
-            if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
-                trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
-            events = 0;
-        }
-        if (!done && o.max_steps_per_packet && packet_steps >= o.max_steps_per_packet) {
-            done = true;
-            status |= MCGB_STATUS_STEP_LIMIT;
-        }
-        if (done) {
+        if (mcvox_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
             ++packets;
-            steps += packet_steps;
-            packet_steps = 0;
-            if (use_trace) b.int_buffer[c.trace.count_offset + p] = (int32_t)trace_count;
-            p += T;
-            if (p >= c.num_packets) break;
-            trace_count = 0;
-            opl = 0.0f;
-            events = MCGB_EV_LAUNCH;
-            mcvox_launch(c, g, M, vox, rng, pos, dir, w, vi, mat, accu);
-            if (use_trace && (c.trace.flags & MCGB_TRACE_START))
-                trace_event(c.trace, p, trace_count, events, pos, dir, w, opl, b.float_buffer);
+            steps += s.steps;
+            mcvox_end(c, b, x, s);
+            uint64_t p = s.p + T;
+            if (p >= c.num_packets) {
+                s.steps = 0;
+                break;
+            }
+            mcvox_begin(c, b, x, s, rng, p);
         }
-        if ((iter & 1023u) == 0) {
+        if (((++iter) & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
             if (*(volatile uint64_t *)(b.counters + MCGB_CNT_ABORT)) { status |= MCGB_STATUS_ABORTED; break; }
         }
     }
-    steps += packet_steps;
-    if (FLU) fcache.flush(accu);
+    steps += s.steps;
+    if (FLU) fcache.flush(b.accumulator);
     b.rng_x[t] = rng.x;
-    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_STEPS), (unsigned long long)steps);
-    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_PACKETS), (unsigned long long)packets);
-    atomicAdd((unsigned long long *)(b.counters + MCGB_CNT_THREADS), 1ull);
-    if (status) atomicOr((unsigned long long *)(b.counters + MCGB_CNT_STATUS), (unsigned long long)status);
+    mv_finish(b, steps, packets, status, true);
+}
+
+/* DYNAMIC scheduling (per-packet streams, warp refill). */
+template <int PF, int METHOD, bool FLU>
+__global__ void __launch_bounds__(256)
+mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
+                     uint64_t deadline_ns, int lut_in_smem) {
+    __shared__ MvSmem sm;
+    extern __shared__ float s_lut[];
+    const float *lut = mcvox_stage<PF>(c, b, sm, s_lut, lut_in_smem);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
+    const MvCtx x = mcvox_ctx(c, b, sm.materials, lut);
+    const uint64_t N = c.num_packets;
+    const uint64_t B = 128;
+    unsigned long long *queue = (unsigned long long *)(b.counters + MCGB_CNT_QUEUE);
+    uint64_t item_next = 0, item_end = 0;
+    bool more = true, active = false;
+    Rng rng{0ull, 1u};
+    FluenceCache fcache{~0ull, 0};
+    uint64_t steps = 0, packets = 0;
+    uint32_t iter = 0, status = 0;
+    MvPacket s;
+    s.steps = 0;
+    for (;;) {
+        uint32_t need = __ballot_sync(0xffffffffu, !active);
+        while (need && more) {
+            if (item_next >= item_end) {
+                unsigned long long item = 0;
+                if (lane == 0) item = atomicAdd(queue, 1ull);
+                item = __shfl_sync(0xffffffffu, item, 0);
+                item_next = (uint64_t)item * B;
+                if (item_next >= N) {
+                    more = false;
+                    break;
+                }
+                item_end = min(item_next + B, N);
+            }
+            uint32_t avail = (uint32_t)min(item_end - item_next, (uint64_t)32);
+            uint32_t rank = __popc(need & ((1u << lane) - 1u));
+            bool mine = ((need >> lane) & 1u) && rank < avail;
+            if (mine) {
+                uint64_t p = item_next + rank;
+                uint64_t xs;
+                uint32_t as;
+                br_packet_stream(c.opt.seed, 0u, c.opt.packet_offset + p, b.rng_a, c.num_streams, &xs, &as);
+                rng = Rng{xs, as};
+                mcvox_begin(c, b, x, s, rng, p);
+                active = true;
+            }
+            uint32_t taken = __ballot_sync(0xffffffffu, mine);
+            item_next += __popc(taken);
+            need &= ~taken;
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && mcvox_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
+            ++packets;
+            steps += s.steps;
+            s.steps = 0;
+            mcvox_end(c, b, x, s);
+            active = false;
+        }
+        if (((++iter) & 1023u) == 0) {
+            uint32_t stop = 0;
+            if (lane == 0) {
+                if (globaltimer_ns() > t_deadline) stop = MCGB_STATUS_TIMEOUT;
+                else if (*(volatile uint64_t *)(b.counters + MCGB_CNT_ABORT)) stop = MCGB_STATUS_ABORTED;
+            }
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            if (stop) {
+                status |= stop;
+                break;
+            }
+        }
+    }
+    steps += s.steps;
+    if (FLU) fcache.flush(b.accumulator);
+    mv_finish(b, steps, packets, status, packets > 0);
 }
 
 }  // namespace MCGB_NS

@@ -78,6 +78,30 @@ class McUseNativeMath(McBoolOption):
         super().__init__('MC_USE_NATIVE_MATH', value)
 
 
+class McScheduling(McOption):
+    """How packets are distributed over the GPU threads.
+
+    'dynamic' (default): persistent warps take packets from a device queue
+    and refill idle lanes packet by packet; packet p simulates on its own
+    multiply-with-carry stream derived from (rnginit, p), so results are
+    bit-reproducible and every lane stays busy until the last packets.
+    'static': thread t owns stream t of the seed table and simulates packets
+    t, t+T, t+2T, ... (the reference's per-thread streams, continued from run
+    to run)."""
+    static = None
+    dynamic = None
+
+    def __init__(self, value: str = 'dynamic'):
+        if value not in ('static', 'dynamic'):
+            raise ValueError('scheduling must be "static" or "dynamic"')
+        super().__init__('MCGB_SCHEDULING', value)
+
+
+McScheduling.static = McScheduling('static')
+McScheduling.dynamic = McScheduling('dynamic')
+McScheduling.default = McScheduling.dynamic
+
+
 class McUseHalfMath(McBoolOption):
     """Mapped to McUseNativeMath: the GB300 fast path is the narrowest
     precision offered."""

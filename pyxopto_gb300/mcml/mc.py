@@ -109,19 +109,14 @@ class Mc(McEngine):
         t0 = time.perf_counter()
         if wgsize is not None:
             self._block_size = int(wgsize)
-        cfg = self.pack(nphotons)
-        n_streams = self.suggested_streams(cfg.opt.math) if maxthreads is None \
-            else max(1, int(maxthreads))
-        device = torch.device('cuda', torch.cuda.current_device())
-        self._ensure_streams(torch, n_streams, device)
-        cfg.num_streams = n_streams
-        buffers = self._device_buffers(torch, device, self._lut_array(), {})
+        fn, cfg, buffers = self._prepare(nphotons, maxthreads)
         t1 = time.perf_counter()
-        code, counters = self._launch(lib.mcgb_mcml_run, cfg, buffers, torch)
+        code, counters = self._launch(fn, cfg, buffers, torch)
         t2 = time.perf_counter()
         self._run_report.update(status=counters[_abi.CNT_STATUS],
                                 packets_done=counters[_abi.CNT_PACKETS])
         _lib.check(code)
+        self._packets_total += nphotons
         results = self._download(nphotons, out)
         t3 = time.perf_counter()
         self._run_report.update(upload=t1 - t0, execution=t2 - t1, download=t3 - t2,
@@ -135,6 +130,24 @@ class Mc(McEngine):
                       nphotons, counters[_abi.CNT_THREADS], counters[_abi.CNT_STEPS],
                       (t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3))
         return results
+
+    def _prepare(self, nphotons, maxthreads=None):
+        """Packs the configuration, seeds the device streams and allocates
+        the device buffers; returns (C-ABI launch function, config, buffers)."""
+        torch = torch_cuda()
+        lib = _lib.load()
+        cfg = self.pack(nphotons)
+        device = torch.device('cuda', torch.cuda.current_device())
+        dynamic = cfg.opt.scheduling == _abi.SCHED_DYNAMIC
+        if dynamic:
+            cfg.num_streams = self._ensure_dynamic_streams(torch, device)
+        else:
+            n_streams = self.suggested_streams(cfg.opt.math) if maxthreads is None \
+                else max(1, int(maxthreads))
+            self._ensure_streams(torch, n_streams, device)
+            cfg.num_streams = n_streams
+        buffers = self._device_buffers(torch, device, self._lut_array(), {'_dynamic': dynamic})
+        return lib.mcgb_mcml_run, cfg, buffers
 
     def _download(self, nphotons, out):
         accu = self._dev['accu'].cpu().numpy().view(np.uint64)

@@ -102,27 +102,14 @@ class Mc(McEngine):
         t0 = time.perf_counter()
         if wgsize is not None:
             self._block_size = int(wgsize)
-        cfg, mats = self.pack(nphotons)
-        n_streams = self.suggested_streams(cfg.opt.math) if maxthreads is None \
-            else max(1, int(maxthreads))
-        device = torch.device('cuda', torch.cuda.current_device())
-        self._ensure_streams(torch, n_streams, device)
-        cfg.num_streams = n_streams
-        vox = np.ascontiguousarray(self._voxels.data(), dtype=np.uint8)
-        key = (vox.shape, vox.tobytes().__hash__())
-        if self._dev.get('vox_key') != key:
-            self._dev['vox'] = torch.from_numpy(vox.reshape(-1).copy()).to(device)
-            self._dev['vox_key'] = key
-        mat_bytes = np.frombuffer(bytes(mats), dtype=np.uint8).copy()
-        self._dev['mats'] = torch.from_numpy(mat_bytes).to(device)
-        buffers = self._device_buffers(torch, device, self._lut_array(), {
-            'voxels': self._dev['vox'].data_ptr(), 'materials': self._dev['mats'].data_ptr()})
+        fn, cfg, buffers = self._prepare(nphotons, maxthreads)
         t1 = time.perf_counter()
-        code, counters = self._launch(lib.mcgb_mcvox_run, cfg, buffers, torch)
+        code, counters = self._launch(fn, cfg, buffers, torch)
         t2 = time.perf_counter()
         self._run_report.update(status=counters[_abi.CNT_STATUS],
                                 packets_done=counters[_abi.CNT_PACKETS])
         _lib.check(code)
+        self._packets_total += nphotons
         results = self._download(nphotons, out)
         t3 = time.perf_counter()
         self._run_report.update(upload=t1 - t0, execution=t2 - t1, download=t3 - t2,
@@ -133,6 +120,34 @@ class Mc(McEngine):
             print('McKernel processed {:,d} packets in {:,d} threads in {:.3f} ms'.format(
                 nphotons, counters[_abi.CNT_THREADS], (t2 - t1) * 1e3))
         return results
+
+    def _prepare(self, nphotons, maxthreads=None):
+        """Packs the configuration, seeds the device streams, uploads the
+        voxels and materials and allocates the device buffers; returns
+        (C-ABI launch function, config, buffers)."""
+        torch = torch_cuda()
+        lib = _lib.load()
+        cfg, mats = self.pack(nphotons)
+        device = torch.device('cuda', torch.cuda.current_device())
+        dynamic = cfg.opt.scheduling == _abi.SCHED_DYNAMIC
+        if dynamic:
+            cfg.num_streams = self._ensure_dynamic_streams(torch, device)
+        else:
+            n_streams = self.suggested_streams(cfg.opt.math) if maxthreads is None \
+                else max(1, int(maxthreads))
+            self._ensure_streams(torch, n_streams, device)
+            cfg.num_streams = n_streams
+        vox = np.ascontiguousarray(self._voxels.data(), dtype=np.uint8)
+        key = (vox.shape, hash(vox.tobytes()))
+        if self._dev.get('vox_key') != key:
+            self._dev['vox'] = torch.from_numpy(vox.reshape(-1).copy()).to(device)
+            self._dev['vox_key'] = key
+        mat_bytes = np.frombuffer(bytes(mats), dtype=np.uint8).copy()
+        self._dev['mats'] = torch.from_numpy(mat_bytes).to(device)
+        buffers = self._device_buffers(torch, device, self._lut_array(), {
+            'voxels': self._dev['vox'].data_ptr(), 'materials': self._dev['mats'].data_ptr(),
+            '_dynamic': dynamic})
+        return lib.mcgb_mcvox_run, cfg, buffers
 
     def _download(self, nphotons, out):
         accu = self._dev['accu'].cpu().numpy().view(np.uint64)

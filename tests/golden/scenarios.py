@@ -143,6 +143,26 @@ BENCH = {
         source=dict(type='Line'),
         detectors=dict(top=dict(type='Radial', axis=[0.0, 5e-3, 50]), specular=dict(type='Total')),
         nphotons=1_000_000, streams=0, rnginit=1),
+    # 200^3 uint8 voxels of 0.05 mm: epidermis (0.1 mm) over a dermis-like
+    # background (mua 0.02/mm, mus 15/mm, g 0.9) with a blood vessel
+    # (radius 0.5 mm, mua 2/mm, n 1.33) along y at 1 mm depth; Gaussian beam
+    # sigma 0.3 mm; deposition tally on the voxel grid; 1e8 packets.
+    # Values the benchmark does not fix follow the reference's skin/vessel
+    # dataset template: epidermis optics, blood scattering, n 1.33.
+    'c3_vox_skin_vessel': dict(
+        medium='mcvox',
+        grid=dict(x=[-5e-3, 5e-3, 200], y=[-5e-3, 5e-3, 200], z=[0.0, 10e-3, 200]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.33, mua=20.0, mus=1.5e4, pf=['Hg', 0.9]),
+                   dict(n=1.33, mua=1657.24, mus=37593.98, pf=['Hg', 0.9]),
+                   dict(n=1.33, mua=2000.0, mus=9398.5, pf=['Hg', 0.9])],
+        layout=dict(kind='skin_vessel', epidermis=1e-4, vessel_depth=1.0e-3, vessel_radius=5e-4),
+        source=dict(type='GaussianBeam', sigma=3e-4, clip=5.0),
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-5e-3, 5e-3, 200], y=[-5e-3, 5e-3, 200], z=[0.0, 10e-3, 200],
+                     mode='deposition'),
+        nphotons=100_000_000, streams=0, rnginit=1),
 }
 ALL = dict(SCENARIOS, **BENCH)
 
@@ -211,15 +231,19 @@ def _source(src_mod, spec):
     return getattr(src_mod, spec['type'])(**kw)
 
 
-def options(pkg, scenario, fast=False):
+def options(pkg, scenario, fast=False, scheduling=None):
     opts = [pkg.mcoptions.McMethod(scenario.get('method', 0))]
     if fast:
         opts.append(pkg.mcoptions.McUseNativeMath(True))
+    if scheduling is not None:
+        opts.append(pkg.mcoptions.McScheduling(scheduling))
     return opts
 
 
-def build_mc(name_or_spec, fast=False, package='pyxopto_gb300'):
-    """A pyxopto_gb300 simulator for a scenario."""
+def build_mc(name_or_spec, fast=False, package='pyxopto_gb300', scheduling='static'):
+    """A pyxopto_gb300 simulator for a scenario (static scheduling unless
+    asked otherwise: the reference's per-thread streams, which the golden
+    fixtures pin)."""
     import importlib
     s = ALL[name_or_spec] if isinstance(name_or_spec, str) else name_or_spec
     if s['medium'] == 'mcml':
@@ -228,7 +252,7 @@ def build_mc(name_or_spec, fast=False, package='pyxopto_gb300'):
             mc.mclayer.Layer(d=l['d'], n=l['n'], mua=l['mua'], mus=l['mus'], pf=_pf(mc, l['pf']))
             for l in s['layers']])
         obj = mc.Mc(layers, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
-                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast),
+                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast, scheduling),
                     rnginit=s['rnginit'])
     else:
         mc = importlib.import_module(package + '.mcvox.mc')
@@ -239,7 +263,7 @@ def build_mc(name_or_spec, fast=False, package='pyxopto_gb300'):
         mats = [mc.mcmaterial.Material(n=m['n'], mua=m['mua'], mus=m['mus'], pf=_pf(mc, m['pf']))
                 for m in s['materials']]
         obj = mc.Mc(vox, mats, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
-                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast),
+                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast, scheduling),
                     rnginit=s['rnginit'])
     if 'rmax' in s:
         obj.rmax = s['rmax']

@@ -80,7 +80,7 @@ def test_batched_matches_plain_runs(cuda, lib):
     from pyxopto_gb300.mcml import mc
     sims = BatchedMc.sample_sims(6, seed=11, packets=(400000, 400001))
     b = BatchedMc(sims, raxis=mc.mcdetector.Axis(0.0, 3e-3, 30), fast=True)
-    refl = b.run()
+    raw = b.run_raw().astype(np.float64) / 8388607.0
     for i in range(6):
         layers = mc.mclayer.Layers([
             mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0)),
@@ -93,8 +93,9 @@ def test_batched_matches_plain_runs(cuda, lib):
         m = mc.Mc(layers, mc.mcsource.Line(), det, options=[mc.mcoptions.McUseNativeMath(True)],
                   rnginit=100 + i)
         _, _, d = m.run(400000)
-        ra = refl[i].sum()
-        rb = d.top.reflectance.sum()
+        # total diffuse reflectance per packet: relative MC error ~0.2 % here
+        ra = raw[i].sum() / 400000
+        rb = d.top.raw.sum() / 400000
         assert abs(ra - rb) / rb < 0.01, (i, ra, rb)
 
 

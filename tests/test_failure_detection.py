@@ -13,9 +13,10 @@ import scenarios
 pytestmark = pytest.mark.gpu
 
 
-def test_deadline_expiry_is_reported_and_device_stays_usable(cuda, lib, oracle):
+@pytest.mark.parametrize('scheduling', ['static', 'dynamic'])
+def test_deadline_expiry_is_reported_and_device_stays_usable(cuda, lib, oracle, scheduling):
     from pyxopto_gb300 import _abi, _lib
-    mc = scenarios.build_mc('c2_gk_fluence', fast=True)
+    mc = scenarios.build_mc('c2_gk_fluence', fast=True, scheduling=scheduling)
     mc.deadline = 0.25
     t0 = time.perf_counter()
     with pytest.raises(_lib.McgbError) as ei:

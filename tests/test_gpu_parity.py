@@ -20,25 +20,41 @@ K = 8388607.0
 
 
 def gpu_run(mc, nphotons, streams, torch):
-    trace, fluence, dets = mc.run(nphotons, maxthreads=streams)
+    trace, fluence, dets = mc.run(nphotons, maxthreads=streams or None)
     accu = mc._dev['accu'].cpu().numpy().view(np.uint64).copy()
     return accu, mc.rng_states(), mc.run_report
 
 
 @pytest.mark.parametrize('name', sorted(scenarios.SCENARIOS))
-def test_exact_mode_bit_identical_to_oracle(cuda, lib, oracle, name):
+@pytest.mark.parametrize('scheduling', ['static', 'dynamic'])
+def test_exact_mode_bit_identical_to_oracle(cuda, lib, oracle, name, scheduling):
     s = scenarios.SCENARIOS[name]
     n, t = s['nphotons'], s['streams']
-    mc = scenarios.build_mc(name)
+    mc = scenarios.build_mc(name, scheduling=scheduling)
     ref = oracle.run(mc, n, t, oracle.PORTABLE)
     accu, rng_x, report = gpu_run(mc, n, t, cuda)
     got = oracle.tallies(mc, accu)
     assert set(got) == set(k for k in ref if k in got)
     for k in got:
         assert np.array_equal(got[k], ref[k]), (k, int(got[k].sum()), int(ref[k].sum()))
-    assert np.array_equal(rng_x, ref['rng_x'])
     assert report['steps'] == ref['steps']
-    assert report['threads'] == min(t, n)
+    assert report['packets_done'] == n
+    if scheduling == 'static':
+        assert np.array_equal(rng_x, ref['rng_x'])
+        assert report['threads'] == min(t, n)
+
+
+def test_dynamic_runs_continue_with_new_packets(cuda, lib, oracle):
+    """A second dynamic run simulates packets n..2n-1 (fresh streams)."""
+    mc = scenarios.build_mc('c1_line_hg_radial', scheduling='dynamic')
+    n = 3000
+    a1, _, _ = gpu_run(mc, n, 0, cuda)
+    a2, _, _ = gpu_run(mc, n, 0, cuda)
+    assert not np.array_equal(a1, a2)
+    ref = scenarios.build_mc('c1_line_hg_radial', scheduling='dynamic')
+    ref._packets_total = n
+    r2 = oracle.run(ref, n, 0, oracle.PORTABLE)
+    assert np.array_equal(a2[:r2['accu'].size], r2['accu'])
 
 
 def test_exact_mode_many_streams_bit_identical(cuda, lib, oracle):
@@ -148,10 +164,11 @@ def test_rng_dump_matches_oracle(cuda, lib, oracle):
     assert np.array_equal(out, oracle.rng_dump(18446741578333584324, 4294966893, 5000))
 
 
-def test_trace_bit_identical_to_oracle(cuda, lib, oracle):
+@pytest.mark.parametrize('scheduling', ['static', 'dynamic'])
+def test_trace_bit_identical_to_oracle(cuda, lib, oracle, scheduling):
     from pyxopto_gb300.mcml import mc
     spec = dict(scenarios.SCENARIOS['c1_line_hg_radial'])
-    sim = scenarios.build_mc(spec)
+    sim = scenarios.build_mc(spec, scheduling=scheduling)
     sim._trace = mc.mctrace.Trace(maxlen=64, options=mc.mctrace.Trace.TRACE_ALL)
     n, t = 300, 32
     ref = oracle.run(sim, n, t, oracle.PORTABLE)
