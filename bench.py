@@ -253,7 +253,8 @@ def batched_bench(args):
     persistent launch replayed from a CUDA graph; metric profiles/s."""
     import torch
     from pyxopto_gb300.batched import BatchedMc
-    sims = BatchedMc.sample_sims(4096, seed=1)
+    nsims = args.sims
+    sims = BatchedMc.sample_sims(nsims, seed=1)
     b = BatchedMc(sims, fast=args.math == 'fast')
     tune = b.autotune()
     for _ in range(args.warmup):
@@ -276,16 +277,16 @@ def batched_bench(args):
         b.run(graph=True)
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     steps = b.last_report['steps']
-    return {'metric': 'profiles/s (batched MC, 4096 single-layer simulations)',
-            'value': 4096 / dev_s, 'unit': 'profiles/s', 'ms_per_step': dev_s * 1e3,
+    return {'metric': 'profiles/s (batched MC, {} single-layer simulations)'.format(nsims),
+            'value': nsims / dev_s, 'unit': 'profiles/s', 'ms_per_step': dev_s * 1e3,
             'packets_per_s': npk / dev_s, 'steps_per_s': steps / dev_s,
-            'config': {'workload': 'batched_4096', 'sims': 4096, 'packets_total': npk,
+            'config': {'workload': 'batched_4096', 'sims': nsims, 'packets_total': npk,
                        'radial_bins': 30, 'r_max_m': 3e-3, 'autotuned': {
                            k: tune[k] for k in ('block_size', 'packets_per_item')},
                        'graph': True},
             'clocks': clocks, 'gpu_launches': 2 * args.steps,
-            'e2e': {'value': 4096 / e2e_s, 'unit': 'profiles/s',
-                    'h2d_bytes_per_step': 40 * 4096, 'd2h_bytes_per_step': 8 * 30 * 4096 + 64,
+            'e2e': {'value': nsims / e2e_s, 'unit': 'profiles/s',
+                    'h2d_bytes_per_step': 40 * nsims, 'd2h_bytes_per_step': 8 * 30 * nsims + 64,
                     'path': 'pyxopto_gb300.batched.BatchedMc.run(graph=True)'}}
 
 
@@ -364,6 +365,7 @@ def main():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--sims', type=int, default=4096, help='batched workload: simulations')
     ap.add_argument('--train-sims', type=int, default=1 << 16)
     ap.add_argument('--train-packets', type=int, default=100_000)
     ap.add_argument('--train-epochs', type=int, default=150)
