@@ -13,6 +13,13 @@ the queries (1 % by default) is re-simulated with the batched engine as the
 judge, and every judged query whose relative RMS error exceeds the tolerance
 is replaced by its Monte Carlo profile.  If more than ``max_fail`` of the
 judged queries fail, the whole batch falls back to Monte Carlo.
+
+The judge's own Monte Carlo noise is comparable to the 1 % tolerance at
+1e6 packets, so each judged query is simulated as two independent halves
+(a, b) and the noise is taken out of the measured error:
+err^2 = mean(((pred - m)/m)^2) - mean(((a - b)/(2 m))^2) with m = (a + b)/2,
+an unbiased estimate of the squared error against the exact profile, because
+E[(a - b)^2] / 4 is the variance of m.
 """
 import ctypes as C
 import time
@@ -238,12 +245,38 @@ class Surrogate:
             return np.sqrt((rel ** 2).sum(1) / np.maximum(mask.sum(1), 1))
         return np.sqrt((rel ** 2).mean(1))
 
+    @staticmethod
+    def judge_error(pred, a, b, mask=None):
+        """Noise-corrected relative RMS error of ``pred`` against the exact
+        profile, from two independent Monte Carlo halves ``a`` and ``b``.
+        Returns (corrected error, raw error against (a+b)/2, MC noise of
+        (a+b)/2), all per profile."""
+        m = 0.5 * (a + b)
+        den = np.where(m > 0, m, 1.0)
+        e2 = ((pred - m) / den) ** 2
+        n2 = ((a - b) / (2.0 * den)) ** 2
+        if mask is None:
+            mask = np.ones_like(m, dtype=bool)
+        cnt = np.maximum(mask.sum(1), 1)
+        raw2 = np.where(mask, e2, 0.0).sum(1) / cnt
+        noise2 = np.where(mask, n2, 0.0).sum(1) / cnt
+        return np.sqrt(np.maximum(raw2 - noise2, 0.0)), np.sqrt(raw2), np.sqrt(noise2)
+
+    def simulate_halves(self, sims, packets, seed=7):
+        """Two independent Monte Carlo halves of ``packets``/2 packets each
+        for every simulation, in one batched launch."""
+        k = len(sims['mua'])
+        both = {key: np.concatenate([np.asarray(v), np.asarray(v)]) for key, v in sims.items()}
+        both['num_packets'] = np.full(2 * k, max(int(packets) // 2, 1), dtype=np.uint64)
+        r = self.simulate(both, seed=seed)
+        return r[:k], r[k:]
+
     def serve(self, sims, judge_fraction=0.01, judge_packets=1_000_000, tol=0.01, max_fail=0.1,
               seed=7, rel_floor=None):
         """Answers a batch of queries: network prediction for all, Monte Carlo
-        judge on a fraction, MC fallback where the judge disagrees by more
-        than ``tol`` (relative RMS over the bins above ``rel_floor`` of the
-        profile peak).  Returns (profiles, report)."""
+        judge on a fraction, MC fallback where the judge's noise-corrected
+        relative RMS error (over the bins above ``rel_floor`` of the profile
+        peak) exceeds ``tol``.  Returns (profiles, report)."""
         import torch
         m = len(sims['mua'])
         t0 = time.perf_counter()
@@ -255,13 +288,13 @@ class Surrogate:
         nj = max(1, int(round(judge_fraction * m)))
         jidx = np.sort(rng.choice(m, nj, replace=False))
         jsims = {k: np.asarray(v)[jidx] for k, v in sims.items()}
-        jsims['num_packets'] = np.full(nj, judge_packets, dtype=np.uint64)
-        mc = self.simulate(jsims, seed=seed)
+        a, b = self.simulate_halves(jsims, judge_packets, seed=seed)
+        mc = 0.5 * (a + b)
         t2 = time.perf_counter()
         mask = None
         if rel_floor is not None:
             mask = mc >= rel_floor * mc.max(1, keepdims=True)
-        err = self.rms_rel(pred[jidx], mc, mask)
+        err, raw, noise = self.judge_error(pred[jidx], a, b, mask)
         fail = err > tol
         out = pred.copy()
         out[jidx[fail]] = mc[fail]
@@ -273,9 +306,46 @@ class Surrogate:
             out = self.simulate(all_sims, seed=seed + 1)
             t3 = time.perf_counter()
         rep = {'queries': m, 'judged': nj, 'judge_rms_rel_mean': float(err.mean()),
-               'judge_rms_rel_median': float(np.median(err)), 'judge_fail_fraction': float(fail.mean()),
+               'judge_rms_rel_median': float(np.median(err)),
+               'judge_rms_rel_p90': float(np.percentile(err, 90)),
+               'judge_raw_rms_rel_median': float(np.median(raw)),
+               'judge_noise_rms_rel_median': float(np.median(noise)),
+               'judge_fail_fraction': float(fail.mean()),
                'fallback_all': fallback, 'infer_seconds': t1 - t0, 'judge_seconds': t2 - t1,
                'fallback_seconds': t3 - t2, 'seconds': (t3 if fallback else t2) - t0}
         rep['profiles_per_s'] = m / rep['seconds']
         self.report.update(serve=rep)
         return out, rep
+
+
+def sequential_plain_mc(sims, packets=None):
+    """Profiles/s of the method without the network: one plain Mc.run of
+    ``packets`` packets (default: each simulation's num_packets) per profile,
+    in sequence, on one warm simulator whose
+    layer is updated between runs, as the reference's sweep helpers do
+    (xopto/mcml/mcrun/helper.py:640-686).  The last simulation of ``sims``
+    is the untimed warm-up."""
+    import torch
+    from .mcml import mc
+    layers = mc.mclayer.Layers([
+        mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0)),
+        mc.mclayer.Layer(d=np.inf, n=1.4, mua=10.0, mus=1e4, pf=mc.mcpf.Hg(0.8)),
+        mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0))])
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(mc.mcdetector.Axis(0.0, 3e-3, 30)))
+    sim = mc.Mc(layers, mc.mcsource.Line(), det, options=[mc.mcoptions.McUseNativeMath(True)],
+                rnginit=1)
+    nprof = len(sims['mua']) - 1
+
+    def one(i):
+        layer = sim.layers[1]
+        layer.n, layer.mua, layer.mus = float(sims['n'][i]), float(sims['mua'][i]), float(sims['mus'][i])
+        layer.pf = mc.mcpf.Hg(float(sims['g'][i]))
+        return sim.run(int(sims['num_packets'][i]) if packets is None else packets)
+
+    one(nprof)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(nprof):
+        one(i)
+    torch.cuda.synchronize()
+    return nprof / (time.perf_counter() - t0)

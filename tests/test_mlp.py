@@ -96,7 +96,7 @@ def test_training_reduces_loss(cuda):
 
 def test_surrogate_end_to_end(cuda, lib):
     from pyxopto_gb300.batched import BatchedMc
-    from pyxopto_gb300.surrogate import Surrogate
+    from pyxopto_gb300.surrogate import Surrogate, sequential_plain_mc
     sur = Surrogate()
     train = BatchedMc.sample_sims(8192, seed=21, packets=(20000, 20001))
     refl = sur.simulate(train)
@@ -107,3 +107,8 @@ def test_surrogate_end_to_end(cuda, lib):
                          rel_floor=1e-3)
     assert out.shape == (2048, 30)
     assert rep['judge_rms_rel_median'] < 0.1, rep
+    # what the network gains: the same 2048 profiles from sequential plain
+    # Monte Carlo at the judge's packet count
+    seq = BatchedMc.sample_sims(5, seed=23, packets=(1, 2))
+    plain = sequential_plain_mc(seq, 200000)
+    assert rep['profiles_per_s'] > 10.0 * plain, (rep['profiles_per_s'], plain)
