@@ -98,7 +98,7 @@ enum { MCGB_METHOD_ALBEDO_WEIGHT = 0,       /* MC_METHOD 0 (default)      */
        MCGB_METHOD_ALBEDO_REJECTION = 1,    /* MC_METHOD 1                */
        MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT = 2 };
 enum { MCGB_PF_HG = 0, MCGB_PF_GK = 1, MCGB_PF_LUT = 2 };
-enum { MCGB_SRC_LINE = 0, MCGB_SRC_GAUSSIAN_BEAM = 1 };
+enum { MCGB_SRC_LINE = 0, MCGB_SRC_GAUSSIAN_BEAM = 1, MCGB_SRC_UNIFORM_FIBER_NI = 2 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2 };
 enum { MCGB_FLUENCE_NONE = 0, MCGB_FLUENCE_DEPOSITION = 1, MCGB_FLUENCE_RATE = 2 };
 /* Trace flags (xopto/mcbase/mctrace.py TRACE_START/END/ALL). */
@@ -155,7 +155,11 @@ typedef struct McgbMaterial {
      reflectance.
    GaussianBeam mcvox (xopto/mcvox/mcsource/gaussianbeam.py:112-190):
      transformation, position, direction (in the surrounding medium), sigma,
-     clip. */
+     clip.
+   UniformFiberNI mcml (xopto/mcml/mcsource/fiberni.py:246-290,383-412):
+     position = centre of the fibre core on the sample surface,
+     sigma[0] = core radius, sigma[1] = cosine of the acceptance angle in
+     air, sqrt(1 - NA^2), clip = refractive index of the core. */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];
@@ -212,7 +216,7 @@ typedef struct McgbRunOptions {
     float rmax;                             /* Mc.rmax (inf = no limit)        */
     int32_t track_optical_pathlength;       /* MC_TRACK_OPTICAL_PATHLENGTH     */
     uint32_t block_size;                    /* threads per block (0 = auto)    */
-    uint64_t max_steps_per_packet;          /* 0 = unlimited                   */
+    uint64_t max_steps_per_packet;          /* 0 = unlimited (2^32 - 1 at most) */
     double deadline_s;                      /* device wall-clock limit, 0=300s */
     int32_t scheduling;                     /* MCGB_SCHED_*                    */
     uint32_t reserved;

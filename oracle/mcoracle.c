@@ -118,6 +118,29 @@ static float reflectance(float n1, float n2, float cos1, float cc) {
     return R;
 }
 
+/* reflectance_cos2, xopto/mcbase/kernel/mcbase.template.c:1303-1347 */
+static float reflectance_cos2(float n1, float n2, float cos2) {
+    float Rp, Rs, R = 1.0f, n1_d_n2, sin1, sin2, cos1, n_cos1, n_cos2;
+    cos2 = fabsf(cos2);
+    if (n1 == n2) return 0.0f;
+    sin2 = sqrtf(1.0f - cos2 * cos2);
+    if (cos2 >= 1.0f) sin2 = 0.0f;
+    sin1 = (n2 / n1) * sin2;
+    if (sin1 < 1.0f) {
+        cos1 = sqrtf(1.0f - sin1 * sin1);
+        n1_d_n2 = n1 / n2;
+        n_cos1 = n1_d_n2 * cos1;
+        n_cos2 = n1_d_n2 * cos2;
+        Rs = (n_cos1 - cos2) / (n_cos1 + cos2);
+        Rs *= Rs;
+        Rp = (n_cos2 - cos1) / (n_cos2 + cos1);
+        Rp *= Rp;
+        R = 0.5f * (Rp + Rs);
+        if (cos1 <= 0.0f || sin2 == 1.0f) return 1.0f;
+    }
+    return R;
+}
+
 /* reflect, xopto/mcbase/kernel/mcbase.template.c:1361-1369 */
 static inline v3 reflect3(v3 p, v3 n) {
     float p_n_2 = 2.0f * dot3(p, n);
@@ -296,8 +319,9 @@ typedef struct {
     float opl;
 } MlState;
 
-/* Line.mcsim_launch (xopto/mcml/mcsource/line.py:95-108) and
-   GaussianBeam.mcsim_launch (xopto/mcml/mcsource/gaussianbeam.py:119-170). */
+/* Line.mcsim_launch (xopto/mcml/mcsource/line.py:95-108),
+   GaussianBeam.mcsim_launch (xopto/mcml/mcsource/gaussianbeam.py:119-170) and
+   UniformFiberNI.mcsim_launch (xopto/mcml/mcsource/fiberni.py:246-290). */
 static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x,
                         uint32_t a, uint64_t *accu) {
     const McgbSource *src = &c->source;
@@ -309,6 +333,31 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             v3 d = {src->direction_reflected[0], src->direction_reflected[1],
                     src->direction_reflected[2]};
             detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+        }
+        s->layer = 1;
+    } else if (src->kind == MCGB_SRC_UNIFORM_FIBER_NI) {
+        float sin_fi, cos_fi, sin_theta, cos_theta;
+        float n_sample = c->layers[1].n;
+        float r = sqrtf(rnd(x, a)) * src->sigma[0];
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        s->pos.x = src->position[0] + r * cos_fi;
+        s->pos.y = src->position[1] + r * sin_fi;
+        s->pos.z = 0.0f;
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        cos_theta = 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
+        sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        sin_theta = sin_theta / n_sample;
+        cos_theta = sqrtf(1.0f - sin_theta * sin_theta);
+        s->dir.x = cos_fi * sin_theta;
+        s->dir.y = sin_fi * sin_theta;
+        s->dir.z = cos_theta;
+        r = reflectance_cos2(src->clip, n_sample, s->dir.z);
+        s->w = 1.0f - r;
+        if (c->specular.kind != MCGB_DET_NONE) {
+            v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
+            v3 normal = {0.0f, 0.0f, -1.0f};
+            v3 d = refract3(dir_in, normal, n_sample, src->clip);
+            detector_deposit(mm, &c->specular, s->pos, d, r, accu);
         }
         s->layer = 1;
     } else {

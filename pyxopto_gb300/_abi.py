@@ -19,7 +19,7 @@ SCHED_STATIC, SCHED_DYNAMIC = 0, 1
 
 METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT = 0, 1, 2
 PF_HG, PF_GK, PF_LUT = 0, 1, 2
-SRC_LINE, SRC_GAUSSIAN_BEAM = 0, 1
+SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI = 0, 1, 2
 DET_NONE, DET_TOTAL, DET_RADIAL = 0, 1, 2
 FLUENCE_NONE, FLUENCE_DEPOSITION, FLUENCE_RATE = 0, 1, 2
 TRACE_NONE, TRACE_START, TRACE_END, TRACE_ALL = 0, 1, 2, 7

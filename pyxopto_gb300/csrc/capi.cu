@@ -69,8 +69,13 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
     if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
-    if (src.kind != MCGB_SRC_LINE && src.kind != MCGB_SRC_GAUSSIAN_BEAM)
+    if (src.kind != MCGB_SRC_LINE && src.kind != MCGB_SRC_GAUSSIAN_BEAM &&
+        src.kind != MCGB_SRC_UNIFORM_FIBER_NI)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
+    if (src.kind == MCGB_SRC_UNIFORM_FIBER_NI &&
+        !(src.sigma[0] >= 0.0f && src.sigma[1] >= 0.0f && src.sigma[1] <= 1.0f && src.clip > 0.0f))
+        return fail(MCGB_E_INVALID, "fiber source: core radius %g, acceptance cosine %g, core index %g",
+                    (double)src.sigma[0], (double)src.sigma[1], (double)src.clip);
     if (!(o.lottery_chance > 0.0f && o.lottery_chance <= 1.0f))
         return fail(MCGB_E_INVALID, "lottery chance %g outside (0, 1]", (double)o.lottery_chance);
     if (!(o.packet_weight_min > 0.0f && o.packet_weight_min <= 1.0f))
@@ -95,7 +100,14 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
             return fail(MCGB_E_INVALID, "unknown fluence kind %d", fl.kind);
         if (fl.shape[0] == 0 || fl.shape[1] == 0 || fl.shape[2] == 0)
             return fail(MCGB_E_INVALID, "fluence grid has an empty axis");
-        uint64_t n = (uint64_t)fl.shape[0] * fl.shape[1] * fl.shape[2];
+        /* the kernels index the grid with 32-bit voxel numbers; 0xFFFFFFFF
+           marks an empty fluence cache */
+        uint64_t nxy = (uint64_t)fl.shape[0] * fl.shape[1];
+        if (fl.shape[0] > 0x7FFFFFFFu || fl.shape[1] > 0x7FFFFFFFu || fl.shape[2] > 0x7FFFFFFFu ||
+            nxy >= 0xFFFFFFFFull || nxy * fl.shape[2] >= 0xFFFFFFFFull)
+            return fail(MCGB_E_SIZE, "fluence grid %ux%ux%u has 2^32 - 1 or more voxels", fl.shape[0],
+                        fl.shape[1], fl.shape[2]);
+        uint64_t n = nxy * fl.shape[2];
         if (!b->accumulator || !range_ok(fl.offset, n, b->accumulator_size))
             return fail(MCGB_E_SIZE, "fluence [%llu, +%llu) beyond the accumulator (%llu)",
                         (unsigned long long)fl.offset, (unsigned long long)n,
@@ -239,6 +251,8 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
+    if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI)
+        return fail(MCGB_E_UNSUPPORTED, "the fiber source is implemented for layered media only");
     if (!buf->voxels || !buf->materials) return fail(MCGB_E_INVALID, "voxel or material buffer is NULL");
     /* Voxel material indices are validated by the caller (uint8 < num_materials):
        the host wrapper checks the array before upload. */

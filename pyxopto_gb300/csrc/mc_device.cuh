@@ -100,6 +100,30 @@ MCGB_DEV float reflectance(float n1, float n2, float cos1, float cc) {
     return R;
 }
 
+/* reflectance_cos2: Fresnel reflectance from the cosine of the angle of
+   refraction, xopto/mcbase/kernel/mcbase.template.c:1303-1347 */
+MCGB_DEV float reflectance_cos2(float n1, float n2, float cos2) {
+    cos2 = fabsf(cos2);
+    if (n1 == n2) return 0.0f;
+    float sin2 = mc_sqrt(1.0f - cos2 * cos2);
+    if (cos2 >= 1.0f) sin2 = 0.0f;
+    float sin1 = mc_div(n2, n1) * sin2;
+    float R = 1.0f;
+    if (sin1 < 1.0f) {
+        float cos1 = mc_sqrt(1.0f - sin1 * sin1);
+        float n1_d_n2 = mc_div(n1, n2);
+        float n_cos1 = n1_d_n2 * cos1;
+        float n_cos2 = n1_d_n2 * cos2;
+        float Rs = mc_div(n_cos1 - cos2, n_cos1 + cos2);
+        Rs *= Rs;
+        float Rp = mc_div(n_cos2 - cos1, n_cos2 + cos1);
+        Rp *= Rp;
+        R = 0.5f * (Rp + Rs);
+        if (cos1 <= 0.0f || sin2 == 1.0f) return 1.0f;
+    }
+    return R;
+}
+
 /* reflect, xopto/mcbase/kernel/mcbase.template.c:1361-1369 */
 MCGB_DEV f3 reflect3(const f3 &p, const f3 &n) {
     float p_n_2 = 2.0f * dot3(p, n);
@@ -249,38 +273,47 @@ MCGB_DEV void detector_deposit(const McgbDetector &det, const f3 &pos, const f3 
 /* Fluence deposit (xopto/mcbase/mcfluence/fluence.py:103-143) through a
    one-entry per-thread cache: consecutive deposits into the same voxel are
    summed in a register and flushed with one 64-bit atomic when the voxel
-   changes (integer sums, so the tally is unchanged). */
+   changes (integer sums, so the tally is unchanged).  Voxel numbers are
+   32-bit (the C ABI rejects grids of 2^32 - 1 voxels or more); the cache
+   holds a pointer to the grid's first tally. */
 struct FluenceCache {
-    uint64_t index;
+    uint64_t *base;
+    uint32_t index;
     uint64_t sum;
-    __device__ __forceinline__ void flush(uint64_t *accu) {
-        if (sum) atomicAdd((unsigned long long *)(accu + index), (unsigned long long)sum);
+    __device__ __forceinline__ void flush() {
+        if (sum) atomicAdd((unsigned long long *)(base + index), (unsigned long long)sum);
         sum = 0;
     }
-    __device__ __forceinline__ void add(uint64_t *accu, uint64_t i, uint32_t w) {
+    __device__ __forceinline__ void add(uint32_t i, uint32_t w) {
         if (i != index) {
-            flush(accu);
+            flush();
             index = i;
         }
         sum += w;
     }
 };
 
+MCGB_DEV FluenceCache fluence_cache(const McgbFluence &fl, uint64_t *accu) {
+    return FluenceCache{accu + fl.offset, 0xFFFFFFFFu, 0ull};
+}
+
 MCGB_DEV void fluence_deposit(const McgbFluence &fl, const f3 &pos, float weight, float mua,
-                              uint64_t *accu, FluenceCache &cache) {
+                              FluenceCache &cache) {
     float ix = (pos.x - fl.top_left[0]) * fl.inv_step[0];
     float iy = (pos.y - fl.top_left[1]) * fl.inv_step[1];
     float iz = (pos.z - fl.top_left[2]) * fl.inv_step[2];
-    /* indexf < (float)shape  <=>  trunc(indexf) < shape for indexf >= 0, so
-       the bounds test runs on the truncated integer indices */
-    if (ix >= 0.0f && iy >= 0.0f && iz >= 0.0f) {
-        uint32_t jx = cvt_uint(ix), jy = cvt_uint(iy), jz = cvt_uint(iz);
-        if (jx < fl.shape[0] && jy < fl.shape[1] && jz < fl.shape[2]) {
-            uint64_t index = ((uint64_t)jz * fl.shape[1] + jy) * fl.shape[0] + jx;
-            if (fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
-            uint32_t w = (uint32_t)(weight * (float)fl.k + 0.5f);
-            cache.add(accu, fl.offset + index, w);
-        }
+    /* The reference accepts 0 <= indexf < shape and truncates.  With floor
+       conversion (saturating), 0 <= indexf < shape  <=>  0 <= floor(indexf)
+       < shape, and floor equals truncation there, so one unsigned compare
+       per axis is the same test. */
+    uint32_t jx = (uint32_t)__float2int_rd(ix);
+    uint32_t jy = (uint32_t)__float2int_rd(iy);
+    uint32_t jz = (uint32_t)__float2int_rd(iz);
+    if (jx < fl.shape[0] && jy < fl.shape[1] && jz < fl.shape[2]) {
+        uint32_t index = (jz * fl.shape[1] + jy) * fl.shape[0] + jx;
+        if (fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
+        uint32_t w = (uint32_t)(weight * (float)fl.k + 0.5f);
+        cache.add(index, w);
     }
 }
 

@@ -40,8 +40,8 @@ struct MlSmem {
     MlLayer layers[MCGB_MAX_LAYERS];
 };
 
-/* Line / GaussianBeam launch (xopto/mcml/mcsource/line.py:95-108,
-   gaussianbeam.py:119-170). */
+/* Line / GaussianBeam / UniformFiberNI launch (xopto/mcml/mcsource/line.py:95-108,
+   gaussianbeam.py:119-170, fiberni.py:246-290). */
 static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
                                                    Rng &rng, f3 &pos, f3 &dir, float &w,
                                                    int &layer, uint64_t *accu) {
@@ -53,6 +53,29 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
         if (c.specular.kind != MCGB_DET_NONE) {
             f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
             detector_deposit(c.specular, pos, d, src.reflectance, accu);
+        }
+        layer = 1;
+    } else if (src.kind == MCGB_SRC_UNIFORM_FIBER_NI) {
+        /* uniform over the core, uniform in solid angle within the
+           acceptance cone in air, refracted into the sample */
+        float sin_fi, cos_fi;
+        const float n_sample = L[1].g1.x;
+        float r = mc_sqrt(rng.next()) * src.sigma[0];
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        pos = f3{src.position[0] + r * cos_fi, src.position[1] + r * sin_fi, 0.0f};
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - rng.next() * (1.0f - src.sigma[1]);
+        float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        sin_theta = mc_div(sin_theta, n_sample);
+        cos_theta = mc_sqrt(1.0f - sin_theta * sin_theta);
+        dir = f3{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        float R = reflectance_cos2(src.clip, n_sample, dir.z);
+        w = 1.0f - R;
+        if (c.specular.kind != MCGB_DET_NONE) {
+            f3 dir_in{dir.x, dir.y, -dir.z};
+            f3 normal{0.0f, 0.0f, -1.0f};
+            f3 d = refract3(dir_in, normal, n_sample, src.clip);
+            detector_deposit(c.specular, pos, d, R, accu);
         }
         layer = 1;
     } else {
@@ -133,6 +156,7 @@ struct MlCtx {
     const float *lut;
     float rmax2;
     bool use_rmax, use_trace, track_opl;
+    uint32_t max_steps;   /* per-packet step limit, 0xFFFFFFFF when unlimited */
     int last_layer;
     f3 src_pos;
 };
@@ -156,6 +180,8 @@ static __device__ __forceinline__ MlCtx mcml_ctx(const McgbMcmlConfig &c, const 
     x.use_rmax = x.rmax2 < __int_as_float(0x7f800000);
     x.use_trace = c.trace.flags != MCGB_TRACE_NONE;
     x.track_opl = c.opt.track_optical_pathlength != 0;
+    x.max_steps = (c.opt.max_steps_per_packet == 0 || c.opt.max_steps_per_packet > 0xFFFFFFFFull)
+                      ? 0xFFFFFFFFu : (uint32_t)c.opt.max_steps_per_packet;
     x.last_layer = (int)c.num_layers - 1;
     x.src_pos = f3{c.source.position[0], c.source.position[1], c.source.position[2]};
     return x;
@@ -227,7 +253,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
                                   : 0.0f;
             f3 dp{s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
                   s.pos.z - step_back * s.dir.z};
-            fluence_deposit(c.fluence, dp, deposit, mua, accu, fcache);
+            fluence_deposit(c.fluence, dp, deposit, mua, fcache);
         }
         if (next != s.layer) {
             s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
@@ -264,7 +290,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             done = true;
             s.w -= deposit;
             s.events |= MCGB_EV_ABSORPTION;
-            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, accu, fcache);
+            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         } else {
             const MlLayer &cl = L[s.layer];
             float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
@@ -276,7 +302,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         float deposit = s.w * g0.w;
         s.w -= deposit;
         s.events |= MCGB_EV_ABSORPTION;
-        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, accu, fcache);
+        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         const MlLayer &cl = L[s.layer];
         float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
         scatter_direction(s.dir, ct, az);
@@ -304,7 +330,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
         s.events = 0;
     }
-    if (!done && o.max_steps_per_packet && s.steps >= o.max_steps_per_packet) {
+    if (!done && s.steps >= x.max_steps) {
         done = true;
         status |= MCGB_STATUS_STEP_LIMIT;
     }
@@ -352,7 +378,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
     const MlCtx x = mcml_ctx(c, sm.layers, lut);
     const uint64_t T = c.num_streams;
     Rng rng{b.rng_x[t], b.rng_a[t]};
-    FluenceCache fcache{~0ull, 0};
+    FluenceCache fcache = fluence_cache(c.fluence, b.accumulator);
     uint64_t steps = 0, packets = 0;
     uint32_t iter = 0, status = 0;
     MlPacket s;
@@ -375,7 +401,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
         }
     }
     steps += s.steps;
-    if (FLU) fcache.flush(b.accumulator);
+    if (FLU) fcache.flush();
     b.rng_x[t] = rng.x;
     mc_finish(b, steps, packets, status, true);
 }
@@ -401,7 +427,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
     uint64_t item_next = 0, item_end = 0;   /* warp-uniform */
     bool more = true, active = false;
     Rng rng{0ull, 1u};
-    FluenceCache fcache{~0ull, 0};
+    FluenceCache fcache = fluence_cache(c.fluence, b.accumulator);
     uint64_t steps = 0, packets = 0;
     uint32_t iter = 0, status = 0;
     MlPacket s;
@@ -458,7 +484,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
         }
     }
     steps += s.steps;
-    if (FLU) fcache.flush(b.accumulator);
+    if (FLU) fcache.flush();
     mc_finish(b, steps, packets, status, packets > 0);
 }
 

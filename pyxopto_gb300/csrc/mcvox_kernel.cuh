@@ -186,6 +186,7 @@ struct MvCtx {
     MvGeom g;
     float rmax2;
     bool use_rmax, use_trace, track_opl;
+    uint32_t max_steps;   /* per-packet step limit, 0xFFFFFFFF when unlimited */
     f3 src_pos;
 };
 
@@ -214,6 +215,8 @@ static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, cons
     x.use_rmax = x.rmax2 < __int_as_float(0x7f800000);
     x.use_trace = c.trace.flags != MCGB_TRACE_NONE;
     x.track_opl = c.opt.track_optical_pathlength != 0;
+    x.max_steps = (c.opt.max_steps_per_packet == 0 || c.opt.max_steps_per_packet > 0xFFFFFFFFull)
+                      ? 0xFFFFFFFFu : (uint32_t)c.opt.max_steps_per_packet;
     x.src_pos = f3{c.source.position[0], c.source.position[1], c.source.position[2]};
     return x;
 }
@@ -278,7 +281,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                                   : 0.0f;
             f3 dp{s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
                   s.pos.z - step_back * s.dir.z};
-            fluence_deposit(c.fluence, dp, deposit, mua, accu, fcache);
+            fluence_deposit(c.fluence, dp, deposit, mua, fcache);
         }
         if (d < step) {
             s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
@@ -314,7 +317,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             s.w -= deposit;
             s.events |= MCGB_EV_ABSORPTION;
             done = true;
-            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, accu, fcache);
+            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
         } else {
             const MvMaterial &cm = M[s.mat];
             float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
@@ -325,7 +328,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         float deposit = s.w * g0.w;
         s.w -= deposit;
         s.events |= MCGB_EV_ABSORPTION;
-        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, accu, fcache);
+        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
         const MvMaterial &cm = M[s.mat];
         float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
         scatter_direction(s.dir, ct, az);
@@ -355,7 +358,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
         s.events = 0;
     }
-    if (!done && o.max_steps_per_packet && s.steps >= o.max_steps_per_packet) {
+    if (!done && s.steps >= x.max_steps) {
         done = true;
         status |= MCGB_STATUS_STEP_LIMIT;
     }
@@ -401,7 +404,7 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
     const MvCtx x = mcvox_ctx(c, b, sm.materials, lut);
     const uint64_t T = c.num_streams;
     Rng rng{b.rng_x[t], b.rng_a[t]};
-    FluenceCache fcache{~0ull, 0};
+    FluenceCache fcache = fluence_cache(c.fluence, b.accumulator);
     uint64_t steps = 0, packets = 0;
     uint32_t iter = 0, status = 0;
     MvPacket s;
@@ -424,7 +427,7 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
         }
     }
     steps += s.steps;
-    if (FLU) fcache.flush(b.accumulator);
+    if (FLU) fcache.flush();
     b.rng_x[t] = rng.x;
     mv_finish(b, steps, packets, status, true);
 }
@@ -446,7 +449,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
     uint64_t item_next = 0, item_end = 0;
     bool more = true, active = false;
     Rng rng{0ull, 1u};
-    FluenceCache fcache{~0ull, 0};
+    FluenceCache fcache = fluence_cache(c.fluence, b.accumulator);
     uint64_t steps = 0, packets = 0;
     uint32_t iter = 0, status = 0;
     MvPacket s;
@@ -503,7 +506,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
         }
     }
     steps += s.steps;
-    if (FLU) fcache.flush(b.accumulator);
+    if (FLU) fcache.flush();
     mv_finish(b, steps, packets, status, packets > 0);
 }
 

@@ -1,0 +1,61 @@
+"""Optical fibre parameters (xopto/mcbase/mcutil/fiber.py:38-224, MultimodeFiber)."""
+
+
+class MultimodeFiber:
+    """Multimode fibre: core and cladding diameters (m), core refractive
+    index and numerical aperture; the cladding index follows from
+    NA = sqrt(ncore^2 - ncladding^2)."""
+
+    @staticmethod
+    def compute_na(ncore: float, ncladding: float) -> float:
+        return (ncore ** 2 - ncladding ** 2) ** 0.5
+
+    @staticmethod
+    def compute_ncladding(ncore: float, na: float) -> float:
+        return (ncore ** 2 - na ** 2) ** 0.5
+
+    def __init__(self, dcore: float, dcladding: float, ncore: float, na: float):
+        self._dcore = float(dcore)
+        self._dcladding = float(dcladding)
+        self._ncore = float(ncore)
+        self._na = float(na)
+
+    def validate(self):
+        if self._dcore > self._dcladding:
+            raise ValueError('Fiber core diameter must be smaller than the fiber cladding diameter!')
+
+    def _set_dcore(self, v):
+        self._dcore = float(v)
+
+    def _set_dcladding(self, v):
+        self._dcladding = float(v)
+
+    def _set_ncore(self, v):
+        self._ncore = float(v)
+
+    def _set_na(self, v):
+        self._na = float(v)
+
+    dcore = property(lambda self: self._dcore, _set_dcore, None, 'Diameter (m) of the fiber core.')
+    dcladding = property(lambda self: self._dcladding, _set_dcladding, None,
+                         'Diameter (m) of the fiber cladding.')
+    ncore = property(lambda self: self._ncore, _set_ncore, None, 'Refractive index of the fiber core.')
+    ncladding = property(lambda self: self.compute_ncladding(self._ncore, self._na), None, None,
+                         'Refractive index of the fiber cladding.')
+    na = property(lambda self: self._na, _set_na, None, 'Numerical aperture of the fiber core.')
+
+    def todict(self) -> dict:
+        return {'type': 'MultimodeFiber', 'dcore': self._dcore, 'dcladding': self._dcladding,
+                'ncore': self._ncore, 'na': self._na}
+
+    @staticmethod
+    def fromdict(data: dict) -> 'MultimodeFiber':
+        data = dict(data)
+        data.pop('type', None)
+        return MultimodeFiber(**data)
+
+    def __str__(self):
+        return 'MultimodeFiber(dcore={}, dcladding={}, ncore={}, na={})'.format(
+            self._dcore, self._dcladding, self._ncore, self._na)
+
+    __repr__ = __str__

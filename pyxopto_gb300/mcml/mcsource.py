@@ -1,9 +1,10 @@
-"""Photon packet sources of the layered simulator: Line and GaussianBeam
-(xopto/mcml/mcsource/line.py, gaussianbeam.py)."""
+"""Photon packet sources of the layered simulator: Line, GaussianBeam and
+UniformFiberNI (xopto/mcml/mcsource/line.py, gaussianbeam.py, fiberni.py)."""
 import numpy as np
 
 from .. import _abi
 from ..mcbase import mcutil
+from ..mcbase.mcutil.fiber import MultimodeFiber
 
 
 def _unit(v):
@@ -124,5 +125,54 @@ class GaussianBeam(Source):
 
     def __str__(self):
         return 'GaussianBeam(sigma=({}, {}), clip={})'.format(*self._sigma, self._clip)
+
+    __repr__ = __str__
+
+
+class UniformFiberNI(Source):
+    """Optical fibre source with normal incidence: packets start uniformly
+    over the core and uniformly in solid angle within the acceptance cone
+    (xopto/mcml/mcsource/fiberni.py:180-438)."""
+
+    def __init__(self, fiber: MultimodeFiber, position=(0.0, 0.0, 0.0)):
+        if isinstance(fiber, UniformFiberNI):
+            fiber, position = fiber.fiber, fiber.position
+        self._fiber = fiber
+        self._position = np.zeros((3,))
+        self._set_position(position)
+
+    def _set_fiber(self, fib):
+        self._fiber = fib
+
+    def _set_position(self, p):
+        self._position[:] = p
+        self._position[2] = 0.0
+
+    fiber = property(lambda self: self._fiber, _set_fiber, None, 'Multimode optical fiber.')
+    position = property(lambda self: self._position, _set_position, None, 'Source position.')
+
+    def update(self, other):
+        if isinstance(other, UniformFiberNI):
+            self.fiber, self.position = other.fiber, other.position
+        elif isinstance(other, dict):
+            self.fiber = other.get('fiber', self.fiber)
+            self.position = other.get('position', self.position)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiberni.py:383-412: core radius, acceptance cosine in air,
+        core refractive index."""
+        target.kind = _abi.SRC_UNIFORM_FIBER_NI
+        target.position[:] = [float(v) for v in self._position]
+        target.sigma[0] = self._fiber.dcore * 0.5
+        target.sigma[1] = (1.0 - self._fiber.na ** 2) ** 0.5
+        target.clip = self._fiber.ncore
+        return target
+
+    def todict(self):
+        return {'type': 'UniformFiberNI', 'fiber': self._fiber.todict(),
+                'position': self._position.tolist()}
+
+    def __str__(self):
+        return 'UniformFiberNI(fiber={}, position=({}, {}, {}))'.format(self._fiber, *self._position)
 
     __repr__ = __str__

@@ -1,0 +1,66 @@
+"""The reference's fibre validation and performance workload
+(xopto/mcml/test/validate.py:348-511, SingleLayerUniformFiberRadial, timed by
+test/performance.py): a normally incident multimode fibre (UniformFiberNI)
+on an 8 mm layer between a fused-silica half-space and a water-like
+half-space, a radial detector with the fibre's acceptance angle and rmax
+5 mm, run once for each point of a 20 x 20 (mua, mus') grid; the radial
+profiles are integrated over 200 um fibres at 5 source-detector separations
+and compared with the CUDA-MCML values in cuda_mcml_fiber.npz.  The pass
+criterion of the reference is |mean relative error| < 0.5 %.
+"""
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load():
+    return np.load(os.path.join(HERE, 'cuda_mcml_fiber.npz'))
+
+
+def build(data, fast=True, scheduling='dynamic', rnginit=1):
+    from pyxopto_gb300.mcml import mc
+    from pyxopto_gb300.mcml.mcutil import fiber
+    g = data['g']
+    layers = mc.mclayer.Layers([
+        mc.mclayer.Layer(d=float(data['d'][i]), n=float(data['n'][i]), mua=0.0, mus=0.0,
+                         pf=mc.mcpf.Hg(float(g[i]))) for i in range(3)])
+    dcore, dclad, ncore, na = (float(v) for v in data['fiber'])
+    source = mc.mcsource.UniformFiberNI(fiber.MultimodeFiber(dcore, dclad, ncore, na))
+    start, stop, n = data['axis']
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(
+        mc.mcdetector.RadialAxis(float(start), float(stop), int(n)), cosmin=float(data['cosmin'][0])))
+    opts = [mc.mcoptions.McScheduling(scheduling)]
+    if fast:
+        opts.append(mc.mcoptions.McUseNativeMath(True))
+    sim = mc.Mc(layers, source, det, options=opts, rnginit=rnginit)
+    sim.rmax = float(data['rmax'][0])
+    return sim
+
+
+def run(sim, data, nphotons):
+    """Runs the 400 simulations in sequence (as the reference does); returns
+    (fibre reflectance [20, 20, 5], seconds spent in Mc.run)."""
+    from pyxopto_gb300.util import convolve
+    mua, musr = np.meshgrid(data['mua'], data['musr'], indexing='ij')
+    g = float(data['g'][1])
+    profiles, r = [], None
+    t = 0.0
+    for i in range(mua.size):
+        sim.layers[1].mua = float(mua.flat[i])
+        sim.layers[1].mus = float(musr.flat[i]) / (1.0 - g)
+        t0 = time.perf_counter()
+        _, _, det = sim.run(nphotons)
+        t += time.perf_counter() - t0
+        profiles.append(det.top.reflectance)
+        r = det.top.r
+    refl = convolve.fiber_reflectance(r, np.asarray(profiles), sds=list(data['sds']),
+                                      dcore=float(data['sds_dcore'][0]))
+    return refl.reshape(data['reflectance'].shape), t
+
+
+def relative_error(data, refl):
+    """Relative error (%) against the CUDA-MCML values."""
+    return (refl - data['reflectance']) / data['reflectance'] * 100.0

@@ -19,6 +19,11 @@ Writes
                          reference's validation suite compares against
                          (xopto/mcml/test/reference/cuda_singlelayer_linesource_radial.pkl,
                          test xopto/mcml/test/validate.py:219-345).
+  cuda_mcml_fiber.npz    the CUDA-MCML fibre reflectances of the 20 x 20
+                         (mua, mus') sweep at 5 source-detector separations
+                         (xopto/mcml/test/reference/cuda_singlelayer_uniformfiber.pkl,
+                         test xopto/mcml/test/validate.py:348-511), with the
+                         geometry of that test.
 """
 import os
 import pickle
@@ -91,6 +96,31 @@ def make_cuda_mcml():
     print('cuda_mcml_radial', len(d['reflectance']))
 
 
+def make_cuda_fiber():
+    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference',
+                        'cuda_singlelayer_uniformfiber.pkl')
+    with open(path, 'rb') as f:
+        d = pickle.load(f)
+    layers = d['layers']
+    np.savez_compressed(
+        os.path.join(HERE, 'cuda_mcml_fiber.npz'),
+        reflectance=np.asarray(d['reflectance'], dtype=np.float64),
+        n=np.array([l['basic']['n'] for l in layers]),
+        d=np.array([l['basic']['d'] for l in layers]),
+        g=np.array([l['pf']['pfparams'][0] for l in layers]),
+        fiber=np.array([d['source']['dcore'], d['source']['dcladding'], d['source']['ncore'],
+                        d['source']['na']]),
+        axis=np.array([d['detector']['axis']['start'], d['detector']['axis']['stop'],
+                       d['detector']['axis']['n']]),
+        cosmin=np.array([d['detector']['cosmin']]),
+        sds=np.asarray(d['detector']['fibers']['sds'], dtype=np.float64),
+        sds_dcore=np.array([d['detector']['fibers']['dcore']]),
+        mua=np.asarray(d['lut']['mua'], dtype=np.float64),
+        musr=np.asarray(d['lut']['musr'], dtype=np.float64),
+        rmax=np.array([d['mc']['rmax']]))
+    print('cuda_mcml_fiber', np.asarray(d['reflectance']).shape)
+
+
 if __name__ == '__main__':
     names = sys.argv[1:] or list(scenarios.SCENARIOS)
     for n in names:
@@ -98,3 +128,4 @@ if __name__ == '__main__':
     if not sys.argv[1:]:
         make_rng_tables()
         make_cuda_mcml()
+        make_cuda_fiber()

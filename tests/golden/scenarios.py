@@ -115,6 +115,19 @@ SCENARIOS = {
                        specular=dict(type='Total')),
         fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='fluence'),
         nphotons=2000, streams=20, rnginit=13),
+    # the reference's fibre validation geometry (xopto/mcml/test/validate.py:348-511):
+    # fused-silica fibre (n 1.452, NA 0.22, 200 um core) on an 8 mm layer,
+    # radial detector with the fibre's acceptance, rmax 5 mm
+    'fiber_ni_radial': dict(
+        medium='mcml',
+        layers=[dict(d=INF, n=1.452, mua=0.0, mus=0.0, pf=['Hg', 0.85]),
+                dict(d=8e-3, n=1.33, mua=300.0, mus=1.2e4, pf=['Hg', 0.85]),
+                dict(d=INF, n=1.33, mua=0.0, mus=0.0, pf=['Hg', 0.85])],
+        source=dict(type='UniformFiberNI',
+                    fiber=dict(dcore=200e-6, dcladding=200e-6, ncore=1.452, na=0.22)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1.7e-3, 34], cosmin=0.9884549351697024),
+                       specular=dict(type='Total')),
+        rmax=5e-3, nphotons=3000, streams=32, rnginit=17),
 }
 
 # Bench workloads (not golden-tested at these sizes): the layered
@@ -227,7 +240,12 @@ def _fluence(pkg, spec):
 
 
 def _source(src_mod, spec):
+    import importlib
     kw = {k: v for k, v in spec.items() if k != 'type'}
+    if 'fiber' in kw:
+        medium_pkg = src_mod.__name__.rsplit('.', 1)[0]          # e.g. xopto.mcml
+        fiber = importlib.import_module(medium_pkg + '.mcutil.fiber')
+        kw['fiber'] = fiber.MultimodeFiber(**kw['fiber'])
     return getattr(src_mod, spec['type'])(**kw)
 
 

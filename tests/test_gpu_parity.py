@@ -11,6 +11,7 @@ import os
 import numpy as np
 import pytest
 
+import fiber_sweep
 import scenarios
 
 pytestmark = pytest.mark.gpu
@@ -179,3 +180,17 @@ def test_trace_bit_identical_to_oracle(cuda, lib, oracle, scheduling):
     got = np.ascontiguousarray(tr.data).view(np.float32).reshape(-1)
     assert np.array_equal(got, ref['float'][off:off + cnt])
     assert tr.n.min() >= 1
+
+
+def test_cuda_mcml_fiber_sweep(cuda, lib):
+    """The reference's validation test SingleLayerUniformFiberRadial
+    (xopto/mcml/test/validate.py:348-511): fibre reflectance of a 20 x 20
+    (mua, mus') sweep at 5 source-detector separations against CUDA-MCML,
+    pass if |mean relative error| < 0.5 % (1e6 packets per point here, 1e7
+    in the reference)."""
+    data = fiber_sweep.load()
+    sim = fiber_sweep.build(data, fast=True)
+    refl, _ = fiber_sweep.run(sim, data, 1_000_000)
+    err = fiber_sweep.relative_error(data, refl)
+    assert abs(err.mean()) < 0.5, err.mean()
+    assert np.median(np.abs(err)) < 3.0, np.median(np.abs(err))
