@@ -98,8 +98,16 @@ enum { MCGB_METHOD_ALBEDO_WEIGHT = 0,       /* MC_METHOD 0 (default)      */
        MCGB_METHOD_ALBEDO_REJECTION = 1,    /* MC_METHOD 1                */
        MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT = 2 };
 enum { MCGB_PF_HG = 0, MCGB_PF_GK = 1, MCGB_PF_LUT = 2 };
-enum { MCGB_SRC_LINE = 0, MCGB_SRC_GAUSSIAN_BEAM = 1, MCGB_SRC_UNIFORM_FIBER_NI = 2 };
-enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2 };
+enum {
+    MCGB_SRC_LINE = 0,
+    MCGB_SRC_GAUSSIAN_BEAM = 1,
+    MCGB_SRC_UNIFORM_FIBER_NI = 2,
+    MCGB_SRC_LAMBERTIAN_FIBER_NI = 3,
+    MCGB_SRC_UNIFORM_FIBER = 4,
+    MCGB_SRC_LAMBERTIAN_FIBER = 5
+};
+enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
+       MCGB_DET_TOTAL_PL = 4 };
 enum { MCGB_FLUENCE_NONE = 0, MCGB_FLUENCE_DEPOSITION = 1, MCGB_FLUENCE_RATE = 2 };
 /* Trace flags (xopto/mcbase/mctrace.py TRACE_START/END/ALL). */
 enum { MCGB_TRACE_NONE = 0, MCGB_TRACE_START = 1, MCGB_TRACE_END = 2, MCGB_TRACE_ALL = 7 };
@@ -156,10 +164,17 @@ typedef struct McgbMaterial {
    GaussianBeam mcvox (xopto/mcvox/mcsource/gaussianbeam.py:112-190):
      transformation, position, direction (in the surrounding medium), sigma,
      clip.
-   UniformFiberNI mcml (xopto/mcml/mcsource/fiberni.py:246-290,383-412):
-     position = centre of the fibre core on the sample surface,
-     sigma[0] = core radius, sigma[1] = cosine of the acceptance angle in
-     air, sqrt(1 - NA^2), clip = refractive index of the core. */
+   Fibre sources, layered media only (xopto/mcml/mcsource/fiberni.py,
+   fiber.py): position = centre of the fibre core on the sample surface,
+   sigma[0] = core radius, clip = refractive index of the core, and
+     UniformFiberNI (fiberni.py:246-290,383-412): sigma[1] = cosine of the
+       acceptance angle in air, sqrt(1 - NA^2);
+     LambertianFiberNI (fiberni.py:485-534,562-573): sigma[1] = NA;
+     UniformFiber (fiber.py:267-330,429-470): sigma[1] = sqrt(1 - NA^2),
+       direction = fibre axis, transformation = rotation of the z axis onto
+       it;
+     LambertianFiber (fiber.py:576-640,660-681): sigma[1] = NA, direction
+       and transformation as UniformFiber. */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];
@@ -172,18 +187,25 @@ typedef struct McgbSource {
     float reserved[2];
 } McgbSource;                               /* 104 bytes */
 
-/* Radial or Total detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;
-   total.py:52-56,86-108). */
+/* Surface detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;
+   total.py:52-56,86-108; radialpl.py:138-179,343-378; totalpl.py:107-135).
+   Total: one bin.  Radial: n radial bins.  TotalPl: n_pl optical path-length
+   bins.  RadialPl: n_pl x n bins, path length first.  Indices outside an
+   axis are clipped into its first or last bin; the path-length kinds need
+   McgbRunOptions.track_optical_pathlength. */
 typedef struct McgbDetector {
     int32_t kind;
     float direction[3];
     float position[2];
     float r_min, inv_dr, cos_min;
-    uint32_t n;
-    int32_t log_scale;
+    uint32_t n;                             /* radial bins                     */
+    int32_t log_scale;                      /* radial axis in log scale        */
+    int32_t pl_log_scale;                   /* path-length axis in log scale   */
+    uint64_t offset;                        /* first accumulator               */
+    float pl_min, inv_dpl;                  /* path-length axis start, 1/step  */
+    uint32_t n_pl;                          /* path-length bins                */
     uint32_t reserved;
-    uint64_t offset;                        /* first accumulator */
-} McgbDetector;                             /* 56 bytes */
+} McgbDetector;                             /* 72 bytes */
 
 /* Cartesian fluence (xopto/mcbase/mcfluence/fluence.py:56-62,103-143). */
 typedef struct McgbFluence {

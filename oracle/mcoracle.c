@@ -244,21 +244,30 @@ static inline uint32_t weight_to_u32(float w, float accept) {
     return (uint32_t)((w * (float)MCGB_ACCU_K + 0.5f) * accept);
 }
 
-/* Radial / Total detector deposit:
-   xopto/mcml/mcdetector/radial.py:117-150, total.py:86-108 */
+/* Surface detector deposit: Total (xopto/mcml/mcdetector/total.py:86-108),
+   Radial (radial.py:117-150), TotalPl (totalpl.py:107-135), RadialPl
+   (radialpl.py:138-179); opl = mcsim_optical_pathlength. */
 static void detector_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir,
-                             float weight, uint64_t *accu) {
+                             float weight, float opl, uint64_t *accu) {
     if (det->kind == MCGB_DET_NONE) return;
     v3 ddir = {det->direction[0], det->direction[1], det->direction[2]};
     float accept = (float)(det->cos_min <= fabsf(dot3(dir, ddir)));
     uint64_t index = 0;
-    if (det->kind == MCGB_DET_RADIAL) {
+    if (det->kind == MCGB_DET_RADIAL || det->kind == MCGB_DET_RADIAL_PL) {
         float dx = pos.x - det->position[0];
         float dy = pos.y - det->position[1];
         float r = sqrtf(dx * dx + dy * dy);
         if (det->log_scale) r = m_log(mm, fmaxf(r, 1e-12f));
         int32_t r_index = cvt_int((r - det->r_min) * det->inv_dr);
         index = (uint64_t)clip_i(r_index, 0, (int32_t)det->n - 1);
+    }
+    if (det->kind == MCGB_DET_RADIAL_PL || det->kind == MCGB_DET_TOTAL_PL) {
+        float pl = opl;
+        if (det->pl_log_scale) pl = m_log(mm, fmaxf(pl, 1e-12f));
+        int32_t pl_index = clip_i(cvt_int((pl - det->pl_min) * det->inv_dpl), 0,
+                                  (int32_t)det->n_pl - 1);
+        uint64_t nr = det->kind == MCGB_DET_RADIAL_PL ? det->n : 1u;
+        index += (uint64_t)pl_index * nr;
     }
     uint32_t w = weight_to_u32(weight, accept);
     if (w > 0) accu[det->offset + index] += w;
@@ -319,9 +328,75 @@ typedef struct {
     float opl;
 } MlState;
 
+/* mcsim_launch of the fibre sources: UniformFiberNI
+   (xopto/mcml/mcsource/fiberni.py:246-290), LambertianFiberNI
+   (fiberni.py:485-534), UniformFiber (fiber.py:267-330) and LambertianFiber
+   (fiber.py:576-640).  The tilted kinds test pt_mc.z (0 after the move to
+   the surface) against the critical cosine before refracting, so their
+   direction is never refracted. */
+static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x,
+                              uint32_t a, uint64_t *accu) {
+    const McgbSource *src = &c->source;
+    int tilted = src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER;
+    int lambertian = src->kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
+                     src->kind == MCGB_SRC_LAMBERTIAN_FIBER;
+    float n_sample = c->layers[1].n, n_core = src->clip;
+    const float *T = src->transformation;
+    float sin_fi, cos_fi, sin_theta, cos_theta, R;
+    float r = sqrtf(rnd(x, a)) * src->sigma[0];
+    m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+    if (tilted) {
+        v3 ps = {r * cos_fi, r * sin_fi, 0.0f}, pm;
+        /* mc_transform_fpv3, xopto/mcbase/kernel/mcbase.template.c:380-386 */
+        pm.x = T[0] * ps.x + T[1] * ps.y + T[2] * ps.z;
+        pm.y = T[3] * ps.x + T[4] * ps.y + T[5] * ps.z;
+        pm.z = T[6] * ps.x + T[7] * ps.y + T[8] * ps.z;
+        float k = (0.0f - pm.z) / src->direction[2];
+        pm.x += k * src->direction[0];
+        pm.y += k * src->direction[1];
+        s->pos.x = src->position[0] + pm.x;
+        s->pos.y = src->position[1] + pm.y;
+    } else {
+        s->pos.x = src->position[0] + r * cos_fi;
+        s->pos.y = src->position[1] + r * sin_fi;
+    }
+    s->pos.z = 0.0f;
+    m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+    if (lambertian) {
+        sin_theta = sqrtf(rnd(x, a)) * src->sigma[1];
+    } else {
+        cos_theta = 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
+        sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+    }
+    sin_theta = sin_theta / (tilted ? n_core : n_sample);
+    cos_theta = sqrtf(1.0f - sin_theta * sin_theta);
+    v3 pt = {cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+    if (tilted) {
+        v3 d;
+        d.x = T[0] * pt.x + T[1] * pt.y + T[2] * pt.z;
+        d.y = T[3] * pt.x + T[4] * pt.y + T[5] * pt.z;
+        d.z = T[6] * pt.x + T[7] * pt.y + T[8] * pt.z;
+        float cc = cos_critical(n_core, n_sample);
+        s->dir = d;
+        R = reflectance(n_core, n_sample, d.z, cc);
+        if (c->specular.kind != MCGB_DET_NONE)
+            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu);
+    } else {
+        s->dir = pt;
+        R = reflectance_cos2(n_core, n_sample, pt.z);
+        if (c->specular.kind != MCGB_DET_NONE) {
+            v3 dir_in = {pt.x, pt.y, -pt.z};
+            v3 normal = {0.0f, 0.0f, -1.0f};
+            v3 d = refract3(dir_in, normal, n_sample, n_core);
+            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu);
+        }
+    }
+    s->w = 1.0f - R;
+}
+
 /* Line.mcsim_launch (xopto/mcml/mcsource/line.py:95-108),
    GaussianBeam.mcsim_launch (xopto/mcml/mcsource/gaussianbeam.py:119-170) and
-   UniformFiberNI.mcsim_launch (xopto/mcml/mcsource/fiberni.py:246-290). */
+   the fibre sources (mcml_launch_fiber). */
 static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x,
                         uint32_t a, uint64_t *accu) {
     const McgbSource *src = &c->source;
@@ -332,33 +407,11 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
         if (c->specular.kind != MCGB_DET_NONE) {
             v3 d = {src->direction_reflected[0], src->direction_reflected[1],
                     src->direction_reflected[2]};
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
         }
         s->layer = 1;
-    } else if (src->kind == MCGB_SRC_UNIFORM_FIBER_NI) {
-        float sin_fi, cos_fi, sin_theta, cos_theta;
-        float n_sample = c->layers[1].n;
-        float r = sqrtf(rnd(x, a)) * src->sigma[0];
-        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
-        s->pos.x = src->position[0] + r * cos_fi;
-        s->pos.y = src->position[1] + r * sin_fi;
-        s->pos.z = 0.0f;
-        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
-        cos_theta = 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
-        sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
-        sin_theta = sin_theta / n_sample;
-        cos_theta = sqrtf(1.0f - sin_theta * sin_theta);
-        s->dir.x = cos_fi * sin_theta;
-        s->dir.y = sin_fi * sin_theta;
-        s->dir.z = cos_theta;
-        r = reflectance_cos2(src->clip, n_sample, s->dir.z);
-        s->w = 1.0f - r;
-        if (c->specular.kind != MCGB_DET_NONE) {
-            v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
-            v3 normal = {0.0f, 0.0f, -1.0f};
-            v3 d = refract3(dir_in, normal, n_sample, src->clip);
-            detector_deposit(mm, &c->specular, s->pos, d, r, accu);
-        }
+    } else if (src->kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
+        mcml_launch_fiber(mm, c, s, x, a, accu);
         s->layer = 1;
     } else {
         float cos_fi, sin_fi, r;
@@ -388,7 +441,7 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
             v3 normal = {0.0f, 0.0f, -1.0f};
             v3 d = refract3(dir_in, normal, c->layers[1].n, c->layers[0].n);
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
         }
     }
 }
@@ -511,9 +564,9 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                     events |= mcml_boundary(c, &s, next, &x, a) | EV_BOUNDARY_HIT;
                     if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
                         if (s.layer <= 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
                         else if (s.layer >= (int32_t)c->num_layers - 1)
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
                         done = 1;
                     }
                 } else {
@@ -534,9 +587,9 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                     events |= mcml_boundary(c, &s, next, &x, a) | EV_BOUNDARY_HIT;
                     if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
                         if (s.layer <= 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
                         else if (s.layer >= (int32_t)c->num_layers - 1)
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
                         done = 1;
                     }
                 } else if (o->method == MCGB_METHOD_ALBEDO_REJECTION) {
@@ -675,7 +728,7 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         if (c->specular.kind != MCGB_DET_NONE) {
             v3 d = {src->direction_reflected[0], src->direction_reflected[1],
                     src->direction_reflected[2]};
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
         }
     } else {
         float specular_r = 0.0f;
@@ -719,7 +772,7 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
             specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
                                      cos_critical(n_outside, n_inside));
             if (c->specular.kind != MCGB_DET_NONE)
-                detector_deposit(mm, &c->specular, s->pos, direction, specular_r, accu);
+                detector_deposit(mm, &c->specular, s->pos, direction, specular_r, 0.0f, accu);
         } else {
             s->pos.x = c->top_left[0]; s->pos.y = c->top_left[1]; s->pos.z = c->top_left[2];
             s->dir.x = 0.0f; s->dir.y = 0.0f; s->dir.z = 1.0f;
@@ -839,9 +892,9 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                     events |= mv_boundary(c, mats, vox, &s, dist, &x, a) | EV_BOUNDARY_HIT;
                     if (!mv_valid(c, s.vox)) {
                         if (s.vox.z < 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
                         else if (s.vox.z >= c->shape[2])
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
                         done = 1;
                     }
                 } else {
@@ -862,9 +915,9 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                     events |= mv_boundary(c, mats, vox, &s, dist, &x, a) | EV_BOUNDARY_HIT;
                     if (!mv_valid(c, s.vox)) {
                         if (s.vox.z < 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
                         else if (s.vox.z >= c->shape[2])
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
                         done = 1;
                     }
                 } else if (o->method == MCGB_METHOD_ALBEDO_REJECTION) {

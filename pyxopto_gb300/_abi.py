@@ -19,8 +19,9 @@ SCHED_STATIC, SCHED_DYNAMIC = 0, 1
 
 METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT = 0, 1, 2
 PF_HG, PF_GK, PF_LUT = 0, 1, 2
-SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI = 0, 1, 2
-DET_NONE, DET_TOTAL, DET_RADIAL = 0, 1, 2
+SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI, SRC_LAMBERTIAN_FIBER_NI = 0, 1, 2, 3
+SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER = 4, 5
+DET_NONE, DET_TOTAL, DET_RADIAL, DET_RADIAL_PL, DET_TOTAL_PL = 0, 1, 2, 3, 4
 FLUENCE_NONE, FLUENCE_DEPOSITION, FLUENCE_RATE = 0, 1, 2
 TRACE_NONE, TRACE_START, TRACE_END, TRACE_ALL = 0, 1, 2, 7
 MATH_EXACT, MATH_FAST = 0, 1
@@ -57,7 +58,8 @@ class McgbSource(C.Structure):
 class McgbDetector(C.Structure):
     _fields_ = [('kind', i32), ('direction', f32 * 3), ('position', f32 * 2),
                 ('r_min', f32), ('inv_dr', f32), ('cos_min', f32), ('n', u32),
-                ('log_scale', i32), ('reserved', u32), ('offset', u64)]
+                ('log_scale', i32), ('pl_log_scale', i32), ('offset', u64),
+                ('pl_min', f32), ('inv_dpl', f32), ('n_pl', u32), ('reserved', u32)]
 
 
 class McgbFluence(C.Structure):

@@ -75,15 +75,15 @@ __global__ void batch_prep_kernel(const McgbBatchSim *sims, uint32_t S, uint64_t
         BatchPrep p;
         McgbPf hg0 = {{0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, 0u, 0u, 0u};
         McgbPf hg1 = {{m.g, 0.0f, 0.0f, 0.0f, 0.0f}, 0u, 0u, 0u};
-        p.L[0].g0 = make_float4(-inf, 0.0f, inf, 1.0f);
+        p.L[0].g0 = make_float4(-inf, 0.0f, step_factor(inf), 1.0f);
         p.L[0].g1 = make_float4(m.n_above, 0.0f, 0.0f, 0.0f);
         p.L[0].g2 = make_float4((float)cc_d(m.n_above, m.n), 0.0f, 0.0f, 0.0f);
         pf_prepare(MCGB_PF_HG, hg0, p.L[0].pf0, p.L[0].pf1);
-        p.L[1].g0 = make_float4(0.0f, m.thickness, inv_mut, mua_inv_mut);
+        p.L[1].g0 = make_float4(0.0f, m.thickness, step_factor(inv_mut), mua_inv_mut);
         p.L[1].g1 = make_float4(m.n, m.mua, m.mus, (float)cc_d(m.n, m.n_above));
         p.L[1].g2 = make_float4((float)cc_d(m.n, m.n_below), 0.0f, 0.0f, 0.0f);
         pf_prepare(MCGB_PF_HG, hg1, p.L[1].pf0, p.L[1].pf1);
-        p.L[2].g0 = make_float4(m.thickness, inf, inf, 1.0f);
+        p.L[2].g0 = make_float4(m.thickness, inf, step_factor(inf), 1.0f);
         p.L[2].g1 = make_float4(m.n_below, 0.0f, 0.0f, (float)cc_d(m.n_below, m.n));
         p.L[2].g2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         pf_prepare(MCGB_PF_HG, hg0, p.L[2].pf0, p.L[2].pf1);
@@ -171,7 +171,7 @@ batched_kernel(const McgbBatchConfig cfg, const uint32_t *__restrict__ mult,
         if (active) {
             const float4 g0 = L[layer].g0;
             ++steps;
-            float step = -mc_log(rng.next()) * g0.z;
+            float step = sample_step(rng.next(), g0.z);
             step = fminf(step, FLT_MAX);
             int next = layer;
             if (pos.z + step * dir.z < g0.x) {

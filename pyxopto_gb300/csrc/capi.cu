@@ -69,13 +69,15 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
     if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
-    if (src.kind != MCGB_SRC_LINE && src.kind != MCGB_SRC_GAUSSIAN_BEAM &&
-        src.kind != MCGB_SRC_UNIFORM_FIBER_NI)
+    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_LAMBERTIAN_FIBER)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
-    if (src.kind == MCGB_SRC_UNIFORM_FIBER_NI &&
+    if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI &&
         !(src.sigma[0] >= 0.0f && src.sigma[1] >= 0.0f && src.sigma[1] <= 1.0f && src.clip > 0.0f))
-        return fail(MCGB_E_INVALID, "fiber source: core radius %g, acceptance cosine %g, core index %g",
+        return fail(MCGB_E_INVALID, "fiber source: core radius %g, angular parameter %g, core index %g",
                     (double)src.sigma[0], (double)src.sigma[1], (double)src.clip);
+    if ((src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER) &&
+        !(src.direction[2] > 0.0f))
+        return fail(MCGB_E_INVALID, "fiber source: the z component of the fibre axis must be positive");
     if (!(o.lottery_chance > 0.0f && o.lottery_chance <= 1.0f))
         return fail(MCGB_E_INVALID, "lottery chance %g outside (0, 1]", (double)o.lottery_chance);
     if (!(o.packet_weight_min > 0.0f && o.packet_weight_min <= 1.0f))
@@ -86,9 +88,20 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     for (int i = 0; i < 3; ++i) {
         const McgbDetector &d = dets[i];
         if (d.kind == MCGB_DET_NONE) continue;
-        if (d.kind != MCGB_DET_TOTAL && d.kind != MCGB_DET_RADIAL)
+        if (d.kind != MCGB_DET_TOTAL && d.kind != MCGB_DET_RADIAL && d.kind != MCGB_DET_RADIAL_PL &&
+            d.kind != MCGB_DET_TOTAL_PL)
             return fail(MCGB_E_INVALID, "%s detector: unknown kind %d", names[i], d.kind);
-        uint64_t n = d.kind == MCGB_DET_RADIAL ? d.n : 1;
+        if (d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL) {
+            if (!o.track_optical_pathlength)
+                return fail(MCGB_E_INVALID, "%s path-length detector needs track_optical_pathlength",
+                            names[i]);
+            if (i == 2) return fail(MCGB_E_INVALID, "the specular slot takes no path-length detector");
+        }
+        uint64_t nr = (d.kind == MCGB_DET_RADIAL || d.kind == MCGB_DET_RADIAL_PL) ? d.n : 1;
+        uint64_t npl = (d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL) ? d.n_pl : 1;
+        if (nr > 0x7FFFFFFFu || npl > 0x7FFFFFFFu)
+            return fail(MCGB_E_SIZE, "%s detector has too many bins", names[i]);
+        uint64_t n = nr * npl;
         if (n == 0) return fail(MCGB_E_INVALID, "%s detector has no bins", names[i]);
         if (!b->accumulator || !range_ok(d.offset, n, b->accumulator_size))
             return fail(MCGB_E_SIZE, "%s detector [%llu, +%llu) beyond the accumulator (%llu)", names[i],
@@ -251,8 +264,8 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
-    if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI)
-        return fail(MCGB_E_UNSUPPORTED, "the fiber source is implemented for layered media only");
+    if (cfg->source.kind >= MCGB_SRC_UNIFORM_FIBER_NI)
+        return fail(MCGB_E_UNSUPPORTED, "the fiber sources are implemented for layered media only");
     if (!buf->voxels || !buf->materials) return fail(MCGB_E_INVALID, "voxel or material buffer is NULL");
     /* Voxel material indices are validated by the caller (uint8 < num_materials):
        the host wrapper checks the array before upload. */

@@ -152,8 +152,22 @@ MCGB_DEV int refract_safe3(const f3 &p, const f3 &n, float n1, float n2, f3 *r) 
     return 0;
 }
 
+/* Free path length -log(u)/mu_t from a per-medium factor stored in the
+   shared-memory tables (step sampling, xopto/mcml/kernel/mcml.template.c:528-536).
+   EXACT: the factor is 1/mu_t and the step is -log(u)*factor, the
+   reference's expression.  FAST: the factor is -ln(2)/mu_t, folded once per
+   block, and the step is log2(u)*factor, since log(u) = ln(2)*log2(u). */
+#if MCGB_FAST_MATH
+MCGB_DEV float step_factor(float inv_mut) { return -0.693147182f * inv_mut; }
+MCGB_DEV float sample_step(float u, float factor) { return __log2f(u) * factor; }
+#else
+MCGB_DEV float step_factor(float inv_mut) { return inv_mut; }
+MCGB_DEV float sample_step(float u, float factor) { return -mc_log(u) * factor; }
+#endif
+
 /* scatter_direction + unconditional renormalisation,
-   xopto/mcbase/kernel/mcbase.template.c:1522-1555 */
+   xopto/mcbase/kernel/mcbase.template.c:1522-1555.  FAST mode divides by
+   sqrt(1 - uz^2) through one reciprocal square root. */
 MCGB_DEV void scatter_direction(f3 &dir, float cos_theta, float fi) {
     float sin_fi, cos_fi;
     float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
@@ -166,9 +180,17 @@ MCGB_DEV void scatter_direction(f3 &dir, float cos_theta, float fi) {
         dir.y = stsf;
         dir.z = copysignf(cos_theta, dir.z * cos_theta);
     } else {
+#if MCGB_FAST_MATH
+        float t = 1.0f - dir.z * dir.z;
+        float rk = rsqrtf(t);
+        float k = t * rk;
+        dir.x = (stcf * px * dir.z - stsf * dir.y) * rk + px * cos_theta;
+        dir.y = (stcf * dir.y * dir.z + stsf * px) * rk + dir.y * cos_theta;
+#else
         float k = mc_sqrt(1.0f - dir.z * dir.z);
         dir.x = mc_div(stcf * px * dir.z - stsf * dir.y, k) + px * cos_theta;
         dir.y = mc_div(stcf * dir.y * dir.z + stsf * px, k) + dir.y * cos_theta;
+#endif
         dir.z = (-stcf) * k + dir.z * cos_theta;
     }
     float k = mc_rcp_length(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
@@ -250,21 +272,29 @@ MCGB_DEV void accu_add(uint64_t *accu, uint64_t index, uint32_t w) {
     atomicAdd((unsigned long long *)(accu + index), (unsigned long long)w);
 }
 
-/* Radial / Total detector deposit:
-   xopto/mcml/mcdetector/radial.py:117-150, total.py:86-108 */
+/* Surface detector deposit: Total (xopto/mcml/mcdetector/total.py:86-108),
+   Radial (radial.py:117-150), TotalPl (totalpl.py:107-135) and RadialPl
+   (radialpl.py:138-179); opl is the packet's optical path length. */
 MCGB_DEV void detector_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir,
-                               float weight, uint64_t *accu) {
+                               float weight, float opl, uint64_t *accu) {
     if (det.kind == MCGB_DET_NONE) return;
     f3 ddir{det.direction[0], det.direction[1], det.direction[2]};
     float accept = (float)(det.cos_min <= fabsf(dot3(dir, ddir)));
     uint64_t index = 0;
-    if (det.kind == MCGB_DET_RADIAL) {
+    if (det.kind == MCGB_DET_RADIAL || det.kind == MCGB_DET_RADIAL_PL) {
         float dx = pos.x - det.position[0];
         float dy = pos.y - det.position[1];
         float r = mc_sqrt(dx * dx + dy * dy);
         if (det.log_scale) r = mc_log(fmaxf(r, 1e-12f));
         int r_index = cvt_int((r - det.r_min) * det.inv_dr);
         index = (uint64_t)clip_i(r_index, 0, (int)det.n - 1);
+    }
+    if (det.kind == MCGB_DET_RADIAL_PL || det.kind == MCGB_DET_TOTAL_PL) {
+        float pl = opl;
+        if (det.pl_log_scale) pl = mc_log(fmaxf(pl, 1e-12f));
+        int pl_index = clip_i(cvt_int((pl - det.pl_min) * det.inv_dpl), 0, (int)det.n_pl - 1);
+        uint64_t nr = det.kind == MCGB_DET_RADIAL_PL ? det.n : 1u;
+        index += (uint64_t)pl_index * nr;
     }
     uint32_t w = weight_to_u32(weight, accept);
     if (w > 0) accu_add(accu, det.offset + index, w);

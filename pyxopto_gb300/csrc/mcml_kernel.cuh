@@ -29,7 +29,7 @@ namespace MCGB_NS {
 
 /* Shared-memory record of one layer. */
 struct __align__(16) MlLayer {
-    float4 g0;    /* top, bottom, inv_mut, mua_inv_mut */
+    float4 g0;    /* top, bottom, step_factor(inv_mut), mua_inv_mut */
     float4 g1;    /* n, mua, mus, cos_critical_top */
     float4 pf0;   /* phase-function constants (pf_prepare) */
     float4 pf1;
@@ -40,8 +40,72 @@ struct MlSmem {
     MlLayer layers[MCGB_MAX_LAYERS];
 };
 
-/* Line / GaussianBeam / UniformFiberNI launch (xopto/mcml/mcsource/line.py:95-108,
-   gaussianbeam.py:119-170, fiberni.py:246-290). */
+/* Fibre sources (xopto/mcml/mcsource/fiberni.py:246-290,485-534;
+   fiber.py:267-330,576-640): a point uniform over the core; a direction
+   uniform in solid angle within the acceptance cone (Uniform*) or with
+   sin(theta) = sqrt(u)*NA (Lambertian*); the NI kinds refract the angle into
+   the sample and weigh the launch with reflectance_cos2, the tilted kinds
+   scale it by the core index, rotate both the point and the direction onto
+   the fibre axis and weigh with the reflectance at the core/sample
+   boundary.  The tilted kinds compare the launch point's z (0 on the
+   surface) with the critical cosine before refracting, so the reference
+   never refracts their direction; that is restated as is. */
+static __device__ __forceinline__ void mcml_launch_fiber(const McgbMcmlConfig &c, const MlLayer *L,
+                                                         Rng &rng, f3 &pos, f3 &dir, float &w,
+                                                         uint64_t *accu) {
+    const McgbSource &src = c.source;
+    const bool tilted = src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER;
+    const bool lambertian = src.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
+                            src.kind == MCGB_SRC_LAMBERTIAN_FIBER;
+    const float n_sample = L[1].g1.x, n_core = src.clip;
+    const float *T = src.transformation;
+    float sin_fi, cos_fi, sin_theta, cos_theta;
+    float r = mc_sqrt(rng.next()) * src.sigma[0];
+    mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+    if (tilted) {
+        f3 ps{r * cos_fi, r * sin_fi, 0.0f};
+        f3 pm{T[0] * ps.x + T[1] * ps.y + T[2] * ps.z, T[3] * ps.x + T[4] * ps.y + T[5] * ps.z,
+              T[6] * ps.x + T[7] * ps.y + T[8] * ps.z};
+        float k = mc_div(0.0f - pm.z, src.direction[2]);
+        pm.x += k * src.direction[0];
+        pm.y += k * src.direction[1];
+        pos = f3{src.position[0] + pm.x, src.position[1] + pm.y, 0.0f};
+    } else {
+        pos = f3{src.position[0] + r * cos_fi, src.position[1] + r * sin_fi, 0.0f};
+    }
+    mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+    if (lambertian) {
+        sin_theta = mc_sqrt(rng.next()) * src.sigma[1];
+    } else {
+        cos_theta = 1.0f - rng.next() * (1.0f - src.sigma[1]);
+        sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+    }
+    sin_theta = mc_div(sin_theta, tilted ? n_core : n_sample);
+    cos_theta = mc_sqrt(1.0f - sin_theta * sin_theta);
+    f3 pt{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+    float R;
+    if (tilted) {
+        f3 d{T[0] * pt.x + T[1] * pt.y + T[2] * pt.z, T[3] * pt.x + T[4] * pt.y + T[5] * pt.z,
+             T[6] * pt.x + T[7] * pt.y + T[8] * pt.z};
+        float cc = cos_critical(n_core, n_sample);
+        dir = d;
+        R = reflectance(n_core, n_sample, d.z, cc);
+        if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, R, 0.0f, accu);
+    } else {
+        dir = pt;
+        R = reflectance_cos2(n_core, n_sample, pt.z);
+        if (c.specular.kind != MCGB_DET_NONE) {
+            f3 dir_in{dir.x, dir.y, -dir.z};
+            f3 normal{0.0f, 0.0f, -1.0f};
+            f3 d = refract3(dir_in, normal, n_sample, n_core);
+            detector_deposit(c.specular, pos, d, R, 0.0f, accu);
+        }
+    }
+    w = 1.0f - R;
+}
+
+/* Line / GaussianBeam / fibre launch (xopto/mcml/mcsource/line.py:95-108,
+   gaussianbeam.py:119-170, fiberni.py, fiber.py). */
 static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
                                                    Rng &rng, f3 &pos, f3 &dir, float &w,
                                                    int &layer, uint64_t *accu) {
@@ -52,31 +116,11 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
         dir = f3{src.direction[0], src.direction[1], src.direction[2]};
         if (c.specular.kind != MCGB_DET_NONE) {
             f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
-            detector_deposit(c.specular, pos, d, src.reflectance, accu);
+            detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
         layer = 1;
-    } else if (src.kind == MCGB_SRC_UNIFORM_FIBER_NI) {
-        /* uniform over the core, uniform in solid angle within the
-           acceptance cone in air, refracted into the sample */
-        float sin_fi, cos_fi;
-        const float n_sample = L[1].g1.x;
-        float r = mc_sqrt(rng.next()) * src.sigma[0];
-        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
-        pos = f3{src.position[0] + r * cos_fi, src.position[1] + r * sin_fi, 0.0f};
-        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
-        float cos_theta = 1.0f - rng.next() * (1.0f - src.sigma[1]);
-        float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
-        sin_theta = mc_div(sin_theta, n_sample);
-        cos_theta = mc_sqrt(1.0f - sin_theta * sin_theta);
-        dir = f3{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
-        float R = reflectance_cos2(src.clip, n_sample, dir.z);
-        w = 1.0f - R;
-        if (c.specular.kind != MCGB_DET_NONE) {
-            f3 dir_in{dir.x, dir.y, -dir.z};
-            f3 normal{0.0f, 0.0f, -1.0f};
-            f3 d = refract3(dir_in, normal, n_sample, src.clip);
-            detector_deposit(c.specular, pos, d, R, accu);
-        }
+    } else if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
+        mcml_launch_fiber(c, L, rng, pos, dir, w, accu);
         layer = 1;
     } else {
         float sin_fi, cos_fi;
@@ -99,7 +143,7 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
             f3 dir_in{dir.x, dir.y, -dir.z};
             f3 normal{0.0f, 0.0f, -1.0f};
             f3 d = refract3(dir_in, normal, L[1].g1.x, L[0].g1.x);
-            detector_deposit(c.specular, pos, d, src.reflectance, accu);
+            detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
     }
 }
@@ -214,14 +258,14 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
     const MlLayer *L = x.L;
     const McgbRunOptions &o = c.opt;
     uint64_t *accu = b.accumulator;
-    const float4 g0 = L[s.layer].g0;   /* top, bottom, inv_mut, mua_inv_mut */
+    const float4 g0 = L[s.layer].g0;   /* top, bottom, step factor, mua_inv_mut */
     ++s.steps;
     float u = rng.next();
     float step;
     if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT)
         step = mc_div(-mc_log(u), L[s.layer].g1.z);
     else
-        step = -mc_log(u) * g0.z;
+        step = sample_step(u, g0.z);
     step = fminf(step, FLT_MAX);
     int next = s.layer;
     if (s.pos.z + step * s.dir.z < g0.x) {
@@ -258,8 +302,8 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         if (next != s.layer) {
             s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
             if (!(s.layer > 0 && s.layer < x.last_layer)) {
-                if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
-                else detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+                if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
+                else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
                 done = true;
             }
         } else {
@@ -279,8 +323,8 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
     } else if (next != s.layer) {
         s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
         if (!(s.layer > 0 && s.layer < x.last_layer)) {
-            if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
-            else detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+            if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
+            else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
             done = true;
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
@@ -344,7 +388,7 @@ static __device__ __forceinline__ const float *mcml_stage(const McgbMcmlConfig &
     for (uint32_t i = threadIdx.x; i < c.num_layers; i += blockDim.x) {
         const McgbLayer &l = c.layers[i];
         MlLayer h;
-        h.g0 = make_float4(l.top, l.bottom, l.inv_mut, l.mua_inv_mut);
+        h.g0 = make_float4(l.top, l.bottom, step_factor(l.inv_mut), l.mua_inv_mut);
         h.g1 = make_float4(l.n, l.mua, l.mus, l.cos_critical_top);
         h.g2 = make_float4(l.cos_critical_bottom, 0.0f, 0.0f, 0.0f);
         pf_prepare(PF, l.pf, h.pf0, h.pf1);

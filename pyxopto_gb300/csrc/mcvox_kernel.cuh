@@ -16,7 +16,7 @@ namespace MCGB_NS {
 
 /* Shared-memory record of one material. */
 struct __align__(16) MvMaterial {
-    float4 g0;    /* mus, mua, inv_mut, mua_inv_mut */
+    float4 g0;    /* mus, mua, step_factor(inv_mut), mua_inv_mut */
     float4 g1;    /* n, -, -, - */
     float4 pf0;   /* phase-function constants (pf_prepare) */
     float4 pf1;
@@ -90,7 +90,7 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
         dir = f3{src.direction[0], src.direction[1], src.direction[2]};
         if (c.specular.kind != MCGB_DET_NONE) {
             f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
-            detector_deposit(c.specular, pos, d, src.reflectance, accu);
+            detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
     } else {
         float sin_fi, cos_fi, specular_r;
@@ -127,7 +127,7 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
             specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
                                      cos_critical(n_outside, n_inside));
             if (c.specular.kind != MCGB_DET_NONE)
-                detector_deposit(c.specular, pos, direction, specular_r, accu);
+                detector_deposit(c.specular, pos, direction, specular_r, 0.0f, accu);
         } else {
             pos = f3{g.tl[0], g.tl[1], g.tl[2]};
             dir = f3{0.0f, 0.0f, 1.0f};
@@ -247,11 +247,11 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     const MvGeom &g = x.g;
     const McgbRunOptions &o = c.opt;
     uint64_t *accu = b.accumulator;
-    const float4 g0 = M[s.mat].g0;   /* mus, mua, inv_mut, mua_inv_mut */
+    const float4 g0 = M[s.mat].g0;   /* mus, mua, step factor, mua_inv_mut */
     ++s.steps;
     float u = rng.next();
     float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) ? mc_div(-mc_log(u), g0.x)
-                                                                   : -mc_log(u) * g0.z;
+                                                                   : sample_step(u, g0.z);
     step = fminf(step, FLT_MAX);
     /* mcsim_intersect, mcvox.template.c:173-196 */
     f3 dist;
@@ -286,8 +286,8 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         if (d < step) {
             s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
             if (!mv_valid(g, s.vi)) {
-                if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
-                else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+                if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
+                else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
                 done = true;
             }
         } else {
@@ -307,8 +307,8 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     } else if (d < step) {
         s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
         if (!mv_valid(g, s.vi)) {
-            if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, accu);
-            else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, accu);
+            if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
+            else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
             done = true;
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
@@ -371,7 +371,7 @@ static __device__ __forceinline__ const float *mcvox_stage(const McgbMcvoxConfig
     for (uint32_t i = threadIdx.x; i < c.num_materials; i += blockDim.x) {
         const McgbMaterial &m = b.materials[i];
         MvMaterial h;
-        h.g0 = make_float4(m.mus, m.mua, m.inv_mut, m.mua_inv_mut);
+        h.g0 = make_float4(m.mus, m.mua, step_factor(m.inv_mut), m.mua_inv_mut);
         h.g1 = make_float4(m.n, 0.0f, 0.0f, 0.0f);
         pf_prepare(PF, m.pf, h.pf0, h.pf1);
         sm.materials[i] = h;

@@ -1,6 +1,7 @@
-"""Surface detectors: Total and Radial, grouped by Detectors into the top,
-bottom and specular slots (xopto/mcml/mcdetector/base.py, total.py,
-radial.py; the mcvox package uses the same classes).
+"""Surface detectors: Total, Radial and their optical path-length variants
+TotalPl and RadialPl, grouped by Detectors into the top, bottom and specular
+slots (xopto/mcml/mcdetector/base.py, total.py, radial.py, totalpl.py,
+radialpl.py; the mcvox package uses the same classes).
 
 Tallies come back from the device as uint64 fixed-point integers and are
 converted with the reference's rule raw += accumulator/K
@@ -189,6 +190,101 @@ class Radial(Detector):
             self._r_axis, *self._position, self._cosmin)
 
 
+def _pack_pl_axis(axis, target):
+    target.pl_min = axis.scaled_start
+    target.inv_dpl = 1.0 / axis.step if axis.step != 0.0 else 0.0
+    target.pl_log_scale = int(axis.logscale)
+    target.n_pl = axis.n
+
+
+class TotalPl(Total):
+    """Total reflectance/transmittance resolved by optical path length
+    (xopto/mcml/mcdetector/totalpl.py:30-300); raw has shape (n_pl, 1).
+    Turns on optical path-length tracking."""
+    kind = _abi.DET_TOTAL_PL
+    tracks_pathlength = True
+
+    def __init__(self, plaxis=None, cosmin=0.0, direction=(0.0, 0.0, 1.0)):
+        if isinstance(plaxis, TotalPl):
+            other = plaxis
+            Total.__init__(self, cosmin=other.cosmin, direction=other.direction)
+            self._pl_axis = type(other.plaxis)(other.plaxis)
+            self._raw_data = np.copy(other.raw)
+            self._nphotons = other.nphotons
+            return
+        Total.__init__(self, cosmin=cosmin, direction=direction)
+        self._pl_axis = plaxis if plaxis is not None else Axis(0.0, 1.0, 1)
+        self._raw_data = np.zeros((self._pl_axis.n, 1))
+
+    plaxis = property(lambda self: self._pl_axis)
+    pl = property(lambda self: self._pl_axis.centers)
+    pledges = property(lambda self: self._pl_axis.edges)
+    npl = property(lambda self: self._pl_axis.n)
+
+    def pack(self, mc, target):
+        Total.pack(self, mc, target)
+        target.kind = _abi.DET_TOTAL_PL
+        _pack_pl_axis(self._pl_axis, target)
+        return target
+
+    def copy(self):
+        return TotalPl(self)
+
+    def todict(self):
+        return {'type': 'TotalPl', 'pl_axis': self._pl_axis.todict(), 'cosmin': self._cosmin,
+                'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'TotalPl(plaxis={}, cosmin={})'.format(self._pl_axis, self._cosmin)
+
+
+class RadialPl(Radial):
+    """Radial reflectance/transmittance resolved by optical path length
+    (xopto/mcml/mcdetector/radialpl.py:30-470); raw has shape (n_pl, n_r),
+    path length first.  Turns on optical path-length tracking."""
+    kind = _abi.DET_RADIAL_PL
+    tracks_pathlength = True
+
+    def __init__(self, raxis, plaxis=None, position=(0.0, 0.0), cosmin=0.0,
+                 direction=(0.0, 0.0, 1.0)):
+        if isinstance(raxis, RadialPl):
+            other = raxis
+            Radial.__init__(self, type(other.raxis)(other.raxis), position=other.position,
+                            cosmin=other.cosmin, direction=other.direction)
+            self._pl_axis = type(other.plaxis)(other.plaxis)
+            self._raw_data = np.copy(other.raw)
+            self._nphotons = other.nphotons
+        else:
+            Radial.__init__(self, raxis, position=position, cosmin=cosmin, direction=direction)
+            self._pl_axis = plaxis if plaxis is not None else Axis(0.0, 1.0, 1)
+            self._raw_data = np.zeros((self._pl_axis.n, raxis.n))
+        self._inv_accumulators_area = self._inv_accumulators_area.reshape(1, -1)
+
+    plaxis = property(lambda self: self._pl_axis)
+    pl = property(lambda self: self._pl_axis.centers)
+    pledges = property(lambda self: self._pl_axis.edges)
+    npl = property(lambda self: self._pl_axis.n)
+    nr = property(lambda self: self._r_axis.n)
+
+    def pack(self, mc, target):
+        Radial.pack(self, mc, target)
+        target.kind = _abi.DET_RADIAL_PL
+        _pack_pl_axis(self._pl_axis, target)
+        return target
+
+    def copy(self):
+        return RadialPl(self)
+
+    def todict(self):
+        return {'type': 'RadialPl', 'r_axis': self._r_axis.todict(),
+                'pl_axis': self._pl_axis.todict(), 'position': self._position.tolist(),
+                'cosmin': self._cosmin, 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'RadialPl(raxis={}, plaxis={}, cosmin={})'.format(self._r_axis, self._pl_axis,
+                                                                 self._cosmin)
+
+
 class Detectors:
     """Top, bottom and specular detectors
     (xopto/mcml/mcdetector/base.py:295-568)."""
@@ -212,6 +308,11 @@ class Detectors:
         return iter([d for d in (self._top, self._bottom, self._specular)
                      if not isinstance(d, DetectorDefault)])
 
+    def tracks_pathlength(self) -> bool:
+        """True if a detector needs the packets' optical path length."""
+        return any(getattr(d, 'tracks_pathlength', False)
+                   for d in (self._top, self._bottom, self._specular))
+
     def pack(self, mc, cfg):
         self._top.pack(mc, cfg.top)
         self._bottom.pack(mc, cfg.bottom)
@@ -227,4 +328,5 @@ class Detectors:
     __repr__ = __str__
 
 
-__all__ = ['Axis', 'RadialAxis', 'Detector', 'DetectorDefault', 'Total', 'Radial', 'Detectors']
+__all__ = ['Axis', 'RadialAxis', 'Detector', 'DetectorDefault', 'Total', 'Radial', 'TotalPl',
+           'RadialPl', 'Detectors']

@@ -85,10 +85,10 @@ class Mc(McEngine):
             self._detectors.pack(self, cfg)
         if self._fluence is not None:
             self._fluence.pack(self, cfg.fluence)
-        track_opl = False
+        track_opl = self._detectors is not None and self._detectors.tracks_pathlength()
         if self._trace is not None:
             self._trace.pack(self, cfg.trace, int(nphotons))
-            track_opl = self._trace.plon
+            track_opl = track_opl or self._trace.plon
         cfg.opt = self._run_options(track_opl)
         return cfg
 

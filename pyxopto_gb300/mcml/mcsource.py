@@ -1,5 +1,7 @@
-"""Photon packet sources of the layered simulator: Line, GaussianBeam and
-UniformFiberNI (xopto/mcml/mcsource/line.py, gaussianbeam.py, fiberni.py)."""
+"""Photon packet sources of the layered simulator: Line, GaussianBeam and the
+fibre sources UniformFiberNI, LambertianFiberNI, UniformFiber and
+LambertianFiber (xopto/mcml/mcsource/line.py, gaussianbeam.py, fiberni.py,
+fiber.py)."""
 import numpy as np
 
 from .. import _abi
@@ -176,3 +178,94 @@ class UniformFiberNI(Source):
         return 'UniformFiberNI(fiber={}, position=({}, {}, {}))'.format(self._fiber, *self._position)
 
     __repr__ = __str__
+
+
+class LambertianFiberNI(UniformFiberNI):
+    """Fibre source with normal incidence and a Lambertian angular
+    distribution, sin(theta) = sqrt(u)*NA (xopto/mcml/mcsource/fiberni.py:422-578)."""
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiberni.py:562-573: core radius, NA, core refractive index."""
+        UniformFiberNI.pack(self, mc, target)
+        target.kind = _abi.SRC_LAMBERTIAN_FIBER_NI
+        target.sigma[1] = self._fiber.na
+        return target
+
+    def todict(self):
+        d = UniformFiberNI.todict(self)
+        d['type'] = 'LambertianFiberNI'
+        return d
+
+    def __str__(self):
+        return 'LambertianFiberNI(fiber={}, position=({}, {}, {}))'.format(self._fiber, *self._position)
+
+    __repr__ = __str__
+
+
+class UniformFiber(Source):
+    """Fibre source tilted along ``direction`` (z component positive):
+    packets start uniformly over the core projected onto the surface,
+    uniformly in solid angle within the acceptance cone around the fibre axis
+    (xopto/mcml/mcsource/fiber.py:190-496)."""
+    _kind = _abi.SRC_UNIFORM_FIBER
+
+    def __init__(self, fiber: MultimodeFiber, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0)):
+        if isinstance(fiber, UniformFiber):
+            fiber, position, direction = fiber.fiber, fiber.position, fiber.direction
+        self._fiber = fiber
+        self._position = np.zeros((3,))
+        self._direction = np.zeros((3,))
+        self._set_position(position)
+        self._set_direction(direction)
+
+    def _set_fiber(self, fib):
+        self._fiber = fib
+
+    def _set_position(self, p):
+        self._position[:] = p
+        self._position[2] = 0.0
+
+    def _set_direction(self, d):
+        d = _unit(d)
+        if d[-1] <= 0.0:
+            raise ValueError('Z component of the propagation direction must be positive!')
+        self._direction[:] = d
+
+    fiber = property(lambda self: self._fiber, _set_fiber, None, 'Multimode optical fiber.')
+    position = property(lambda self: self._position, _set_position, None, 'Source position.')
+    direction = property(lambda self: self._direction, _set_direction, None, 'Source direction.')
+
+    def _angular(self):
+        return (1.0 - self._fiber.na ** 2) ** 0.5
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiber.py:429-470: rotation onto the fibre axis, core refractive
+        index, angular parameter, position, axis, core radius."""
+        T = mcutil.transform_base((0.0, 0.0, 1.0), self._direction)
+        target.kind = self._kind
+        target.transformation[:] = [float(v) for v in np.asarray(T).ravel()]
+        target.position[:] = [float(v) for v in self._position]
+        target.direction[:] = [float(v) for v in self._direction]
+        target.sigma[0] = self._fiber.dcore * 0.5
+        target.sigma[1] = self._angular()
+        target.clip = self._fiber.ncore
+        return target
+
+    def todict(self):
+        return {'type': type(self).__name__, 'fiber': self._fiber.todict(),
+                'position': self._position.tolist(), 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return '{}(fiber={}, position=({}, {}, {}), direction=({}, {}, {}))'.format(
+            type(self).__name__, self._fiber, *self._position, *self._direction)
+
+    __repr__ = __str__
+
+
+class LambertianFiber(UniformFiber):
+    """Tilted fibre source with a Lambertian angular distribution
+    (xopto/mcml/mcsource/fiber.py:499-687)."""
+    _kind = _abi.SRC_LAMBERTIAN_FIBER
+
+    def _angular(self):
+        return self._fiber.na

@@ -128,6 +128,52 @@ SCENARIOS = {
         detectors=dict(top=dict(type='Radial', axis=[0.0, 1.7e-3, 34], cosmin=0.9884549351697024),
                        specular=dict(type='Total')),
         rmax=5e-3, nphotons=3000, streams=32, rnginit=17),
+    # the other fibre sources (xopto/mcml/mcsource/fiberni.py, fiber.py) on a
+    # two-layer sample, with a specular detector
+    'fiber_lambertian_ni': dict(
+        medium='mcml',
+        layers=[dict(d=INF, n=1.452, mua=0.0, mus=0.0, pf=['Hg', 0.9]),
+                dict(d=1e-3, n=1.38, mua=200.0, mus=1.5e4, pf=['Hg', 0.9]),
+                dict(d=INF, n=1.33, mua=20.0, mus=1e4, pf=['Hg', 0.8])],
+        source=dict(type='LambertianFiberNI',
+                    fiber=dict(dcore=400e-6, dcladding=420e-6, ncore=1.452, na=0.39)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]), specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=23),
+    'fiber_tilted_uniform': dict(
+        medium='mcml',
+        layers=[dict(d=INF, n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.9]),
+                dict(d=2e-3, n=1.4, mua=150.0, mus=2e4, pf=['Hg', 0.85]),
+                dict(d=INF, n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.85])],
+        source=dict(type='UniformFiber',
+                    fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22),
+                    position=(1e-4, -2e-4, 0.0), direction=(0.3, 0.1, 1.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=29),
+    'fiber_tilted_lambertian': dict(
+        medium='mcml',
+        layers=[dict(d=INF, n=1.6, mua=0.0, mus=0.0, pf=['Hg', 0.9]),
+                dict(d=2e-3, n=1.33, mua=150.0, mus=2e4, pf=['Hg', 0.85]),
+                dict(d=INF, n=1.33, mua=0.0, mus=0.0, pf=['Hg', 0.85])],
+        source=dict(type='LambertianFiber',
+                    fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22),
+                    direction=(-0.2, 0.25, 1.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]), specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=31),
+    # optical path-length resolved detectors (xopto/mcml/mcdetector/radialpl.py,
+    # totalpl.py): two layers, RadialPl on top (linear path-length axis),
+    # TotalPl below (log path-length axis)
+    'pl_detectors': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1e-3, n=1.4, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
+                dict(d=2e-3, n=1.35, mua=50.0, mus=5e3, pf=['Hg', 0.9]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='RadialPl', axis=[0.0, 2e-3, 10], plaxis=[0.0, 20e-3, 16]),
+                       bottom=dict(type='TotalPl', plaxis=[1e-4, 1e-1, 12], pllogscale=True),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=19),
 }
 
 # Bench workloads (not golden-tested at these sizes): the layered
@@ -226,6 +272,14 @@ def _detectors(pkg, spec):
             continue
         if d['type'] == 'Total':
             slots[slot] = pkg.mcdetector.Total(cosmin=d.get('cosmin', 0.0))
+        elif d['type'] == 'TotalPl':
+            slots[slot] = pkg.mcdetector.TotalPl(_axis(pkg, {'axis': d['plaxis'],
+                                                             'logscale': d.get('pllogscale', False)}),
+                                                 cosmin=d.get('cosmin', 0.0))
+        elif d['type'] == 'RadialPl':
+            slots[slot] = pkg.mcdetector.RadialPl(
+                _axis(pkg, d), _axis(pkg, {'axis': d['plaxis'], 'logscale': d.get('pllogscale', False)}),
+                position=d.get('position', (0.0, 0.0)), cosmin=d.get('cosmin', 0.0))
         else:
             slots[slot] = pkg.mcdetector.Radial(_axis(pkg, d), position=d.get('position', (0.0, 0.0)),
                                                 cosmin=d.get('cosmin', 0.0))
