@@ -104,7 +104,9 @@ enum {
     MCGB_SRC_UNIFORM_FIBER_NI = 2,
     MCGB_SRC_LAMBERTIAN_FIBER_NI = 3,
     MCGB_SRC_UNIFORM_FIBER = 4,
-    MCGB_SRC_LAMBERTIAN_FIBER = 5
+    MCGB_SRC_LAMBERTIAN_FIBER = 5,
+    MCGB_SRC_UNIFORM_BEAM = 6,
+    MCGB_SRC_ISOTROPIC_POINT = 7
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
        MCGB_DET_TOTAL_PL = 4 };
@@ -174,7 +176,13 @@ typedef struct McgbMaterial {
        direction = fibre axis, transformation = rotation of the z axis onto
        it;
      LambertianFiber (fiber.py:576-640,660-681): sigma[1] = NA, direction
-       and transformation as UniformFiber. */
+       and transformation as UniformFiber.
+   UniformBeam mcml (xopto/mcml/mcsource/uniformbeam.py:107-146,243-292):
+     elliptical flat-top beam; transformation, position on the surface,
+     direction (refracted), sigma = radii along x and y, reflectance.
+   IsotropicPoint mcml (xopto/mcml/mcsource/point.py:76-128,188-226):
+     position (above the sample: z <= 0, or inside it) and layer_index of
+     the layer that holds it (1 for a point above the sample). */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];
@@ -184,7 +192,8 @@ typedef struct McgbSource {
     float transformation[9];                /* row-major a_11 .. a_33 */
     float sigma[2];
     float clip;
-    float reserved[2];
+    int32_t layer_index;                    /* IsotropicPoint                  */
+    float reserved;
 } McgbSource;                               /* 104 bytes */
 
 /* Surface detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;

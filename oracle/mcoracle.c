@@ -51,6 +51,10 @@ static inline float m_pow(int mm, float x, float y) { return mm ? pm_powrf(x, y)
 static inline void m_sincos(int mm, float x, float *s, float *c) {
     if (mm) pm_sincosf(x, s, c); else sincosf(x, s, c);
 }
+/* separate mc_sin / mc_cos calls of the reference (UniformBeam) */
+static inline void m_sin_cos(int mm, float x, float *s, float *c) {
+    if (mm) pm_sincosf(x, s, c); else { *s = sinf(x); *c = cosf(x); }
+}
 
 /* convert_int / convert_uint with round-toward-zero and saturation, the
    behaviour of the GPU's float-to-int conversion. */
@@ -410,6 +414,62 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
         }
         s->layer = 1;
+    } else if (src->kind == MCGB_SRC_UNIFORM_BEAM) {
+        /* UniformBeam.mcsim_launch, xopto/mcml/mcsource/uniformbeam.py:107-146 */
+        float rand_sqrt = sqrtf(rnd(x, a));
+        float fi = 6.28318548f * rnd(x, a);
+        float sin_fi, cos_fi;
+        m_sin_cos(mm, fi, &sin_fi, &cos_fi);
+        v3 ps = {rand_sqrt * cos_fi * src->sigma[0], rand_sqrt * sin_fi * src->sigma[1], 0.0f}, pm;
+        const float *T = src->transformation;
+        pm.x = T[0] * ps.x + T[1] * ps.y + T[2] * ps.z;
+        pm.y = T[3] * ps.x + T[4] * ps.y + T[5] * ps.z;
+        pm.z = T[6] * ps.x + T[7] * ps.y + T[8] * ps.z;
+        float k = (0.0f - pm.z) / src->direction[2];
+        pm.x += k * src->direction[0];
+        pm.y += k * src->direction[1];
+        s->pos.x = src->position[0] + pm.x;
+        s->pos.y = src->position[1] + pm.y;
+        s->pos.z = 0.0f;
+        s->dir.x = src->direction[0]; s->dir.y = src->direction[1]; s->dir.z = src->direction[2];
+        s->w = 1.0f - src->reflectance;
+        s->layer = 1;
+        if (c->specular.kind != MCGB_DET_NONE) {
+            v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
+            v3 normal = {0.0f, 0.0f, -1.0f};
+            v3 d = refract3(dir_in, normal, c->layers[1].n, c->layers[0].n);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
+        }
+    } else if (src->kind == MCGB_SRC_ISOTROPIC_POINT) {
+        /* IsotropicPoint.mcsim_launch, xopto/mcml/mcsource/point.py:76-128 */
+        float sin_fi, cos_fi, R = 0.0f;
+        v3 pos = {src->position[0], src->position[1], src->position[2]};
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - 2.0f * rnd(x, a);
+        float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        v3 d = {cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        v3 refracted = d;
+        if (pos.z <= 0.0f) {
+            float cc = c->layers[0].cos_critical_bottom;
+            if (d.z > cc) {
+                v3 normal = {0.0f, 0.0f, 1.0f};
+                float n_sample = c->layers[1].n, n_medium = c->layers[0].n;
+                refracted = refract3(d, normal, n_sample, n_medium);
+                R = reflectance(n_medium, n_sample, d.z, cc);
+                float t = -pos.z / d.z;
+                pos.x += d.x * t;
+                pos.y += d.y * t;
+            } else {
+                R = 1.0f;
+            }
+            pos.z = 0.0f;
+        }
+        s->dir = refracted;
+        s->pos = pos;
+        if (c->specular.kind != MCGB_DET_NONE)
+            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu);
+        s->w = 1.0f - R;
+        s->layer = src->layer_index;
     } else if (src->kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
         mcml_launch_fiber(mm, c, s, x, a, accu);
         s->layer = 1;

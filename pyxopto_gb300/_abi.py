@@ -20,7 +20,7 @@ SCHED_STATIC, SCHED_DYNAMIC = 0, 1
 METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT = 0, 1, 2
 PF_HG, PF_GK, PF_LUT = 0, 1, 2
 SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI, SRC_LAMBERTIAN_FIBER_NI = 0, 1, 2, 3
-SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER = 4, 5
+SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT = 4, 5, 6, 7
 DET_NONE, DET_TOTAL, DET_RADIAL, DET_RADIAL_PL, DET_TOTAL_PL = 0, 1, 2, 3, 4
 FLUENCE_NONE, FLUENCE_DEPOSITION, FLUENCE_RATE = 0, 1, 2
 TRACE_NONE, TRACE_START, TRACE_END, TRACE_ALL = 0, 1, 2, 7
@@ -52,7 +52,7 @@ class McgbSource(C.Structure):
     _fields_ = [('kind', i32), ('position', f32 * 3), ('direction', f32 * 3),
                 ('direction_reflected', f32 * 3), ('reflectance', f32),
                 ('transformation', f32 * 9), ('sigma', f32 * 2), ('clip', f32),
-                ('reserved', f32 * 2)]
+                ('layer_index', i32), ('reserved', f32)]
 
 
 class McgbDetector(C.Structure):

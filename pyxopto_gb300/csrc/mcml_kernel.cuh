@@ -119,6 +119,58 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
             detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
         layer = 1;
+    } else if (src.kind == MCGB_SRC_UNIFORM_BEAM) {
+        /* xopto/mcml/mcsource/uniformbeam.py:107-146 */
+        float rand_sqrt = mc_sqrt(rng.next());
+        float fi = 6.28318548f * rng.next();
+        float sin_fi, cos_fi;
+        mc_sincos(fi, &sin_fi, &cos_fi);
+        f3 ps{rand_sqrt * cos_fi * src.sigma[0], rand_sqrt * sin_fi * src.sigma[1], 0.0f};
+        const float *T = src.transformation;
+        f3 pm{T[0] * ps.x + T[1] * ps.y + T[2] * ps.z, T[3] * ps.x + T[4] * ps.y + T[5] * ps.z,
+              T[6] * ps.x + T[7] * ps.y + T[8] * ps.z};
+        float k = mc_div(0.0f - pm.z, src.direction[2]);
+        pm.x += k * src.direction[0];
+        pm.y += k * src.direction[1];
+        pos = f3{src.position[0] + pm.x, src.position[1] + pm.y, 0.0f};
+        dir = f3{src.direction[0], src.direction[1], src.direction[2]};
+        w = 1.0f - src.reflectance;
+        layer = 1;
+        if (c.specular.kind != MCGB_DET_NONE) {
+            f3 dir_in{dir.x, dir.y, -dir.z};
+            f3 normal{0.0f, 0.0f, -1.0f};
+            f3 d = refract3(dir_in, normal, L[1].g1.x, L[0].g1.x);
+            detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
+        }
+    } else if (src.kind == MCGB_SRC_ISOTROPIC_POINT) {
+        /* xopto/mcml/mcsource/point.py:76-128; the refraction into the
+           sample passes (n_sample, n_medium) as (n1, n2), as the reference does */
+        float sin_fi, cos_fi;
+        float R = 0.0f;
+        pos = f3{src.position[0], src.position[1], src.position[2]};
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - 2.0f * rng.next();
+        float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        f3 d{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        dir = d;
+        if (pos.z <= 0.0f) {
+            float cc = L[0].g2.x;
+            if (d.z > cc) {
+                f3 normal{0.0f, 0.0f, 1.0f};
+                float n_sample = L[1].g1.x, n_medium = L[0].g1.x;
+                dir = refract3(d, normal, n_sample, n_medium);
+                R = reflectance(n_medium, n_sample, d.z, cc);
+                float t = mc_div(-pos.z, d.z);
+                pos.x += d.x * t;
+                pos.y += d.y * t;
+            } else {
+                R = 1.0f;
+            }
+            pos.z = 0.0f;
+        }
+        if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, R, 0.0f, accu);
+        w = 1.0f - R;
+        layer = src.layer_index;
     } else if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
         mcml_launch_fiber(c, L, rng, pos, dir, w, accu);
         layer = 1;

@@ -1,7 +1,8 @@
-"""Photon packet sources of the layered simulator: Line, GaussianBeam and the
-fibre sources UniformFiberNI, LambertianFiberNI, UniformFiber and
-LambertianFiber (xopto/mcml/mcsource/line.py, gaussianbeam.py, fiberni.py,
-fiber.py)."""
+"""Photon packet sources of the layered simulator: Line, GaussianBeam,
+UniformBeam, IsotropicPoint and the fibre sources UniformFiberNI,
+LambertianFiberNI, UniformFiber and LambertianFiber
+(xopto/mcml/mcsource/line.py, gaussianbeam.py, uniformbeam.py, point.py,
+fiberni.py, fiber.py)."""
 import numpy as np
 
 from .. import _abi
@@ -269,3 +270,88 @@ class LambertianFiber(UniformFiber):
 
     def _angular(self):
         return self._fiber.na
+
+
+class UniformBeam(Source):
+    """Collimated beam of uniform intensity over an ellipse of the given
+    diameters (xopto/mcml/mcsource/uniformbeam.py:32-330)."""
+
+    def __init__(self, diameter, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0)):
+        if isinstance(diameter, UniformBeam):
+            o = diameter
+            diameter, position, direction = o.diameter, o.position, o.direction
+        self._diameter = np.zeros((2,))
+        self._diameter[:] = diameter
+        if np.any(self._diameter < 0.0):
+            raise ValueError('Beam diameter must not be negative!')
+        self._position = np.zeros((3,))
+        self._position[:] = position
+        self._direction = _unit(direction)
+        if self._direction[-1] <= 0.0:
+            raise ValueError('Z component of the propagation direction must be positive!')
+
+    diameter = property(lambda self: self._diameter)
+    position = property(lambda self: self._position)
+    direction = property(lambda self: self._direction)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """uniformbeam.py:243-292: move to the surface, refract, specular
+        reflectance, rotation of the beam plane."""
+        k = (0.0 - self._position[2]) / self._direction[2]
+        position = self._position + k * self._direction
+        position[2] = 0.0
+        n1, n2 = mc.layers[0].n, mc.layers[1].n
+        direction = mcutil.refract(self._direction, (0.0, 0.0, 1.0), n1, n2)
+        reflectance = mcutil.reflectance(n1, n2, abs(self._direction[-1]))
+        T = mcutil.transform_base((0.0, 0.0, 1.0), self._direction)
+        target.kind = _abi.SRC_UNIFORM_BEAM
+        target.transformation[:] = [float(v) for v in np.asarray(T).ravel()]
+        target.position[:] = [float(v) for v in position]
+        target.direction[:] = [float(v) for v in direction]
+        target.sigma[:] = [float(v) * 0.5 for v in self._diameter]
+        target.reflectance = reflectance
+        return target
+
+    def todict(self):
+        return {'type': 'UniformBeam', 'diameter': self._diameter.tolist(),
+                'position': self._position.tolist(), 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'UniformBeam(diameter=({}, {}), position=({}, {}, {}), direction=({}, {}, {}))'.format(
+            *self._diameter, *self._position, *self._direction)
+
+    __repr__ = __str__
+
+
+class IsotropicPoint(Source):
+    """Isotropic point source above (z <= 0) or inside the sample
+    (xopto/mcml/mcsource/point.py:31-260)."""
+
+    def __init__(self, position=(0.0, 0.0, 0.0)):
+        if isinstance(position, IsotropicPoint):
+            position = position.position
+        self._position = np.zeros((3,))
+        self._position[:] = position
+
+    def _set_position(self, p):
+        self._position[:] = p
+
+    position = property(lambda self: self._position, _set_position)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """point.py:188-226: position and the index of the layer holding it."""
+        if self._position[2] >= mc.layers.thickness():
+            raise ValueError('The source must be located above or within the sample but not '
+                             'under the sample!')
+        target.kind = _abi.SRC_ISOTROPIC_POINT
+        target.position[:] = [float(v) for v in self._position]
+        target.layer_index = 1 if self._position[2] <= 0.0 else mc.layer_index(self._position[2])
+        return target
+
+    def todict(self):
+        return {'type': 'IsotropicPoint', 'position': self._position.tolist()}
+
+    def __str__(self):
+        return 'IsotropicPoint(position=({}, {}, {}))'.format(*self._position)
+
+    __repr__ = __str__

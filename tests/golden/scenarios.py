@@ -160,6 +160,36 @@ SCENARIOS = {
                     direction=(-0.2, 0.25, 1.0)),
         detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]), specular=dict(type='Total')),
         nphotons=3000, streams=32, rnginit=31),
+    # UniformBeam (xopto/mcml/mcsource/uniformbeam.py), oblique, elliptical
+    'beam_uniform_oblique': dict(
+        medium='mcml',
+        layers=[_air(['Gk', 0.0, 0.5]),
+                dict(d=1.5e-3, n=1.4, mua=120.0, mus=1.5e4, pf=['Gk', 0.85, 0.5]),
+                dict(d=INF, n=1.33, mua=30.0, mus=1e4, pf=['Gk', 0.8, 0.5])],
+        source=dict(type='UniformBeam', diameter=(1e-3, 5e-4), position=(2e-4, 0.0, -1e-3),
+                    direction=(0.2, -0.1, 1.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=37),
+    # IsotropicPoint (xopto/mcml/mcsource/point.py) inside the second layer
+    # and above the sample
+    'point_inside': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=5e-4, n=1.45, mua=80.0, mus=1e4, pf=['Hg', 0.8]),
+                dict(d=3e-3, n=1.37, mua=40.0, mus=8e3, pf=['Hg', 0.9]),
+                _air(['Hg', 0.0])],
+        source=dict(type='IsotropicPoint', position=(1e-4, 2e-4, 1.2e-3)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), bottom=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=41),
+    'point_above': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=2e-3, n=1.4, mua=80.0, mus=1e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='IsotropicPoint', position=(0.0, 0.0, -5e-4)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=43),
     # optical path-length resolved detectors (xopto/mcml/mcdetector/radialpl.py,
     # totalpl.py): two layers, RadialPl on top (linear path-length axis),
     # TotalPl below (log path-length axis)
