@@ -224,7 +224,7 @@ def render(name, nphotons=None):
         offsets['fluence'] = (a.offset, a.size)
     for k, (o, n) in offsets.items():
         blobs['off_' + k] = np.array([o, n])
-    np.savez(os.path.join(REF_DIR, name + '.npz'), **blobs)
+    np.savez_compressed(os.path.join(REF_DIR, name + '.npz'), **blobs)
     return compile_ref(name)
 
 
