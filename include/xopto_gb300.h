@@ -250,7 +250,10 @@ typedef struct McgbRunOptions {
     uint64_t max_steps_per_packet;          /* 0 = unlimited (2^32 - 1 at most) */
     double deadline_s;                      /* device wall-clock limit, 0=300s */
     int32_t scheduling;                     /* MCGB_SCHED_*                    */
-    uint32_t reserved;
+    uint32_t packets_per_item;              /* DYNAMIC: packets a warp takes
+                                               from the queue at a time, 1-128
+                                               (0 = chosen from the packet
+                                               count and the grid)             */
     uint64_t seed;                          /* DYNAMIC: stream derivation seed */
     uint64_t packet_offset;                 /* DYNAMIC: index of packet 0      */
 } McgbRunOptions;

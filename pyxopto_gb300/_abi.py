@@ -77,7 +77,8 @@ class McgbRunOptions(C.Structure):
                 ('packet_weight_min', f32), ('lottery_chance', f32), ('rmax', f32),
                 ('track_optical_pathlength', i32), ('block_size', u32),
                 ('max_steps_per_packet', u64), ('deadline_s', C.c_double),
-                ('scheduling', i32), ('reserved', u32), ('seed', u64), ('packet_offset', u64)]
+                ('scheduling', i32), ('packets_per_item', u32), ('seed', u64),
+                ('packet_offset', u64)]
 
 
 class McgbMcmlConfig(C.Structure):
@@ -147,6 +148,7 @@ def default_options():
     o.max_steps_per_packet = 0
     o.deadline_s = 0.0
     o.scheduling = SCHED_STATIC
+    o.packets_per_item = 0
     o.seed = 0
     o.packet_offset = 0
     return o

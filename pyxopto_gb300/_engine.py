@@ -132,6 +132,18 @@ class McEngine:
     max_steps_per_packet = property(lambda self: self._max_steps, _set_max_steps, None,
                                     'Terminate a packet after this many steps (0 = no limit).')
 
+    def _set_packets_per_item(self, n):
+        n = int(n or 0)
+        if not 0 <= n <= 128:
+            raise ValueError('packets_per_item must be in [0, 128]')
+        self._packets_per_item = n
+
+    packets_per_item = property(lambda self: getattr(self, '_packets_per_item', 0),
+                                _set_packets_per_item, None,
+                                'Dynamic scheduling: packets a warp takes from the work queue at '
+                                'a time (0 = chosen from the packet count and the grid).  The '
+                                'tallies do not depend on it.')
+
     def shard(self, rank: int, world: int):
         """Use slice ``rank`` of a stream table ``world`` times larger than
         one run needs: replicas on different GPUs then simulate disjoint
@@ -168,6 +180,7 @@ class McEngine:
             rank, world = self._shard
             o.seed = (int(self._rnginit) + 0x9E3779B97F4A7C15 * rank) & 0xFFFFFFFFFFFFFFFF
             o.packet_offset = self._packets_total
+            o.packets_per_item = self.packets_per_item
         else:
             o.scheduling = _abi.SCHED_STATIC
         return o

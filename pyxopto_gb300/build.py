@@ -21,8 +21,10 @@ NVCC_COMMON = ARCH + ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC',
 
 # (source, extra flags); exact-math units must not contract a*b+c into FMA.
 UNITS = [
-    ('transport_exact.cu', ['-fmad=false']),
-    ('transport_fast.cu', ['-use_fast_math']),
+    ('transport_exact_mcml.cu', ['-fmad=false']),
+    ('transport_exact_mcvox.cu', ['-fmad=false']),
+    ('transport_fast_mcml.cu', ['-use_fast_math']),
+    ('transport_fast_mcvox.cu', ['-use_fast_math']),
     ('capi.cu', []),
     ('batched.cu', ['-use_fast_math']),
     ('batched_exact.cu', ['-fmad=false']),

@@ -61,6 +61,8 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (num_streams > (1u << 24)) return fail(MCGB_E_SIZE, "num_streams %u exceeds 2^24", num_streams);
     if (o.scheduling != MCGB_SCHED_STATIC && o.scheduling != MCGB_SCHED_DYNAMIC)
         return fail(MCGB_E_INVALID, "unknown scheduling %d", o.scheduling);
+    if (o.packets_per_item > 128)
+        return fail(MCGB_E_INVALID, "packets per item %u outside [0, 128]", o.packets_per_item);
     if (!b->rng_a) return fail(MCGB_E_INVALID, "RNG multiplier buffer is NULL");
     if (o.scheduling == MCGB_SCHED_STATIC && !b->rng_x)
         return fail(MCGB_E_INVALID, "RNG state buffer is NULL");
@@ -221,8 +223,13 @@ int mcgb_suggest_streams(int medium, int math, uint32_t block_size, uint32_t *st
     if (r) return r;
     int bps = 0;
     unsigned block = block_size ? block_size : 128;
-    cudaError_t e = (math == MCGB_MATH_FAST) ? mcgb_fast::occupancy(medium, (int)block, 0, &bps)
-                                             : mcgb_exact::occupancy(medium, (int)block, 0, &bps);
+    cudaError_t e;
+    if (math == MCGB_MATH_FAST)
+        e = medium == 0 ? mcgb_fast::occupancy_mcml((int)block, 0, &bps)
+                        : mcgb_fast::occupancy_mcvox((int)block, 0, &bps);
+    else
+        e = medium == 0 ? mcgb_exact::occupancy_mcml((int)block, 0, &bps)
+                        : mcgb_exact::occupancy_mcvox((int)block, 0, &bps);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     *streams = (uint32_t)sms * (uint32_t)bps * block;
     return MCGB_OK;

@@ -1,5 +1,5 @@
-/* launch.h - launch shape passed from the C ABI layer to the per-math-mode
- * kernel translation units. */
+/* launch.h - launch shape passed from the C ABI layer to the kernel
+ * translation units (one per medium and math mode). */
 #pragma once
 #include <cstdint>
 #include <cstddef>
@@ -20,7 +20,8 @@ struct LaunchShape {
                             const LaunchShape &);                                            \
     cudaError_t launch_mcvox(const McgbMcvoxConfig &, const McgbBuffers &, cudaStream_t,     \
                              const LaunchShape &);                                           \
-    cudaError_t occupancy(int medium, int block, size_t dyn_smem, int *blocks_per_sm);       \
+    cudaError_t occupancy_mcml(int block, size_t dyn_smem, int *blocks_per_sm);              \
+    cudaError_t occupancy_mcvox(int block, size_t dyn_smem, int *blocks_per_sm);             \
     }
 MCGB_DECLARE_LAUNCHERS(mcgb_exact)
 MCGB_DECLARE_LAUNCHERS(mcgb_fast)

@@ -3,11 +3,13 @@
  * voxelized (mcvox) transport kernels: random numbers, boundary optics,
  * direction sampling, phase functions and integer tallies.
  *
- * Included by exactly one translation unit per math mode:
- *   transport_exact.cu  MCGB_FAST_MATH == 0, compiled with -fmad=false:
+ * Included by the translation units of each math mode:
+ *   transport_exact_*.cu, batched_exact.cu
+ *                       MCGB_FAST_MATH == 0, compiled with -fmad=false:
  *                       IEEE +,-,*,/,sqrt and the portable log/exp/sincos/powr
  *                       routines, bit-identical to a CPU evaluation.
- *   transport_fast.cu   MCGB_FAST_MATH == 1, compiled with -use_fast_math:
+ *   transport_fast_*.cu, batched.cu
+ *                       MCGB_FAST_MATH == 1, compiled with -use_fast_math:
  *                       special-function-unit log2/sin/cos/ex2, approximate
  *                       division and square root (the reference's
  *                       MC_USE_NATIVE_MATH, xopto/mcbase/kernel/mcbase.template.h:522-556).

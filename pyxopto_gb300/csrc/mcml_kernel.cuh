@@ -104,22 +104,14 @@ static __device__ __forceinline__ void mcml_launch_fiber(const McgbMcmlConfig &c
     w = 1.0f - R;
 }
 
-/* Line / GaussianBeam / fibre launch (xopto/mcml/mcsource/line.py:95-108,
-   gaussianbeam.py:119-170, fiberni.py, fiber.py). */
-static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
-                                                   Rng &rng, f3 &pos, f3 &dir, float &w,
-                                                   int &layer, uint64_t *accu) {
+/* GaussianBeam / UniformBeam / IsotropicPoint / fibre launch
+   (xopto/mcml/mcsource/gaussianbeam.py:119-170, uniformbeam.py:107-146,
+   point.py:76-128, fiberni.py, fiber.py). */
+static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c, const MlLayer *L,
+                                                         Rng &rng, f3 &pos, f3 &dir, float &w,
+                                                         int &layer, uint64_t *accu) {
     const McgbSource &src = c.source;
-    if (src.kind == MCGB_SRC_LINE) {
-        w = 1.0f - src.reflectance;
-        pos = f3{src.position[0], src.position[1], src.position[2]};
-        dir = f3{src.direction[0], src.direction[1], src.direction[2]};
-        if (c.specular.kind != MCGB_DET_NONE) {
-            f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
-            detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
-        }
-        layer = 1;
-    } else if (src.kind == MCGB_SRC_UNIFORM_BEAM) {
+    if (src.kind == MCGB_SRC_UNIFORM_BEAM) {
         /* xopto/mcml/mcsource/uniformbeam.py:107-146 */
         float rand_sqrt = mc_sqrt(rng.next());
         float fi = 6.28318548f * rng.next();
@@ -197,6 +189,27 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
             f3 d = refract3(dir_in, normal, L[1].g1.x, L[0].g1.x);
             detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
+    }
+}
+
+/* Packet launch: Line (xopto/mcml/mcsource/line.py:95-108) or any other
+   source (mcml_launch_other).  Everything stays inline: an out-of-line call
+   measured slower on the layered workloads. */
+static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
+                                                   Rng &rng, f3 &pos, f3 &dir, float &w,
+                                                   int &layer, uint64_t *accu) {
+    const McgbSource &src = c.source;
+    if (src.kind == MCGB_SRC_LINE) {
+        w = 1.0f - src.reflectance;
+        pos = f3{src.position[0], src.position[1], src.position[2]};
+        dir = f3{src.direction[0], src.direction[1], src.direction[2]};
+        if (c.specular.kind != MCGB_DET_NONE) {
+            f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
+            detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
+        }
+        layer = 1;
+    } else {
+        mcml_launch_other(c, L, rng, pos, dir, w, layer, accu);
     }
 }
 
@@ -303,7 +316,7 @@ static __device__ __forceinline__ void mcml_end(const McgbMcmlConfig &c, const M
 /* One interaction step of a packet (the body of McKernel's while(!done)
    loop, xopto/mcml/kernel/mcml.template.c:525-814).  Returns true when the
    packet terminated. */
-template <int PF, int METHOD, bool FLU>
+template <int PF, int METHOD, bool FLU, bool XTRA>
 static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const McgbBuffers &b,
                                                  const MlCtx &x, MlPacket &s, Rng &rng,
                                                  FluenceCache &fcache, uint32_t &status) {
@@ -331,7 +344,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
     s.pos.x = s.pos.x + s.dir.x * step;
     s.pos.y = s.pos.y + s.dir.y * step;
     s.pos.z = s.pos.z + s.dir.z * step;
-    if (x.track_opl) s.opl += L[s.layer].g1.x * step;
+    if (XTRA && x.track_opl) s.opl += L[s.layer].g1.x * step;
     if (s.layer < next) s.pos.z = g0.y;
     if (s.layer > next) s.pos.z = g0.x;
 
@@ -342,7 +355,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         float fraction = 1.0f - mc_exp(-mua * step);
         float deposit = fraction * s.w;
         s.w -= deposit;
-        s.events |= MCGB_EV_ABSORPTION;
+        if (XTRA) s.events |= MCGB_EV_ABSORPTION;
         if (FLU) {
             float step_back = (mua != 0.0f)
                                   ? step - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
@@ -352,7 +365,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             fluence_deposit(c.fluence, dp, deposit, mua, fcache);
         }
         if (next != s.layer) {
-            s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
+            { uint32_t ev = mcml_boundary(L, s.layer, next, s.dir, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
             if (!(s.layer > 0 && s.layer < x.last_layer)) {
                 if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
                 else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
@@ -362,7 +375,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             const MlLayer &cl = L[s.layer];
             float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
             scatter_direction(s.dir, ct, az);
-            s.events |= MCGB_EV_SCATTERING;
+            if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
         if (s.w < o.packet_weight_min) {
             if (o.use_lottery) {
@@ -373,7 +386,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             }
         }
     } else if (next != s.layer) {
-        s.events |= mcml_boundary(L, s.layer, next, s.dir, rng) | MCGB_EV_BOUNDARY_HIT;
+        { uint32_t ev = mcml_boundary(L, s.layer, next, s.dir, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
         if (!(s.layer > 0 && s.layer < x.last_layer)) {
             if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
             else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
@@ -385,24 +398,24 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             float deposit = s.w;
             done = true;
             s.w -= deposit;
-            s.events |= MCGB_EV_ABSORPTION;
+            if (XTRA) s.events |= MCGB_EV_ABSORPTION;
             if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         } else {
             const MlLayer &cl = L[s.layer];
             float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
             scatter_direction(s.dir, ct, az);
-            s.events |= MCGB_EV_SCATTERING;
+            if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
     } else {
         /* albedo weight, mcml.template.c:722-753 */
         float deposit = s.w * g0.w;
         s.w -= deposit;
-        s.events |= MCGB_EV_ABSORPTION;
+        if (XTRA) s.events |= MCGB_EV_ABSORPTION;
         if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         const MlLayer &cl = L[s.layer];
         float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
         scatter_direction(s.dir, ct, az);
-        s.events |= MCGB_EV_SCATTERING;
+        if (XTRA) s.events |= MCGB_EV_SCATTERING;
         if (s.w < o.packet_weight_min) {
             if (o.use_lottery) {
                 if (rng.next() > o.lottery_chance) done = true;
@@ -417,16 +430,16 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         f3 d{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
         if (dot3(d, d) > x.rmax2) {
             done = true;
-            s.events |= MCGB_EV_ESCAPED;
+            if (XTRA) s.events |= MCGB_EV_ESCAPED;
         }
     }
-    if (x.use_trace) {
+    if (XTRA && x.use_trace) {
         if (done) s.events |= MCGB_EV_TERMINATED;
         if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
             trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
         s.events = 0;
     }
-    if (!done && s.steps >= x.max_steps) {
+    if (XTRA && !done && s.steps >= x.max_steps) {
         done = true;
         status |= MCGB_STATUS_STEP_LIMIT;
     }
@@ -464,7 +477,7 @@ static __device__ __forceinline__ void mc_finish(const McgbBuffers &b, uint64_t 
 template <int PF, int METHOD, bool FLU>
 __global__ void __launch_bounds__(256)
 mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
-                      uint64_t deadline_ns, int lut_in_smem) {
+                      uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MlSmem sm;
     extern __shared__ float s_lut[];
     const float *lut = mcml_stage<PF>(c, b, sm, s_lut, lut_in_smem);
@@ -480,7 +493,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
     MlPacket s;
     mcml_begin(c, b, x, s, rng, t);
     for (;;) {
-        if (mcml_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
+        if (mcml_step<PF, METHOD, FLU, true>(c, b, x, s, rng, fcache, status)) {
             ++packets;
             steps += s.steps;
             mcml_end(c, b, x, s);
@@ -507,10 +520,10 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
 /* DYNAMIC scheduling: persistent warps refill idle lanes packet by packet
    from the queue counters[MCGB_CNT_QUEUE]; packet p runs on the stream of
    (seed, packet_offset + p). */
-template <int PF, int METHOD, bool FLU>
+template <int PF, int METHOD, bool FLU, bool XTRA>
 __global__ void __launch_bounds__(256)
 mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
-                    uint64_t deadline_ns, int lut_in_smem) {
+                    uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MlSmem sm;
     extern __shared__ float s_lut[];
     const float *lut = mcml_stage<PF>(c, b, sm, s_lut, lut_in_smem);
@@ -518,7 +531,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
     const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
     const MlCtx x = mcml_ctx(c, sm.layers, lut);
     const uint64_t N = c.num_packets;
-    const uint64_t B = 128;
+    const uint64_t B = packets_per_item;
     unsigned long long *queue = (unsigned long long *)(b.counters + MCGB_CNT_QUEUE);
     uint64_t item_next = 0, item_end = 0;   /* warp-uniform */
     bool more = true, active = false;
@@ -559,7 +572,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
             need &= ~taken;
         }
         if (!__any_sync(MCGB_FULL_MASK, active)) break;
-        if (active && mcml_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
+        if (active && mcml_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
             ++packets;
             steps += s.steps;
             s.steps = 0;

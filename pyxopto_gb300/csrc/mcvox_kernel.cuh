@@ -239,7 +239,7 @@ static __device__ __forceinline__ void mcvox_end(const McgbMcvoxConfig &c, const
 }
 
 /* One step of McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:760-1038. */
-template <int PF, int METHOD, bool FLU>
+template <int PF, int METHOD, bool FLU, bool XTRA>
 static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
                                                   FluenceCache &fcache, uint32_t &status) {
@@ -266,7 +266,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     s.pos.x = s.pos.x + d_ok * s.dir.x;
     s.pos.y = s.pos.y + d_ok * s.dir.y;
     s.pos.z = s.pos.z + d_ok * s.dir.z;
-    if (x.track_opl) s.opl += M[s.mat].g1.x * d_ok;
+    if (XTRA && x.track_opl) s.opl += M[s.mat].g1.x * d_ok;
 
     bool done = false;
     if (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
@@ -274,7 +274,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         float fraction = 1.0f - mc_exp(-mua * d_ok);
         float deposit = fraction * s.w;
         s.w -= deposit;
-        s.events |= MCGB_EV_ABSORPTION;
+        if (XTRA) s.events |= MCGB_EV_ABSORPTION;
         if (FLU) {
             float step_back = (mua != 0.0f)
                                   ? d_ok - mc_div(-mc_log(1.0f - rng.next() * fraction), mua)
@@ -294,7 +294,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             const MvMaterial &cm = M[s.mat];
             float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
             scatter_direction(s.dir, ct, az);
-            s.events |= MCGB_EV_SCATTERING;
+            if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
         if (s.w < o.packet_weight_min) {
             if (o.use_lottery) {
@@ -315,24 +315,24 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         if (rng.next() < g0.w) {
             float deposit = s.w;
             s.w -= deposit;
-            s.events |= MCGB_EV_ABSORPTION;
+            if (XTRA) s.events |= MCGB_EV_ABSORPTION;
             done = true;
             if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
         } else {
             const MvMaterial &cm = M[s.mat];
             float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
             scatter_direction(s.dir, ct, az);
-            s.events |= MCGB_EV_SCATTERING;
+            if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
     } else {
         float deposit = s.w * g0.w;
         s.w -= deposit;
-        s.events |= MCGB_EV_ABSORPTION;
+        if (XTRA) s.events |= MCGB_EV_ABSORPTION;
         if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
         const MvMaterial &cm = M[s.mat];
         float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
         scatter_direction(s.dir, ct, az);
-        s.events |= MCGB_EV_SCATTERING;
+        if (XTRA) s.events |= MCGB_EV_SCATTERING;
         if (s.w < o.packet_weight_min) {
             if (o.use_lottery) {
                 if (rng.next() > o.lottery_chance) done = true;
@@ -350,15 +350,15 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     }
     if (escaped) {
         done = true;
-        s.events |= MCGB_EV_ESCAPED;
+        if (XTRA) s.events |= MCGB_EV_ESCAPED;
     }
-    if (x.use_trace) {
+    if (XTRA && x.use_trace) {
         if (done) s.events |= MCGB_EV_TERMINATED;
         if (c.trace.flags == MCGB_TRACE_ALL || ((c.trace.flags & MCGB_TRACE_END) && done))
             trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
         s.events = 0;
     }
-    if (!done && s.steps >= x.max_steps) {
+    if (XTRA && !done && s.steps >= x.max_steps) {
         done = true;
         status |= MCGB_STATUS_STEP_LIMIT;
     }
@@ -394,7 +394,7 @@ static __device__ __forceinline__ void mv_finish(const McgbBuffers &b, uint64_t 
 template <int PF, int METHOD, bool FLU>
 __global__ void __launch_bounds__(256)
 mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
-                       uint64_t deadline_ns, int lut_in_smem) {
+                       uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MvSmem sm;
     extern __shared__ float s_lut[];
     const float *lut = mcvox_stage<PF>(c, b, sm, s_lut, lut_in_smem);
@@ -410,7 +410,7 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
     MvPacket s;
     mcvox_begin(c, b, x, s, rng, t);
     for (;;) {
-        if (mcvox_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
+        if (mcvox_step<PF, METHOD, FLU, true>(c, b, x, s, rng, fcache, status)) {
             ++packets;
             steps += s.steps;
             mcvox_end(c, b, x, s);
@@ -433,10 +433,10 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
 }
 
 /* DYNAMIC scheduling (per-packet streams, warp refill). */
-template <int PF, int METHOD, bool FLU>
+template <int PF, int METHOD, bool FLU, bool XTRA>
 __global__ void __launch_bounds__(256)
 mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
-                     uint64_t deadline_ns, int lut_in_smem) {
+                     uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MvSmem sm;
     extern __shared__ float s_lut[];
     const float *lut = mcvox_stage<PF>(c, b, sm, s_lut, lut_in_smem);
@@ -444,7 +444,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
     const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
     const MvCtx x = mcvox_ctx(c, b, sm.materials, lut);
     const uint64_t N = c.num_packets;
-    const uint64_t B = 128;
+    const uint64_t B = packets_per_item;
     unsigned long long *queue = (unsigned long long *)(b.counters + MCGB_CNT_QUEUE);
     uint64_t item_next = 0, item_end = 0;
     bool more = true, active = false;
@@ -485,7 +485,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
             need &= ~taken;
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && mcvox_step<PF, METHOD, FLU>(c, b, x, s, rng, fcache, status)) {
+        if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
             ++packets;
             steps += s.steps;
             s.steps = 0;

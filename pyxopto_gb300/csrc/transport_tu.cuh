@@ -1,0 +1,129 @@
+/*
+ * transport_tu.cuh - kernel table and launcher of one medium in one math
+ * mode.  Included by the four translation units transport_{exact,fast}_
+ * {mcml,mcvox}.cu, which define MCGB_FAST_MATH, MCGB_NS and MCGB_MEDIUM
+ * (0 layered, 1 voxelized), so that the kernel variants compile in parallel.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <mutex>
+#include "launch.h"
+#if MCGB_MEDIUM == 0
+#include "mcml_kernel.cuh"
+#define MCGB_STATIC_KERNEL mcml_transport_kernel
+#define MCGB_DYNAMIC_KERNEL mcml_dynamic_kernel
+#define MCGB_CFG McgbMcmlConfig
+#define MCGB_LAUNCH launch_mcml
+#define MCGB_OCCUPANCY occupancy_mcml
+#else
+#include "mcvox_kernel.cuh"
+#define MCGB_STATIC_KERNEL mcvox_transport_kernel
+#define MCGB_DYNAMIC_KERNEL mcvox_dynamic_kernel
+#define MCGB_CFG McgbMcvoxConfig
+#define MCGB_LAUNCH launch_mcvox
+#define MCGB_OCCUPANCY occupancy_mcvox
+#endif
+
+namespace MCGB_NS {
+
+/* Kernel variants: scheduling x phase function x method x fluence x
+   optional features (trace, optical path length, per-packet step limit).
+   The static kernels always carry the optional features. */
+#define MCGB_VS(K, PF, M, F) {(const void *)K<PF, M, F>, (const void *)K<PF, M, F>}
+#define MCGB_VD(K, PF, M, F) {(const void *)K<PF, M, F, false>, (const void *)K<PF, M, F, true>}
+#define MCGB_F(V, K, PF, M) {V(K, PF, M, false), V(K, PF, M, true)}
+#define MCGB_METHODS(V, K, PF) {MCGB_F(V, K, PF, 0), MCGB_F(V, K, PF, 1), MCGB_F(V, K, PF, 2)}
+#define MCGB_TABLE(V, K) {MCGB_METHODS(V, K, 0), MCGB_METHODS(V, K, 1), MCGB_METHODS(V, K, 2)}
+
+static const void *const kTable[2][3][3][2][2] = {MCGB_TABLE(MCGB_VS, MCGB_STATIC_KERNEL),
+                                                  MCGB_TABLE(MCGB_VD, MCGB_DYNAMIC_KERNEL)};
+
+static const void *select(int sched, int pf, int method, bool fluence, bool xtra) {
+    if (pf < 0 || pf > 2 || method < 0 || method > 2 || sched < 0 || sched > 1) return nullptr;
+    return kTable[sched][pf][method][fluence ? 1 : 0][xtra ? 1 : 0];
+}
+
+/* Resident blocks per SM of a kernel variant for a block size, queried once
+   per (device, variant, block size) and remembered. */
+static cudaError_t resident_blocks(const void *k, int block, size_t dyn_smem, int *bps) {
+    struct Entry { int dev; const void *k; int block; size_t smem; int bps; };
+    static std::mutex lock;
+    static Entry cache[64];
+    static int used = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> g(lock);
+        for (int i = 0; i < used; ++i)
+            if (cache[i].dev == dev && cache[i].k == k && cache[i].block == block &&
+                cache[i].smem == dyn_smem) {
+                *bps = cache[i].bps;
+                return cudaSuccess;
+            }
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, block, dyn_smem);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(lock);
+    if (used < 64) cache[used++] = Entry{dev, k, block, dyn_smem, *bps};
+    return cudaSuccess;
+}
+
+cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_t stream,
+                        const LaunchShape &shape) {
+    const int sched = cfg.opt.scheduling;
+    const bool xtra = cfg.trace.flags != MCGB_TRACE_NONE || cfg.opt.track_optical_pathlength != 0 ||
+                      cfg.opt.max_steps_per_packet != 0;
+    const void *k = select(sched, cfg.pf_kind, cfg.opt.method, cfg.fluence.kind != MCGB_FLUENCE_NONE,
+                           xtra);
+    if (!k) return cudaErrorInvalidValue;
+    if (shape.dyn_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)shape.dyn_smem);
+        if (e != cudaSuccess) return e;
+    }
+    unsigned grid = shape.grid;
+    if (sched == MCGB_SCHED_DYNAMIC) {
+        /* persistent: as many blocks as stay resident */
+        int dev = 0, sms = 0, bps = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = resident_blocks(k, (int)shape.block, shape.dyn_smem, &bps);
+        if (e != cudaSuccess) return e;
+        if (bps < 1) return cudaErrorInvalidConfiguration;
+        grid = (unsigned)(sms * bps);
+    }
+    /* dynamic scheduling: packets per queue item; by default at least 4
+       items per warp of the grid (so that short runs still spread over every
+       warp), at most 128 (one queue access per 128 packets in long runs) */
+    uint32_t items = cfg.opt.packets_per_item;
+    if (items == 0) {
+        uint64_t warps = (uint64_t)grid * (shape.block / 32u);
+        uint64_t b = cfg.num_packets / (warps * 4u);
+        items = (uint32_t)(b < 1 ? 1 : (b > 128 ? 128 : b));
+    }
+    McgbBuffers b = buf;
+    uint64_t deadline = shape.deadline_ns;
+    int lut = shape.lut_in_smem;
+    void *args[] = {(void *)&cfg, (void *)&b, (void *)&deadline, (void *)&lut, (void *)&items};
+    return cudaLaunchKernel(k, dim3(grid), dim3(shape.block), args, shape.dyn_smem, stream);
+}
+
+cudaError_t MCGB_OCCUPANCY(int block, size_t dyn_smem, int *blocks_per_sm) {
+    /* the smallest residency over the static variants of the medium, so that
+       one wave of the suggested stream count fits whichever variant runs */
+    int best = 1 << 30;
+    for (int pf = 0; pf < 3; ++pf)
+        for (int m = 0; m < 3; ++m)
+            for (int fl = 0; fl < 2; ++fl) {
+                int n = 0;
+                cudaError_t e = resident_blocks(select(MCGB_SCHED_STATIC, pf, m, fl != 0, true), block,
+                                                dyn_smem, &n);
+                if (e != cudaSuccess) return e;
+                best = n < best ? n : best;
+            }
+    *blocks_per_sm = best;
+    return cudaSuccess;
+}
+
+}  // namespace MCGB_NS

@@ -58,6 +58,22 @@ def test_dynamic_runs_continue_with_new_packets(cuda, lib, oracle):
     assert np.array_equal(a2[:r2['accu'].size], r2['accu'])
 
 
+@pytest.mark.parametrize('name', ['c1_line_hg_radial', 'c3_vox_cylinder'])
+def test_dynamic_tallies_independent_of_packets_per_item(cuda, lib, oracle, name):
+    """Dynamic scheduling: packet p runs on the stream of (seed, p) whatever
+    warp takes it, so the queue granularity cannot change the tallies."""
+    s = scenarios.SCENARIOS[name]
+    ref = None
+    for ppi in (0, 1, 7, 128):
+        mc = scenarios.build_mc(name, scheduling='dynamic')
+        mc.packets_per_item = ppi
+        accu, _, report = gpu_run(mc, s['nphotons'], None, cuda)
+        assert report['packets_done'] == s['nphotons']
+        if ref is None:
+            ref = accu
+        assert np.array_equal(accu, ref), ppi
+
+
 def test_exact_mode_many_streams_bit_identical(cuda, lib, oracle):
     """Full-occupancy launch (many blocks) on config 2's stack."""
     mc = scenarios.build_mc('c2_gk_fluence')
