@@ -45,12 +45,17 @@ for _p in (ROOT, os.path.join(ROOT, 'oracle'), os.path.join(ROOT, 'tests', 'gold
 # roofline figure.
 OPS_PER_STEP = 91
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) per launch of the transport kernel from ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum, one-pass capture of the full
-# workload, mean of two launches): the one-time fill of the tallies and
-# tables into L2; it does not grow with the packet count.
+# From ncu captures of the transport kernel (the summary file named beside
+# each entry): DRAM bytes (read + write) per launch, one-pass capture of the
+# full workload, mean of three launches -- the one-time fill of the tallies
+# and tables into L2, which does not grow with the packet count -- and the
+# fraction of issue slots in use (smsp__issue_active), the resource that
+# bounds this kernel.
 PROFILED_TRAFFIC = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (8.51e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (8.91e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+}
+PROFILED_ISSUE_ACTIVE = {
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.889, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
 }
 METRIC = 'packets/s (1 GB300)'
 
@@ -491,6 +496,8 @@ def main():
     roofline = {'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
                 'frac': achieved / fp32_peak, 'traffic': traffic[0] if traffic else None,
                 'traffic_source': traffic[1] if traffic else None,
+                'issue_active': (PROFILED_ISSUE_ACTIVE.get((args.workload, args.math, args.scheduling))
+                                 or (None,))[0],
                 'peak_source': 'derived: 152 SMs x 128 FP32 lanes x 2 x sm_max_mhz {} '
                                '(MEASURED_PEAKS.json); no FP32 peak is measured there'.format(sm_max),
                 'ops_per_step': OPS_PER_STEP, 'steps_per_launch': res['steps_per_launch'],
