@@ -106,7 +106,8 @@ enum {
     MCGB_SRC_UNIFORM_FIBER = 4,
     MCGB_SRC_LAMBERTIAN_FIBER = 5,
     MCGB_SRC_UNIFORM_BEAM = 6,
-    MCGB_SRC_ISOTROPIC_POINT = 7
+    MCGB_SRC_ISOTROPIC_POINT = 7,
+    MCGB_SRC_ISOTROPIC_VOXEL = 8
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
        MCGB_DET_TOTAL_PL = 4 };
@@ -182,7 +183,15 @@ typedef struct McgbMaterial {
      direction (refracted), sigma = radii along x and y, reflectance.
    IsotropicPoint mcml (xopto/mcml/mcsource/point.py:76-128,188-226):
      position (above the sample: z <= 0, or inside it) and layer_index of
-     the layer that holds it (1 for a point above the sample). */
+     the layer that holds it (1 for a point above the sample).
+   Voxelized media (xopto/mcvox/mcsource): UniformBeam (uniformbeam.py:
+     104-186) and the tilted fibres UniformFiber / LambertianFiber
+     (fiber.py:257-352,603-700) take transformation, position (anywhere;
+     moved onto the voxel box along the direction), direction (in the
+     surrounding medium), sigma (beam radii; fibre core radius and
+     sqrt(1 - NA^2) or NA) and clip (fibre core index); IsotropicPoint
+     (point.py:74-140) takes position; IsotropicVoxel (voxel.py:78-107) takes
+     the voxel index as floats in position. */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];

@@ -772,13 +772,75 @@ static int mv_box_intersect(const McgbMcvoxConfig *c, v3 pos, v3 dir, v3 *isec, 
     return tmax >= tmin && tmax >= 0.0f;
 }
 
-/* GaussianBeam.mcsim_launch (mcvox), xopto/mcvox/mcsource/gaussianbeam.py:112-190,
-   Line.mcsim_launch (mcvox), xopto/mcvox/mcsource/line.py, followed by
-   mcsim_set_voxel_index_from_position (mcvox.template.c:240-262). */
+/* mcsim_sample_box_contains, xopto/mcvox/kernel/mcvox.template.h:1227-1235 */
+static int mv_contains(const McgbMcvoxConfig *c, v3 p) {
+    return p.x >= c->top_left[0] && p.x < c->bottom_right[0] && p.y >= c->top_left[1] &&
+           p.y < c->bottom_right[1] && p.z >= c->top_left[2] && p.z < c->bottom_right[2];
+}
+
+/* refractive index of the voxel at a point on the box surface
+   (mcsim_position_to_voxel_index_safe + material lookup) */
+static float mv_n_at_surface(const McgbMcvoxConfig *c, const McgbMaterial *mats,
+                             const uint8_t *vox, v3 p) {
+    i3 vi = mv_index(c, p);
+    vi.x = clip_i(vi.x, 0, c->shape[0] - 1);
+    vi.y = clip_i(vi.y, 0, c->shape[1] - 1);
+    vi.z = clip_i(vi.z, 0, c->shape[2] - 1);
+    return mats[mv_material_at(c, vox, vi)].n;
+}
+
+/* The beam entry into the voxel box of GaussianBeam.mcsim_launch
+   (xopto/mcvox/mcsource/gaussianbeam.py:112-190) and UniformBeam.mcsim_launch
+   (xopto/mcvox/mcsource/uniformbeam.py:104-186), from the beam point pt_mc. */
+static void mv_beam_enter(int mm, const McgbMcvoxConfig *c, const McgbMaterial *mats,
+                          const uint8_t *vox, MvState *s, v3 pt_mc, uint64_t *accu) {
+    const McgbSource *src = &c->source;
+    float specular_r;
+    v3 direction = {src->direction[0], src->direction[1], src->direction[2]};
+    if (mv_contains(c, pt_mc)) {
+        direction.x = -direction.x; direction.y = -direction.y; direction.z = -direction.z;
+    }
+    v3 isec, normal;
+    if (mv_box_intersect(c, pt_mc, direction, &isec, &normal)) {
+        s->pos = isec;
+        direction.x = -direction.x; direction.y = -direction.y; direction.z = -direction.z;
+        normal.x = -normal.x; normal.y = -normal.y; normal.z = -normal.z;
+        float n_outside = mats[0].n;
+        float n_inside = mv_n_at_surface(c, mats, vox, s->pos);
+        v3 refracted = direction;
+        refract_safe3(direction, normal, n_outside, n_inside, &refracted);
+        s->dir = refracted;
+        specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
+                                 cos_critical(n_outside, n_inside));
+        if (c->specular.kind != MCGB_DET_NONE)
+            detector_deposit(mm, &c->specular, s->pos, direction, specular_r, 0.0f, accu);
+    } else {
+        s->pos.x = c->top_left[0]; s->pos.y = c->top_left[1]; s->pos.z = c->top_left[2];
+        s->dir.x = 0.0f; s->dir.y = 0.0f; s->dir.z = 1.0f;
+        specular_r = 1.0f;
+    }
+    s->w = 1.0f - specular_r;
+}
+
+static inline v3 transform3(const float *T, v3 p) {
+    /* mc_transform_fpv3, xopto/mcbase/kernel/mcbase.template.c:380-386 */
+    v3 r;
+    r.x = T[0] * p.x + T[1] * p.y + T[2] * p.z;
+    r.y = T[3] * p.x + T[4] * p.y + T[5] * p.z;
+    r.z = T[6] * p.x + T[7] * p.y + T[8] * p.z;
+    return r;
+}
+
+/* mcsim_launch of the voxelized-medium sources: Line (xopto/mcvox/mcsource/line.py),
+   GaussianBeam (gaussianbeam.py:112-190), UniformBeam (uniformbeam.py:104-186),
+   IsotropicPoint (point.py:74-140), UniformFiber and LambertianFiber
+   (fiber.py:257-352,603-700), IsotropicVoxel (voxel.py:78-107); then the voxel
+   of the launch position (xopto/mcvox/kernel/mcvox.template.c:240-262). */
 static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *mats,
                          const uint8_t *vox, MvState *s, uint64_t *x, uint32_t a,
-                         uint64_t *accu) {
+                         uint64_t *accu, v3 prev_pos) {
     const McgbSource *src = &c->source;
+    const float *T = src->transformation;
     if (src->kind == MCGB_SRC_LINE) {
         /* xopto/mcvox/mcsource/line.py: position and directions are
            precomputed on the host by Line.cl_pack */
@@ -790,55 +852,118 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
                     src->direction_reflected[2]};
             detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
         }
-    } else {
-        float specular_r = 0.0f;
-        float cos_fi, sin_fi, r;
+    } else if (src->kind == MCGB_SRC_GAUSSIAN_BEAM || src->kind == MCGB_SRC_UNIFORM_BEAM) {
+        float cos_fi, sin_fi;
         v3 pt_src, pt_mc;
-        r = sqrtf(-2.0f * m_log(mm, 1.0f - rnd(x, a)));
-        r = fminf(r, src->clip);
-        m_sincos(mm, 6.28318548f * rnd(x, a), &sin_fi, &cos_fi);
-        pt_src.x = r * cos_fi * src->sigma[0];
-        pt_src.y = r * sin_fi * src->sigma[1];
+        if (src->kind == MCGB_SRC_GAUSSIAN_BEAM) {
+            float r = sqrtf(-2.0f * m_log(mm, 1.0f - rnd(x, a)));
+            r = fminf(r, src->clip);
+            m_sincos(mm, 6.28318548f * rnd(x, a), &sin_fi, &cos_fi);
+            pt_src.x = r * cos_fi * src->sigma[0];
+            pt_src.y = r * sin_fi * src->sigma[1];
+        } else {
+            float rand_sqrt = sqrtf(rnd(x, a));
+            float fi = 6.28318548f * rnd(x, a);
+            m_sin_cos(mm, fi, &sin_fi, &cos_fi);
+            pt_src.x = rand_sqrt * cos_fi * src->sigma[0];
+            pt_src.y = rand_sqrt * sin_fi * src->sigma[1];
+        }
         pt_src.z = 0.0f;
-        const float *T = src->transformation;
-        pt_mc.x = T[0] * pt_src.x + T[1] * pt_src.y + T[2] * pt_src.z;
-        pt_mc.y = T[3] * pt_src.x + T[4] * pt_src.y + T[5] * pt_src.z;
-        pt_mc.z = T[6] * pt_src.x + T[7] * pt_src.y + T[8] * pt_src.z;
+        pt_mc = transform3(T, pt_src);
         pt_mc.x += src->position[0];
         pt_mc.y += src->position[1];
         pt_mc.z += src->position[2];
-        v3 direction = {src->direction[0], src->direction[1], src->direction[2]};
-        /* mcsim_sample_box_contains, xopto/mcvox/kernel/mcvox.template.h:1227-1235 */
-        if (pt_mc.x >= c->top_left[0] && pt_mc.x < c->bottom_right[0] &&
-            pt_mc.y >= c->top_left[1] && pt_mc.y < c->bottom_right[1] &&
-            pt_mc.z >= c->top_left[2] && pt_mc.z < c->bottom_right[2]) {
-            direction.x = -direction.x; direction.y = -direction.y; direction.z = -direction.z;
+        mv_beam_enter(mm, c, mats, vox, s, pt_mc, accu);
+    } else if (src->kind == MCGB_SRC_ISOTROPIC_POINT) {
+        /* Two quirks of the reference, restated: the refraction goes to a
+           shadowing local variable, so the direction stays unrefracted
+           (point.py:115-117); and mcsim_position_to_voxel_index reads the
+           simulator's current position, not its argument
+           (xopto/mcvox/kernel/mcvox.template.c:206-220), so the material
+           that sets n_inside is the one at the previous packet's final
+           position (prev_pos; the origin for a stream's first packet). */
+        float sin_fi, cos_fi, specular_r = 0.0f;
+        v3 pos = {src->position[0], src->position[1], src->position[2]};
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - 2.0f * rnd(x, a);
+        float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        v3 d = {cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        if (!mv_contains(c, pos)) {
+            v3 isec, normal;
+            if (mv_box_intersect(c, pos, d, &isec, &normal)) {
+                pos = isec;
+                float n_outside = mats[0].n;
+                float n_inside = mv_n_at_surface(c, mats, vox, prev_pos);
+                specular_r = reflectance(n_outside, n_inside, dot3(normal, d),
+                                         cos_critical(n_outside, n_inside));
+            } else {
+                pos.x = c->top_left[0]; pos.y = c->top_left[1]; pos.z = c->top_left[2];
+                specular_r = 1.0f;
+            }
         }
-        v3 isec, normal;
-        if (mv_box_intersect(c, pt_mc, direction, &isec, &normal)) {
-            s->pos = isec;
-            direction.x = -direction.x; direction.y = -direction.y; direction.z = -direction.z;
+        s->pos = pos;
+        s->dir = d;
+        if (c->specular.kind != MCGB_DET_NONE)
+            detector_deposit(mm, &c->specular, s->pos, d, specular_r, 0.0f, accu);
+        s->w = 1.0f - specular_r;
+    } else if (src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER) {
+        float sin_fi, cos_fi, sin_theta, cos_theta, specular_r;
+        float r = sqrtf(rnd(x, a)) * src->sigma[0];
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        v3 ps = {r * cos_fi, r * sin_fi, 0.0f};
+        v3 pm = transform3(T, ps);
+        pm.x += src->position[0];
+        pm.y += src->position[1];
+        pm.z += src->position[2];
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        if (src->kind == MCGB_SRC_LAMBERTIAN_FIBER) {
+            sin_theta = sqrtf(rnd(x, a)) * src->sigma[1];
+        } else {
+            cos_theta = 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
+            sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        }
+        sin_theta = sin_theta / src->clip;
+        cos_theta = sqrtf(1.0f - sin_theta * sin_theta);
+        v3 pt = {cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        v3 packet_dir = transform3(T, pt);
+        v3 source_dir = {src->direction[0], src->direction[1], src->direction[2]};
+        if (mv_contains(c, pm)) {
+            source_dir.x = -source_dir.x; source_dir.y = -source_dir.y; source_dir.z = -source_dir.z;
+        }
+        v3 refracted = packet_dir, isec, normal;
+        if (mv_box_intersect(c, pm, source_dir, &isec, &normal)) {
             normal.x = -normal.x; normal.y = -normal.y; normal.z = -normal.z;
-            float n_outside = mats[0].n;
-            i3 vi = mv_index(c, s->pos);
-            vi.x = clip_i(vi.x, 0, c->shape[0] - 1);
-            vi.y = clip_i(vi.y, 0, c->shape[1] - 1);
-            vi.z = clip_i(vi.z, 0, c->shape[2] - 1);
-            int32_t mi = mv_material_at(c, vox, vi);
-            float n_inside = mats[mi].n;
-            v3 refracted = direction;
-            refract_safe3(direction, normal, n_outside, n_inside, &refracted);
-            s->dir = refracted;
-            specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
+            s->pos = isec;
+            float n_outside = src->clip;
+            float n_inside = mv_n_at_surface(c, mats, vox, isec);
+            refract_safe3(packet_dir, normal, n_outside, n_inside, &refracted);
+            specular_r = reflectance(n_outside, n_inside, dot3(normal, packet_dir),
                                      cos_critical(n_outside, n_inside));
-            if (c->specular.kind != MCGB_DET_NONE)
-                detector_deposit(mm, &c->specular, s->pos, direction, specular_r, 0.0f, accu);
         } else {
             s->pos.x = c->top_left[0]; s->pos.y = c->top_left[1]; s->pos.z = c->top_left[2];
-            s->dir.x = 0.0f; s->dir.y = 0.0f; s->dir.z = 1.0f;
             specular_r = 1.0f;
         }
+        s->dir = refracted;
+        if (c->specular.kind != MCGB_DET_NONE)
+            detector_deposit(mm, &c->specular, s->pos, packet_dir, specular_r, 0.0f, accu);
         s->w = 1.0f - specular_r;
+    } else {
+        /* IsotropicVoxel */
+        const float one_minus_eps = 1.0f - 1.1920929e-07f;
+        s->pos.x = (src->position[0] + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[0] +
+                   c->top_left[0];
+        s->pos.y = (src->position[1] + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[1] +
+                   c->top_left[1];
+        s->pos.z = (src->position[2] + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[2] +
+                   c->top_left[2];
+        float sin_fi, cos_fi;
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - 2.0f * rnd(x, a);
+        float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        s->dir.x = cos_fi * sin_theta;
+        s->dir.y = sin_fi * sin_theta;
+        s->dir.z = cos_theta;
+        s->w = 1.0f;
     }
     s->vox = mv_index(c, s->pos);
     s->mat = mv_valid(c, s->vox) ? mv_material_at(c, vox, s->vox) : 0;
@@ -904,12 +1029,13 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
     v3 src_pos = {c->source.position[0], c->source.position[1], c->source.position[2]};
     float rmax2 = o->rmax * o->rmax;
     int use_trace = c->trace.flags != MCGB_TRACE_NONE;
+    v3 prev_pos = {0.0f, 0.0f, 0.0f};     /* the stream's state position before launch */
     for (uint64_t p = first; p < c->num_packets; p += stride) {
         MvState s;
         TraceState ts;
         memset(&s, 0, sizeof(s));
         ts.photon_index = p; ts.trace_count = 0; ts.events = 0;
-        mcvox_launch(mm, c, mats, vox, &s, &x, a, accu);
+        mcvox_launch(mm, c, mats, vox, &s, &x, a, accu, prev_pos);
         uint32_t events = EV_LAUNCH;
 #define MV_TRACE_SNAPSHOT() do { ts.pos = s.pos; ts.dir = s.dir; ts.w = s.w; ts.opl = s.opl; \
                                  ts.events = events; } while (0)
@@ -1032,6 +1158,7 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
         }
         if (use_trace)
             ibuf[c->trace.count_offset + p] = (int32_t)ts.trace_count;
+        prev_pos = s.pos;
 #undef MV_TRACE_SNAPSHOT
     }
     *rng_x = x;

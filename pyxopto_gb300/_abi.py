@@ -21,6 +21,7 @@ METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT =
 PF_HG, PF_GK, PF_LUT = 0, 1, 2
 SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI, SRC_LAMBERTIAN_FIBER_NI = 0, 1, 2, 3
 SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT = 4, 5, 6, 7
+SRC_ISOTROPIC_VOXEL = 8
 DET_NONE, DET_TOTAL, DET_RADIAL, DET_RADIAL_PL, DET_TOTAL_PL = 0, 1, 2, 3, 4
 FLUENCE_NONE, FLUENCE_DEPOSITION, FLUENCE_RATE = 0, 1, 2
 TRACE_NONE, TRACE_START, TRACE_END, TRACE_ALL = 0, 1, 2, 7

@@ -71,15 +71,13 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
     if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
-    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_ISOTROPIC_POINT)
+    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_ISOTROPIC_VOXEL)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
     if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI && src.kind <= MCGB_SRC_LAMBERTIAN_FIBER &&
         !(src.sigma[0] >= 0.0f && src.sigma[1] >= 0.0f && src.sigma[1] <= 1.0f && src.clip > 0.0f))
         return fail(MCGB_E_INVALID, "fiber source: core radius %g, angular parameter %g, core index %g",
                     (double)src.sigma[0], (double)src.sigma[1], (double)src.clip);
-    if ((src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
-         src.kind == MCGB_SRC_UNIFORM_BEAM) && !(src.direction[2] > 0.0f))
-        return fail(MCGB_E_INVALID, "source: the z component of the direction must be positive");
+
     if (!(o.lottery_chance > 0.0f && o.lottery_chance <= 1.0f))
         return fail(MCGB_E_INVALID, "lottery chance %g outside (0, 1]", (double)o.lottery_chance);
     if (!(o.packet_weight_min > 0.0f && o.packet_weight_min <= 1.0f))
@@ -243,6 +241,11 @@ int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *strea
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
+    if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL)
+        return fail(MCGB_E_UNSUPPORTED, "the voxel source is implemented for voxelized media only");
+    if ((cfg->source.kind == MCGB_SRC_UNIFORM_FIBER || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
+         cfg->source.kind == MCGB_SRC_UNIFORM_BEAM) && !(cfg->source.direction[2] > 0.0f))
+        return fail(MCGB_E_INVALID, "source: the z component of the direction must be positive");
     if (cfg->source.kind == MCGB_SRC_ISOTROPIC_POINT &&
         (cfg->source.layer_index < 1 || cfg->source.layer_index > (int32_t)cfg->num_layers - 2))
         return fail(MCGB_E_INVALID, "point source layer index %d outside the sample layers [1, %u]",
@@ -275,9 +278,16 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
-    if (cfg->source.kind >= MCGB_SRC_UNIFORM_FIBER_NI)
+    if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI)
         return fail(MCGB_E_UNSUPPORTED, "source kind %d is implemented for layered media only",
                     cfg->source.kind);
+    if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL) {
+        for (int k = 0; k < 3; ++k) {
+            float v = cfg->source.position[k];
+            if (!(v >= 0.0f && v < (float)cfg->shape[k] && v == (float)(int)v))
+                return fail(MCGB_E_INVALID, "voxel source index %g outside the grid", (double)v);
+        }
+    }
     if (!buf->voxels || !buf->materials) return fail(MCGB_E_INVALID, "voxel or material buffer is NULL");
     /* Voxel material indices are validated by the caller (uint8 < num_materials):
        the host wrapper checks the array before upload. */

@@ -76,14 +76,70 @@ static __device__ __forceinline__ int mv_box_intersect(const MvGeom &g, const f3
     return tmax >= tmin && tmax >= 0.0f;
 }
 
-/* Line launch (xopto/mcvox/mcsource/line.py) and GaussianBeam launch
-   (xopto/mcvox/mcsource/gaussianbeam.py:112-190), then the voxel index of
-   the launch position (mcvox.template.c:240-262). */
+/* mcsim_sample_box_contains, xopto/mcvox/kernel/mcvox.template.h:1227-1235 */
+static __device__ __forceinline__ bool mv_contains(const MvGeom &g, const f3 &p) {
+    return p.x >= g.tl[0] && p.x < g.br[0] && p.y >= g.tl[1] && p.y < g.br[1] && p.z >= g.tl[2] &&
+           p.z < g.br[2];
+}
+
+/* Refractive index of the voxel at a point on the box surface
+   (mcsim_position_to_voxel_index_safe + material lookup). */
+static __device__ __forceinline__ float mv_n_at_surface(const MvGeom &g, const MvMaterial *M,
+                                                        const uint8_t *vox, const f3 &p) {
+    i3 li = mv_index(g, p);
+    li.x = clip_i(li.x, 0, g.sh[0] - 1);
+    li.y = clip_i(li.y, 0, g.sh[1] - 1);
+    li.z = clip_i(li.z, 0, g.sh[2] - 1);
+    return M[mv_material_at(g, vox, li)].g1.x;
+}
+
+/* Entry of a collimated beam into the voxel box, shared by GaussianBeam
+   (xopto/mcvox/mcsource/gaussianbeam.py:112-190) and UniformBeam
+   (uniformbeam.py:104-186): from a point pm of the beam, move along the
+   beam direction (backwards if pm lies inside the box) to the box surface,
+   refract and weigh with the Fresnel reflectance; a beam that misses the
+   box starts at the top-left corner with zero weight. */
+static __device__ __forceinline__ void mv_beam_enter(const McgbMcvoxConfig &c, const MvGeom &g,
+                                                     const MvMaterial *M, const uint8_t *vox,
+                                                     f3 pm, f3 &pos, f3 &dir, float &w,
+                                                     uint64_t *accu) {
+    const McgbSource &src = c.source;
+    float specular_r;
+    f3 direction{src.direction[0], src.direction[1], src.direction[2]};
+    if (mv_contains(g, pm)) direction = f3{-direction.x, -direction.y, -direction.z};
+    f3 isec, normal;
+    if (mv_box_intersect(g, pm, direction, isec, normal)) {
+        pos = isec;
+        direction = f3{-direction.x, -direction.y, -direction.z};
+        normal = f3{-normal.x, -normal.y, -normal.z};
+        float n_outside = M[0].g1.x;
+        float n_inside = mv_n_at_surface(g, M, vox, pos);
+        f3 refracted = direction;
+        refract_safe3(direction, normal, n_outside, n_inside, &refracted);
+        dir = refracted;
+        specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
+                                 cos_critical(n_outside, n_inside));
+        if (c.specular.kind != MCGB_DET_NONE)
+            detector_deposit(c.specular, pos, direction, specular_r, 0.0f, accu);
+    } else {
+        pos = f3{g.tl[0], g.tl[1], g.tl[2]};
+        dir = f3{0.0f, 0.0f, 1.0f};
+        specular_r = 1.0f;
+    }
+    w = 1.0f - specular_r;
+}
+
+/* Packet launch of the voxelized medium: Line (xopto/mcvox/mcsource/line.py),
+   GaussianBeam (gaussianbeam.py:112-190), UniformBeam (uniformbeam.py:104-186),
+   IsotropicPoint (point.py:74-140), UniformFiber / LambertianFiber
+   (fiber.py:257-352,603-700) and IsotropicVoxel (voxel.py:78-107); then the
+   voxel index of the launch position (mcvox.template.c:240-262). */
 static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, const MvGeom &g,
                                                     const MvMaterial *M, const uint8_t *vox,
                                                     Rng &rng, f3 &pos, f3 &dir, float &w, i3 &vi,
-                                                    int &mat, uint64_t *accu) {
+                                                    int &mat, uint64_t *accu, f3 prev_pos) {
     const McgbSource &src = c.source;
+    const float *T = src.transformation;
     if (src.kind == MCGB_SRC_LINE) {
         w = 1.0f - src.reflectance;
         pos = f3{src.position[0], src.position[1], src.position[2]};
@@ -92,48 +148,118 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
             f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
             detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
-    } else {
-        float sin_fi, cos_fi, specular_r;
-        float r = mc_sqrt(-2.0f * mc_log(1.0f - rng.next()));
-        r = fminf(r, src.clip);
-        mc_sincos(6.28318548f * rng.next(), &sin_fi, &cos_fi);
-        f3 ps{r * cos_fi * src.sigma[0], r * sin_fi * src.sigma[1], 0.0f};
-        const float *T = src.transformation;
+    } else if (src.kind == MCGB_SRC_GAUSSIAN_BEAM || src.kind == MCGB_SRC_UNIFORM_BEAM) {
+        float sin_fi, cos_fi;
+        f3 ps;
+        if (src.kind == MCGB_SRC_GAUSSIAN_BEAM) {
+            float r = mc_sqrt(-2.0f * mc_log(1.0f - rng.next()));
+            r = fminf(r, src.clip);
+            mc_sincos(6.28318548f * rng.next(), &sin_fi, &cos_fi);
+            ps = f3{r * cos_fi * src.sigma[0], r * sin_fi * src.sigma[1], 0.0f};
+        } else {
+            float rand_sqrt = mc_sqrt(rng.next());
+            float fi = 6.28318548f * rng.next();
+            mc_sincos(fi, &sin_fi, &cos_fi);
+            ps = f3{rand_sqrt * cos_fi * src.sigma[0], rand_sqrt * sin_fi * src.sigma[1], 0.0f};
+        }
         f3 pm{T[0] * ps.x + T[1] * ps.y + T[2] * ps.z,
               T[3] * ps.x + T[4] * ps.y + T[5] * ps.z,
               T[6] * ps.x + T[7] * ps.y + T[8] * ps.z};
         pm.x += src.position[0];
         pm.y += src.position[1];
         pm.z += src.position[2];
-        f3 direction{src.direction[0], src.direction[1], src.direction[2]};
-        if (pm.x >= g.tl[0] && pm.x < g.br[0] && pm.y >= g.tl[1] && pm.y < g.br[1] &&
-            pm.z >= g.tl[2] && pm.z < g.br[2]) {
-            direction = f3{-direction.x, -direction.y, -direction.z};
+        mv_beam_enter(c, g, M, vox, pm, pos, dir, w, accu);
+    } else if (src.kind == MCGB_SRC_ISOTROPIC_POINT) {
+        /* Two quirks of the reference, restated: the refraction goes to a
+           shadowing local variable, so the direction stays unrefracted
+           (xopto/mcvox/mcsource/point.py:115-117); and the voxel lookup of
+           n_inside reads the simulator's current position instead of the
+           intersection (xopto/mcvox/kernel/mcvox.template.c:206-220), i.e.
+           the previous packet's final position on the same stream (prev_pos;
+           the origin for a stream's first packet and under dynamic
+           scheduling, where a packet has no predecessor). */
+        float sin_fi, cos_fi, specular_r = 0.0f;
+        pos = f3{src.position[0], src.position[1], src.position[2]};
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - 2.0f * rng.next();
+        float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        f3 d{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        if (!mv_contains(g, pos)) {
+            f3 isec, normal;
+            if (mv_box_intersect(g, pos, d, isec, normal)) {
+                pos = isec;
+                float n_outside = M[0].g1.x;
+                float n_inside = mv_n_at_surface(g, M, vox, prev_pos);
+                specular_r = reflectance(n_outside, n_inside, dot3(normal, d),
+                                         cos_critical(n_outside, n_inside));
+            } else {
+                pos = f3{g.tl[0], g.tl[1], g.tl[2]};
+                specular_r = 1.0f;
+            }
         }
+        dir = d;
+        if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, specular_r, 0.0f, accu);
+        w = 1.0f - specular_r;
+    } else if (src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER) {
+        float sin_fi, cos_fi, sin_theta, cos_theta, specular_r;
+        float r = mc_sqrt(rng.next()) * src.sigma[0];
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        f3 ps{r * cos_fi, r * sin_fi, 0.0f};
+        f3 pm{T[0] * ps.x + T[1] * ps.y + T[2] * ps.z,
+              T[3] * ps.x + T[4] * ps.y + T[5] * ps.z,
+              T[6] * ps.x + T[7] * ps.y + T[8] * ps.z};
+        pm.x += src.position[0];
+        pm.y += src.position[1];
+        pm.z += src.position[2];
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        if (src.kind == MCGB_SRC_LAMBERTIAN_FIBER) {
+            sin_theta = mc_sqrt(rng.next()) * src.sigma[1];
+        } else {
+            cos_theta = 1.0f - rng.next() * (1.0f - src.sigma[1]);
+            sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        }
+        sin_theta = mc_div(sin_theta, src.clip);
+        cos_theta = mc_sqrt(1.0f - sin_theta * sin_theta);
+        f3 pt{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        f3 packet_dir{T[0] * pt.x + T[1] * pt.y + T[2] * pt.z,
+                      T[3] * pt.x + T[4] * pt.y + T[5] * pt.z,
+                      T[6] * pt.x + T[7] * pt.y + T[8] * pt.z};
+        f3 source_dir{src.direction[0], src.direction[1], src.direction[2]};
+        if (mv_contains(g, pm)) source_dir = f3{-source_dir.x, -source_dir.y, -source_dir.z};
+        f3 refracted = packet_dir;
         f3 isec, normal;
-        if (mv_box_intersect(g, pm, direction, isec, normal)) {
-            pos = isec;
-            direction = f3{-direction.x, -direction.y, -direction.z};
+        if (mv_box_intersect(g, pm, source_dir, isec, normal)) {
             normal = f3{-normal.x, -normal.y, -normal.z};
-            float n_outside = M[0].g1.x;
-            i3 li = mv_index(g, pos);
-            li.x = clip_i(li.x, 0, g.sh[0] - 1);
-            li.y = clip_i(li.y, 0, g.sh[1] - 1);
-            li.z = clip_i(li.z, 0, g.sh[2] - 1);
-            float n_inside = M[mv_material_at(g, vox, li)].g1.x;
-            f3 refracted = direction;
-            refract_safe3(direction, normal, n_outside, n_inside, &refracted);
-            dir = refracted;
-            specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
+            pos = isec;
+            float n_outside = src.clip;
+            float n_inside = mv_n_at_surface(g, M, vox, isec);
+            refract_safe3(packet_dir, normal, n_outside, n_inside, &refracted);
+            specular_r = reflectance(n_outside, n_inside, dot3(normal, packet_dir),
                                      cos_critical(n_outside, n_inside));
-            if (c.specular.kind != MCGB_DET_NONE)
-                detector_deposit(c.specular, pos, direction, specular_r, 0.0f, accu);
         } else {
             pos = f3{g.tl[0], g.tl[1], g.tl[2]};
-            dir = f3{0.0f, 0.0f, 1.0f};
             specular_r = 1.0f;
         }
+        dir = refracted;
+        if (c.specular.kind != MCGB_DET_NONE)
+            detector_deposit(c.specular, pos, packet_dir, specular_r, 0.0f, accu);
         w = 1.0f - specular_r;
+    } else {
+        /* IsotropicVoxel: uniform in the voxel, isotropic direction */
+        const float one_minus_eps = 1.0f - 1.1920929e-07f;
+        float ux = fminf(rng.next(), one_minus_eps);
+        float px = (src.position[0] + ux) * g.vs[0] + g.tl[0];
+        float uy = fminf(rng.next(), one_minus_eps);
+        float py = (src.position[1] + uy) * g.vs[1] + g.tl[1];
+        float uz = fminf(rng.next(), one_minus_eps);
+        float pz = (src.position[2] + uz) * g.vs[2] + g.tl[2];
+        pos = f3{px, py, pz};
+        float sin_fi, cos_fi;
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        float cos_theta = 1.0f - 2.0f * rng.next();
+        float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        dir = f3{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        w = 1.0f;
     }
     vi = mv_index(g, pos);
     mat = mv_valid(g, vi) ? mv_material_at(g, vox, vi) : 0;
@@ -222,13 +348,14 @@ static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, cons
 }
 
 static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, const McgbBuffers &b,
-                                                   const MvCtx &x, MvPacket &s, Rng &rng, uint64_t p) {
+                                                   const MvCtx &x, MvPacket &s, Rng &rng, uint64_t p,
+                                                   f3 prev_pos) {
     s.p = p;
     s.opl = 0.0f;
     s.trace_count = 0;
     s.steps = 0;
     s.events = MCGB_EV_LAUNCH;
-    mcvox_launch(c, x.g, x.M, x.vox, rng, s.pos, s.dir, s.w, s.vi, s.mat, b.accumulator);
+    mcvox_launch(c, x.g, x.M, x.vox, rng, s.pos, s.dir, s.w, s.vi, s.mat, b.accumulator, prev_pos);
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -408,7 +535,8 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
     uint64_t steps = 0, packets = 0;
     uint32_t iter = 0, status = 0;
     MvPacket s;
-    mcvox_begin(c, b, x, s, rng, t);
+    s.pos = f3{0.0f, 0.0f, 0.0f};
+    mcvox_begin(c, b, x, s, rng, t, s.pos);
     for (;;) {
         if (mcvox_step<PF, METHOD, FLU, true>(c, b, x, s, rng, fcache, status)) {
             ++packets;
@@ -419,7 +547,7 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
                 s.steps = 0;
                 break;
             }
-            mcvox_begin(c, b, x, s, rng, p);
+            mcvox_begin(c, b, x, s, rng, p, s.pos);
         }
         if (((++iter) & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
@@ -477,7 +605,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                 uint32_t as;
                 br_packet_stream(c.opt.seed, 0u, c.opt.packet_offset + p, b.rng_a, c.num_streams, &xs, &as);
                 rng = Rng{xs, as};
-                mcvox_begin(c, b, x, s, rng, p);
+                mcvox_begin(c, b, x, s, rng, p, f3{0.0f, 0.0f, 0.0f});
                 active = true;
             }
             uint32_t taken = __ballot_sync(0xffffffffu, mine);

@@ -1,9 +1,12 @@
-"""Photon packet sources of the voxelized simulator: Line and GaussianBeam
-(xopto/mcvox/mcsource/line.py, gaussianbeam.py)."""
+"""Photon packet sources of the voxelized simulator: Line, GaussianBeam,
+UniformBeam, IsotropicPoint, UniformFiber, LambertianFiber and IsotropicVoxel
+(xopto/mcvox/mcsource/line.py, gaussianbeam.py, uniformbeam.py, point.py,
+fiber.py, voxel.py)."""
 import numpy as np
 
 from .. import _abi
 from ..mcbase import mcutil
+from ..mcbase.mcutil.fiber import MultimodeFiber
 
 
 def _unit(v):
@@ -102,5 +105,154 @@ class GaussianBeam:
 
     def __str__(self):
         return 'GaussianBeam(sigma=({}, {}), clip={})'.format(*self._sigma, self._clip)
+
+    __repr__ = __str__
+
+
+class UniformBeam:
+    """Collimated beam of uniform intensity over an ellipse, entering the
+    voxel box (xopto/mcvox/mcsource/uniformbeam.py:32-340)."""
+
+    def __init__(self, diameter, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0)):
+        if isinstance(diameter, UniformBeam):
+            o = diameter
+            diameter, position, direction = o.diameter, o.position, o.direction
+        self._diameter = np.zeros((2,))
+        self._diameter[:] = diameter
+        if np.any(self._diameter < 0.0):
+            raise ValueError('Beam diameter must not be negative!')
+        self._position = np.zeros((3,))
+        self._position[:] = position
+        self._direction = _unit(direction)
+
+    diameter = property(lambda self: self._diameter)
+    position = property(lambda self: self._position)
+    direction = property(lambda self: self._direction)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """uniformbeam.py:271-310."""
+        T = mcutil.transform_base((0.0, 0.0, 1.0), self._direction)
+        target.kind = _abi.SRC_UNIFORM_BEAM
+        target.transformation[:] = [float(v) for v in np.asarray(T).ravel()]
+        target.position[:] = [float(v) for v in self._position]
+        target.direction[:] = [float(v) for v in self._direction]
+        target.sigma[:] = [float(v) * 0.5 for v in self._diameter]
+        return target
+
+    def todict(self):
+        return {'type': 'UniformBeam', 'diameter': self._diameter.tolist(),
+                'position': self._position.tolist(), 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'UniformBeam(diameter=({}, {}))'.format(*self._diameter)
+
+    __repr__ = __str__
+
+
+class IsotropicPoint:
+    """Isotropic point source inside or outside the voxel box
+    (xopto/mcvox/mcsource/point.py:31-230)."""
+
+    def __init__(self, position=(0.0, 0.0, 0.0)):
+        if isinstance(position, IsotropicPoint):
+            position = position.position
+        self._position = np.zeros((3,))
+        self._position[:] = position
+
+    position = property(lambda self: self._position)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        target.kind = _abi.SRC_ISOTROPIC_POINT
+        target.position[:] = [float(v) for v in self._position]
+        return target
+
+    def todict(self):
+        return {'type': 'IsotropicPoint', 'position': self._position.tolist()}
+
+    def __str__(self):
+        return 'IsotropicPoint(position=({}, {}, {}))'.format(*self._position)
+
+    __repr__ = __str__
+
+
+class UniformFiber:
+    """Optical fibre source with its axis along ``direction``, launching
+    onto the voxel box; uniform over the core and in solid angle within the
+    acceptance cone (xopto/mcvox/mcsource/fiber.py:178-520)."""
+    _kind = _abi.SRC_UNIFORM_FIBER
+
+    def __init__(self, fiber: MultimodeFiber, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0)):
+        if isinstance(fiber, UniformFiber):
+            fiber, position, direction = fiber.fiber, fiber.position, fiber.direction
+        self._fiber = fiber
+        self._position = np.zeros((3,))
+        self._position[:] = position
+        self._direction = _unit(direction)
+
+    fiber = property(lambda self: self._fiber)
+    position = property(lambda self: self._position)
+    direction = property(lambda self: self._direction)
+
+    def _angular(self):
+        return (1.0 - self._fiber.na ** 2) ** 0.5
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiber.py:455-493 (UniformFiber), 700-740 (LambertianFiber)."""
+        T = mcutil.transform_base((0.0, 0.0, 1.0), self._direction)
+        target.kind = self._kind
+        target.transformation[:] = [float(v) for v in np.asarray(T).ravel()]
+        target.position[:] = [float(v) for v in self._position]
+        target.direction[:] = [float(v) for v in self._direction]
+        target.sigma[0] = self._fiber.dcore * 0.5
+        target.sigma[1] = self._angular()
+        target.clip = self._fiber.ncore
+        return target
+
+    def todict(self):
+        return {'type': type(self).__name__, 'fiber': self._fiber.todict(),
+                'position': self._position.tolist(), 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return '{}(fiber={})'.format(type(self).__name__, self._fiber)
+
+    __repr__ = __str__
+
+
+class LambertianFiber(UniformFiber):
+    """Fibre source with a Lambertian angular distribution
+    (xopto/mcvox/mcsource/fiber.py:523-744)."""
+    _kind = _abi.SRC_LAMBERTIAN_FIBER
+
+    def _angular(self):
+        return self._fiber.na
+
+
+class IsotropicVoxel:
+    """Isotropic source uniformly distributed within one voxel
+    (xopto/mcvox/mcsource/voxel.py:31-192)."""
+
+    def __init__(self, voxel):
+        if isinstance(voxel, IsotropicVoxel):
+            voxel = voxel.voxel
+        self._voxel = np.zeros((3,), dtype=np.int64)
+        self._voxel[:] = voxel
+
+    voxel = property(lambda self: self._voxel)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        shape = mc.voxels.shape          # (nz, ny, nx)
+        nx, ny, nz = shape[2], shape[1], shape[0]
+        x, y, z = (int(v) for v in self._voxel)
+        if not (0 <= x < nx and 0 <= y < ny and 0 <= z < nz):
+            raise ValueError('Voxel index ({}, {}, {}) is not valid!'.format(x, y, z))
+        target.kind = _abi.SRC_ISOTROPIC_VOXEL
+        target.position[:] = [float(x), float(y), float(z)]
+        return target
+
+    def todict(self):
+        return {'type': 'IsotropicVoxel', 'voxel': self._voxel.tolist()}
+
+    def __str__(self):
+        return 'IsotropicVoxel(voxel=({}, {}, {}))'.format(*self._voxel)
 
     __repr__ = __str__

@@ -1,0 +1,5 @@
+"""Utilities of the voxelized simulator (the items of pyxopto_gb300.mcbase.mcutil,
+as xopto/mcvox/mcutil re-exports xopto/mcbase/mcutil)."""
+from ...mcbase.mcutil import *  # noqa: F401,F403
+from ...mcbase.mcutil import Axis, RadialAxis  # noqa: F401
+from . import fiber  # noqa: F401

@@ -190,6 +190,72 @@ SCENARIOS = {
         detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), bottom=dict(type='Total'),
                        specular=dict(type='Total')),
         nphotons=3000, streams=32, rnginit=43),
+    # voxelized-medium sources (xopto/mcvox/mcsource/uniformbeam.py, point.py,
+    # fiber.py, voxel.py), with the path-length detector on the bottom
+    'vox_uniform_beam': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='UniformBeam', diameter=(8e-4, 5e-4), position=(1e-4, 0.0, -1e-3),
+                    direction=(0.15, 0.1, 1.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]),
+                       bottom=dict(type='RadialPl', axis=[0.0, 1e-3, 5], plaxis=[0.0, 1e-2, 8]),
+                       specular=dict(type='Total')),
+        fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='deposition'),
+        nphotons=2000, streams=20, rnginit=47),
+    'vox_point_outside': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='IsotropicPoint', position=(2e-4, -1e-4, -5e-4)),
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Total'), specular=dict(type='Total')),
+        nphotons=2000, streams=20, rnginit=53),
+    'vox_point_inside': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='IsotropicPoint', position=(2e-4, -1e-4, 7e-4)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), bottom=dict(type='Total')),
+        fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='fluence'),
+        nphotons=2000, streams=20, rnginit=59),
+    'vox_fiber_uniform': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='UniformFiber',
+                    fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22),
+                    position=(0.0, 1e-4, -2e-4), direction=(0.2, -0.1, 1.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), specular=dict(type='Total')),
+        nphotons=2000, streams=20, rnginit=61),
+    'vox_fiber_lambertian': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='LambertianFiber',
+                    fiber=dict(dcore=400e-6, dcladding=420e-6, ncore=1.452, na=0.39),
+                    position=(1e-4, 0.0, 0.0), direction=(0.0, 0.0, 1.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), specular=dict(type='Total')),
+        nphotons=2000, streams=20, rnginit=67),
+    'vox_isotropic_voxel': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='IsotropicVoxel', voxel=(4, 6, 3)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), bottom=dict(type='Total')),
+        fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='deposition'),
+        nphotons=2000, streams=20, rnginit=71),
     # optical path-length resolved detectors (xopto/mcml/mcdetector/radialpl.py,
     # totalpl.py): two layers, RadialPl on top (linear path-length axis),
     # TotalPl below (log path-length axis)
