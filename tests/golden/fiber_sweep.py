@@ -16,8 +16,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def load():
-    return np.load(os.path.join(HERE, 'cuda_mcml_fiber.npz'))
+def load(double=False):
+    """The single-layer golden, or the two-layer one (validate.py:692-866:
+    layer 1 fixed, the sweep on layer 2)."""
+    return np.load(os.path.join(HERE, 'cuda_mcml_fiber2.npz' if double else 'cuda_mcml_fiber.npz'))
 
 
 def build(data, fast=True, scheduling='dynamic', rnginit=1):
@@ -26,7 +28,11 @@ def build(data, fast=True, scheduling='dynamic', rnginit=1):
     g = data['g']
     layers = mc.mclayer.Layers([
         mc.mclayer.Layer(d=float(data['d'][i]), n=float(data['n'][i]), mua=0.0, mus=0.0,
-                         pf=mc.mcpf.Hg(float(g[i]))) for i in range(3)])
+                         pf=mc.mcpf.Hg(float(g[i]))) for i in range(len(g))])
+    if 'fixed_layer' in data.files:
+        k = int(data['fixed_layer'][0])
+        layers[k].mua = float(data['fixed_mua'][0])
+        layers[k].mus = float(data['fixed_musr'][0]) / (1.0 - float(g[k]))
     dcore, dclad, ncore, na = (float(v) for v in data['fiber'])
     source = mc.mcsource.UniformFiberNI(fiber.MultimodeFiber(dcore, dclad, ncore, na))
     start, stop, n = data['axis']
@@ -45,12 +51,13 @@ def run(sim, data, nphotons):
     (fibre reflectance [20, 20, 5], seconds spent in Mc.run)."""
     from pyxopto_gb300.util import convolve
     mua, musr = np.meshgrid(data['mua'], data['musr'], indexing='ij')
-    g = float(data['g'][1])
+    k = int(data['sweep_layer'][0]) if 'sweep_layer' in data.files else 1
+    g = float(data['g'][k])
     profiles, r = [], None
     t = 0.0
     for i in range(mua.size):
-        sim.layers[1].mua = float(mua.flat[i])
-        sim.layers[1].mus = float(musr.flat[i]) / (1.0 - g)
+        sim.layers[k].mua = float(mua.flat[i])
+        sim.layers[k].mus = float(musr.flat[i]) / (1.0 - g)
         t0 = time.perf_counter()
         _, _, det = sim.run(nphotons)
         t += time.perf_counter() - t0

@@ -24,6 +24,9 @@ Writes
                          (xopto/mcml/test/reference/cuda_singlelayer_uniformfiber.pkl,
                          test xopto/mcml/test/validate.py:348-511), with the
                          geometry of that test.
+  cuda_mcml_fiber2.npz   the same for the two-layer sample, sweep on the
+                         second layer (cuda_doublelayer_uniformfiber.pkl,
+                         test validate.py:692-866).
 """
 import os
 import pickle
@@ -96,14 +99,22 @@ def make_cuda_mcml():
     print('cuda_mcml_radial', len(d['reflectance']))
 
 
-def make_cuda_fiber():
-    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference',
-                        'cuda_singlelayer_uniformfiber.pkl')
+def make_cuda_fiber(double=False):
+    name = 'cuda_doublelayer_uniformfiber.pkl' if double else 'cuda_singlelayer_uniformfiber.pkl'
+    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference', name)
     with open(path, 'rb') as f:
         d = pickle.load(f)
     layers = d['layers']
+    lut = d['lut']
+    extra = {}
+    if double:
+        # validate.py:759-790: layer 1 fixed, the (mua, mus') sweep on layer 2
+        extra = dict(fixed_layer=np.array([1]), fixed_mua=np.asarray(lut[0]['mua'], np.float64),
+                     fixed_musr=np.asarray(lut[0]['musr'], np.float64), sweep_layer=np.array([2]))
+        lut = lut[1]
     np.savez_compressed(
-        os.path.join(HERE, 'cuda_mcml_fiber.npz'),
+        os.path.join(HERE, 'cuda_mcml_fiber2.npz' if double else 'cuda_mcml_fiber.npz'),
+        **extra,
         reflectance=np.asarray(d['reflectance'], dtype=np.float64),
         n=np.array([l['basic']['n'] for l in layers]),
         d=np.array([l['basic']['d'] for l in layers]),
@@ -115,10 +126,10 @@ def make_cuda_fiber():
         cosmin=np.array([d['detector']['cosmin']]),
         sds=np.asarray(d['detector']['fibers']['sds'], dtype=np.float64),
         sds_dcore=np.array([d['detector']['fibers']['dcore']]),
-        mua=np.asarray(d['lut']['mua'], dtype=np.float64),
-        musr=np.asarray(d['lut']['musr'], dtype=np.float64),
+        mua=np.asarray(lut['mua'], dtype=np.float64),
+        musr=np.asarray(lut['musr'], dtype=np.float64),
         rmax=np.array([d['mc']['rmax']]))
-    print('cuda_mcml_fiber', np.asarray(d['reflectance']).shape)
+    print(name, np.asarray(d['reflectance']).shape)
 
 
 if __name__ == '__main__':
@@ -129,3 +140,4 @@ if __name__ == '__main__':
         make_rng_tables()
         make_cuda_mcml()
         make_cuda_fiber()
+        make_cuda_fiber(double=True)

@@ -198,13 +198,14 @@ def test_trace_bit_identical_to_oracle(cuda, lib, oracle, scheduling):
     assert tr.n.min() >= 1
 
 
-def test_cuda_mcml_fiber_sweep(cuda, lib):
-    """The reference's validation test SingleLayerUniformFiberRadial
-    (xopto/mcml/test/validate.py:348-511): fibre reflectance of a 20 x 20
-    (mua, mus') sweep at 5 source-detector separations against CUDA-MCML,
-    pass if |mean relative error| < 0.5 % (1e6 packets per point here, 1e7
-    in the reference)."""
-    data = fiber_sweep.load()
+@pytest.mark.parametrize('double', [False, True])
+def test_cuda_mcml_fiber_sweep(cuda, lib, double):
+    """The reference's validation tests SingleLayerUniformFiberRadial and
+    DoubleLayerUniformFiberRadial (xopto/mcml/test/validate.py:348-511,
+    692-866): fibre reflectance of a 20 x 20 (mua, mus') sweep at 5
+    source-detector separations against CUDA-MCML, pass if |mean relative
+    error| < 0.5 % (1e6 packets per point here, 1e7 in the reference)."""
+    data = fiber_sweep.load(double)
     sim = fiber_sweep.build(data, fast=True)
     refl, _ = fiber_sweep.run(sim, data, 1_000_000)
     err = fiber_sweep.relative_error(data, refl)
