@@ -255,7 +255,9 @@ typedef struct McgbRunOptions {
     float lottery_chance;                   /* MC_PACKET_LOTTERY_CHANCE (0.1)  */
     float rmax;                             /* Mc.rmax (inf = no limit)        */
     int32_t track_optical_pathlength;       /* MC_TRACK_OPTICAL_PATHLENGTH     */
-    uint32_t block_size;                    /* threads per block (0 = auto)    */
+    uint32_t block_size;                    /* threads per block (0 = auto);
+                                               STATIC scheduling only, the
+                                               DYNAMIC kernels use 128         */
     uint64_t max_steps_per_packet;          /* 0 = unlimited (2^32 - 1 at most) */
     double deadline_s;                      /* device wall-clock limit, 0=300s */
     int32_t scheduling;                     /* MCGB_SCHED_*                    */

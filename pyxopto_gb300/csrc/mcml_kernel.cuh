@@ -521,7 +521,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
    from the queue counters[MCGB_CNT_QUEUE]; packet p runs on the stream of
    (seed, packet_offset + p). */
 template <int PF, int METHOD, bool FLU, bool XTRA>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
                     uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MlSmem sm;

@@ -561,8 +561,11 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
 }
 
 /* DYNAMIC scheduling (per-packet streams, warp refill). */
+/* 128-thread blocks, at least 9 resident per SM (at most 56 registers):
+   the launch code of the less common sources would otherwise raise the
+   register count and cut the resident warps. */
 template <int PF, int METHOD, bool FLU, bool XTRA>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128, 9)
 mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
                      uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MvSmem sm;

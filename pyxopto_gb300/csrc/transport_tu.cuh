@@ -82,13 +82,15 @@ cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_
                                              (int)shape.dyn_smem);
         if (e != cudaSuccess) return e;
     }
-    unsigned grid = shape.grid;
+    unsigned grid = shape.grid, block = shape.block;
     if (sched == MCGB_SCHED_DYNAMIC) {
-        /* persistent: as many blocks as stay resident */
+        /* persistent: as many 128-thread blocks as stay resident (the
+           dynamic kernels are compiled for 128-thread blocks) */
+        block = 128;
         int dev = 0, sms = 0, bps = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = resident_blocks(k, (int)shape.block, shape.dyn_smem, &bps);
+        if (e == cudaSuccess) e = resident_blocks(k, (int)block, shape.dyn_smem, &bps);
         if (e != cudaSuccess) return e;
         if (bps < 1) return cudaErrorInvalidConfiguration;
         grid = (unsigned)(sms * bps);
@@ -98,7 +100,7 @@ cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_
        warp), at most 128 (one queue access per 128 packets in long runs) */
     uint32_t items = cfg.opt.packets_per_item;
     if (items == 0) {
-        uint64_t warps = (uint64_t)grid * (shape.block / 32u);
+        uint64_t warps = (uint64_t)grid * (block / 32u);
         uint64_t b = cfg.num_packets / (warps * 4u);
         items = (uint32_t)(b < 1 ? 1 : (b > 128 ? 128 : b));
     }
@@ -106,7 +108,7 @@ cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_
     uint64_t deadline = shape.deadline_ns;
     int lut = shape.lut_in_smem;
     void *args[] = {(void *)&cfg, (void *)&b, (void *)&deadline, (void *)&lut, (void *)&items};
-    return cudaLaunchKernel(k, dim3(grid), dim3(shape.block), args, shape.dyn_smem, stream);
+    return cudaLaunchKernel(k, dim3(grid), dim3(block), args, shape.dyn_smem, stream);
 }
 
 cudaError_t MCGB_OCCUPANCY(int block, size_t dyn_smem, int *blocks_per_sm) {
