@@ -110,7 +110,8 @@ enum {
     MCGB_SRC_ISOTROPIC_VOXEL = 8
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
-       MCGB_DET_TOTAL_PL = 4 };
+       MCGB_DET_TOTAL_PL = 4, MCGB_DET_CARTESIAN = 5, MCGB_DET_CARTESIAN_PL = 6,
+       MCGB_DET_SYMMETRIC_X = 7 };
 enum { MCGB_FLUENCE_NONE = 0, MCGB_FLUENCE_DEPOSITION = 1, MCGB_FLUENCE_RATE = 2 };
 /* Trace flags (xopto/mcbase/mctrace.py TRACE_START/END/ALL). */
 enum { MCGB_TRACE_NONE = 0, MCGB_TRACE_START = 1, MCGB_TRACE_END = 2, MCGB_TRACE_ALL = 7 };
@@ -206,24 +207,33 @@ typedef struct McgbSource {
 } McgbSource;                               /* 104 bytes */
 
 /* Surface detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;
-   total.py:52-56,86-108; radialpl.py:138-179,343-378; totalpl.py:107-135).
-   Total: one bin.  Radial: n radial bins.  TotalPl: n_pl optical path-length
-   bins.  RadialPl: n_pl x n bins, path length first.  Indices outside an
-   axis are clipped into its first or last bin; the path-length kinds need
+   total.py:52-56,86-108; radialpl.py:138-179,343-378; totalpl.py:107-135;
+   cartesian.py:124-157,340-372; cartesianpl.py:150-190; symmetric.py:124-156,
+   260-285).
+   Total: one bin.  Radial: n radial bins (r_min, inv_dr, log_scale).
+   TotalPl: n_pl optical path-length bins.  RadialPl: n_pl x n bins, path
+   length first.  Cartesian: n_y x n bins, x axis (r_min, inv_dr, n) and y
+   axis (y_min, inv_dy, n_y).  CartesianPl: n_pl x n_y x n bins.  SymmetricX:
+   2n bins symmetric about x = position[0], half axis offset r_min, 1/step
+   inv_dr, log_scale.  Indices outside an axis are clipped into its first or
+   last bin; the path-length kinds need
    McgbRunOptions.track_optical_pathlength. */
 typedef struct McgbDetector {
     int32_t kind;
     float direction[3];
     float position[2];
     float r_min, inv_dr, cos_min;
-    uint32_t n;                             /* radial bins                     */
-    int32_t log_scale;                      /* radial axis in log scale        */
+    uint32_t n;                             /* radial / x bins                 */
+    int32_t log_scale;                      /* radial / x axis in log scale    */
     int32_t pl_log_scale;                   /* path-length axis in log scale   */
     uint64_t offset;                        /* first accumulator               */
     float pl_min, inv_dpl;                  /* path-length axis start, 1/step  */
     uint32_t n_pl;                          /* path-length bins                */
     uint32_t reserved;
-} McgbDetector;                             /* 72 bytes */
+    float y_min, inv_dy;                    /* Cartesian y axis start, 1/step  */
+    uint32_t n_y;                           /* Cartesian y bins                */
+    uint32_t reserved2;
+} McgbDetector;                             /* 88 bytes */
 
 /* Cartesian fluence (xopto/mcbase/mcfluence/fluence.py:56-62,103-143). */
 typedef struct McgbFluence {

@@ -250,7 +250,9 @@ static inline uint32_t weight_to_u32(float w, float accept) {
 
 /* Surface detector deposit: Total (xopto/mcml/mcdetector/total.py:86-108),
    Radial (radial.py:117-150), TotalPl (totalpl.py:107-135), RadialPl
-   (radialpl.py:138-179); opl = mcsim_optical_pathlength. */
+   (radialpl.py:138-179), Cartesian (cartesian.py:124-157), CartesianPl
+   (cartesianpl.py:146-185), SymmetricX (symmetric.py:124-156);
+   opl = mcsim_optical_pathlength. */
 static void detector_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir,
                              float weight, float opl, uint64_t *accu) {
     if (det->kind == MCGB_DET_NONE) return;
@@ -265,13 +267,27 @@ static void detector_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir,
         int32_t r_index = cvt_int((r - det->r_min) * det->inv_dr);
         index = (uint64_t)clip_i(r_index, 0, (int32_t)det->n - 1);
     }
-    if (det->kind == MCGB_DET_RADIAL_PL || det->kind == MCGB_DET_TOTAL_PL) {
+    if (det->kind == MCGB_DET_CARTESIAN || det->kind == MCGB_DET_CARTESIAN_PL) {
+        int32_t ix = clip_i(cvt_int((pos.x - det->r_min) * det->inv_dr), 0, (int32_t)det->n - 1);
+        int32_t iy = clip_i(cvt_int((pos.y - det->y_min) * det->inv_dy), 0, (int32_t)det->n_y - 1);
+        index = (uint64_t)iy * det->n + (uint64_t)ix;
+    } else if (det->kind == MCGB_DET_SYMMETRIC_X) {
+        float xx = fabsf(pos.x - det->position[0]);
+        if (det->log_scale) xx = m_log(mm, fmaxf(xx, 1e-12f));
+        int32_t ix = clip_i(cvt_int((xx - det->r_min) * det->inv_dr), 0, (int32_t)det->n - 1);
+        index = (pos.x - det->position[0] >= 0.0f) ? (uint64_t)(ix + (int32_t)det->n)
+                                                   : (uint64_t)((int32_t)det->n - ix - 1);
+    }
+    if (det->kind == MCGB_DET_RADIAL_PL || det->kind == MCGB_DET_TOTAL_PL ||
+        det->kind == MCGB_DET_CARTESIAN_PL) {
         float pl = opl;
         if (det->pl_log_scale) pl = m_log(mm, fmaxf(pl, 1e-12f));
         int32_t pl_index = clip_i(cvt_int((pl - det->pl_min) * det->inv_dpl), 0,
                                   (int32_t)det->n_pl - 1);
-        uint64_t nr = det->kind == MCGB_DET_RADIAL_PL ? det->n : 1u;
-        index += (uint64_t)pl_index * nr;
+        uint64_t plane = det->kind == MCGB_DET_RADIAL_PL   ? (uint64_t)det->n
+                         : det->kind == MCGB_DET_CARTESIAN_PL ? (uint64_t)det->n * det->n_y
+                                                             : 1u;
+        index += (uint64_t)pl_index * plane;
     }
     uint32_t w = weight_to_u32(weight, accept);
     if (w > 0) accu[det->offset + index] += w;

@@ -88,20 +88,27 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     for (int i = 0; i < 3; ++i) {
         const McgbDetector &d = dets[i];
         if (d.kind == MCGB_DET_NONE) continue;
-        if (d.kind != MCGB_DET_TOTAL && d.kind != MCGB_DET_RADIAL && d.kind != MCGB_DET_RADIAL_PL &&
-            d.kind != MCGB_DET_TOTAL_PL)
+        if (d.kind < MCGB_DET_TOTAL || d.kind > MCGB_DET_SYMMETRIC_X)
             return fail(MCGB_E_INVALID, "%s detector: unknown kind %d", names[i], d.kind);
-        if (d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL) {
+        const bool pl = d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL ||
+                        d.kind == MCGB_DET_CARTESIAN_PL;
+        if (pl) {
             if (!o.track_optical_pathlength)
                 return fail(MCGB_E_INVALID, "%s path-length detector needs track_optical_pathlength",
                             names[i]);
             if (i == 2) return fail(MCGB_E_INVALID, "the specular slot takes no path-length detector");
         }
-        uint64_t nr = (d.kind == MCGB_DET_RADIAL || d.kind == MCGB_DET_RADIAL_PL) ? d.n : 1;
-        uint64_t npl = (d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL) ? d.n_pl : 1;
-        if (nr > 0x7FFFFFFFu || npl > 0x7FFFFFFFu)
+        uint64_t nr = 1;
+        if (d.kind == MCGB_DET_RADIAL || d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_CARTESIAN ||
+            d.kind == MCGB_DET_CARTESIAN_PL)
+            nr = d.n;
+        else if (d.kind == MCGB_DET_SYMMETRIC_X)
+            nr = 2ull * d.n;
+        uint64_t ny = (d.kind == MCGB_DET_CARTESIAN || d.kind == MCGB_DET_CARTESIAN_PL) ? d.n_y : 1;
+        uint64_t npl = pl ? d.n_pl : 1;
+        if (nr > 0x7FFFFFFFu || ny > 0x7FFFFFFFu || npl > 0x7FFFFFFFu || nr * ny * npl > 0xFFFFFFFFull)
             return fail(MCGB_E_SIZE, "%s detector has too many bins", names[i]);
-        uint64_t n = nr * npl;
+        uint64_t n = nr * ny * npl;
         if (n == 0) return fail(MCGB_E_INVALID, "%s detector has no bins", names[i]);
         if (!b->accumulator || !range_ok(d.offset, n, b->accumulator_size))
             return fail(MCGB_E_SIZE, "%s detector [%llu, +%llu) beyond the accumulator (%llu)", names[i],

@@ -275,8 +275,10 @@ MCGB_DEV void accu_add(uint64_t *accu, uint64_t index, uint32_t w) {
 }
 
 /* Surface detector deposit: Total (xopto/mcml/mcdetector/total.py:86-108),
-   Radial (radial.py:117-150), TotalPl (totalpl.py:107-135) and RadialPl
-   (radialpl.py:138-179); opl is the packet's optical path length. */
+   Radial (radial.py:117-150), TotalPl (totalpl.py:107-135), RadialPl
+   (radialpl.py:138-179), Cartesian (cartesian.py:124-157), CartesianPl
+   (cartesianpl.py:146-185) and SymmetricX (symmetric.py:124-156); opl is
+   the packet's optical path length. */
 MCGB_DEV void detector_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir,
                                float weight, float opl, uint64_t *accu) {
     if (det.kind == MCGB_DET_NONE) return;
@@ -291,12 +293,26 @@ MCGB_DEV void detector_deposit(const McgbDetector &det, const f3 &pos, const f3 
         int r_index = cvt_int((r - det.r_min) * det.inv_dr);
         index = (uint64_t)clip_i(r_index, 0, (int)det.n - 1);
     }
-    if (det.kind == MCGB_DET_RADIAL_PL || det.kind == MCGB_DET_TOTAL_PL) {
+    if (det.kind == MCGB_DET_CARTESIAN || det.kind == MCGB_DET_CARTESIAN_PL) {
+        int ix = clip_i(cvt_int((pos.x - det.r_min) * det.inv_dr), 0, (int)det.n - 1);
+        int iy = clip_i(cvt_int((pos.y - det.y_min) * det.inv_dy), 0, (int)det.n_y - 1);
+        index = (uint64_t)iy * det.n + (uint64_t)ix;
+    } else if (det.kind == MCGB_DET_SYMMETRIC_X) {
+        float x = fabsf(pos.x - det.position[0]);
+        if (det.log_scale) x = mc_log(fmaxf(x, 1e-12f));
+        int ix = clip_i(cvt_int((x - det.r_min) * det.inv_dr), 0, (int)det.n - 1);
+        index = (pos.x - det.position[0] >= 0.0f) ? (uint64_t)(ix + (int)det.n)
+                                                  : (uint64_t)((int)det.n - ix - 1);
+    }
+    if (det.kind == MCGB_DET_RADIAL_PL || det.kind == MCGB_DET_TOTAL_PL ||
+        det.kind == MCGB_DET_CARTESIAN_PL) {
         float pl = opl;
         if (det.pl_log_scale) pl = mc_log(fmaxf(pl, 1e-12f));
         int pl_index = clip_i(cvt_int((pl - det.pl_min) * det.inv_dpl), 0, (int)det.n_pl - 1);
-        uint64_t nr = det.kind == MCGB_DET_RADIAL_PL ? det.n : 1u;
-        index += (uint64_t)pl_index * nr;
+        uint64_t plane = det.kind == MCGB_DET_RADIAL_PL   ? (uint64_t)det.n
+                         : det.kind == MCGB_DET_CARTESIAN_PL ? (uint64_t)det.n * det.n_y
+                                                            : 1u;
+        index += (uint64_t)pl_index * plane;
     }
     uint32_t w = weight_to_u32(weight, accept);
     if (w > 0) accu_add(accu, det.offset + index, w);

@@ -1,7 +1,9 @@
-"""Surface detectors: Total, Radial and their optical path-length variants
-TotalPl and RadialPl, grouped by Detectors into the top, bottom and specular
-slots (xopto/mcml/mcdetector/base.py, total.py, radial.py, totalpl.py,
-radialpl.py; the mcvox package uses the same classes).
+"""Surface detectors: Total, Radial, Cartesian and SymmetricX, the optical
+path-length variants TotalPl, RadialPl and CartesianPl, grouped by
+Detectors into the top, bottom and specular slots
+(xopto/mcml/mcdetector/base.py, total.py, radial.py, cartesian.py,
+symmetric.py, totalpl.py, radialpl.py, cartesianpl.py; the mcvox package uses
+the same classes).
 
 Tallies come back from the device as uint64 fixed-point integers and are
 converted with the reference's rule raw += accumulator/K
@@ -11,7 +13,7 @@ from typing import Tuple
 import numpy as np
 
 from .. import _abi
-from .mcutil import Axis, RadialAxis
+from .mcutil import Axis, RadialAxis, SymmetricAxis
 
 
 class Detector:
@@ -285,6 +287,176 @@ class RadialPl(Radial):
                                                                  self._cosmin)
 
 
+class _Directional(Detector):
+    """Acceptance cosine and reference direction shared by the detectors."""
+
+    def _init_direction(self, cosmin, direction):
+        self._cosmin = 0.0
+        self._direction = np.zeros((3,))
+        self.cosmin = cosmin
+        self.direction = direction
+
+    def _set_cosmin(self, v):
+        self._cosmin = min(max(float(v), 0.0), 1.0)
+
+    cosmin = property(lambda self: self._cosmin, _set_cosmin)
+
+    def _set_direction(self, d):
+        self._direction[:] = d
+        n = np.linalg.norm(self._direction)
+        if n == 0.0:
+            raise ValueError('Direction vector norm/length must not be 0!')
+        self._direction *= 1.0 / n
+
+    direction = property(lambda self: self._direction, _set_direction)
+
+
+class Cartesian(_Directional):
+    """Reflectance/transmittance on a 2-D x-y grid; raw has shape (n_y, n_x)
+    and positions beyond the grid are clipped into the edge bins
+    (xopto/mcml/mcdetector/cartesian.py:33-420)."""
+    kind = _abi.DET_CARTESIAN
+
+    def __init__(self, xaxis, yaxis=None, cosmin=0.0, direction=(0.0, 0.0, 1.0)):
+        if isinstance(xaxis, Cartesian):
+            other = xaxis
+            xaxis, yaxis = type(other.xaxis)(other.xaxis), type(other.yaxis)(other.yaxis)
+            cosmin, direction = other.cosmin, other.direction
+            raw, nphotons = np.copy(other.raw), other.nphotons
+        else:
+            if yaxis is None:
+                yaxis = Axis(xaxis)
+            raw, nphotons = np.zeros((yaxis.n, xaxis.n)), 0
+        super().__init__(raw, nphotons)
+        self._x_axis, self._y_axis = xaxis, yaxis
+        self._init_direction(cosmin, direction)
+        self._accumulators_area = self._x_axis.step * self._y_axis.step
+
+    xaxis = property(lambda self: self._x_axis)
+    yaxis = property(lambda self: self._y_axis)
+    x = property(lambda self: self._x_axis.centers)
+    y = property(lambda self: self._y_axis.centers)
+
+    def _get_normalized(self):
+        return self.raw * (1.0 / (max(self.nphotons, 1.0) * self._accumulators_area))
+
+    normalized = property(_get_normalized)
+    reflectance = property(_get_normalized)
+    transmittance = property(_get_normalized)
+
+    def pack(self, mc, target):
+        """cartesian.py:340-372."""
+        target.kind = self.kind
+        target.offset = mc.cl_allocate_rw_accumulator_buffer(self, self.shape)
+        target.direction[:] = [float(v) for v in self._direction]
+        target.r_min = self._x_axis.start
+        target.inv_dr = 1.0 / self._x_axis.step if self._x_axis.n > 1 else 0.0
+        target.y_min = self._y_axis.start
+        target.inv_dy = 1.0 / self._y_axis.step if self._y_axis.n > 1 else 0.0
+        target.cos_min = self._cosmin
+        target.n = self._x_axis.n
+        target.n_y = self._y_axis.n
+        return target
+
+    def copy(self):
+        return type(self)(self)
+
+    def todict(self):
+        return {'type': 'Cartesian', 'x_axis': self._x_axis.todict(),
+                'y_axis': self._y_axis.todict(), 'cosmin': self._cosmin,
+                'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'Cartesian(xaxis={}, yaxis={}, cosmin={})'.format(self._x_axis, self._y_axis,
+                                                                self._cosmin)
+
+
+class CartesianPl(Cartesian):
+    """Cartesian detector resolved by optical path length; raw has shape
+    (n_pl, n_y, n_x) (xopto/mcml/mcdetector/cartesianpl.py:33-470).  Turns
+    on optical path-length tracking."""
+    kind = _abi.DET_CARTESIAN_PL
+    tracks_pathlength = True
+
+    def __init__(self, xaxis, yaxis=None, plaxis=None, cosmin=0.0, direction=(0.0, 0.0, 1.0)):
+        if isinstance(xaxis, CartesianPl):
+            other = xaxis
+            Cartesian.__init__(self, type(other.xaxis)(other.xaxis), type(other.yaxis)(other.yaxis),
+                               other.cosmin, other.direction)
+            self._pl_axis = type(other.plaxis)(other.plaxis)
+            self._raw_data = np.copy(other.raw)
+            self._nphotons = other.nphotons
+            return
+        Cartesian.__init__(self, xaxis, yaxis, cosmin, direction)
+        self._pl_axis = plaxis if plaxis is not None else Axis(0.0, 1.0, 1)
+        self._raw_data = np.zeros((self._pl_axis.n, self._y_axis.n, self._x_axis.n))
+
+    plaxis = property(lambda self: self._pl_axis)
+    pl = property(lambda self: self._pl_axis.centers)
+
+    def pack(self, mc, target):
+        Cartesian.pack(self, mc, target)
+        _pack_pl_axis(self._pl_axis, target)
+        return target
+
+    def todict(self):
+        d = Cartesian.todict(self)
+        d.update(type='CartesianPl', pl_axis=self._pl_axis.todict())
+        return d
+
+
+class SymmetricX(_Directional):
+    """Reflectance/transmittance in 2*n_half bins symmetric about
+    x = center, linear or logarithmic in |x - center|
+    (xopto/mcml/mcdetector/symmetric.py:33-320)."""
+    kind = _abi.DET_SYMMETRIC_X
+
+    def __init__(self, xaxis: SymmetricAxis, cosmin=0.0, direction=(0.0, 0.0, 1.0)):
+        if isinstance(xaxis, SymmetricX):
+            other = xaxis
+            xaxis, cosmin, direction = SymmetricAxis(other.xaxis), other.cosmin, other.direction
+            raw, nphotons = np.copy(other.raw), other.nphotons
+        else:
+            raw, nphotons = np.zeros((xaxis.n,)), 0
+        super().__init__(raw, nphotons)
+        self._x_axis = xaxis
+        self._init_direction(cosmin, direction)
+        self._inv_dx = 1.0 / (self._x_axis.edges[1:] - self._x_axis.edges[:-1])
+
+    xaxis = property(lambda self: self._x_axis)
+    x = property(lambda self: self._x_axis.centers)
+
+    def _get_normalized(self):
+        return self.raw * self._inv_dx * (1.0 / max(self.nphotons, 1.0))
+
+    normalized = property(_get_normalized)
+    reflectance = property(_get_normalized)
+    transmittance = property(_get_normalized)
+
+    def pack(self, mc, target):
+        """symmetric.py:260-285."""
+        target.kind = self.kind
+        target.offset = mc.cl_allocate_rw_accumulator_buffer(self, self.shape)
+        target.direction[:] = [float(v) for v in self._direction]
+        target.position[0] = self._x_axis.center
+        target.r_min = self._x_axis.scaled_offset
+        target.inv_dr = 1.0 / self._x_axis.step if self._x_axis.step != 0.0 else 0.0
+        target.log_scale = int(self._x_axis.logscale)
+        target.n = self._x_axis.n_half
+        target.cos_min = self._cosmin
+        return target
+
+    def copy(self):
+        return SymmetricX(self)
+
+    def todict(self):
+        return {'type': 'SymmetricX', 'x_axis': self._x_axis.todict(), 'cosmin': self._cosmin,
+                'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'SymmetricX(xaxis={}, cosmin={})'.format(self._x_axis, self._cosmin)
+
+
 class Detectors:
     """Top, bottom and specular detectors
     (xopto/mcml/mcdetector/base.py:295-568)."""
@@ -328,5 +500,5 @@ class Detectors:
     __repr__ = __str__
 
 
-__all__ = ['Axis', 'RadialAxis', 'Detector', 'DetectorDefault', 'Total', 'Radial', 'TotalPl',
-           'RadialPl', 'Detectors']
+__all__ = ['Axis', 'RadialAxis', 'SymmetricAxis', 'Detector', 'DetectorDefault', 'Total', 'Radial',
+           'TotalPl', 'RadialPl', 'Cartesian', 'CartesianPl', 'SymmetricX', 'Detectors']

@@ -71,6 +71,61 @@ class RadialAxis(Axis):
         self._centers = (2.0 / 3.0) * (e[:-1] ** 2 + e[:-1] * e[1:] + e[1:] ** 2) / (e[:-1] + e[1:])
 
 
+class SymmetricAxis:
+    """Accumulator axis with 2*n_half bins placed symmetrically about a
+    center, linear or logarithmic in the distance from the center
+    (xopto/mcbase/mcutil/axis.py:267-480)."""
+
+    def __init__(self, center: float = 0.0, range: float = 1.0, n_half: int = 1000,
+                 logscale: bool = False):
+        if isinstance(center, SymmetricAxis):
+            ax = center
+            center, range, n_half, logscale = ax.center, ax.range, ax.n_half, ax.logscale
+        self._center, self._range = float(center), float(range)
+        self._n_half, self._logscale = int(n_half), bool(logscale)
+        self._n = 2 * self._n_half
+        if self._logscale:
+            eps = np.finfo(np.float64).eps
+            right = (self._center + np.logspace(np.log(eps), np.log(self._range), self._n_half + 1,
+                                                base=np.e))[1:]
+            self._offset = eps
+            self._edges = np.hstack((-right[::-1], [self._center], right))
+            self._step = (np.log(self._range) - np.log(eps)) / self._n_half
+            self._scaled_offset = np.log(self._offset)
+        else:
+            self._offset = 0.0
+            self._edges = np.linspace(self._center - self._range, self._center + self._range,
+                                      self._n + 1)
+            self._step = (self._edges[-1] - self._edges[0]) / self._n
+            self._scaled_offset = 0.0
+        self._span = np.array((self._center + self._offset, self._center + self._range))
+        self._centers = 0.5 * (self._edges[:-1] + self._edges[1:])
+
+    center = property(lambda self: self._center)
+    range = property(lambda self: self._range)
+    n_half = property(lambda self: self._n_half)
+    n = property(lambda self: self._n)
+    logscale = property(lambda self: self._logscale)
+    step = property(lambda self: self._step)
+    span = property(lambda self: self._span)
+    start = property(lambda self: self._span[0])
+    stop = property(lambda self: self._span[1])
+    offset = property(lambda self: self._offset)
+    scaled_offset = property(lambda self: self._scaled_offset)
+    edges = property(lambda self: self._edges)
+    centers = property(lambda self: self._centers)
+
+    def todict(self):
+        return {'range': self._range, 'center': self._center, 'n_half': self._n_half,
+                'logscale': self._logscale, 'type': 'SymmetricAxis'}
+
+    def __str__(self):
+        return 'SymmetricAxis(center={}, range={}, n_half={}, logscale={})'.format(
+            self._center, self._range, self._n_half, self._logscale)
+
+    __repr__ = __str__
+
+
 def cos_critical(n1: float, n2: float) -> float:
     """Cosine of the critical incidence angle at the n1 -> n2 boundary
     (xopto/mcbase/mcutil/boundary.py:25-41)."""

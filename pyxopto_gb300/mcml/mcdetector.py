@@ -1,4 +1,4 @@
 """Surface detectors (re-exported from pyxopto_gb300.mcbase.mcdetector)."""
-from ..mcbase.mcdetector import (Axis, RadialAxis, Detector, DetectorDefault, Total, Radial,
-                                 TotalPl, RadialPl,
-                                 Detectors)
+from ..mcbase.mcdetector import (Axis, RadialAxis, SymmetricAxis, Detector, DetectorDefault,
+                                 Total, Radial, TotalPl, RadialPl, Cartesian, CartesianPl,
+                                 SymmetricX, Detectors)

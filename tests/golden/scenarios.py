@@ -256,6 +256,40 @@ SCENARIOS = {
         detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), bottom=dict(type='Total')),
         fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='deposition'),
         nphotons=2000, streams=20, rnginit=71),
+    # Cartesian, CartesianPl and SymmetricX detectors (xopto/mcml/mcdetector/
+    # cartesian.py, cartesianpl.py, symmetric.py), oblique beam
+    'cartesian_detectors': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1e-3, n=1.4, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
+                dict(d=2e-3, n=1.35, mua=50.0, mus=5e3, pf=['Hg', 0.9]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line', position=(0.0, 0.0, 0.0), direction=(0.3, 0.0, 1.0)),
+        detectors=dict(top=dict(type='Cartesian', x=[-2e-3, 2e-3, 8], y=[-1e-3, 1.5e-3, 5], cosmin=0.2),
+                       bottom=dict(type='SymmetricX', axis=[2e-4, 3e-3, 6], logscale=True),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=73),
+    'cartesian_pl_symmetric': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1.5e-3, n=1.4, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='CartesianPl', x=[-2e-3, 2e-3, 6], y=[-2e-3, 2e-3, 4],
+                                plaxis=[0.0, 2e-2, 5]),
+                       bottom=dict(type='SymmetricX', axis=[0.0, 2e-3, 5])),
+        nphotons=3000, streams=32, rnginit=79),
+    'vox_cartesian': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='Line', position=(1e-4, 0.0, -1e-3), direction=(0.0, 0.0, 1.0)),
+        detectors=dict(top=dict(type='CartesianPl', x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 4],
+                                plaxis=[0.0, 1e-2, 4]),
+                       bottom=dict(type='SymmetricX', axis=[0.0, 1e-3, 4])),
+        nphotons=2000, streams=20, rnginit=83),
     # optical path-length resolved detectors (xopto/mcml/mcdetector/radialpl.py,
     # totalpl.py): two layers, RadialPl on top (linear path-length axis),
     # TotalPl below (log path-length axis)
@@ -372,6 +406,19 @@ def _detectors(pkg, spec):
             slots[slot] = pkg.mcdetector.TotalPl(_axis(pkg, {'axis': d['plaxis'],
                                                              'logscale': d.get('pllogscale', False)}),
                                                  cosmin=d.get('cosmin', 0.0))
+        elif d['type'] == 'Cartesian':
+            slots[slot] = pkg.mcdetector.Cartesian(_axis(pkg, {'axis': d['x']}), _axis(pkg, {'axis': d['y']}),
+                                                   cosmin=d.get('cosmin', 0.0))
+        elif d['type'] == 'CartesianPl':
+            slots[slot] = pkg.mcdetector.CartesianPl(
+                _axis(pkg, {'axis': d['x']}), _axis(pkg, {'axis': d['y']}),
+                _axis(pkg, {'axis': d['plaxis'], 'logscale': d.get('pllogscale', False)}),
+                cosmin=d.get('cosmin', 0.0))
+        elif d['type'] == 'SymmetricX':
+            center, rng, n_half = d['axis']
+            slots[slot] = pkg.mcdetector.SymmetricX(
+                pkg.mcdetector.SymmetricAxis(center, rng, n_half, logscale=d.get('logscale', False)),
+                cosmin=d.get('cosmin', 0.0))
         elif d['type'] == 'RadialPl':
             slots[slot] = pkg.mcdetector.RadialPl(
                 _axis(pkg, d), _axis(pkg, {'axis': d['plaxis'], 'logscale': d.get('pllogscale', False)}),
