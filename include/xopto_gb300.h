@@ -279,6 +279,42 @@ typedef struct McgbRunOptions {
     uint64_t packet_offset;                 /* DYNAMIC: index of packet 0      */
 } McgbRunOptions;
 
+/* Layout of the top or bottom sample surface (xopto/mcml/mcsurface): the
+   handler runs where a packet meets that surface and may change the
+   refractive index and critical cosine of the boundary or reflect the
+   packet itself.  The parameters are n floats of the float table
+   (McgbBuffers.fp_lut) from table_offset on:
+     LAMBERTIAN (lambertian.py:70-106): reflectance, specular fraction;
+     LINEAR_ARRAY (probe/lineararray.py:167-239,492-552): transformation (9),
+       probe position (2), first fibre position (2), fibre step (2), core r^2,
+       core n, core critical cosine, cladding r^2, cladding n, cladding
+       critical cosine, probe r^2, probe reflectivity, cutout transformation
+       (4), cutout half width, cutout half height, cutout n, cutout critical
+       cosine; n_fibers = fibres;
+     SIX_AROUND_ONE (probe/sixaroundone.py:158-262,495-545): transformation
+       (9), position (2), core spacing, core r^2, core n, core critical cosine,
+       cladding r^2, cladding n, cladding critical cosine, cutout r^2, cutout
+       n, cutout critical cosine, probe r^2, probe reflectivity;
+     FIBER_ARRAY (probe/fiberarray.py:136-187,330-390): probe position (2),
+       probe r^2, probe reflectivity, then per fibre: transformation (9),
+       position (2), cladding r^2, cladding n, cladding critical cosine, core
+       r^2, core n, core critical cosine; n_fibers = fibres. */
+enum {
+    MCGB_SURFACE_NONE = 0,
+    MCGB_SURFACE_LAMBERTIAN = 1,
+    MCGB_SURFACE_LINEAR_ARRAY = 2,
+    MCGB_SURFACE_SIX_AROUND_ONE = 3,
+    MCGB_SURFACE_FIBER_ARRAY = 4
+};
+#define MCGB_SURFACE_FIBER_FLOATS 17        /* floats per FIBER_ARRAY fibre    */
+
+typedef struct McgbSurface {
+    int32_t kind;                           /* MCGB_SURFACE_*                  */
+    uint32_t n_fibers;
+    uint32_t table_offset;                  /* first float in the float table  */
+    uint32_t table_size;                    /* floats                          */
+} McgbSurface;                              /* 16 bytes */
+
 /* Layered medium run (the reference's McKernel arguments for mcml). */
 typedef struct McgbMcmlConfig {
     uint64_t num_packets;
@@ -291,6 +327,7 @@ typedef struct McgbMcmlConfig {
     McgbDetector top, bottom, specular;
     McgbFluence fluence;
     McgbTrace trace;
+    McgbSurface surface_top, surface_bottom;
     McgbLayer layers[MCGB_MAX_LAYERS];
 } McgbMcmlConfig;
 
@@ -339,7 +376,8 @@ int mcgb_abi_version(void);
    (replaces the reference's sizeof_datatypes kernel).  kind: 0 McgbLayer,
    1 McgbSource, 2 McgbDetector, 3 McgbFluence, 4 McgbTrace, 5 McgbMaterial,
    6 McgbMcmlConfig, 7 McgbMcvoxConfig, 8 McgbBuffers, 9 McgbRunOptions,
-   10 McgbPf.  Returns -1 for an unknown kind. */
+   10 McgbPf, 11 McgbBatchSim, 12 McgbBatchConfig, 13 McgbSurface.  Returns -1
+   for an unknown kind. */
 int mcgb_sizeof(int kind);
 
 /* Number of streams (device threads) that fills every SM of the current

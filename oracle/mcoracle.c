@@ -523,14 +523,132 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
 }
 
 /* mcsim_boundary (mcml), xopto/mcml/kernel/mcml.template.c:80-203 */
-static uint32_t mcml_boundary(const McgbMcmlConfig *c, MlState *s, int32_t next,
-                              uint64_t *x, uint32_t a) {
+/* mc_transform_fpv3 of (x, y, 0), xopto/mcbase/kernel/mcbase.template.c:683-690 */
+static inline void ml_transform_xy(const float *T, float x, float y, float *ox, float *oy) {
+    *ox = T[0] * x + T[1] * y + T[2] * 0.0f;
+    *oy = T[3] * x + T[4] * y + T[5] * 0.0f;
+}
+
+static int ml_fiber_hit(const float *T, float x, float y, float core_r2, float core_n,
+                        float core_cc, float clad_r2, float clad_n, float clad_cc, float *n2,
+                        float *cc) {
+    float lx, ly;
+    ml_transform_xy(T, x, y, &lx, &ly);
+    float r2 = lx * lx + ly * ly;
+    if (r2 <= clad_r2) {
+        if (r2 <= core_r2) {
+            *n2 = core_n;
+            *cc = core_cc;
+        } else {
+            *n2 = clad_n;
+            *cc = clad_cc;
+        }
+        return 1;
+    }
+    return 0;
+}
+
+/* Surface layout handlers: LambertianReflector (xopto/mcml/mcsurface/lambertian.py:70-106),
+   LinearArray (probe/lineararray.py:167-239), SixAroundOne (probe/sixaroundone.py:158-262),
+   FiberArray (probe/fiberarray.py:136-187).  Returns 1 when the packet continues with the
+   boundary parameters n2, cc and 0 when the layout reflected it; the LinearArray probe tip
+   is tested around the last fibre (the loop's final relative position), as in the reference. */
+static int mcml_surface(int mm, const McgbSurface *sf, const float *lut, MlState *s, float *n2,
+                        float *cc, uint64_t *x, uint32_t a) {
+    const float *t = lut + sf->table_offset;
+    float px = s->pos.x, py = s->pos.y;
+    if (sf->kind == MCGB_SURFACE_LAMBERTIAN) {
+        if (rnd(x, a) > t[1]) {
+            float sin_fi, cos_fi;
+            float sin_theta = sqrtf(rnd(x, a));
+            float cos_theta = sqrtf(1.0f - sin_theta * sin_theta);
+            m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+            float z = (float)fsign(-s->dir.z) * cos_theta;
+            s->dir.x = cos_fi * sin_theta;
+            s->dir.y = sin_fi * sin_theta;
+            s->dir.z = z;
+        } else {
+            s->dir.z = -s->dir.z;
+        }
+        s->w = s->w * t[0];
+        return 0;
+    }
+    if (sf->kind == MCGB_SURFACE_LINEAR_ARRAY) {
+        float fx = t[11], fy = t[12], mx = 0.0f, my = 0.0f;
+        for (uint32_t i = 0; i < sf->n_fibers; ++i) {
+            mx = px - fx;
+            my = py - fy;
+            if (ml_fiber_hit(t, mx, my, t[15], t[16], t[17], t[18], t[19], t[20], n2, cc)) return 1;
+            fx += t[13];
+            fy += t[14];
+        }
+        float cx = px - t[9], cy = py - t[10];
+        /* mc_transform_fpv2, xopto/mcbase/kernel/mcbase.template.c:675-680 */
+        float ox = fabsf(t[23] * cx + t[24] * cy);
+        float oy = fabsf(t[25] * cx + t[26] * cy);
+        if (ox <= t[27] && oy < t[28]) {
+            *n2 = t[29];
+            *cc = t[30];
+            return 1;
+        }
+        if (mx * mx + my * my <= t[21]) {
+            s->dir.z = -s->dir.z;
+            s->w = s->w * t[22];
+            return 0;
+        }
+        return 1;
+    }
+    if (sf->kind == MCGB_SURFACE_SIX_AROUND_ONE) {
+        float rx = px - t[9], ry = py - t[10];
+        if (ml_fiber_hit(t, rx, ry, t[12], t[13], t[14], t[15], t[16], t[17], n2, cc)) return 1;
+        if (ml_fiber_hit(t, fabsf(rx) - t[11], ry, t[12], t[13], t[14], t[15], t[16], t[17], n2, cc))
+            return 1;
+        if (ml_fiber_hit(t, fabsf(rx) - t[11] * 0.5f, fabsf(ry) - t[11] * 0.8660254037844386f, t[12],
+                         t[13], t[14], t[15], t[16], t[17], n2, cc))
+            return 1;
+        float r2 = rx * rx + ry * ry;
+        if (r2 <= t[18]) {
+            *n2 = t[19];
+            *cc = t[20];
+            return 1;
+        }
+        if (r2 <= t[21]) {
+            s->dir.z = -s->dir.z;
+            s->w = s->w * t[22];
+            return 0;
+        }
+        return 1;
+    }
+    for (uint32_t i = 0; i < sf->n_fibers; ++i) {
+        const float *f = t + 4 + (size_t)i * MCGB_SURFACE_FIBER_FLOATS;
+        if (ml_fiber_hit(f, px - f[9], py - f[10], f[14], f[15], f[16], f[11], f[12], f[13], n2, cc))
+            return 1;
+    }
+    float dx = px - t[0], dy = py - t[1];
+    if (dx * dx + dy * dy <= t[2]) {
+        s->dir.z = -s->dir.z;
+        s->w = s->w * t[3];
+        return 0;
+    }
+    return 1;
+}
+
+static uint32_t mcml_boundary(int mm, const McgbMcmlConfig *c, const float *lut, MlState *s,
+                              int32_t next, uint64_t *x, uint32_t a) {
     float cc, cos1, sin1, cos2, sin2, n_cos1, n_cos2, n2, n1_d_n2, R, Rs, Rp;
     const McgbLayer *cur = &c->layers[s->layer];
     const McgbLayer *nxt = &c->layers[s->layer + fsign(s->dir.z)];
     cc = (s->dir.z < 0.0f) ? cur->cos_critical_top : cur->cos_critical_bottom;
     n2 = nxt->n;
-    if (cur->n == n2) {
+    /* surface layouts, xopto/mcml/kernel/mcml.template.c:104-124 */
+    int layout = 0;
+    int32_t last = (int32_t)c->num_layers - 1;
+    const McgbSurface *sf = (next == 0) ? &c->surface_top : &c->surface_bottom;
+    if ((next == 0 || next == last) && sf->kind != MCGB_SURFACE_NONE) {
+        layout = 1;
+        if (!mcml_surface(mm, sf, lut, s, &n2, &cc, x, a)) return EV_REFLECTION;
+    }
+    if (!layout && cur->n == n2) {
         s->layer = next;
         return EV_REFRACTION;
     }
@@ -637,7 +755,7 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                     fluence_deposit(&c->fluence, dp, deposit, L->mua, accu);
                 }
                 if (next != s.layer) {
-                    events |= mcml_boundary(c, &s, next, &x, a) | EV_BOUNDARY_HIT;
+                    events |= mcml_boundary(mm, c, lut, &s, next, &x, a) | EV_BOUNDARY_HIT;
                     if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
                         if (s.layer <= 0)
                             detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
@@ -660,7 +778,7 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                 }
             } else {
                 if (next != s.layer) {
-                    events |= mcml_boundary(c, &s, next, &x, a) | EV_BOUNDARY_HIT;
+                    events |= mcml_boundary(mm, c, lut, &s, next, &x, a) | EV_BOUNDARY_HIT;
                     if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
                         if (s.layer <= 0)
                             detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);

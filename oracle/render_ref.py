@@ -96,6 +96,7 @@ def reference_mc(name):
         obj = mc.Mc(layers, scenarios._source(mc.mcsource, s['source']),
                     scenarios._detectors(mc, s.get('detectors')),
                     fluence=scenarios._fluence(mc, s.get('fluence')),
+                    surface=scenarios._surface(mc, s.get('surface')),
                     options=scenarios.options(mc, s), rnginit=s['rnginit'])
     else:
         from xopto.mcvox import mc

@@ -84,11 +84,21 @@ class McgbRunOptions(C.Structure):
                 ('packet_offset', u64)]
 
 
+SURFACE_NONE, SURFACE_LAMBERTIAN, SURFACE_LINEAR_ARRAY = 0, 1, 2
+SURFACE_SIX_AROUND_ONE, SURFACE_FIBER_ARRAY = 3, 4
+SURFACE_FIBER_FLOATS = 17
+
+
+class McgbSurface(C.Structure):
+    _fields_ = [('kind', i32), ('n_fibers', u32), ('table_offset', u32), ('table_size', u32)]
+
+
 class McgbMcmlConfig(C.Structure):
     _fields_ = [('num_packets', u64), ('num_streams', u32), ('pf_kind', i32),
                 ('num_layers', u32), ('reserved', u32), ('opt', McgbRunOptions),
                 ('source', McgbSource), ('top', McgbDetector), ('bottom', McgbDetector),
                 ('specular', McgbDetector), ('fluence', McgbFluence), ('trace', McgbTrace),
+                ('surface_top', McgbSurface), ('surface_bottom', McgbSurface),
                 ('layers', McgbLayer * MAX_LAYERS)]
 
 
@@ -126,7 +136,7 @@ class McgbBatchConfig(C.Structure):
 
 SIZEOF_KINDS = [McgbLayer, McgbSource, McgbDetector, McgbFluence, McgbTrace,
                 McgbMaterial, McgbMcmlConfig, McgbMcvoxConfig, McgbBuffers,
-                McgbRunOptions, McgbPf, McgbBatchSim, McgbBatchConfig]
+                McgbRunOptions, McgbPf, McgbBatchSim, McgbBatchConfig, McgbSurface]
 
 
 def check_layout(sizeof_fn):

@@ -21,10 +21,14 @@ NVCC_COMMON = ARCH + ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC',
 
 # (source, extra flags); exact-math units must not contract a*b+c into FMA.
 UNITS = [
-    ('transport_exact_mcml.cu', ['-fmad=false']),
-    ('transport_exact_mcvox.cu', ['-fmad=false']),
-    ('transport_fast_mcml.cu', ['-use_fast_math']),
-    ('transport_fast_mcvox.cu', ['-use_fast_math']),
+    ('transport_exact_mcml_static.cu', ['-fmad=false']),
+    ('transport_exact_mcml_dynamic.cu', ['-fmad=false']),
+    ('transport_exact_mcvox_static.cu', ['-fmad=false']),
+    ('transport_exact_mcvox_dynamic.cu', ['-fmad=false']),
+    ('transport_fast_mcml_static.cu', ['-use_fast_math']),
+    ('transport_fast_mcml_dynamic.cu', ['-use_fast_math']),
+    ('transport_fast_mcvox_static.cu', ['-use_fast_math']),
+    ('transport_fast_mcvox_dynamic.cu', ['-use_fast_math']),
     ('capi.cu', []),
     ('batched.cu', ['-use_fast_math']),
     ('batched_exact.cu', ['-fmad=false']),

@@ -53,6 +53,34 @@ int check_pf(int kind, const McgbPf &pf, const McgbBuffers *b, const char *who, 
     return MCGB_OK;
 }
 
+/* Floats that a surface layout of kind/n_fibers needs in the float table. */
+uint64_t surface_floats(int kind, uint32_t n_fibers) {
+    switch (kind) {
+        case MCGB_SURFACE_LAMBERTIAN: return 2;
+        case MCGB_SURFACE_LINEAR_ARRAY: return 31;
+        case MCGB_SURFACE_SIX_AROUND_ONE: return 23;
+        case MCGB_SURFACE_FIBER_ARRAY: return 4 + (uint64_t)MCGB_SURFACE_FIBER_FLOATS * n_fibers;
+        default: return 0;
+    }
+}
+
+int check_surface(const McgbSurface &sf, const McgbBuffers *b, const char *where) {
+    if (sf.kind == MCGB_SURFACE_NONE) return MCGB_OK;
+    if (sf.kind < MCGB_SURFACE_LAMBERTIAN || sf.kind > MCGB_SURFACE_FIBER_ARRAY)
+        return fail(MCGB_E_INVALID, "%s surface layout: unknown kind %d", where, sf.kind);
+    if ((sf.kind == MCGB_SURFACE_LINEAR_ARRAY || sf.kind == MCGB_SURFACE_FIBER_ARRAY) &&
+        (sf.n_fibers == 0 || sf.n_fibers > 4096))
+        return fail(MCGB_E_INVALID, "%s surface layout: %u fibres outside [1, 4096]", where, sf.n_fibers);
+    uint64_t need = surface_floats(sf.kind, sf.n_fibers);
+    if (sf.table_size < need)
+        return fail(MCGB_E_SIZE, "%s surface layout: table of %u floats, %llu needed", where, sf.table_size,
+                    (unsigned long long)need);
+    if (!b->fp_lut || !range_ok(sf.table_offset, sf.table_size, b->fp_lut_size))
+        return fail(MCGB_E_SIZE, "%s surface layout: table [%u, +%u) beyond the float table (%llu)", where,
+                    sf.table_offset, sf.table_size, (unsigned long long)b->fp_lut_size);
+    return MCGB_OK;
+}
+
 int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uint32_t num_streams,
                  const McgbSource &src, const McgbDetector *dets, const McgbFluence &fl,
                  const McgbTrace &tr, const McgbBuffers *b) {
@@ -218,6 +246,7 @@ int mcgb_sizeof(int kind) {
         case 10: return (int)sizeof(McgbPf);
         case 11: return (int)sizeof(McgbBatchSim);
         case 12: return (int)sizeof(McgbBatchConfig);
+        case 13: return (int)sizeof(McgbSurface);
         default: return -1;
     }
 }
@@ -261,6 +290,10 @@ int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *strea
         r = check_pf(cfg->pf_kind, cfg->layers[i].pf, buf, "layer", i);
         if (r) return r;
     }
+    r = check_surface(cfg->surface_top, buf, "top");
+    if (r) return r;
+    r = check_surface(cfg->surface_bottom, buf, "bottom");
+    if (r) return r;
     if (cfg->num_packets == 0) return MCGB_OK;
     LaunchShape s;
     r = make_shape(0, cfg->opt.math, cfg->opt.block_size, cfg->num_streams, buf, cfg->opt.deadline_s, &s);

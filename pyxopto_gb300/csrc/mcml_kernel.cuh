@@ -193,13 +193,15 @@ static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c
 }
 
 /* Packet launch: Line (xopto/mcml/mcsource/line.py:95-108) or any other
-   source (mcml_launch_other).  Everything stays inline: an out-of-line call
-   measured slower on the layered workloads. */
+   source (mcml_launch_other).  SIMPLE kernels are compiled for the Line
+   source only, which keeps the packet loop compact; everything stays inline
+   (an out-of-line call measured slower). */
+template <bool SIMPLE>
 static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
                                                    Rng &rng, f3 &pos, f3 &dir, float &w,
                                                    int &layer, uint64_t *accu) {
     const McgbSource &src = c.source;
-    if (src.kind == MCGB_SRC_LINE) {
+    if (SIMPLE || src.kind == MCGB_SRC_LINE) {
         w = 1.0f - src.reflectance;
         pos = f3{src.position[0], src.position[1], src.position[2]};
         dir = f3{src.direction[0], src.direction[1], src.direction[2]};
@@ -213,16 +215,125 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
     }
 }
 
-/* mcsim_boundary (mcml), xopto/mcml/kernel/mcml.template.c:80-203 */
-static __device__ __forceinline__ uint32_t mcml_boundary(const MlLayer *L, int &layer, int next,
-                                                         f3 &dir, Rng &rng) {
-    float cc = (dir.z < 0.0f) ? L[layer].g1.w : L[layer].g2.x;
-    float n1 = L[layer].g1.x;
-    float n2 = L[layer + fsign(dir.z)].g1.x;
-    if (n1 == n2) {
-        layer = next;
-        return MCGB_EV_REFRACTION;
+/* 3x3 transformation of a point with z = 0 (mc_transform_fpv3,
+   xopto/mcbase/kernel/mcbase.template.c:683-690; the z term is kept so the
+   float operations match). */
+static __device__ __forceinline__ float2 ml_transform_xy(const float *T, float x, float y) {
+    return make_float2(T[0] * x + T[1] * y + T[2] * 0.0f, T[3] * x + T[4] * y + T[5] * 0.0f);
+}
+
+/* One fibre of a probe layout: core or cladding under the point (x, y)
+   relative to the fibre centre, in the fibre's transformed frame. */
+static __device__ __forceinline__ bool ml_fiber_hit(const float *T, float x, float y, float core_r2,
+                                                    float core_n, float core_cc, float clad_r2,
+                                                    float clad_n, float clad_cc, float &n2, float &cc,
+                                                    float *r2_out = nullptr) {
+    float2 lp = ml_transform_xy(T, x, y);
+    float r2 = lp.x * lp.x + lp.y * lp.y;
+    if (r2_out) *r2_out = r2;
+    if (r2 <= clad_r2) {
+        if (r2 <= core_r2) {
+            n2 = core_n;
+            cc = core_cc;
+        } else {
+            n2 = clad_n;
+            cc = clad_cc;
+        }
+        return true;
     }
+    return false;
+}
+
+/* Surface layout handler (mcsim_top/bottom_surface_layout_handler):
+   LambertianReflector (xopto/mcml/mcsurface/lambertian.py:70-106),
+   LinearArray (probe/lineararray.py:167-239), SixAroundOne
+   (probe/sixaroundone.py:158-262) and FiberArray (probe/fiberarray.py:
+   136-187).  Returns true when the packet continues with the boundary
+   parameters n2, cc (possibly changed), false when the layout reflected it.
+   As in the reference, the LinearArray probe tip is tested around the last
+   fibre of the array (the loop's final relative position). */
+static __device__ __forceinline__ bool mcml_surface(const McgbSurface &sf, const float *lut, f3 &dir,
+                                                    float &w, float px, float py, float &n2,
+                                                    float &cc, Rng &rng) {
+    const float *t = lut + sf.table_offset;
+    if (sf.kind == MCGB_SURFACE_LAMBERTIAN) {
+        if (rng.next() > t[1]) {
+            float sin_fi, cos_fi;
+            float sin_theta = mc_sqrt(rng.next());
+            float cos_theta = mc_sqrt(1.0f - sin_theta * sin_theta);
+            mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+            float z = (float)fsign(-dir.z) * cos_theta;
+            dir = f3{cos_fi * sin_theta, sin_fi * sin_theta, z};
+        } else {
+            dir.z = -dir.z;
+        }
+        w = w * t[0];
+        return false;
+    }
+    if (sf.kind == MCGB_SURFACE_LINEAR_ARRAY) {
+        float fx = t[11], fy = t[12], mx = 0.0f, my = 0.0f;
+        for (uint32_t i = 0; i < sf.n_fibers; ++i) {
+            mx = px - fx;
+            my = py - fy;
+            if (ml_fiber_hit(t, mx, my, t[15], t[16], t[17], t[18], t[19], t[20], n2, cc)) return true;
+            fx += t[13];
+            fy += t[14];
+        }
+        float cx = px - t[9], cy = py - t[10];
+        float ox = fabsf(t[23] * cx + t[24] * cy);
+        float oy = fabsf(t[25] * cx + t[26] * cy);
+        if (ox <= t[27] && oy < t[28]) {
+            n2 = t[29];
+            cc = t[30];
+            return true;
+        }
+        if (mx * mx + my * my <= t[21]) {
+            dir.z = -dir.z;
+            w = w * t[22];
+            return false;
+        }
+        return true;
+    }
+    if (sf.kind == MCGB_SURFACE_SIX_AROUND_ONE) {
+        float rx = px - t[9], ry = py - t[10];
+        if (ml_fiber_hit(t, rx, ry, t[12], t[13], t[14], t[15], t[16], t[17], n2, cc)) return true;
+        if (ml_fiber_hit(t, fabsf(rx) - t[11], ry, t[12], t[13], t[14], t[15], t[16], t[17], n2, cc))
+            return true;
+        if (ml_fiber_hit(t, fabsf(rx) - t[11] * 0.5f, fabsf(ry) - t[11] * 0.8660254037844386f, t[12],
+                         t[13], t[14], t[15], t[16], t[17], n2, cc))
+            return true;
+        float r2 = rx * rx + ry * ry;
+        if (r2 <= t[18]) {
+            n2 = t[19];
+            cc = t[20];
+            return true;
+        }
+        if (r2 <= t[21]) {
+            dir.z = -dir.z;
+            w = w * t[22];
+            return false;
+        }
+        return true;
+    }
+    /* FIBER_ARRAY */
+    for (uint32_t i = 0; i < sf.n_fibers; ++i) {
+        const float *f = t + 4 + (size_t)i * MCGB_SURFACE_FIBER_FLOATS;
+        if (ml_fiber_hit(f, px - f[9], py - f[10], f[14], f[15], f[16], f[11], f[12], f[13], n2, cc))
+            return true;
+    }
+    float dx = px - t[0], dy = py - t[1];
+    if (dx * dx + dy * dy <= t[2]) {
+        dir.z = -dir.z;
+        w = w * t[3];
+        return false;
+    }
+    return true;
+}
+
+/* Reflect or refract at a layer boundary with Fresnel's equations, the
+   common part of mcsim_boundary (xopto/mcml/kernel/mcml.template.c:135-203). */
+static __device__ __forceinline__ uint32_t mcml_fresnel(int &layer, int next, float n1, float n2,
+                                                        float cc, f3 &dir, Rng &rng) {
     dir.z = -dir.z;
     float cos1 = fabsf(dir.z);
     if (cos1 > cc) {
@@ -257,6 +368,46 @@ static __device__ __forceinline__ uint32_t mcml_boundary(const MlLayer *L, int &
         }
     }
     return MCGB_EV_REFLECTION;
+}
+
+/* mcsim_boundary (mcml), xopto/mcml/kernel/mcml.template.c:80-203.  With
+   XTRA the top and bottom surface layouts get the boundary first
+   (mcml.template.c:104-124); a layout that lets the packet continue also
+   skips the matched-index shortcut, as in the reference. */
+template <bool XTRA>
+static __device__ __forceinline__ uint32_t mcml_boundary(const McgbMcmlConfig &c, const float *lut,
+                                                         const MlLayer *L, int &layer, int next,
+                                                         int last, const f3 &pos, f3 &dir, float &w,
+                                                         Rng &rng) {
+    float cc = (dir.z < 0.0f) ? L[layer].g1.w : L[layer].g2.x;
+    float n1 = L[layer].g1.x;
+    float n2 = L[layer + fsign(dir.z)].g1.x;
+    bool layout = false;
+    if (XTRA) {
+        const McgbSurface &sf = (next == 0) ? c.surface_top : c.surface_bottom;
+        if ((next == 0 || next == last) && sf.kind != MCGB_SURFACE_NONE) {
+            layout = true;
+            if (!mcml_surface(sf, lut, dir, w, pos.x, pos.y, n2, cc, rng)) return MCGB_EV_REFLECTION;
+        }
+    }
+    if (!layout && n1 == n2) {
+        layer = next;
+        return MCGB_EV_REFRACTION;
+    }
+    return mcml_fresnel(layer, next, n1, n2, cc, dir, rng);
+}
+
+/* mcsim_boundary without surface layouts (the batched engine). */
+static __device__ __forceinline__ uint32_t mcml_boundary(const MlLayer *L, int &layer, int next,
+                                                         f3 &dir, Rng &rng) {
+    float cc = (dir.z < 0.0f) ? L[layer].g1.w : L[layer].g2.x;
+    float n1 = L[layer].g1.x;
+    float n2 = L[layer + fsign(dir.z)].g1.x;
+    if (n1 == n2) {
+        layer = next;
+        return MCGB_EV_REFRACTION;
+    }
+    return mcml_fresnel(layer, next, n1, n2, cc, dir, rng);
 }
 
 /* Per-thread constants of a run. */
@@ -296,6 +447,7 @@ static __device__ __forceinline__ MlCtx mcml_ctx(const McgbMcmlConfig &c, const 
     return x;
 }
 
+template <bool SIMPLE>
 static __device__ __forceinline__ void mcml_begin(const McgbMcmlConfig &c, const McgbBuffers &b,
                                                   const MlCtx &x, MlPacket &s, Rng &rng, uint64_t p) {
     s.p = p;
@@ -303,7 +455,7 @@ static __device__ __forceinline__ void mcml_begin(const McgbMcmlConfig &c, const
     s.trace_count = 0;
     s.steps = 0;
     s.events = MCGB_EV_LAUNCH;
-    mcml_launch(c, x.L, rng, s.pos, s.dir, s.w, s.layer, b.accumulator);
+    mcml_launch<SIMPLE>(c, x.L, rng, s.pos, s.dir, s.w, s.layer, b.accumulator);
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -365,7 +517,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             fluence_deposit(c.fluence, dp, deposit, mua, fcache);
         }
         if (next != s.layer) {
-            { uint32_t ev = mcml_boundary(L, s.layer, next, s.dir, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
+            { uint32_t ev = mcml_boundary<XTRA>(c, x.lut, L, s.layer, next, x.last_layer, s.pos, s.dir, s.w, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
             if (!(s.layer > 0 && s.layer < x.last_layer)) {
                 if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
                 else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
@@ -386,7 +538,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             }
         }
     } else if (next != s.layer) {
-        { uint32_t ev = mcml_boundary(L, s.layer, next, s.dir, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
+        { uint32_t ev = mcml_boundary<XTRA>(c, x.lut, L, s.layer, next, x.last_layer, s.pos, s.dir, s.w, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
         if (!(s.layer > 0 && s.layer < x.last_layer)) {
             if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
             else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
@@ -491,7 +643,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
     uint64_t steps = 0, packets = 0;
     uint32_t iter = 0, status = 0;
     MlPacket s;
-    mcml_begin(c, b, x, s, rng, t);
+    mcml_begin<false>(c, b, x, s, rng, t);
     for (;;) {
         if (mcml_step<PF, METHOD, FLU, true>(c, b, x, s, rng, fcache, status)) {
             ++packets;
@@ -502,7 +654,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
                 s.steps = 0;
                 break;
             }
-            mcml_begin(c, b, x, s, rng, p);
+            mcml_begin<false>(c, b, x, s, rng, p);
         }
         if (((++iter) & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
@@ -520,7 +672,7 @@ mcml_transport_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffer
 /* DYNAMIC scheduling: persistent warps refill idle lanes packet by packet
    from the queue counters[MCGB_CNT_QUEUE]; packet p runs on the stream of
    (seed, packet_offset + p). */
-template <int PF, int METHOD, bool FLU, bool XTRA>
+template <int PF, int METHOD, bool FLU, bool XTRA, bool SIMPLE>
 __global__ void __launch_bounds__(128)
 mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers b,
                     uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
@@ -564,7 +716,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
                 uint32_t as;
                 br_packet_stream(c.opt.seed, 0u, c.opt.packet_offset + p, b.rng_a, c.num_streams, &xs, &as);
                 rng = Rng{xs, as};
-                mcml_begin(c, b, x, s, rng, p);
+                mcml_begin<SIMPLE>(c, b, x, s, rng, p);
                 active = true;
             }
             uint32_t taken = __ballot_sync(MCGB_FULL_MASK, mine);
@@ -572,14 +724,18 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
             need &= ~taken;
         }
         if (!__any_sync(MCGB_FULL_MASK, active)) break;
-        if (active && mcml_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
-            ++packets;
-            steps += s.steps;
-            s.steps = 0;
-            mcml_end(c, b, x, s);
-            active = false;
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            if (active && mcml_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
+                ++packets;
+                steps += s.steps;
+                s.steps = 0;
+                mcml_end(c, b, x, s);
+                active = false;
+            }
         }
-        if (((++iter) & 1023u) == 0) {
+        iter += 4;
+        if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {
                 if (globaltimer_ns() > t_deadline) stop = MCGB_STATUS_TIMEOUT;

@@ -134,6 +134,7 @@ static __device__ __forceinline__ void mv_beam_enter(const McgbMcvoxConfig &c, c
    IsotropicPoint (point.py:74-140), UniformFiber / LambertianFiber
    (fiber.py:257-352,603-700) and IsotropicVoxel (voxel.py:78-107); then the
    voxel index of the launch position (mcvox.template.c:240-262). */
+template <bool SIMPLE>
 static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, const MvGeom &g,
                                                     const MvMaterial *M, const uint8_t *vox,
                                                     Rng &rng, f3 &pos, f3 &dir, float &w, i3 &vi,
@@ -148,10 +149,10 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
             f3 d{src.direction_reflected[0], src.direction_reflected[1], src.direction_reflected[2]};
             detector_deposit(c.specular, pos, d, src.reflectance, 0.0f, accu);
         }
-    } else if (src.kind == MCGB_SRC_GAUSSIAN_BEAM || src.kind == MCGB_SRC_UNIFORM_BEAM) {
+    } else if (SIMPLE || src.kind == MCGB_SRC_GAUSSIAN_BEAM || src.kind == MCGB_SRC_UNIFORM_BEAM) {
         float sin_fi, cos_fi;
         f3 ps;
-        if (src.kind == MCGB_SRC_GAUSSIAN_BEAM) {
+        if (SIMPLE || src.kind == MCGB_SRC_GAUSSIAN_BEAM) {
             float r = mc_sqrt(-2.0f * mc_log(1.0f - rng.next()));
             r = fminf(r, src.clip);
             mc_sincos(6.28318548f * rng.next(), &sin_fi, &cos_fi);
@@ -347,6 +348,7 @@ static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, cons
     return x;
 }
 
+template <bool SIMPLE>
 static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                    const MvCtx &x, MvPacket &s, Rng &rng, uint64_t p,
                                                    f3 prev_pos) {
@@ -355,7 +357,8 @@ static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, con
     s.trace_count = 0;
     s.steps = 0;
     s.events = MCGB_EV_LAUNCH;
-    mcvox_launch(c, x.g, x.M, x.vox, rng, s.pos, s.dir, s.w, s.vi, s.mat, b.accumulator, prev_pos);
+    mcvox_launch<SIMPLE>(c, x.g, x.M, x.vox, rng, s.pos, s.dir, s.w, s.vi, s.mat, b.accumulator,
+                         prev_pos);
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -536,7 +539,7 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
     uint32_t iter = 0, status = 0;
     MvPacket s;
     s.pos = f3{0.0f, 0.0f, 0.0f};
-    mcvox_begin(c, b, x, s, rng, t, s.pos);
+    mcvox_begin<false>(c, b, x, s, rng, t, s.pos);
     for (;;) {
         if (mcvox_step<PF, METHOD, FLU, true>(c, b, x, s, rng, fcache, status)) {
             ++packets;
@@ -547,7 +550,7 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
                 s.steps = 0;
                 break;
             }
-            mcvox_begin(c, b, x, s, rng, p, s.pos);
+            mcvox_begin<false>(c, b, x, s, rng, p, s.pos);
         }
         if (((++iter) & 1023u) == 0) {
             if (globaltimer_ns() > t_deadline) { status |= MCGB_STATUS_TIMEOUT; break; }
@@ -561,11 +564,8 @@ mcvox_transport_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuff
 }
 
 /* DYNAMIC scheduling (per-packet streams, warp refill). */
-/* 128-thread blocks, at least 9 resident per SM (at most 56 registers):
-   the launch code of the less common sources would otherwise raise the
-   register count and cut the resident warps. */
-template <int PF, int METHOD, bool FLU, bool XTRA>
-__global__ void __launch_bounds__(128, 9)
+template <int PF, int METHOD, bool FLU, bool XTRA, bool SIMPLE>
+__global__ void __launch_bounds__(128)
 mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffers b,
                      uint64_t deadline_ns, int lut_in_smem, uint32_t packets_per_item) {
     __shared__ MvSmem sm;
@@ -608,7 +608,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                 uint32_t as;
                 br_packet_stream(c.opt.seed, 0u, c.opt.packet_offset + p, b.rng_a, c.num_streams, &xs, &as);
                 rng = Rng{xs, as};
-                mcvox_begin(c, b, x, s, rng, p, f3{0.0f, 0.0f, 0.0f});
+                mcvox_begin<SIMPLE>(c, b, x, s, rng, p, f3{0.0f, 0.0f, 0.0f});
                 active = true;
             }
             uint32_t taken = __ballot_sync(0xffffffffu, mine);
@@ -616,14 +616,18 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
             need &= ~taken;
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
-            ++packets;
-            steps += s.steps;
-            s.steps = 0;
-            mcvox_end(c, b, x, s);
-            active = false;
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
+                ++packets;
+                steps += s.steps;
+                s.steps = 0;
+                mcvox_end(c, b, x, s);
+                active = false;
+            }
         }
-        if (((++iter) & 1023u) == 0) {
+        iter += 4;
+        if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {
                 if (globaltimer_ns() > t_deadline) stop = MCGB_STATUS_TIMEOUT;

@@ -1,0 +1,11 @@
+/*
+ * transport_exact_mcvox_static.cu - Voxelized-medium transport kernels, static scheduling, in
+ * EXACT math: IEEE arithmetic without FMA contraction (built with -fmad=false) and the
+ * portable log/exp/sincos/powr routines; bit-identical to a CPU evaluation of the same
+ * algorithm.
+ */
+#define MCGB_FAST_MATH 0
+#define MCGB_NS mcgb_exact
+#define MCGB_MEDIUM 1
+#define MCGB_PART 0
+#include "transport_tu.cuh"

@@ -1,8 +1,10 @@
 /*
- * transport_tu.cuh - kernel table and launcher of one medium in one math
- * mode.  Included by the four translation units transport_{exact,fast}_
- * {mcml,mcvox}.cu, which define MCGB_FAST_MATH, MCGB_NS and MCGB_MEDIUM
- * (0 layered, 1 voxelized), so that the kernel variants compile in parallel.
+ * transport_tu.cuh - kernel tables and launcher of one medium in one math
+ * mode.  Included by the eight translation units
+ * transport_{exact,fast}_{mcml,mcvox}_{static,dynamic}.cu, which define
+ * MCGB_FAST_MATH, MCGB_NS, MCGB_MEDIUM (0 layered, 1 voxelized) and
+ * MCGB_PART (0 the static-scheduling kernels, 1 the dynamic-scheduling
+ * kernels and the launcher), so that the kernel variants compile in parallel.
  */
 #pragma once
 #include <cuda_runtime.h>
@@ -15,6 +17,7 @@
 #define MCGB_CFG McgbMcmlConfig
 #define MCGB_LAUNCH launch_mcml
 #define MCGB_OCCUPANCY occupancy_mcml
+#define MCGB_SELECT_STATIC select_static_mcml
 #else
 #include "mcvox_kernel.cuh"
 #define MCGB_STATIC_KERNEL mcvox_transport_kernel
@@ -22,25 +25,51 @@
 #define MCGB_CFG McgbMcvoxConfig
 #define MCGB_LAUNCH launch_mcvox
 #define MCGB_OCCUPANCY occupancy_mcvox
+#define MCGB_SELECT_STATIC select_static_mcvox
 #endif
 
 namespace MCGB_NS {
 
-/* Kernel variants: scheduling x phase function x method x fluence x
-   optional features (trace, optical path length, per-packet step limit).
-   The static kernels always carry the optional features. */
-#define MCGB_VS(K, PF, M, F) {(const void *)K<PF, M, F>, (const void *)K<PF, M, F>}
-#define MCGB_VD(K, PF, M, F) {(const void *)K<PF, M, F, false>, (const void *)K<PF, M, F, true>}
-#define MCGB_F(V, K, PF, M) {V(K, PF, M, false), V(K, PF, M, true)}
-#define MCGB_METHODS(V, K, PF) {MCGB_F(V, K, PF, 0), MCGB_F(V, K, PF, 1), MCGB_F(V, K, PF, 2)}
+#define MCGB_METHODS(V, K, PF) {V(K, PF, 0), V(K, PF, 1), V(K, PF, 2)}
 #define MCGB_TABLE(V, K) {MCGB_METHODS(V, K, 0), MCGB_METHODS(V, K, 1), MCGB_METHODS(V, K, 2)}
 
-static const void *const kTable[2][3][3][2][2] = {MCGB_TABLE(MCGB_VS, MCGB_STATIC_KERNEL),
-                                                  MCGB_TABLE(MCGB_VD, MCGB_DYNAMIC_KERNEL)};
+/* Static scheduling kernels: phase function x method x fluence; they carry
+   every optional feature and every source. */
+const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence);
 
-static const void *select(int sched, int pf, int method, bool fluence, bool xtra) {
+#if MCGB_PART == 0
+
+#define MCGB_VS(K, PF, M) {(const void *)K<PF, M, false>, (const void *)K<PF, M, true>}
+static const void *const kStatic[3][3][2] = MCGB_TABLE(MCGB_VS, MCGB_STATIC_KERNEL);
+
+const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence) {
+    if (pf < 0 || pf > 2 || method < 0 || method > 2) return nullptr;
+    return kStatic[pf][method][fluence ? 1 : 0];
+}
+
+#else
+
+/* Dynamic scheduling kernels: phase function x method x fluence x optional
+   features (trace, optical path length, per-packet step limit) x simple
+   source (the common sources only: Line in layered media, Line and
+   GaussianBeam in voxelized media). */
+#define MCGB_VX(K, PF, M, F) {{(const void *)K<PF, M, F, false, false>, (const void *)K<PF, M, F, false, true>}, \
+                              {(const void *)K<PF, M, F, true, false>, (const void *)K<PF, M, F, true, true>}}
+#define MCGB_VD(K, PF, M) {MCGB_VX(K, PF, M, false), MCGB_VX(K, PF, M, true)}
+static const void *const kDynamic[3][3][2][2][2] = MCGB_TABLE(MCGB_VD, MCGB_DYNAMIC_KERNEL);
+
+static const void *select(int sched, int pf, int method, bool fluence, bool xtra, bool simple) {
     if (pf < 0 || pf > 2 || method < 0 || method > 2 || sched < 0 || sched > 1) return nullptr;
-    return kTable[sched][pf][method][fluence ? 1 : 0][xtra ? 1 : 0];
+    if (sched == MCGB_SCHED_STATIC) return MCGB_SELECT_STATIC(pf, method, fluence);
+    return kDynamic[pf][method][fluence ? 1 : 0][xtra ? 1 : 0][simple ? 1 : 0];
+}
+
+static bool simple_source(int kind) {
+#if MCGB_MEDIUM == 0
+    return kind == MCGB_SRC_LINE;
+#else
+    return kind == MCGB_SRC_LINE || kind == MCGB_SRC_GAUSSIAN_BEAM;
+#endif
 }
 
 /* Resident blocks per SM of a kernel variant for a block size, queried once
@@ -72,10 +101,14 @@ static cudaError_t resident_blocks(const void *k, int block, size_t dyn_smem, in
 cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_t stream,
                         const LaunchShape &shape) {
     const int sched = cfg.opt.scheduling;
-    const bool xtra = cfg.trace.flags != MCGB_TRACE_NONE || cfg.opt.track_optical_pathlength != 0 ||
-                      cfg.opt.max_steps_per_packet != 0;
+    bool xtra = cfg.trace.flags != MCGB_TRACE_NONE || cfg.opt.track_optical_pathlength != 0 ||
+                cfg.opt.max_steps_per_packet != 0;
+#if MCGB_MEDIUM == 0
+    xtra = xtra || cfg.surface_top.kind != MCGB_SURFACE_NONE ||
+           cfg.surface_bottom.kind != MCGB_SURFACE_NONE;
+#endif
     const void *k = select(sched, cfg.pf_kind, cfg.opt.method, cfg.fluence.kind != MCGB_FLUENCE_NONE,
-                           xtra);
+                           xtra, simple_source(cfg.source.kind));
     if (!k) return cudaErrorInvalidValue;
     if (shape.dyn_smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -119,13 +152,14 @@ cudaError_t MCGB_OCCUPANCY(int block, size_t dyn_smem, int *blocks_per_sm) {
         for (int m = 0; m < 3; ++m)
             for (int fl = 0; fl < 2; ++fl) {
                 int n = 0;
-                cudaError_t e = resident_blocks(select(MCGB_SCHED_STATIC, pf, m, fl != 0, true), block,
-                                                dyn_smem, &n);
+                cudaError_t e = resident_blocks(MCGB_SELECT_STATIC(pf, m, fl != 0), block, dyn_smem, &n);
                 if (e != cudaSuccess) return e;
                 best = n < best ? n : best;
             }
     *blocks_per_sm = best;
     return cudaSuccess;
 }
+
+#endif
 
 }  // namespace MCGB_NS

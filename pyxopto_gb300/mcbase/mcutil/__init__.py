@@ -126,6 +126,19 @@ class SymmetricAxis:
     __repr__ = __str__
 
 
+def rotation_matrix_2d(a, b) -> np.ndarray:
+    """2-D rotation matrix taking the direction of a onto the direction of b
+    (xopto/mcbase/mcutil/geometry.py:33-59; the sine is taken as
+    non-negative, as there)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    b = b / np.linalg.norm(b)
+    cos_theta = np.dot(a, b)
+    sin_theta = np.sqrt(1.0 - cos_theta ** 2)
+    return np.array([[cos_theta, -sin_theta], [sin_theta, cos_theta]])
+
+
 def cos_critical(n1: float, n2: float) -> float:
     """Cosine of the critical incidence angle at the n1 -> n2 boundary
     (xopto/mcbase/mcutil/boundary.py:25-41)."""

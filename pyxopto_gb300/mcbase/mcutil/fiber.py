@@ -1,4 +1,7 @@
-"""Optical fibre parameters (xopto/mcbase/mcutil/fiber.py:38-224, MultimodeFiber)."""
+"""Optical fibre parameters (xopto/mcbase/mcutil/fiber.py:38-224,
+MultimodeFiber) and the placement of a fibre in a probe (fiber.py:381-470,
+FiberLayout)."""
+import numpy as np
 
 
 class MultimodeFiber:
@@ -57,5 +60,43 @@ class MultimodeFiber:
     def __str__(self):
         return 'MultimodeFiber(dcore={}, dcladding={}, ncore={}, na={})'.format(
             self._dcore, self._dcladding, self._ncore, self._na)
+
+    __repr__ = __str__
+
+
+class FiberLayout:
+    """A fibre of a probe: the fibre, the position of its tip centre and its
+    direction (xopto/mcbase/mcutil/fiber.py:381-470)."""
+
+    def __init__(self, fiber, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0)):
+        if isinstance(fiber, FiberLayout):
+            fiber, position, direction = fiber.fiber, fiber.position, fiber.direction
+        self._fiber = fiber
+        self._position = np.zeros((3,))
+        self._direction = np.array((0.0, 0.0, 1.0))
+        self.position = position
+        self.direction = direction
+
+    def _set_position(self, p):
+        self._position[:] = p
+
+    def _set_direction(self, d):
+        self._direction[:] = d
+        n = np.linalg.norm(self._direction)
+        if n == 0.0:
+            raise ValueError('Fiber direction vector norm/length must not be 0!')
+        self._direction *= 1.0 / n
+
+    fiber = property(lambda self: self._fiber)
+    position = property(lambda self: self._position, _set_position)
+    direction = property(lambda self: self._direction, _set_direction)
+
+    def todict(self):
+        return {'type': 'FiberLayout', 'fiber': self._fiber.todict(),
+                'position': self._position.tolist(), 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'FiberLayout(fiber={}, position=({}, {}, {}), direction=({}, {}, {}))'.format(
+            self._fiber, *self._position, *self._direction)
 
     __repr__ = __str__

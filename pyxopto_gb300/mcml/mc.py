@@ -21,7 +21,8 @@ import numpy as np
 from .. import _abi, _lib
 from .._engine import McEngine, torch_cuda
 from ..mcbase.mcutil import Axis, RadialAxis
-from . import mclayer, mcsource, mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes
+from . import (mclayer, mcsource, mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes,
+               mcsurface)
 
 MC_RESULT_TYPE = Tuple[mctrace.Trace, mcfluence.Fluence, mcdetector.Detectors]
 
@@ -33,8 +34,9 @@ class Mc(McEngine):
                  types=mctypes.McDataTypesSingle, options=None, rnginit=None,
                  cl_devices=None, cl_build_options=None, cl_profiling=False):
         super().__init__(options=options, rnginit=rnginit, types=types)
-        if surface is not None:
-            raise ValueError('Surface layouts are not supported by the GB300 kernels.')
+        if surface is not None and not isinstance(surface, mcsurface.SurfaceLayouts):
+            raise TypeError('surface must be a SurfaceLayouts instance')
+        self._surface = surface
         self._layers = mclayer.Layers(layers)
         self._layers.check()
         self._pf_type = type(self._layers[0].pf)
@@ -50,6 +52,7 @@ class Mc(McEngine):
     detectors = property(lambda self: self._detectors)
     trace = property(lambda self: self._trace)
     fluence = property(lambda self: self._fluence)
+    surface = property(lambda self: self._surface)
 
     def layer(self, index: int) -> mclayer.Layer:
         return self._layers[index]
@@ -85,6 +88,8 @@ class Mc(McEngine):
             self._detectors.pack(self, cfg)
         if self._fluence is not None:
             self._fluence.pack(self, cfg.fluence)
+        if self._surface is not None:
+            self._surface.pack(self, cfg)
         track_opl = self._detectors is not None and self._detectors.tracks_pathlength()
         if self._trace is not None:
             self._trace.pack(self, cfg.trace, int(nphotons))

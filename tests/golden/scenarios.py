@@ -290,6 +290,48 @@ SCENARIOS = {
                                 plaxis=[0.0, 1e-2, 4]),
                        bottom=dict(type='SymmetricX', axis=[0.0, 1e-3, 4])),
         nphotons=2000, streams=20, rnginit=83),
+    # surface layouts (xopto/mcml/mcsurface): Lambertian reflector below, a
+    # linear fibre-array probe face on top (tilted fibres, cutout, metal face)
+    'surface_lambertian_linear': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1e-3, n=1.4, mua=100.0, mus=1.5e4, pf=['Hg', 0.85]),
+                _air(['Hg', 0.0])],
+        source=dict(type='UniformFiber', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22), position=(-5e-4, 0.0, 0.0),
+                    direction=(0.1, 0.0, 1.0)),
+        surface=dict(top=dict(type='LinearArray', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22), n=4, spacing=2.5e-4,
+                              orientation=(1.0, 0.2), diameter=3e-3, reflectivity=0.6,
+                              cutout=(1.2e-3, 4e-4), cutoutn=1.6, position=(0.0, 0.0),
+                              direction=(0.1, 0.0, 1.0)),
+                     bottom=dict(type='LambertianReflector', reflectance=0.8, specular=0.3)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), bottom=dict(type='Total'),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=89),
+    'surface_six_around_one': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=2e-3, n=1.38, mua=80.0, mus=1.2e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='UniformFiber', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22)),
+        surface=dict(top=dict(type='SixAroundOne', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22), spacing=2.3e-4,
+                              diameter=2e-3, reflectivity=0.5, cutout=9e-4, cutoutn=1.5)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]), specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=97),
+    'surface_fiber_array': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1.5e-3, n=1.4, mua=100.0, mus=1.2e4, pf=['Hg', 0.85]),
+                dict(d=INF, n=1.33, mua=20.0, mus=8e3, pf=['Hg', 0.8])],
+        source=dict(type='Line'),
+        surface=dict(top=dict(type='FiberArray',
+                              fibers=[dict(fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22), position=(0.0, 0.0, 0.0),
+                                           direction=(0.0, 0.0, 1.0)),
+                                      dict(fiber=dict(dcore=400e-6, dcladding=440e-6, ncore=1.46,
+                                                      na=0.39), position=(5e-4, 1e-4, 0.0),
+                                           direction=(0.2, 0.1, 1.0))],
+                              diameter=2e-3, reflectivity=0.7, position=(1e-4, 0.0))),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]), specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=101),
     # optical path-length resolved detectors (xopto/mcml/mcdetector/radialpl.py,
     # totalpl.py): two layers, RadialPl on top (linear path-length axis),
     # TotalPl below (log path-length axis)
@@ -436,6 +478,29 @@ def _fluence(pkg, spec):
     return pkg.mcfluence.Fluence(A(*spec['x']), A(*spec['y']), A(*spec['z']), mode=spec['mode'])
 
 
+def _surface(pkg, spec):
+    """SurfaceLayouts of a scenario (xopto/mcml/mcsurface)."""
+    if not spec:
+        return None
+    import importlib
+    fibermod = importlib.import_module(pkg.__name__.rsplit('.', 1)[0] + '.mcutil.fiber')
+    sm = pkg.mcsurface
+
+    def layout(d):
+        if d is None:
+            return None
+        kw = {k: v for k, v in d.items() if k != 'type'}
+        if 'fiber' in kw:
+            kw['fiber'] = fibermod.MultimodeFiber(**kw['fiber'])
+        if 'fibers' in kw:
+            kw['fibers'] = [fibermod.FiberLayout(fibermod.MultimodeFiber(**f['fiber']),
+                                                 position=f['position'], direction=f['direction'])
+                            for f in kw['fibers']]
+        return getattr(sm, d['type'])(**kw)
+
+    return sm.SurfaceLayouts(top=layout(spec.get('top')), bottom=layout(spec.get('bottom')))
+
+
 def _source(src_mod, spec):
     import importlib
     kw = {k: v for k, v in spec.items() if k != 'type'}
@@ -467,8 +532,8 @@ def build_mc(name_or_spec, fast=False, package='pyxopto_gb300', scheduling='stat
             mc.mclayer.Layer(d=l['d'], n=l['n'], mua=l['mua'], mus=l['mus'], pf=_pf(mc, l['pf']))
             for l in s['layers']])
         obj = mc.Mc(layers, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
-                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast, scheduling),
-                    rnginit=s['rnginit'])
+                    fluence=_fluence(mc, s.get('fluence')), surface=_surface(mc, s.get('surface')),
+                    options=options(mc, s, fast, scheduling), rnginit=s['rnginit'])
     else:
         mc = importlib.import_module(package + '.mcvox.mc')
         g = s['grid']
