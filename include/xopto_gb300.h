@@ -111,7 +111,10 @@ enum {
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
        MCGB_DET_TOTAL_PL = 4, MCGB_DET_CARTESIAN = 5, MCGB_DET_CARTESIAN_PL = 6,
-       MCGB_DET_SYMMETRIC_X = 7 };
+       MCGB_DET_SYMMETRIC_X = 7, MCGB_DET_LINEAR_ARRAY = 8, MCGB_DET_SIX_AROUND_ONE = 9,
+       MCGB_DET_FIBER_ARRAY = 10, MCGB_DET_LINEAR_ARRAY_PL = 11, MCGB_DET_SIX_AROUND_ONE_PL = 12,
+       MCGB_DET_FIBER_ARRAY_PL = 13 };
+#define MCGB_DET_FIBER_FLOATS 13            /* floats per FIBER_ARRAY fibre    */
 enum { MCGB_FLUENCE_NONE = 0, MCGB_FLUENCE_DEPOSITION = 1, MCGB_FLUENCE_RATE = 2 };
 /* Trace flags (xopto/mcbase/mctrace.py TRACE_START/END/ALL). */
 enum { MCGB_TRACE_NONE = 0, MCGB_TRACE_START = 1, MCGB_TRACE_END = 2, MCGB_TRACE_ALL = 7 };
@@ -217,7 +220,18 @@ typedef struct McgbSource {
    2n bins symmetric about x = position[0], half axis offset r_min, 1/step
    inv_dr, log_scale.  Indices outside an axis are clipped into its first or
    last bin; the path-length kinds need
-   McgbRunOptions.track_optical_pathlength. */
+   McgbRunOptions.track_optical_pathlength.
+   Fibre-probe detectors (xopto/mcml/mcdetector/probe): one bin per fibre
+   (n fibres; the _PL kinds n_pl x n, path length first) and a float table
+   in McgbBuffers.fp_lut from table_offset:
+     LINEAR_ARRAY (lineararray.py:103-162,341-380): transformation (9),
+       first fibre position (2), fibre step (2), core r^2, acceptance cosine;
+     SIX_AROUND_ONE (sixaroundone.py:103-184,346-386; n = 7):
+       transformation (9), position (2), core r^2, core spacing, acceptance
+       cosine;
+     FIBER_ARRAY (fiberarray.py:103-162,270-312): per fibre transformation
+       (9), position (2), core r^2, acceptance cosine.  Top and bottom slots
+       only. */
 typedef struct McgbDetector {
     int32_t kind;
     float direction[3];
@@ -229,7 +243,7 @@ typedef struct McgbDetector {
     uint64_t offset;                        /* first accumulator               */
     float pl_min, inv_dpl;                  /* path-length axis start, 1/step  */
     uint32_t n_pl;                          /* path-length bins                */
-    uint32_t reserved;
+    uint32_t table_offset;                  /* fibre probes: first float       */
     float y_min, inv_dy;                    /* Cartesian y axis start, 1/step  */
     uint32_t n_y;                           /* Cartesian y bins                */
     uint32_t reserved2;

@@ -248,14 +248,87 @@ static inline uint32_t weight_to_u32(float w, float accept) {
     return (uint32_t)((w * (float)MCGB_ACCU_K + 0.5f) * accept);
 }
 
+/* (x, y, 0) through a 3x3 transformation (mc_transform_fpv3,
+   xopto/mcbase/kernel/mcbase.template.c:683-690). */
+static inline void xf_xy(const float *T, float x, float y, float *ox, float *oy) {
+    *ox = T[0] * x + T[1] * y + T[2] * 0.0f;
+    *oy = T[3] * x + T[4] * y + T[5] * 0.0f;
+}
+
+/* Fibre-probe detectors: LinearArray (xopto/mcml/mcdetector/probe/lineararray.py:103-162),
+   SixAroundOne (sixaroundone.py:103-184; a later ring test overrides an earlier hit),
+   FiberArray (fiberarray.py:103-162) and the path-length variants (lineararraypl.py,
+   sixaroundonepl.py, fiberarraypl.py: bin pl_index*n + fibre). */
+static void probe_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir, float weight,
+                          float opl, uint64_t *accu, const float *lut) {
+    int base = det->kind >= MCGB_DET_LINEAR_ARRAY_PL ? det->kind - 3 : det->kind;
+    const float *t = lut + det->table_offset;
+    const float *T = t;
+    uint32_t fiber = det->n;
+    float cos_min, lx, ly;
+    if (base == MCGB_DET_LINEAR_ARRAY) {
+        float fx = t[9], fy = t[10];
+        for (uint32_t i = 0; i < det->n; ++i) {
+            xf_xy(t, pos.x - fx, pos.y - fy, &lx, &ly);
+            if (lx * lx + ly * ly <= t[13]) {
+                fiber = i;
+                break;
+            }
+            fx += t[11];
+            fy += t[12];
+        }
+        cos_min = t[14];
+    } else if (base == MCGB_DET_SIX_AROUND_ONE) {
+        float rx = pos.x - t[9], ry = pos.y - t[10];
+        xf_xy(t, rx, ry, &lx, &ly);
+        if (lx * lx + ly * ly <= t[11]) fiber = 0;
+        xf_xy(t, fabsf(rx) - t[12], ry, &lx, &ly);
+        if (lx * lx + ly * ly <= t[11]) fiber = (rx >= 0.0f) ? 1 : 4;
+        xf_xy(t, fabsf(rx) - t[12] * 0.5f, fabsf(ry) - t[12] * 0.8660254037844386f, &lx, &ly);
+        if (lx * lx + ly * ly <= t[11])
+            fiber = (rx >= 0.0f) ? ((ry >= 0.0f) ? 2 : 6) : ((ry >= 0.0f) ? 3 : 5);
+        cos_min = t[13];
+    } else {
+        for (uint32_t i = 0; i < det->n; ++i) {
+            const float *f = t + (size_t)i * MCGB_DET_FIBER_FLOATS;
+            xf_xy(f, pos.x - f[9], pos.y - f[10], &lx, &ly);
+            if (lx * lx + ly * ly <= f[11]) {
+                fiber = i;
+                break;
+            }
+        }
+        if (fiber >= det->n) return;
+        T = t + (size_t)fiber * MCGB_DET_FIBER_FLOATS;
+        cos_min = T[12];
+    }
+    if (fiber >= det->n) return;
+    /* transform_point3f_z, xopto/mcbase/kernel/mcbase.template.h:1875-1876 */
+    float pz = T[6] * dir.x + T[7] * dir.y + T[8] * dir.z;
+    float accept = (float)(cos_min <= fabsf(pz));
+    uint64_t index = fiber;
+    if (det->kind >= MCGB_DET_LINEAR_ARRAY_PL) {
+        float pl = opl;
+        if (det->pl_log_scale) pl = m_log(mm, fmaxf(pl, 1e-12f));
+        int32_t pl_index = clip_i(cvt_int((pl - det->pl_min) * det->inv_dpl), 0,
+                                  (int32_t)det->n_pl - 1);
+        index += (uint64_t)pl_index * det->n;
+    }
+    uint32_t w = weight_to_u32(weight, accept);
+    if (w > 0) accu[det->offset + index] += w;
+}
+
 /* Surface detector deposit: Total (xopto/mcml/mcdetector/total.py:86-108),
    Radial (radial.py:117-150), TotalPl (totalpl.py:107-135), RadialPl
    (radialpl.py:138-179), Cartesian (cartesian.py:124-157), CartesianPl
    (cartesianpl.py:146-185), SymmetricX (symmetric.py:124-156);
    opl = mcsim_optical_pathlength. */
 static void detector_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir,
-                             float weight, float opl, uint64_t *accu) {
+                             float weight, float opl, uint64_t *accu, const float *lut) {
     if (det->kind == MCGB_DET_NONE) return;
+    if (det->kind >= MCGB_DET_LINEAR_ARRAY) {
+        probe_deposit(mm, det, pos, dir, weight, opl, accu, lut);
+        return;
+    }
     v3 ddir = {det->direction[0], det->direction[1], det->direction[2]};
     float accept = (float)(det->cos_min <= fabsf(dot3(dir, ddir)));
     uint64_t index = 0;
@@ -400,7 +473,7 @@ static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint6
         s->dir = d;
         R = reflectance(n_core, n_sample, d.z, cc);
         if (c->specular.kind != MCGB_DET_NONE)
-            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu, NULL);
     } else {
         s->dir = pt;
         R = reflectance_cos2(n_core, n_sample, pt.z);
@@ -408,7 +481,7 @@ static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint6
             v3 dir_in = {pt.x, pt.y, -pt.z};
             v3 normal = {0.0f, 0.0f, -1.0f};
             v3 d = refract3(dir_in, normal, n_sample, n_core);
-            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu, NULL);
         }
     }
     s->w = 1.0f - R;
@@ -427,7 +500,7 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
         if (c->specular.kind != MCGB_DET_NONE) {
             v3 d = {src->direction_reflected[0], src->direction_reflected[1],
                     src->direction_reflected[2]};
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu, NULL);
         }
         s->layer = 1;
     } else if (src->kind == MCGB_SRC_UNIFORM_BEAM) {
@@ -454,7 +527,7 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
             v3 normal = {0.0f, 0.0f, -1.0f};
             v3 d = refract3(dir_in, normal, c->layers[1].n, c->layers[0].n);
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu, NULL);
         }
     } else if (src->kind == MCGB_SRC_ISOTROPIC_POINT) {
         /* IsotropicPoint.mcsim_launch, xopto/mcml/mcsource/point.py:76-128 */
@@ -483,7 +556,7 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
         s->dir = refracted;
         s->pos = pos;
         if (c->specular.kind != MCGB_DET_NONE)
-            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu, NULL);
         s->w = 1.0f - R;
         s->layer = src->layer_index;
     } else if (src->kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
@@ -517,7 +590,7 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             v3 dir_in = {s->dir.x, s->dir.y, -s->dir.z};
             v3 normal = {0.0f, 0.0f, -1.0f};
             v3 d = refract3(dir_in, normal, c->layers[1].n, c->layers[0].n);
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu, NULL);
         }
     }
 }
@@ -758,9 +831,9 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                     events |= mcml_boundary(mm, c, lut, &s, next, &x, a) | EV_BOUNDARY_HIT;
                     if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
                         if (s.layer <= 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu, lut);
                         else if (s.layer >= (int32_t)c->num_layers - 1)
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu, lut);
                         done = 1;
                     }
                 } else {
@@ -781,9 +854,9 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                     events |= mcml_boundary(mm, c, lut, &s, next, &x, a) | EV_BOUNDARY_HIT;
                     if (!(s.layer > 0 && s.layer < (int32_t)c->num_layers - 1)) {
                         if (s.layer <= 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu, lut);
                         else if (s.layer >= (int32_t)c->num_layers - 1)
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu, lut);
                         done = 1;
                     }
                 } else if (o->method == MCGB_METHOD_ALBEDO_REJECTION) {
@@ -947,7 +1020,7 @@ static void mv_beam_enter(int mm, const McgbMcvoxConfig *c, const McgbMaterial *
         specular_r = reflectance(n_outside, n_inside, dot3(normal, direction),
                                  cos_critical(n_outside, n_inside));
         if (c->specular.kind != MCGB_DET_NONE)
-            detector_deposit(mm, &c->specular, s->pos, direction, specular_r, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, direction, specular_r, 0.0f, accu, NULL);
     } else {
         s->pos.x = c->top_left[0]; s->pos.y = c->top_left[1]; s->pos.z = c->top_left[2];
         s->dir.x = 0.0f; s->dir.y = 0.0f; s->dir.z = 1.0f;
@@ -984,7 +1057,7 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         if (c->specular.kind != MCGB_DET_NONE) {
             v3 d = {src->direction_reflected[0], src->direction_reflected[1],
                     src->direction_reflected[2]};
-            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, src->reflectance, 0.0f, accu, NULL);
         }
     } else if (src->kind == MCGB_SRC_GAUSSIAN_BEAM || src->kind == MCGB_SRC_UNIFORM_BEAM) {
         float cos_fi, sin_fi;
@@ -1038,7 +1111,7 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         s->pos = pos;
         s->dir = d;
         if (c->specular.kind != MCGB_DET_NONE)
-            detector_deposit(mm, &c->specular, s->pos, d, specular_r, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, d, specular_r, 0.0f, accu, NULL);
         s->w = 1.0f - specular_r;
     } else if (src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER) {
         float sin_fi, cos_fi, sin_theta, cos_theta, specular_r;
@@ -1079,7 +1152,7 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         }
         s->dir = refracted;
         if (c->specular.kind != MCGB_DET_NONE)
-            detector_deposit(mm, &c->specular, s->pos, packet_dir, specular_r, 0.0f, accu);
+            detector_deposit(mm, &c->specular, s->pos, packet_dir, specular_r, 0.0f, accu, NULL);
         s->w = 1.0f - specular_r;
     } else {
         /* IsotropicVoxel */
@@ -1212,9 +1285,9 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                     events |= mv_boundary(c, mats, vox, &s, dist, &x, a) | EV_BOUNDARY_HIT;
                     if (!mv_valid(c, s.vox)) {
                         if (s.vox.z < 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu, lut);
                         else if (s.vox.z >= c->shape[2])
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu, lut);
                         done = 1;
                     }
                 } else {
@@ -1235,9 +1308,9 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                     events |= mv_boundary(c, mats, vox, &s, dist, &x, a) | EV_BOUNDARY_HIT;
                     if (!mv_valid(c, s.vox)) {
                         if (s.vox.z < 0)
-                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->top, s.pos, s.dir, s.w, s.opl, accu, lut);
                         else if (s.vox.z >= c->shape[2])
-                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu);
+                            detector_deposit(mm, &c->bottom, s.pos, s.dir, s.w, s.opl, accu, lut);
                         done = 1;
                     }
                 } else if (o->method == MCGB_METHOD_ALBEDO_REJECTION) {

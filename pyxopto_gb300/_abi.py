@@ -24,6 +24,9 @@ SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT =
 SRC_ISOTROPIC_VOXEL = 8
 DET_NONE, DET_TOTAL, DET_RADIAL, DET_RADIAL_PL, DET_TOTAL_PL = 0, 1, 2, 3, 4
 DET_CARTESIAN, DET_CARTESIAN_PL, DET_SYMMETRIC_X = 5, 6, 7
+DET_LINEAR_ARRAY, DET_SIX_AROUND_ONE, DET_FIBER_ARRAY = 8, 9, 10
+DET_LINEAR_ARRAY_PL, DET_SIX_AROUND_ONE_PL, DET_FIBER_ARRAY_PL = 11, 12, 13
+DET_FIBER_FLOATS = 13
 FLUENCE_NONE, FLUENCE_DEPOSITION, FLUENCE_RATE = 0, 1, 2
 TRACE_NONE, TRACE_START, TRACE_END, TRACE_ALL = 0, 1, 2, 7
 MATH_EXACT, MATH_FAST = 0, 1
@@ -61,7 +64,7 @@ class McgbDetector(C.Structure):
     _fields_ = [('kind', i32), ('direction', f32 * 3), ('position', f32 * 2),
                 ('r_min', f32), ('inv_dr', f32), ('cos_min', f32), ('n', u32),
                 ('log_scale', i32), ('pl_log_scale', i32), ('offset', u64),
-                ('pl_min', f32), ('inv_dpl', f32), ('n_pl', u32), ('reserved', u32),
+                ('pl_min', f32), ('inv_dpl', f32), ('n_pl', u32), ('table_offset', u32),
                 ('y_min', f32), ('inv_dy', f32), ('n_y', u32), ('reserved2', u32)]
 
 

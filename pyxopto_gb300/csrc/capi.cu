@@ -116,10 +116,25 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     for (int i = 0; i < 3; ++i) {
         const McgbDetector &d = dets[i];
         if (d.kind == MCGB_DET_NONE) continue;
-        if (d.kind < MCGB_DET_TOTAL || d.kind > MCGB_DET_SYMMETRIC_X)
+        if (d.kind < MCGB_DET_TOTAL || d.kind > MCGB_DET_FIBER_ARRAY_PL)
             return fail(MCGB_E_INVALID, "%s detector: unknown kind %d", names[i], d.kind);
         const bool pl = d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL ||
-                        d.kind == MCGB_DET_CARTESIAN_PL;
+                        d.kind == MCGB_DET_CARTESIAN_PL || d.kind == MCGB_DET_LINEAR_ARRAY_PL ||
+                        d.kind == MCGB_DET_SIX_AROUND_ONE_PL || d.kind == MCGB_DET_FIBER_ARRAY_PL;
+        if (d.kind >= MCGB_DET_LINEAR_ARRAY) {
+            if (i == 2) return fail(MCGB_E_INVALID, "the specular slot takes no fibre-probe detector");
+            const int base = d.kind >= MCGB_DET_LINEAR_ARRAY_PL ? d.kind - 3 : d.kind;
+            if (base == MCGB_DET_SIX_AROUND_ONE && d.n != 7)
+                return fail(MCGB_E_INVALID, "%s six-around-one detector needs n = 7", names[i]);
+            if (d.n == 0 || d.n > 4096)
+                return fail(MCGB_E_INVALID, "%s probe detector: %u fibres outside [1, 4096]", names[i], d.n);
+            uint64_t floats = base == MCGB_DET_LINEAR_ARRAY     ? 15
+                              : base == MCGB_DET_SIX_AROUND_ONE ? 14
+                                                                : (uint64_t)MCGB_DET_FIBER_FLOATS * d.n;
+            if (!b->fp_lut || !range_ok(d.table_offset, floats, b->fp_lut_size))
+                return fail(MCGB_E_SIZE, "%s probe detector table [%u, +%llu) beyond the float table", names[i],
+                            d.table_offset, (unsigned long long)floats);
+        }
         if (pl) {
             if (!o.track_optical_pathlength)
                 return fail(MCGB_E_INVALID, "%s path-length detector needs track_optical_pathlength",
@@ -128,7 +143,7 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
         }
         uint64_t nr = 1;
         if (d.kind == MCGB_DET_RADIAL || d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_CARTESIAN ||
-            d.kind == MCGB_DET_CARTESIAN_PL)
+            d.kind == MCGB_DET_CARTESIAN_PL || d.kind >= MCGB_DET_LINEAR_ARRAY)
             nr = d.n;
         else if (d.kind == MCGB_DET_SYMMETRIC_X)
             nr = 2ull * d.n;

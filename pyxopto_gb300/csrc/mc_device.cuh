@@ -274,14 +274,89 @@ MCGB_DEV void accu_add(uint64_t *accu, uint64_t index, uint32_t w) {
     atomicAdd((unsigned long long *)(accu + index), (unsigned long long)w);
 }
 
+/* (x, y, 0) through a 3x3 transformation (mc_transform_fpv3,
+   xopto/mcbase/kernel/mcbase.template.c:683-690; the z term is kept so that
+   the float operations match the reference). */
+MCGB_DEV float2 transform_xy(const float *T, float x, float y) {
+    return make_float2(T[0] * x + T[1] * y + T[2] * 0.0f, T[3] * x + T[4] * y + T[5] * 0.0f);
+}
+
+MCGB_DEV int probe_pl_index(const McgbDetector &det, float opl) {
+    float pl = opl;
+    if (det.pl_log_scale) pl = mc_log(fmaxf(pl, 1e-12f));
+    return clip_i(cvt_int((pl - det.pl_min) * det.inv_dpl), 0, (int)det.n_pl - 1);
+}
+
+/* Fibre-probe detectors: LinearArray (xopto/mcml/mcdetector/probe/
+   lineararray.py:103-162), SixAroundOne (sixaroundone.py:103-184; a later
+   ring test overrides an earlier hit, as there), FiberArray
+   (fiberarray.py:103-162) and their path-length variants (lineararraypl.py,
+   sixaroundonepl.py, fiberarraypl.py: bin pl_index*n + fibre). */
+MCGB_DEV void probe_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir, float weight,
+                            float opl, uint64_t *accu, const float *lut) {
+    const int base = det.kind >= MCGB_DET_LINEAR_ARRAY_PL ? det.kind - 3 : det.kind;
+    const float *t = lut + det.table_offset;
+    const float *T = t;
+    uint32_t fiber = det.n;
+    float cos_min;
+    if (base == MCGB_DET_LINEAR_ARRAY) {
+        float fx = t[9], fy = t[10];
+        for (uint32_t i = 0; i < det.n; ++i) {
+            float2 lp = transform_xy(t, pos.x - fx, pos.y - fy);
+            if (lp.x * lp.x + lp.y * lp.y <= t[13]) {
+                fiber = i;
+                break;
+            }
+            fx += t[11];
+            fy += t[12];
+        }
+        cos_min = t[14];
+    } else if (base == MCGB_DET_SIX_AROUND_ONE) {
+        float rx = pos.x - t[9], ry = pos.y - t[10];
+        float2 lp = transform_xy(t, rx, ry);
+        if (lp.x * lp.x + lp.y * lp.y <= t[11]) fiber = 0;
+        lp = transform_xy(t, fabsf(rx) - t[12], ry);
+        if (lp.x * lp.x + lp.y * lp.y <= t[11]) fiber = (rx >= 0.0f) ? 1 : 4;
+        lp = transform_xy(t, fabsf(rx) - t[12] * 0.5f, fabsf(ry) - t[12] * 0.8660254037844386f);
+        if (lp.x * lp.x + lp.y * lp.y <= t[11])
+            fiber = (rx >= 0.0f) ? ((ry >= 0.0f) ? 2 : 6) : ((ry >= 0.0f) ? 3 : 5);
+        cos_min = t[13];
+    } else {
+        for (uint32_t i = 0; i < det.n; ++i) {
+            const float *f = t + (size_t)i * MCGB_DET_FIBER_FLOATS;
+            float2 lp = transform_xy(f, pos.x - f[9], pos.y - f[10]);
+            if (lp.x * lp.x + lp.y * lp.y <= f[11]) {
+                fiber = i;
+                break;
+            }
+        }
+        if (fiber >= det.n) return;
+        T = t + (size_t)fiber * MCGB_DET_FIBER_FLOATS;
+        cos_min = T[12];
+    }
+    if (fiber >= det.n) return;
+    float pz = T[6] * dir.x + T[7] * dir.y + T[8] * dir.z;
+    float accept = (float)(cos_min <= fabsf(pz));
+    uint64_t index = fiber;
+    if (det.kind >= MCGB_DET_LINEAR_ARRAY_PL) index += (uint64_t)probe_pl_index(det, opl) * det.n;
+    uint32_t w = weight_to_u32(weight, accept);
+    if (w > 0) accu_add(accu, det.offset + index, w);
+}
+
 /* Surface detector deposit: Total (xopto/mcml/mcdetector/total.py:86-108),
    Radial (radial.py:117-150), TotalPl (totalpl.py:107-135), RadialPl
    (radialpl.py:138-179), Cartesian (cartesian.py:124-157), CartesianPl
    (cartesianpl.py:146-185) and SymmetricX (symmetric.py:124-156); opl is
    the packet's optical path length. */
+template <bool PROBES = false>
 MCGB_DEV void detector_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir,
-                               float weight, float opl, uint64_t *accu) {
+                               float weight, float opl, uint64_t *accu,
+                               const float *lut = nullptr) {
     if (det.kind == MCGB_DET_NONE) return;
+    if (PROBES && det.kind >= MCGB_DET_LINEAR_ARRAY) {
+        probe_deposit(det, pos, dir, weight, opl, accu, lut);
+        return;
+    }
     f3 ddir{det.direction[0], det.direction[1], det.direction[2]};
     float accept = (float)(det.cos_min <= fabsf(dot3(dir, ddir)));
     uint64_t index = 0;

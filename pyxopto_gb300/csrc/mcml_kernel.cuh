@@ -519,8 +519,8 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         if (next != s.layer) {
             { uint32_t ev = mcml_boundary<XTRA>(c, x.lut, L, s.layer, next, x.last_layer, s.pos, s.dir, s.w, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
             if (!(s.layer > 0 && s.layer < x.last_layer)) {
-                if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
-                else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
+                if (s.layer <= 0) detector_deposit<XTRA>(c.top, s.pos, s.dir, s.w, s.opl, accu, x.lut);
+                else detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
                 done = true;
             }
         } else {
@@ -540,8 +540,8 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
     } else if (next != s.layer) {
         { uint32_t ev = mcml_boundary<XTRA>(c, x.lut, L, s.layer, next, x.last_layer, s.pos, s.dir, s.w, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
         if (!(s.layer > 0 && s.layer < x.last_layer)) {
-            if (s.layer <= 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
-            else detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
+            if (s.layer <= 0) detector_deposit<XTRA>(c.top, s.pos, s.dir, s.w, s.opl, accu, x.lut);
+            else detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             done = true;
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {

@@ -416,8 +416,8 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         if (d < step) {
             s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
             if (!mv_valid(g, s.vi)) {
-                if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
-                else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
+                if (s.vi.z < 0) detector_deposit<XTRA>(c.top, s.pos, s.dir, s.w, s.opl, accu, x.lut);
+                else if (s.vi.z >= g.sh[2]) detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
                 done = true;
             }
         } else {
@@ -437,8 +437,8 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     } else if (d < step) {
         s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
         if (!mv_valid(g, s.vi)) {
-            if (s.vi.z < 0) detector_deposit(c.top, s.pos, s.dir, s.w, s.opl, accu);
-            else if (s.vi.z >= g.sh[2]) detector_deposit(c.bottom, s.pos, s.dir, s.w, s.opl, accu);
+            if (s.vi.z < 0) detector_deposit<XTRA>(c.top, s.pos, s.dir, s.w, s.opl, accu, x.lut);
+            else if (s.vi.z >= g.sh[2]) detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             done = true;
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {

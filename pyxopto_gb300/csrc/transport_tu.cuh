@@ -103,6 +103,7 @@ cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_
     const int sched = cfg.opt.scheduling;
     bool xtra = cfg.trace.flags != MCGB_TRACE_NONE || cfg.opt.track_optical_pathlength != 0 ||
                 cfg.opt.max_steps_per_packet != 0;
+    xtra = xtra || cfg.top.kind >= MCGB_DET_LINEAR_ARRAY || cfg.bottom.kind >= MCGB_DET_LINEAR_ARRAY;
 #if MCGB_MEDIUM == 0
     xtra = xtra || cfg.surface_top.kind != MCGB_SURFACE_NONE ||
            cfg.surface_bottom.kind != MCGB_SURFACE_NONE;

@@ -2,3 +2,5 @@
 from ..mcbase.mcdetector import (Axis, RadialAxis, SymmetricAxis, Detector, DetectorDefault,
                                  Total, Radial, TotalPl, RadialPl, Cartesian, CartesianPl,
                                  SymmetricX, Detectors)
+from ..mcbase.mcdetector_probe import (LinearArray, LinearArrayPl, SixAroundOne, SixAroundOnePl,
+                                       FiberArray, FiberArrayPl)

@@ -346,6 +346,63 @@ SCENARIOS = {
                        bottom=dict(type='TotalPl', plaxis=[1e-4, 1e-1, 12], pllogscale=True),
                        specular=dict(type='Total')),
         nphotons=3000, streams=32, rnginit=19),
+    'probe_linear_array': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1e-3, n=1.4, mua=60.0, mus=1.2e4, pf=['Hg', 0.8]),
+                dict(d=INF, n=1.36, mua=30.0, mus=8e3, pf=['Hg', 0.9])],
+        source=dict(type='UniformFiber', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22)),
+        detectors=dict(top=dict(type='LinearArray', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22),
+                                n=6, spacing=2.5e-4, orientation=(1.0, 0.3), position=(7e-4, 1e-4)),
+                       bottom=dict(type='LinearArrayPl', fiber=dict(dcore=400e-6, dcladding=420e-6, ncore=1.46, na=0.39),
+                                   n=3, plaxis=[0.0, 20e-3, 8], direction=(0.2, 0.0, 1.0)),
+                       specular=dict(type='Total')),
+        nphotons=4000, streams=32, rnginit=103),
+    'probe_six_around_one': dict(
+        medium='mcml',
+        layers=[_air(['Gk', 0.0, 0.5]),
+                dict(d=2e-3, n=1.38, mua=40.0, mus=1.5e4, pf=['Gk', 0.7, 0.5]),
+                _air(['Gk', 0.0, 0.5])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='SixAroundOne', fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22),
+                                spacing=3e-4, direction=(0.1, -0.2, 1.0)),
+                       bottom=dict(type='SixAroundOnePl', fiber=dict(dcore=400e-6, dcladding=420e-6, ncore=1.46, na=0.39),
+                                   plaxis=[1e-3, 1e-1, 10], pllogscale=True, position=(1e-4, 2e-4)),
+                       specular=dict(type='Total')),
+        nphotons=4000, streams=32, rnginit=107),
+    'probe_fiber_array': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1.5e-3, n=1.4, mua=100.0, mus=1.2e4, pf=['Hg', 0.85]),
+                dict(d=INF, n=1.33, mua=20.0, mus=8e3, pf=['Hg', 0.8])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='FiberArray',
+                                fibers=[dict(fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22), position=(0.0, 0.0, 0.0),
+                                             direction=(0.0, 0.0, 1.0)),
+                                        dict(fiber=dict(dcore=400e-6, dcladding=440e-6, ncore=1.46, na=0.39),
+                                             position=(5e-4, 1e-4, 0.0), direction=(0.2, 0.1, 1.0)),
+                                        dict(fiber=dict(dcore=600e-6, dcladding=630e-6, ncore=1.45, na=0.5),
+                                             position=(-6e-4, -3e-4, 0.0), direction=(0.0, 0.0, 1.0))]),
+                       specular=dict(type='Total')),
+        nphotons=4000, streams=32, rnginit=109),
+    'vox_probe_fiber_array_pl': dict(
+        medium='mcvox',
+        grid=dict(x=[-1.2e-3, 1.2e-3, 12], y=[-1.2e-3, 1.2e-3, 12], z=[0.0, 8e-4, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.38, mua=80.0, mus=1.2e4, pf=['Hg', 0.8]),
+                   dict(n=1.42, mua=300.0, mus=2e4, pf=['Hg', 0.9])],
+        layout=dict(kind='checker'),
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='FiberArrayPl',
+                                fibers=[dict(fiber=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, na=0.22), position=(1e-4, 0.0, 0.0),
+                                             direction=(0.0, 0.0, 1.0)),
+                                        dict(fiber=dict(dcore=400e-6, dcladding=440e-6, ncore=1.46, na=0.39),
+                                             position=(-4e-4, 2e-4, 0.0), direction=(0.1, 0.1, 1.0))],
+                                plaxis=[0.0, 10e-3, 8]),
+                       bottom=dict(type='LinearArray', fiber=dict(dcore=400e-6, dcladding=420e-6, ncore=1.46, na=0.39),
+                                   n=3, spacing=4.2e-4),
+                       specular=dict(type='Total')),
+        nphotons=4000, streams=32, rnginit=113),
 }
 
 # Bench workloads (not golden-tested at these sizes): the layered
@@ -465,10 +522,29 @@ def _detectors(pkg, spec):
             slots[slot] = pkg.mcdetector.RadialPl(
                 _axis(pkg, d), _axis(pkg, {'axis': d['plaxis'], 'logscale': d.get('pllogscale', False)}),
                 position=d.get('position', (0.0, 0.0)), cosmin=d.get('cosmin', 0.0))
+        elif d['type'] in ('LinearArray', 'LinearArrayPl', 'SixAroundOne', 'SixAroundOnePl',
+                           'FiberArray', 'FiberArrayPl'):
+            slots[slot] = _probe_detector(pkg, d)
         else:
             slots[slot] = pkg.mcdetector.Radial(_axis(pkg, d), position=d.get('position', (0.0, 0.0)),
                                                 cosmin=d.get('cosmin', 0.0))
     return pkg.mcdetector.Detectors(**slots)
+
+
+def _probe_detector(pkg, d):
+    """Fibre-probe detector of a scenario (xopto/mcml/mcdetector/probe)."""
+    import importlib
+    fibermod = importlib.import_module(pkg.__name__.rsplit('.', 1)[0] + '.mcutil.fiber')
+    kw = {k: v for k, v in d.items() if k not in ('type', 'plaxis', 'pllogscale')}
+    if 'fiber' in kw:
+        kw['fiber'] = fibermod.MultimodeFiber(**kw['fiber'])
+    if 'fibers' in kw:
+        kw['fibers'] = [fibermod.FiberLayout(fibermod.MultimodeFiber(**f['fiber']),
+                                             position=f['position'], direction=f['direction'])
+                        for f in kw['fibers']]
+    if 'plaxis' in d:
+        kw['plaxis'] = _axis(pkg, {'axis': d['plaxis'], 'logscale': d.get('pllogscale', False)})
+    return getattr(pkg.mcdetector, d['type'])(**kw)
 
 
 def _fluence(pkg, spec):
