@@ -27,6 +27,10 @@ Writes
   cuda_mcml_fiber2.npz   the same for the two-layer sample, sweep on the
                          second layer (cuda_doublelayer_uniformfiber.pkl,
                          test validate.py:692-866).
+  linear_probe_*.npz     the reflectances of the six- and nine-fibre
+                         linear-probe tests (single_layer_*_linear_probe.pkl,
+                         validate.py:1227-1758); written by
+                         `make_golden.py linear_probe`.
 """
 import os
 import pickle
@@ -132,7 +136,55 @@ def make_cuda_fiber(double=False):
     print(name, np.asarray(d['reflectance']).shape)
 
 
+PROBE_PICKLES = {
+    'hg_six': 'single_layer_hg_lut_six_linear_probe.pkl',
+    'hg_nine': 'single_layer_hg_lut_nine_linear_probe.pkl',
+    'gk_six': 'single_layer_gk_lut_six_linear_probe.pkl',
+}
+
+
+def make_linear_probe(key):
+    """Reflectances of the reference's six- and nine-fibre linear-probe
+    validation tests (validate.py:1227-1758) with their geometry.  The
+    Gegenbauer sweep (30 x 30 x 20 points) keeps every third absorption and
+    scattering value and every sixth gamma to stay small."""
+    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference', PROBE_PICKLES[key])
+    with open(path, 'rb') as f:
+        d = pickle.load(f)
+    layers, lut = d['layers'], d['lut']
+    refl = np.asarray(d['reflectance'], dtype=np.float64)
+    mua, musr = np.asarray(lut['mua'], np.float64), np.asarray(lut['musr'], np.float64)
+    extra = {}
+    if key == 'gk_six':
+        ia, im, ig = np.arange(0, mua.size, 3), np.arange(0, musr.size, 3), np.arange(0, lut['gamma'].size, 6)
+        refl = refl[np.ix_(ia, im, ig)]
+        mua, musr = mua[ia], musr[im]
+        gamma = np.asarray(lut['gamma'], np.float64)[ig]
+        g = float(d['g'])
+        params = np.array([lut['pf_params_lut'][(g, float(v))] for v in gamma], dtype=np.float64)
+        extra = dict(g=np.array([g]), gamma=gamma, gk_g=params[:, 0], gk_a=params[:, 1])
+    pf = np.array([list(l['pf']['pfparams']) + [0.5] * (2 - len(l['pf']['pfparams'])) for l in layers])
+    src, srf, det = d['source'], d['surface'], d['detector']
+    fib = lambda f: np.array([f['dcore'], f['dcladding'], f['ncore'], f['na']])
+    np.savez_compressed(
+        os.path.join(HERE, 'linear_probe_{}.npz'.format(key)), **extra,
+        reflectance=refl, mua=mua, musr=musr,
+        pf_type=np.array([0 if layers[0]['pf']['type'] == 'Hg' else 1]), pf=pf,
+        n=np.array([l['basic']['n'] for l in layers]), d=np.array([l['basic']['d'] for l in layers]),
+        source_fiber=fib(src['fiber']), source_position=np.array(src['position'], np.float64),
+        surface_fiber=fib(srf['fiber']),
+        surface=np.array([srf['n'], srf['spacing'], srf['cutout'][0], srf['cutout'][1], srf['cutoutn'],
+                          srf['diameter'], srf['reflectivity']], np.float64),
+        detector_fiber=fib(det['fiber']), detector=np.array([det['n'], det['spacing']], np.float64),
+        rmax=np.array([d['mc']['rmax']]))
+    print('linear_probe', key, refl.shape)
+
+
 if __name__ == '__main__':
+    if sys.argv[1:2] == ['linear_probe']:
+        for k in PROBE_PICKLES:
+            make_linear_probe(k)
+        sys.exit(0)
     names = sys.argv[1:] or list(scenarios.SCENARIOS)
     for n in names:
         make_scenario(n)
