@@ -64,6 +64,8 @@ extern "C" {
 #define MCGB_MAX_MATERIALS 256
 /* Floats in one trace event (xopto/mcbase/mctrace.py TRACE_ENTRY_LEN). */
 #define MCGB_TRACE_ENTRY_LEN 8
+/* Voxel crossings after which a sampling-volume walk of one packet stops. */
+#define MCGB_SV_MAX_CROSSINGS (1u << 26)
 
 /* ---------------------------------------------------------------- errors */
 enum {
@@ -270,6 +272,23 @@ typedef struct McgbTrace {
     uint64_t count_offset;                  /* in the int buffer   */
 } McgbTrace;                                /* 32 bytes */
 
+/* Sampling volume of a set of packet traces (replaces the reference's
+   SamplingVolume kernel arguments: ClSamplingVolume,
+   xopto/mcbase/mcsv.py:30-95, and the McTrace fields that kernel reads,
+   xopto/mcbase/kernel/mcsv.template.c:236-262).  The traces are
+   num_packets records of max_events events of MCGB_TRACE_ENTRY_LEN floats
+   (x, y, z, px, py, pz, w, pl) plus one int32 event count per packet. */
+typedef struct McgbSamplingVolume {
+    float top_left[3];                      /* x, y, z of the first voxel's corner */
+    float voxel_size[3];
+    uint32_t shape[3];                      /* voxels along x, y, z            */
+    float multiplier;                       /* applied to weight x path length */
+    uint64_t offset;                        /* first voxel in the accumulator  */
+    int32_t k;                              /* float to integer weight factor  */
+    uint32_t max_events;                    /* trace length per packet         */
+    uint64_t num_packets;                   /* traces to process               */
+} McgbSamplingVolume;                       /* 64 bytes */
+
 /* Options shared by both media. */
 typedef struct McgbRunOptions {
     int32_t method;                         /* MCGB_METHOD_*                   */
@@ -390,8 +409,8 @@ int mcgb_abi_version(void);
    (replaces the reference's sizeof_datatypes kernel).  kind: 0 McgbLayer,
    1 McgbSource, 2 McgbDetector, 3 McgbFluence, 4 McgbTrace, 5 McgbMaterial,
    6 McgbMcmlConfig, 7 McgbMcvoxConfig, 8 McgbBuffers, 9 McgbRunOptions,
-   10 McgbPf, 11 McgbBatchSim, 12 McgbBatchConfig, 13 McgbSurface.  Returns -1
-   for an unknown kind. */
+   10 McgbPf, 11 McgbBatchSim, 12 McgbBatchConfig, 13 McgbSurface,
+   14 McgbSamplingVolume.  Returns -1 for an unknown kind. */
 int mcgb_sizeof(int kind);
 
 /* Number of streams (device threads) that fills every SM of the current
@@ -425,6 +444,25 @@ int mcgb_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *dev_out, void *stre
 
 /* Fill a device uint64 buffer with a value (ScalarFillMcAccu). */
 int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream);
+
+/* Sampling volume of packet traces (replaces Mc.sampling_volume and its
+   SamplingVolume kernel, xopto/mcml/mc.py:1040-1217,
+   xopto/mcbase/kernel/mcsv.template.c:236-421).  For every packet the path
+   through the recorded events is walked voxel by voxel; leaving a voxel
+   adds uint32(pl_end * length_in_voxel * multiplier * k + 0.5) to its
+   tally, where pl_end is the last float of the packet's last recorded event
+   (its optical path length when traced), and uint32(pl_end * k + 0.5) goes
+   to dev_total_weight[0].  dev_trace: the event floats (16-byte aligned,
+   at least num_packets * max_events * 8 floats); dev_counts: one int32 per
+   packet, clipped to max_events; a packet with no events is skipped.
+   dev_accu holds the voxel tallies from sv->offset on, flat index
+   (z * ny + y) * nx + x.  A packet whose walk exceeds 2^26 voxel crossings
+   stops and sets MCGB_STATUS_BAD_INDEX in dev_counters[MCGB_CNT_STATUS]
+   (may be NULL).  Deterministic: every tally is an integer sum. */
+int mcgb_sampling_volume(const McgbSamplingVolume *sv, const float *dev_trace,
+                         uint64_t trace_floats, const int32_t *dev_counts,
+                         uint64_t *dev_accu, uint64_t accu_size, uint64_t *dev_total_weight,
+                         uint64_t *dev_counters, void *stream);
 
 /* Exact integer sum of tally arrays (the cross-replica reduction):
    dst[i] += src[i] for i < n, host memory. */

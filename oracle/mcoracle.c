@@ -1460,6 +1460,106 @@ float mco_pm_exp(float x) { return pm_expf(x); }
 float mco_pm_pow(float x, float y) { return pm_powrf(x, y); }
 void mco_pm_sincos(float x, float *s, float *c) { pm_sincosf(x, s, c); }
 
+/* ---------------------------------------------------------------------------
+ * Sampling volume of packet traces: the reference's SamplingVolume kernel
+ * (xopto/mcbase/kernel/mcsv.template.c:236-421) for all packets in order.
+ * Each packet's recorded path is walked voxel by voxel: sva_voxel (:59-66)
+ * truncates the first event's position to a voxel index, which is then only
+ * stepped (sva_next_voxel, :136-160); the length travelled in a voxel is
+ * summed across events and deposited when the walk leaves the voxel or the
+ * path ends (sva_deposit_weight, :198-202).  The "end weight" is the last
+ * float of the last recorded event (:299), which is the optical path length
+ * slot of the trace entry (xopto/mcbase/mctrace.py:564-576).  Casts to
+ * integers saturate (negative -> 0), as device conversions do; a packet with
+ * no events is skipped (the reference would read before its trace).
+ * Returns the status bits (MCGB_STATUS_BAD_INDEX when a walk hit the
+ * crossing limit).
+ * ------------------------------------------------------------------------- */
+typedef struct { float x, y, z, px, py, pz; } SvEv;
+
+static void sv_get(const float *tr, int32_t i, SvEv *e) {
+    const float *f = tr + (size_t)i * MCGB_TRACE_ENTRY_LEN;
+    e->x = f[0]; e->y = f[1]; e->z = f[2];
+    e->px = f[3]; e->py = f[4]; e->pz = f[5];
+}
+
+static float sv_dist(const SvEv *a, const SvEv *b) {
+    float dx = a->x - b->x, dy = a->y - b->y, dz = a->z - b->z;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+/* sva_intersect, mcsv.template.c:97-120 */
+static float sv_axis_distance(float corner, int32_t v, float size, float pos, float dir) {
+    float d = corner + (float)((dir >= 0.0f) + v) * size - pos;
+    return (dir != 0.0f) ? d / dir : INFINITY;
+}
+
+uint64_t mco_sampling_volume(const McgbSamplingVolume *sv, const float *trace,
+                             const int32_t *counts, uint64_t *accu, uint64_t *total_weight) {
+    uint64_t status = 0;
+    const float k = (float)sv->k;
+    for (uint64_t p = 0; p < sv->num_packets; ++p) {
+        int32_t n = counts[p] < (int32_t)sv->max_events ? counts[p] : (int32_t)sv->max_events;
+        if (n <= 0) continue;
+        const float *tr = trace + p * (uint64_t)sv->max_events * MCGB_TRACE_ENTRY_LEN;
+        float end_w = tr[(size_t)n * MCGB_TRACE_ENTRY_LEN - 1];
+        *total_weight += cvt_uint(end_w * k + 0.5f);
+        SvEv e1, e2;
+        int32_t ev = 0;
+        sv_get(tr, 0, &e1);
+        sv_get(tr, n - 1 < 1 ? n - 1 : 1, &e2);
+        float d12 = sv_dist(&e1, &e2);
+        int32_t vx = cvt_int((e1.x - sv->top_left[0]) / sv->voxel_size[0]);
+        int32_t vy = cvt_int((e1.y - sv->top_left[1]) / sv->voxel_size[1]);
+        int32_t vz = cvt_int((e1.z - sv->top_left[2]) / sv->voxel_size[2]);
+        float l_voxel = 0.0f;
+        uint32_t crossings = 0;
+        for (;;) {
+            float dx = sv_axis_distance(sv->top_left[0], vx, sv->voxel_size[0], e1.x, e1.px);
+            float dy = sv_axis_distance(sv->top_left[1], vy, sv->voxel_size[1], e1.y, e1.py);
+            float dz = sv_axis_distance(sv->top_left[2], vz, sv->voxel_size[2], e1.z, e1.pz);
+            float d_voxel = fminf(dz, fminf(dx, dy));
+            float d_move = fminf(d_voxel, d12);
+            l_voxel += d_move;
+            int inside = vx >= 0 && vy >= 0 && vz >= 0 && (uint32_t)vx < sv->shape[0] &&
+                         (uint32_t)vy < sv->shape[1] && (uint32_t)vz < sv->shape[2];
+            uint64_t flat = inside ? ((uint64_t)vz * sv->shape[1] + (uint64_t)vy) * sv->shape[0] +
+                                     (uint64_t)vx : 0;
+            if (d_voxel < d12) {
+                if (inside)
+                    accu[sv->offset + flat] += cvt_uint(end_w * l_voxel * sv->multiplier * k + 0.5f);
+                e1.x += e1.px * d_move;
+                e1.y += e1.py * d_move;
+                e1.z += e1.pz * d_move;
+                d12 -= d_move;
+                int32_t nx = (dx <= dy) && (dx <= dz);
+                int32_t ny = nx ? 0 : ((dy <= dx) && (dy <= dz));
+                int32_t nz = !(nx + ny);
+                vx += e1.px < 0.0f ? -nx : nx;
+                vy += e1.py < 0.0f ? -ny : ny;
+                vz += e1.pz < 0.0f ? -nz : nz;
+                l_voxel = 0.0f;
+                if (++crossings >= MCGB_SV_MAX_CROSSINGS) {
+                    status |= MCGB_STATUS_BAD_INDEX;
+                    break;
+                }
+            } else {
+                e1 = e2;
+                ev += 1;
+                if (ev < n - 1) {
+                    sv_get(tr, ev + 1, &e2);
+                    d12 = sv_dist(&e1, &e2);
+                } else {
+                    if (inside)
+                        accu[sv->offset + flat] += cvt_uint(end_w * l_voxel * sv->multiplier * k + 0.5f);
+                    break;
+                }
+            }
+        }
+    }
+    return status;
+}
+
 int mco_sizeof(int kind) {
     switch (kind) {
         case 0: return (int)sizeof(McgbLayer);
@@ -1468,6 +1568,7 @@ int mco_sizeof(int kind) {
         case 3: return (int)sizeof(McgbFluence);
         case 4: return (int)sizeof(McgbTrace);
         case 5: return (int)sizeof(McgbMaterial);
+        case 14: return (int)sizeof(McgbSamplingVolume);
         case 6: return (int)sizeof(McgbMcmlConfig);
         case 7: return (int)sizeof(McgbMcvoxConfig);
         case 8: return (int)sizeof(McgbBuffers);

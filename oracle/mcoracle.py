@@ -44,6 +44,8 @@ def load():
         lib.mco_pm_pow.argtypes = [C.c_float, C.c_float]
         lib.mco_pm_sincos.argtypes = [C.c_float, vp, vp]
         lib.mco_sizeof.argtypes = [C.c_int]
+        lib.mco_sampling_volume.restype = C.c_uint64
+        lib.mco_sampling_volume.argtypes = [vp, vp, vp, vp, vp]
         lib.mco_batched_run.restype = C.c_uint64
         lib.mco_batched_run.argtypes = [C.c_int, vp, vp, vp, vp, C.c_int]
         _lib = lib
@@ -123,3 +125,19 @@ def batched_run(bmc, math: int = PORTABLE, nthreads: int = 1, **shape):
     steps = lib.mco_batched_run(int(math), C.addressof(cfg), C.addressof(bmc._sims),
                                 mult.ctypes.data, tally.ctypes.data, int(nthreads))
     return tally.reshape(bmc.num_sims, bmc.raxis.n), int(steps)
+
+
+def sampling_volume(sv_cfg, trace_n, trace_data):
+    """The sampling volume of a trace (packets in order) on the CPU; sv_cfg
+    is a packed pyxopto_gb300 McgbSamplingVolume whose max_events and
+    num_packets describe the trace.  Returns (voxel tallies, total weight,
+    status bits)."""
+    n = np.ascontiguousarray(trace_n, dtype=np.int32)
+    f = np.ascontiguousarray(trace_data, dtype=np.float32).reshape(-1)
+    assert n.size == sv_cfg.num_packets
+    assert f.size >= sv_cfg.num_packets * sv_cfg.max_events * 8
+    accu = np.zeros((int(np.prod(list(sv_cfg.shape))),), dtype=np.uint64)
+    total = np.zeros((1,), dtype=np.uint64)
+    status = load().mco_sampling_volume(C.addressof(sv_cfg), f.ctypes.data, n.ctypes.data,
+                                        accu.ctypes.data, total.ctypes.data)
+    return accu, total, int(status)

@@ -97,6 +97,7 @@ def reference_mc(name):
                     scenarios._detectors(mc, s.get('detectors')),
                     fluence=scenarios._fluence(mc, s.get('fluence')),
                     surface=scenarios._surface(mc, s.get('surface')),
+                    trace=scenarios._trace(mc, s.get('trace')),
                     options=scenarios.options(mc, s), rnginit=s['rnginit'])
     else:
         from xopto.mcvox import mc
@@ -109,6 +110,7 @@ def reference_mc(name):
         obj = mc.Mc(vox, mats, scenarios._source(mc.mcsource, s['source']),
                     scenarios._detectors(mc, s.get('detectors')),
                     fluence=scenarios._fluence(mc, s.get('fluence')),
+                    trace=scenarios._trace(mc, s.get('trace')),
                     options=scenarios.options(mc, s), rnginit=s['rnginit'])
         obj.voxels.material[...] = scenarios.voxel_layout(g, s['layout'])
     if 'rmax' in s:
@@ -123,7 +125,7 @@ extern "C" void ref_run(unsigned long num_packets, unsigned num_streams, float r
                         const void *layers, const void *source, const void *surface,
                         const void *trace, const void *fluence, const void *detectors,
                         const float *lut, int *ibuf, float *fbuf, unsigned long *accu,
-                        int nthreads) {
+                        int nthreads, unsigned long ibuf_stride, unsigned long fbuf_stride) {
     #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
     for (long t = 0; t < (long)num_streams; ++t) {
         unsigned long q = num_packets / num_streams + ((unsigned long)t < num_packets % num_streams);
@@ -135,7 +137,7 @@ extern "C" void ref_run(unsigned long num_packets, unsigned num_streams, float r
                  num_layers, (McLayer const *)layers, (McSource const *)source,
                  (McSurfaceLayouts const *)surface, (McTrace const *)trace,
                  (McFluence const *)fluence, (McDetectors const *)detectors, lut,
-                 (mc_int_t *)ibuf, fbuf, (mc_accu_t *)accu);
+                 (mc_int_t *)(ibuf + t * ibuf_stride), fbuf + t * fbuf_stride, (mc_accu_t *)accu);
     }
 }
 '''
@@ -147,7 +149,8 @@ extern "C" void ref_run(unsigned long num_packets, unsigned num_streams, float r
                         const void *voxels, unsigned num_materials, const void *materials,
                         const void *source, const void *surface, const void *trace,
                         const void *fluence, const void *detectors, const float *lut,
-                        int *ibuf, float *fbuf, unsigned long *accu, int nthreads) {
+                        int *ibuf, float *fbuf, unsigned long *accu, int nthreads,
+                        unsigned long ibuf_stride, unsigned long fbuf_stride) {
     #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
     for (long t = 0; t < (long)num_streams; ++t) {
         unsigned long q = num_packets / num_streams + ((unsigned long)t < num_packets % num_streams);
@@ -160,10 +163,28 @@ extern "C" void ref_run(unsigned long num_packets, unsigned num_streams, float r
                  (mc_size_t)num_materials, (McMaterial const *)materials,
                  (McSource const *)source, (McSurfaceLayouts const *)surface,
                  (McTrace const *)trace, (McFluence const *)fluence,
-                 (McDetectors const *)detectors, lut, (mc_int_t *)ibuf, fbuf,
-                 (mc_accu_t *)accu);
+                 (McDetectors const *)detectors, lut, (mc_int_t *)(ibuf + t * ibuf_stride),
+                 fbuf + t * fbuf_stride, (mc_accu_t *)accu);
     }
 }
+'''
+
+
+DRIVER_SV = r'''
+/* ---- driver (oracle/render_ref.py): the reference's SamplingVolume kernel
+   over all packets of a trace, as one work-item ---- */
+#if MC_USE_SAMPLING_VOLUME
+extern "C" void ref_sv(unsigned long num_packets, const void *trace, const void *sv,
+                       unsigned long *total_weight, int *ibuf, float *fbuf,
+                       unsigned long *accu) {
+    ref_set_global_id(0);
+    mc_cnt_t done = 0;
+    uint32_t nk = 0;
+    SamplingVolume((mc_cnt_t)num_packets, &done, &nk, (McTrace const *)trace,
+                   (McSamplingVolume const *)sv, (mc_accu_t *)total_weight,
+                   (mc_int_t *)ibuf, fbuf, (mc_accu_t *)accu);
+}
+#endif
 '''
 
 
@@ -191,6 +212,7 @@ def render(name, nphotons=None):
         f.write('#include "../ref_shim.h"\n')
         f.write(src)
         f.write(DRIVER_MCML if s['medium'] == 'mcml' else DRIVER_MCVOX)
+        f.write(DRIVER_SV)
     packed = m._packed
     blobs = {
         'medium': np.array([0 if s['medium'] == 'mcml' else 1]),
@@ -225,6 +247,21 @@ def render(name, nphotons=None):
         offsets['fluence'] = (a.offset, a.size)
     for k, (o, n) in offsets.items():
         blobs['off_' + k] = np.array([o, n])
+    if m.trace is not None:
+        # per-stream trace buffers: McKernel numbers the packets of each call
+        # from 0, so every stream gets its own slice (remapped in run_ref)
+        blobs['trace_maxlen'] = np.array([m.trace.maxlen])
+        sv_spec = s.get('sampling_volume')
+        if sv_spec:
+            # the SamplingVolume kernel's arguments, packed as Mc.sampling_volume
+            # does after clearing the buffer allocators (xopto/mcml/mc.py:1096-1114)
+            for alloc in (m.cl_rw_accumulator_allocator, m.cl_rw_float_allocator,
+                          m.cl_rw_int_allocator):
+                alloc.clear()
+            sv = scenarios._sampling_volume(m, sv_spec)
+            blobs['sv_trace'] = _blob(m.trace.cl_pack(m, nphotons=nphotons))
+            blobs['sv'] = _blob(sv.cl_pack(m))
+            blobs['sv_size'] = np.array([int(np.prod(sv.shape))])
     np.savez_compressed(os.path.join(REF_DIR, name + '.npz'), **blobs)
     return compile_ref(name)
 
@@ -246,8 +283,11 @@ def run_ref(name, nphotons, streams, seeds, nthreads=1):
     x = np.ascontiguousarray(seeds[0], dtype=np.uint64).copy()
     a = np.ascontiguousarray(seeds[1], dtype=np.uint32)
     accu = np.zeros((int(d['accu_size'][0]),), dtype=np.uint64)
-    fbuf = np.zeros((16,), dtype=np.float32)
-    ibuf = np.zeros((16,), dtype=np.int32)
+    maxlen = int(d['trace_maxlen'][0]) if 'trace_maxlen' in d else 0
+    qmax = -(-int(nphotons) // int(streams))
+    istride, fstride = (qmax, qmax * maxlen * 8) if maxlen else (0, 0)
+    fbuf = np.zeros((max(16, int(streams) * fstride),), dtype=np.float32)
+    ibuf = np.zeros((max(16, int(streams) * istride),), dtype=np.int32)
     p = lambda k: d[k].ctypes.data
     f = lib.ref_run
     f.restype = None
@@ -258,7 +298,8 @@ def run_ref(name, nphotons, streams, seeds, nthreads=1):
           C.c_void_p(p('source')), C.c_void_p(p('surface')), C.c_void_p(p('trace')),
           C.c_void_p(p('fluence')), C.c_void_p(p('detectors')), C.c_void_p(p('lut')),
           ibuf.ctypes.data_as(C.c_void_p), fbuf.ctypes.data_as(C.c_void_p),
-          accu.ctypes.data_as(C.c_void_p), C.c_int(int(nthreads)))
+          accu.ctypes.data_as(C.c_void_p), C.c_int(int(nthreads)), C.c_ulong(istride),
+          C.c_ulong(fstride))
     else:
         f(C.c_ulong(int(nphotons)), C.c_uint(int(streams)), rmax, x.ctypes.data_as(C.c_void_p),
           a.ctypes.data_as(C.c_void_p), C.c_void_p(p('voxel_cfg')), C.c_void_p(p('voxels')),
@@ -266,13 +307,43 @@ def run_ref(name, nphotons, streams, seeds, nthreads=1):
           C.c_void_p(p('source')), C.c_void_p(p('surface')), C.c_void_p(p('trace')),
           C.c_void_p(p('fluence')), C.c_void_p(p('detectors')), C.c_void_p(p('lut')),
           ibuf.ctypes.data_as(C.c_void_p), fbuf.ctypes.data_as(C.c_void_p),
-          accu.ctypes.data_as(C.c_void_p), C.c_int(int(nthreads)))
+          accu.ctypes.data_as(C.c_void_p), C.c_int(int(nthreads)), C.c_ulong(istride),
+          C.c_ulong(fstride))
     out = {'accu': accu, 'rng_x': x}
+    if maxlen:
+        # stream t's j-th packet is packet t + j * streams
+        T, N = int(streams), int(nphotons)
+        n_ev = np.zeros((N,), np.int32)
+        ev = np.zeros((N, maxlen * 8), np.float32)
+        for t in range(T):
+            q = N // T + (t < N % T)
+            pk = t + T * np.arange(q)
+            n_ev[pk] = ibuf[t * istride:t * istride + q]
+            ev[pk] = fbuf[t * fstride:t * fstride + q * maxlen * 8].reshape(q, maxlen * 8)
+        out['trace_n'] = n_ev
+        out['trace_data'] = ev.reshape(-1)
     for k in list(d.keys()):
         if k.startswith('off_'):
             o, n = int(d[k][0]), int(d[k][1])
             out[k[4:]] = accu[o:o + n].copy()
     return out
+
+
+def run_ref_sv(name, trace_n, trace_data):
+    """Runs the reference's own SamplingVolume kernel of a rendered build on
+    a trace (packets in order); returns (voxel tallies, total weight)."""
+    d = dict(np.load(os.path.join(REF_DIR, name + '.npz')))
+    lib = C.CDLL(os.path.join(REF_DIR, name + '.so'))
+    n = np.ascontiguousarray(trace_n, dtype=np.int32)
+    f = np.ascontiguousarray(trace_data, dtype=np.float32)
+    accu = np.zeros((int(d['sv_size'][0]),), dtype=np.uint64)
+    total = np.zeros((1,), dtype=np.uint64)
+    lib.ref_sv.restype = None
+    lib.ref_sv(C.c_ulong(n.size), C.c_void_p(d['sv_trace'].ctypes.data),
+               C.c_void_p(d['sv'].ctypes.data), total.ctypes.data_as(C.c_void_p),
+               n.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p),
+               accu.ctypes.data_as(C.c_void_p))
+    return accu, total
 
 
 if __name__ == '__main__':

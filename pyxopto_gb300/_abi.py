@@ -78,6 +78,12 @@ class McgbTrace(C.Structure):
                 ('reserved', u32), ('data_offset', u64), ('count_offset', u64)]
 
 
+class McgbSamplingVolume(C.Structure):
+    _fields_ = [('top_left', f32 * 3), ('voxel_size', f32 * 3), ('shape', u32 * 3),
+                ('multiplier', f32), ('offset', u64), ('k', i32), ('max_events', u32),
+                ('num_packets', u64)]
+
+
 class McgbRunOptions(C.Structure):
     _fields_ = [('method', i32), ('math', i32), ('use_lottery', i32),
                 ('packet_weight_min', f32), ('lottery_chance', f32), ('rmax', f32),
@@ -139,7 +145,8 @@ class McgbBatchConfig(C.Structure):
 
 SIZEOF_KINDS = [McgbLayer, McgbSource, McgbDetector, McgbFluence, McgbTrace,
                 McgbMaterial, McgbMcmlConfig, McgbMcvoxConfig, McgbBuffers,
-                McgbRunOptions, McgbPf, McgbBatchSim, McgbBatchConfig, McgbSurface]
+                McgbRunOptions, McgbPf, McgbBatchSim, McgbBatchConfig, McgbSurface,
+                McgbSamplingVolume]
 
 
 def check_layout(sizeof_fn):

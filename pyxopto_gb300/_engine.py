@@ -267,6 +267,60 @@ class McEngine:
         b.counters = d['counters'].data_ptr()
         return b
 
+    def sampling_volume(self, trace, sv, wgsize: int = None, maxthreads: int = None,
+                        exportsrc=None, verbose: bool = False):
+        """Adds the sampling volume of a trace to ``sv`` and returns it
+        (xopto/mcml/mc.py:1040-1217).  Every packet of the trace is walked
+        through the voxels of ``sv`` on the GPU; ``wgsize``, ``maxthreads``
+        and ``exportsrc`` are accepted for compatibility and ignored."""
+        if self._trace is None:
+            raise RuntimeError('This Monte Carlo simulator was built without the Trace '
+                               'functionality (the trace argument of Mc.__init__ was None)! '
+                               'Sampling volume analysis requires trace functionality!')
+        torch = torch_cuda()
+        lib = _lib.load()
+        t0 = time.perf_counter()
+        device = torch.device('cuda', torch.cuda.current_device())
+        cfg = sv.pack(self)
+        nphotons = len(trace)
+        cfg.max_events = trace.maxlen
+        cfg.num_packets = nphotons
+        n_vox = int(np.prod(sv.shape))
+        d = self._dev
+        if nphotons:
+            events = np.ascontiguousarray(trace.data).view(np.float32).reshape(-1)
+            d['sv_trace'] = torch.from_numpy(events).pin_memory().to(device, non_blocking=True)
+            d['sv_counts'] = torch.from_numpy(np.ascontiguousarray(trace.n, dtype=np.int32)).to(device)
+        d['sv_accu'] = torch.zeros((n_vox,), dtype=torch.int64, device=device)
+        d['sv_total'] = torch.zeros((1,), dtype=torch.int64, device=device)
+        d['counters'] = torch.zeros((_abi.NUM_COUNTERS,), dtype=torch.int64, device=device)
+        stream = torch.cuda.current_stream().cuda_stream
+        t1 = time.perf_counter()
+        if nphotons:
+            _lib.check(lib.mcgb_sampling_volume(
+                C.byref(cfg), C.c_void_p(d['sv_trace'].data_ptr()), int(d['sv_trace'].numel()),
+                C.c_void_p(d['sv_counts'].data_ptr()), C.c_void_p(d['sv_accu'].data_ptr()), n_vox,
+                C.c_void_p(d['sv_total'].data_ptr()), C.c_void_p(d['counters'].data_ptr()),
+                C.c_void_p(stream)))
+        counters = (C.c_uint64 * _abi.NUM_COUNTERS)()
+        code = lib.mcgb_check_counters(C.c_void_p(d['counters'].data_ptr()), C.c_void_p(stream),
+                                       counters)
+        t2 = time.perf_counter()
+        _lib.check(code)
+        accu = d['sv_accu'].cpu().numpy().view(np.uint64)
+        total = d['sv_total'].cpu().numpy().view(np.uint64)
+        sv.update_data(self, accumulators=[accu], nphotons=nphotons, total_weight=total)
+        t3 = time.perf_counter()
+        self._run_report.update(upload=t1 - t0, execution=t2 - t1, download=t3 - t2,
+                                items=nphotons, threads=None)
+        if verbose:
+            print('SamplingVolume processed {:d} packets:\n'
+                  '    uploaded/built in: {:10.3f} ms\n'
+                  '    executed in      : {:10.3f} ms\n'
+                  '    downloaded in    : {:10.3f} ms'.format(
+                      nphotons, (t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3))
+        return sv
+
     def _launch(self, lib_fn, cfg, buffers, torch):
         stream = torch.cuda.current_stream().cuda_stream
         _lib.check(lib_fn(C.byref(cfg), C.byref(buffers), C.c_void_p(stream)))

@@ -34,6 +34,7 @@ UNITS = [
     ('batched_exact.cu', ['-fmad=false']),
     ('mlp.cu', []),
     ('noalloc.cu', []),
+    ('sampling_volume.cu', ['-fmad=false']),
     ('rng_host.cpp', None),
 ]
 

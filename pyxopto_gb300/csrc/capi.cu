@@ -20,6 +20,11 @@
 #include "errors.h"
 #include "batch_launch.h"
 
+namespace mcgb_sv {
+cudaError_t launch(const McgbSamplingVolume &sv, const float *trace, const int32_t *counts,
+                   uint64_t *accu, uint64_t *total_weight, uint64_t *counters, cudaStream_t stream);
+}
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -262,6 +267,7 @@ int mcgb_sizeof(int kind) {
         case 11: return (int)sizeof(McgbBatchSim);
         case 12: return (int)sizeof(McgbBatchConfig);
         case 13: return (int)sizeof(McgbSurface);
+        case 14: return (int)sizeof(McgbSamplingVolume);
         default: return -1;
     }
 }
@@ -440,6 +446,45 @@ int mcgb_batched_run(const McgbBatchConfig *cfg, const McgbBatchSim *dev_sims,
                                            dev_counters, (cudaStream_t)stream, grid, block, deadline);
     if (e != cudaSuccess) return cuda_fail(e, "batched launch");
     return MCGB_OK;
+}
+
+int mcgb_sampling_volume(const McgbSamplingVolume *sv, const float *dev_trace,
+                         uint64_t trace_floats, const int32_t *dev_counts,
+                         uint64_t *dev_accu, uint64_t accu_size, uint64_t *dev_total_weight,
+                         uint64_t *dev_counters, void *stream) {
+    if (!sv) return fail(MCGB_E_INVALID, "sampling volume is NULL");
+    uint64_t voxels = 1;
+    for (int i = 0; i < 3; ++i) {
+        if (sv->shape[i] == 0 || sv->shape[i] > 2147483647u)
+            return fail(MCGB_E_INVALID, "sampling volume: shape[%d] = %u outside [1, 2^31 - 1]", i,
+                        sv->shape[i]);
+        if (!std::isfinite(sv->voxel_size[i]) || sv->voxel_size[i] == 0.0f ||
+            !std::isfinite(sv->top_left[i]))
+            return fail(MCGB_E_INVALID, "sampling volume: axis %d has corner %g and voxel size %g", i,
+                        (double)sv->top_left[i], (double)sv->voxel_size[i]);
+        voxels *= sv->shape[i];
+    }
+    if (voxels > (1ull << 40)) return fail(MCGB_E_SIZE, "sampling volume: %llu voxels", (unsigned long long)voxels);
+    if (sv->offset > accu_size || voxels > accu_size - sv->offset)
+        return fail(MCGB_E_SIZE, "sampling volume: voxels [%llu, +%llu) beyond the accumulator (%llu)",
+                    (unsigned long long)sv->offset, (unsigned long long)voxels,
+                    (unsigned long long)accu_size);
+    if (sv->num_packets == 0) return MCGB_OK;
+    if (sv->max_events == 0) return fail(MCGB_E_INVALID, "sampling volume: max_events is 0");
+    if (sv->num_packets > (1ull << 40) / sv->max_events)
+        return fail(MCGB_E_SIZE, "sampling volume: %llu packets of %u events",
+                    (unsigned long long)sv->num_packets, sv->max_events);
+    uint64_t need = sv->num_packets * sv->max_events * MCGB_TRACE_ENTRY_LEN;
+    if (trace_floats < need)
+        return fail(MCGB_E_SIZE, "sampling volume: trace of %llu floats, %llu needed",
+                    (unsigned long long)trace_floats, (unsigned long long)need);
+    if (!dev_trace || !dev_counts || !dev_accu || !dev_total_weight)
+        return fail(MCGB_E_INVALID, "sampling volume: NULL trace, count, accumulator or weight buffer");
+    if (reinterpret_cast<uintptr_t>(dev_trace) % 16)
+        return fail(MCGB_E_INVALID, "sampling volume: trace buffer not 16-byte aligned");
+    cudaError_t e = mcgb_sv::launch(*sv, dev_trace, dev_counts, dev_accu, dev_total_weight,
+                                    dev_counters, (cudaStream_t)stream);
+    return e == cudaSuccess ? MCGB_OK : cuda_fail(e, "sampling volume launch");
 }
 
 int mcgb_reduce_tallies(uint64_t *host_dst, const uint64_t *host_src, uint64_t n) {

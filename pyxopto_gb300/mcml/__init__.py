@@ -1,2 +1,2 @@
 """Layered-medium simulator (drop-in for xopto.mcml)."""
-from . import mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes, mclayer, mcsource, mcsurface
+from . import mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes, mclayer, mcsource, mcsurface, mcsv

@@ -22,7 +22,7 @@ from .. import _abi, _lib
 from .._engine import McEngine, torch_cuda
 from ..mcbase.mcutil import Axis, RadialAxis
 from . import (mclayer, mcsource, mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes,
-               mcsurface)
+               mcsurface, mcsv)
 
 MC_RESULT_TYPE = Tuple[mctrace.Trace, mcfluence.Fluence, mcdetector.Detectors]
 

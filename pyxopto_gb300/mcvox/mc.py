@@ -13,7 +13,7 @@ from .._engine import McEngine, torch_cuda
 from ..mcbase.mcmaterial import Material, Materials
 from ..mcbase.mcutil import Axis, RadialAxis
 from . import (mcgeometry, mcsource, mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes,
-               mcmaterial)
+               mcmaterial, mcsv)
 
 
 class Mc(McEngine):

@@ -32,6 +32,7 @@ Writes
                          validate.py:1227-1758); written by
                          `make_golden.py linear_probe`.
 """
+import hashlib
 import os
 import pickle
 import sys
@@ -52,6 +53,24 @@ def reference_seeds(n, xinit):
     return clrng.Random().seeds(n, xinit=xinit)
 
 
+def reference_filters(name, trace_n, trace_data):
+    """Packet counts and event hashes of the traces kept by the reference's
+    own Filter (xopto/mcbase/mctrace.py:216-330) for scenarios.TRACE_FILTERS."""
+    m = render_ref.reference_mc(name)
+    from xopto.mcbase import mctrace
+    out = {}
+    for i, spec in enumerate(scenarios.TRACE_FILTERS):
+        tr = mctrace.Trace(m.trace)
+        tr.data = np.frombuffer(trace_data.tobytes(), dtype=tr.dtype(m)).reshape(trace_n.size, -1)
+        tr.n = np.asarray(trace_n, dtype=np.int32)
+        filt, dropped = mctrace.Filter(**spec)(tr, update=False)
+        out['filter{}_n'.format(i)] = np.asarray(filt.n, dtype=np.int32)
+        out['filter{}_sha256'.format(i)] = np.array(
+            [hashlib.sha256(np.ascontiguousarray(filt.data).tobytes()).hexdigest()])
+        out['filter{}_dropped'.format(i)] = np.array([dropped])
+    return out
+
+
 def make_scenario(name):
     s = scenarios.SCENARIOS[name]
     render_ref.render(name)
@@ -60,8 +79,16 @@ def make_scenario(name):
     data = {'seeds_x': x, 'seeds_a': a, 'rng_x_final': out['rng_x'],
             'nphotons': np.array([s['nphotons']]), 'streams': np.array([s['streams']])}
     for k, v in out.items():
-        if k not in ('accu', 'rng_x'):
+        if k not in ('accu', 'rng_x', 'trace_n', 'trace_data'):
             data['tally_' + k] = v
+    if 'trace_n' in out:
+        data['trace_n'] = out['trace_n']
+        data['trace_sha256'] = np.array([hashlib.sha256(out['trace_data'].tobytes()).hexdigest()])
+        data.update(reference_filters(name, out['trace_n'], out['trace_data']))
+    if s.get('sampling_volume'):
+        sv, total = render_ref.run_ref_sv(name, out['trace_n'], out['trace_data'])
+        data['sv_accu'] = sv
+        data['sv_total'] = total
     np.savez_compressed(os.path.join(HERE, 'golden_{}.npz'.format(name)), **data)
     print(name, {k: int(v.sum()) for k, v in data.items() if k.startswith('tally_')})
 

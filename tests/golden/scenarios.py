@@ -403,6 +403,30 @@ SCENARIOS = {
                                    n=3, spacing=4.2e-4),
                        specular=dict(type='Total')),
         nphotons=4000, streams=32, rnginit=113),
+    # packet traces and their sampling volume (xopto/mcbase/mctrace.py,
+    # xopto/mcbase/kernel/mcsv.template.c); the voxel grid reaches well past
+    # rmax so no event sits less than a voxel below its lower corner
+    'trace_sampling_volume': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=2e-3, n=1.4, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), specular=dict(type='Total')),
+        trace=dict(maxlen=64),
+        sampling_volume=dict(x=[-3e-3, 3e-3, 30], y=[-3e-3, 3e-3, 30], z=[0.0, 2e-3, 10]),
+        rmax=1e-3, nphotons=400, streams=32, rnginit=127),
+    'vox_trace_sampling_volume': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 10], z=[0.0, 1e-3, 10]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=150.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Total'), specular=dict(type='Total')),
+        trace=dict(maxlen=48),
+        sampling_volume=dict(x=[-2e-3, 2e-3, 20], y=[-2e-3, 2e-3, 20], z=[-1e-3, 1e-3, 10]),
+        nphotons=300, streams=30, rnginit=131),
 }
 
 # Bench workloads (not golden-tested at these sizes): the layered
@@ -547,6 +571,38 @@ def _probe_detector(pkg, d):
     return getattr(pkg.mcdetector, d['type'])(**kw)
 
 
+def _trace(pkg, spec):
+    """Trace of a scenario (xopto/mcbase/mctrace.py)."""
+    if not spec:
+        return None
+    return pkg.mctrace.Trace(maxlen=spec['maxlen'], options=spec.get('options', 7),
+                             plon=spec.get('plon', True))
+
+
+# Trace filters checked against the reference's Filter on the traces of the
+# trace scenarios (xopto/mcbase/mctrace.py:53-441).  The third one also shows
+# that a path-length criterion after another criterion has no effect there.
+TRACE_FILTERS = [
+    dict(z=(-1e-9, 1e-9), pz=(-1.0, -0.5), r=(0.0, 5e-4, (0.0, 0.0))),
+    dict(pl=(0.0, 4e-3)),
+    dict(r=[(0.0, 2e-4, (0.0, 0.0)), (4e-4, 8e-4, (1e-4, 0.0))], pl=(0.0, 1e-3)),
+    dict(dir=(0.5, 1.0, (0.0, 0.0, -1.0)), x=[(-1e-3, 0.0), (2e-4, 6e-4)], y=(-5e-4, 5e-4)),
+]
+
+
+def _filter(pkg, spec):
+    return pkg.mctrace.Filter(**spec)
+
+
+def _sampling_volume(mc_obj, spec):
+    """SamplingVolume of a scenario (xopto/mcbase/mcsv.py); ``mc_obj`` is a
+    simulator of either package."""
+    import importlib
+    mod = importlib.import_module(type(mc_obj).__module__.rsplit('.', 1)[0] + '.mcsv')
+    A = mod.Axis
+    return mod.SamplingVolume(A(*spec['x']), A(*spec['y']), A(*spec['z']))
+
+
 def _fluence(pkg, spec):
     if not spec:
         return None
@@ -609,6 +665,7 @@ def build_mc(name_or_spec, fast=False, package='pyxopto_gb300', scheduling='stat
             for l in s['layers']])
         obj = mc.Mc(layers, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
                     fluence=_fluence(mc, s.get('fluence')), surface=_surface(mc, s.get('surface')),
+                    trace=_trace(mc, s.get('trace')),
                     options=options(mc, s, fast, scheduling), rnginit=s['rnginit'])
     else:
         mc = importlib.import_module(package + '.mcvox.mc')
@@ -619,8 +676,8 @@ def build_mc(name_or_spec, fast=False, package='pyxopto_gb300', scheduling='stat
         mats = [mc.mcmaterial.Material(n=m['n'], mua=m['mua'], mus=m['mus'], pf=_pf(mc, m['pf']))
                 for m in s['materials']]
         obj = mc.Mc(vox, mats, _source(mc.mcsource, s['source']), _detectors(mc, s.get('detectors')),
-                    fluence=_fluence(mc, s.get('fluence')), options=options(mc, s, fast, scheduling),
-                    rnginit=s['rnginit'])
+                    fluence=_fluence(mc, s.get('fluence')), trace=_trace(mc, s.get('trace')),
+                    options=options(mc, s, fast, scheduling), rnginit=s['rnginit'])
     if 'rmax' in s:
         obj.rmax = s['rmax']
     return obj

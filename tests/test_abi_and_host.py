@@ -108,3 +108,66 @@ def test_options_and_plugins():
     # Fresnel closed form at normal incidence
     from pyxopto_gb300.mcbase import mcutil
     assert abs(mcutil.reflectance(1.0, 1.33) - (0.33 / 2.33) ** 2) < 1e-15
+
+
+def test_sampling_volume_validation(lib):
+    """mcgb_sampling_volume checks the grid, the accumulator range and the
+    trace size before it launches anything (no GPU needed)."""
+    from pyxopto_gb300 import _abi
+    from pyxopto_gb300.mcml import mcsv
+
+    def cfg():
+        sv = mcsv.SamplingVolume(mcsv.Axis(-1e-3, 1e-3, 4), mcsv.Axis(-1e-3, 1e-3, 5),
+                                 mcsv.Axis(0.0, 1e-3, 3))
+        c = sv.pack(None)
+        c.max_events, c.num_packets = 10, 7
+        return c
+
+    def call(c, trace=16, floats=7 * 10 * 8, accu_size=60):
+        return lib.mcgb_sampling_volume(C.byref(c), C.c_void_p(trace), floats, C.c_void_p(16),
+                                        C.c_void_p(16), accu_size, C.c_void_p(16), None, None)
+
+    assert lib.mcgb_sampling_volume(None, None, 0, None, None, 0, None, None, None) == _abi.E_INVALID
+    c = cfg()
+    c.shape[1] = 0
+    assert call(c) == _abi.E_INVALID
+    c = cfg()
+    c.voxel_size[2] = 0.0
+    assert call(c) == _abi.E_INVALID
+    assert call(cfg(), accu_size=59) == _abi.E_SIZE
+    c = cfg()
+    c.offset = 1
+    assert call(c) == _abi.E_SIZE
+    assert call(cfg(), floats=7 * 10 * 8 - 1) == _abi.E_SIZE
+    c = cfg()
+    c.max_events = 0
+    assert call(c) == _abi.E_INVALID
+    assert call(cfg(), trace=8) == _abi.E_INVALID             # not 16-byte aligned
+    assert b'aligned' in lib.mcgb_last_error()
+    c = cfg()
+    c.num_packets = 0
+    assert call(c) == _abi.OK                                # nothing to do, no launch
+
+
+def test_sampling_volume_host_objects():
+    """SamplingVolume packing and scaling (xopto/mcbase/mcsv.py:313-395) and
+    the trace maxlen rules (xopto/mcbase/mctrace.py:848-857)."""
+    from pyxopto_gb300.mcml import mcsv, mctrace
+    sv = mcsv.SamplingVolume(mcsv.Axis(-1e-3, 1e-3, 4), mcsv.Axis(-1e-3, 1e-3, 5),
+                             mcsv.Axis(0.0, 1e-3, 2))
+    c = sv.pack(None)
+    assert list(c.shape) == [4, 5, 2] and c.k == 0x7FFFFF
+    assert abs(c.multiplier - 1.0 / 4e-4) < 1e-3 and abs(c.top_left[0] + 1e-3) < 1e-9
+    raw = np.arange(40, dtype=np.uint64)
+    sv.update_data(None, [raw], total_weight=np.array([0x7FFFFF * 3], dtype=np.uint64))
+    assert sv.data.shape == (2, 5, 4) and sv.weight == 3.0
+    assert np.allclose(sv.data.ravel(), raw / (0x7FFFFF / 4e-4))
+    sv.update_data(None, [raw], total_weight=np.array([0x7FFFFF], dtype=np.uint64))
+    assert sv.weight == 4.0
+    sv2 = mcsv.SamplingVolume.fromdict(sv.todict())
+    assert sv2.shape == sv.shape and sv2.data is None
+    assert mctrace.Trace(100, options=mctrace.Trace.TRACE_START).maxlen == 1
+    assert mctrace.Trace(100, options=mctrace.Trace.TRACE_START | mctrace.Trace.TRACE_END).maxlen == 2
+    assert mctrace.Trace(100).maxlen == 100
+    with pytest.raises(TypeError):
+        mctrace.Filter(x=0.5)

@@ -232,3 +232,64 @@ def test_linear_probe_sweep(cuda, lib, key):
     assert abs(err.mean()) < 1.0, err.mean()
     ratio = refl.sum(axis=0) / ref.sum(axis=0)
     assert np.all(np.abs(ratio - 1.0) < 0.01), ratio
+
+
+SV_SCENARIOS = sorted(n for n, s in scenarios.SCENARIOS.items() if s.get('sampling_volume'))
+
+
+def _sv_expected(oracle, sim, sv, tr):
+    cfg = sv.pack(sim)
+    cfg.max_events, cfg.num_packets = tr.maxlen, len(tr)
+    accu, total, status = oracle.sampling_volume(cfg, tr.n, np.ascontiguousarray(tr.data).view(np.float32))
+    assert status == 0
+    data = np.reshape(accu.astype(np.float64), sv.shape) * (1.0 / (sv.k * sv._multiplier()))
+    return data, float(total[0]) / sv.k
+
+
+@pytest.mark.parametrize('name', SV_SCENARIOS)
+@pytest.mark.parametrize('scheduling', ['static', 'dynamic'])
+def test_sampling_volume_bit_identical_to_oracle(cuda, lib, oracle, name, scheduling):
+    """Mc.sampling_volume on the GPU equals the oracle's walk (pinned to the
+    reference's SamplingVolume kernel) on the same trace, tally for tally;
+    under static scheduling the trace itself is the oracle's."""
+    s = scenarios.SCENARIOS[name]
+    sim = scenarios.build_mc(name, scheduling=scheduling)
+    tr, _, _ = sim.run(s['nphotons'], maxthreads=s['streams'])
+    if scheduling == 'static':
+        ref = oracle.run(sim, s['nphotons'], s['streams'], oracle.PORTABLE)
+        ioff, icnt = sim._int.find(sim.trace)
+        assert np.array_equal(tr.n, ref['int'][ioff:ioff + icnt])
+    sv = scenarios._sampling_volume(sim, s['sampling_volume'])
+    out = sim.sampling_volume(tr, sv)
+    assert out is sv
+    data, weight = _sv_expected(oracle, sim, sv, tr)
+    assert np.array_equal(out.data, data)
+    assert out.weight == weight
+    assert np.count_nonzero(out.data) > 100
+
+
+def test_sampling_volume_large_trace(cuda, lib, oracle):
+    """A 20,000-packet, 500-event trace of the FAST dynamic kernel, filtered
+    to the packets that leave through the top within 0.5 mm of the source
+    (the reference's sampling-volume example), then a 100^3 sampling volume:
+    bit-identical to the oracle, and a second call accumulates."""
+    from pyxopto_gb300.mcml import mc
+    layers = mc.mclayer.Layers([
+        mc.mclayer.Layer(d=0.0, n=1.45, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0)),
+        mc.mclayer.Layer(d=1e-2, n=1.33, mua=2e2, mus=250e2, pf=mc.mcpf.Hg(0.9)),
+        mc.mclayer.Layer(d=0.0, n=1.45, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.0))])
+    trace = mc.mctrace.Trace(maxlen=500, filter=mc.mctrace.Filter(
+        z=(-1e-9, 1e-9), pz=(-1.0, -0.2), r=(0.0, 5e-4, (0.0, 0.0))))
+    sim = mc.Mc(layers, mc.mcsource.Line(), trace=trace,
+                options=[mc.mcoptions.McUseNativeMath(True), mc.mcoptions.McScheduling('dynamic')],
+                rnginit=3)
+    sim.rmax = 1e-2
+    tr, _, _ = sim.run(20000)
+    assert len(tr) > 500
+    A = mc.mcsv.Axis
+    sv = mc.mcsv.SamplingVolume(A(-1e-3, 1e-3, 100), A(-1e-3, 1e-3, 100), A(0.0, 2e-3, 100))
+    sim.sampling_volume(tr, sv)
+    data, weight = _sv_expected(oracle, sim, sv, tr)
+    assert np.array_equal(sv.data, data) and sv.weight == weight
+    sim.sampling_volume(tr, sv)
+    assert np.array_equal(sv.data, 2.0 * data)
