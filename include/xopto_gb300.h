@@ -109,7 +109,9 @@ enum {
     MCGB_SRC_LAMBERTIAN_FIBER = 5,
     MCGB_SRC_UNIFORM_BEAM = 6,
     MCGB_SRC_ISOTROPIC_POINT = 7,
-    MCGB_SRC_ISOTROPIC_VOXEL = 8
+    MCGB_SRC_ISOTROPIC_VOXEL = 8,
+    MCGB_SRC_UNIFORM_RECTANGULAR = 9,
+    MCGB_SRC_LAMBERTIAN_RECTANGULAR = 10
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
        MCGB_DET_TOTAL_PL = 4, MCGB_DET_CARTESIAN = 5, MCGB_DET_CARTESIAN_PL = 6,
@@ -197,7 +199,15 @@ typedef struct McgbMaterial {
      surrounding medium), sigma (beam radii; fibre core radius and
      sqrt(1 - NA^2) or NA) and clip (fibre core index); IsotropicPoint
      (point.py:74-140) takes position; IsotropicVoxel (voxel.py:78-107) takes
-     the voxel index as floats in position. */
+     the voxel index as floats in position.
+   UniformRectangular / LambertianRectangular, layered media only
+     (xopto/mcml/mcsource/rectangular.py:85-140,363-413): position = centre
+     (z = 0 for a source on the surface), sigma = width (x) and height (y),
+     clip = refractive index of the source, angular = cosine of the maximum
+     emission angle in air (uniform) or NA (Lambertian), layer_index = the
+     layer that holds the source.  The reference's rectangular sources do not
+     build with a specular detector (their launch reads a reflectance field
+     the source lacks), so that combination is rejected. */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];
@@ -207,8 +217,8 @@ typedef struct McgbSource {
     float transformation[9];                /* row-major a_11 .. a_33 */
     float sigma[2];
     float clip;
-    int32_t layer_index;                    /* IsotropicPoint                  */
-    float reserved;
+    int32_t layer_index;                    /* IsotropicPoint, rectangular     */
+    float angular;                          /* rectangular: cos_min or NA      */
 } McgbSource;                               /* 104 bytes */
 
 /* Surface detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;

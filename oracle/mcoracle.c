@@ -559,6 +559,28 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu, NULL);
         s->w = 1.0f - R;
         s->layer = src->layer_index;
+    } else if (src->kind >= MCGB_SRC_UNIFORM_RECTANGULAR) {
+        /* UniformRectangular / LambertianRectangular.mcsim_launch,
+           xopto/mcml/mcsource/rectangular.py:85-140,363-413 */
+        float sin_fi, cos_fi, sin_theta, cos_theta;
+        s->pos.x = src->position[0] + (rnd(x, a) - 0.5f) * src->sigma[0];
+        s->pos.y = src->position[1] + (rnd(x, a) - 0.5f) * src->sigma[1];
+        s->pos.z = src->position[2];
+        m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
+        if (src->kind == MCGB_SRC_UNIFORM_RECTANGULAR) {
+            cos_theta = 1.0f - rnd(x, a) * (1.0f - src->angular);
+            sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        } else {
+            sin_theta = sqrtf(rnd(x, a)) * src->angular;
+        }
+        float n_layer = c->layers[src->layer_index].n;
+        sin_theta = sin_theta / n_layer;
+        cos_theta = sqrtf(1.0f - sin_theta * sin_theta);
+        s->dir.x = cos_fi * sin_theta;
+        s->dir.y = sin_fi * sin_theta;
+        s->dir.z = cos_theta;
+        s->w = 1.0f - reflectance_cos2(src->clip, n_layer, cos_theta);
+        s->layer = src->layer_index;
     } else if (src->kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
         mcml_launch_fiber(mm, c, s, x, a, accu);
         s->layer = 1;

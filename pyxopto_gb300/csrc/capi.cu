@@ -104,7 +104,7 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
     if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
-    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_ISOTROPIC_VOXEL)
+    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_LAMBERTIAN_RECTANGULAR)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
     if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI && src.kind <= MCGB_SRC_LAMBERTIAN_FIBER &&
         !(src.sigma[0] >= 0.0f && src.sigma[1] >= 0.0f && src.sigma[1] <= 1.0f && src.clip > 0.0f))
@@ -303,10 +303,20 @@ int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *strea
     if ((cfg->source.kind == MCGB_SRC_UNIFORM_FIBER || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
          cfg->source.kind == MCGB_SRC_UNIFORM_BEAM) && !(cfg->source.direction[2] > 0.0f))
         return fail(MCGB_E_INVALID, "source: the z component of the direction must be positive");
-    if (cfg->source.kind == MCGB_SRC_ISOTROPIC_POINT &&
+    bool rectangular = cfg->source.kind == MCGB_SRC_UNIFORM_RECTANGULAR ||
+                       cfg->source.kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR;
+    if ((cfg->source.kind == MCGB_SRC_ISOTROPIC_POINT || rectangular) &&
         (cfg->source.layer_index < 1 || cfg->source.layer_index > (int32_t)cfg->num_layers - 2))
-        return fail(MCGB_E_INVALID, "point source layer index %d outside the sample layers [1, %u]",
+        return fail(MCGB_E_INVALID, "source layer index %d outside the sample layers [1, %u]",
                     cfg->source.layer_index, cfg->num_layers - 2);
+    if (rectangular) {
+        if (cfg->specular.kind != MCGB_DET_NONE)
+            return fail(MCGB_E_UNSUPPORTED, "rectangular sources take no specular detector "
+                        "(the reference's launch code for them does not build with one)");
+        if (!(cfg->source.angular >= 0.0f && cfg->source.angular <= 1.0f && cfg->source.clip >= 1.0f))
+            return fail(MCGB_E_INVALID, "rectangular source: angular parameter %g, index %g",
+                        (double)cfg->source.angular, (double)cfg->source.clip);
+    }
     for (uint32_t i = 0; i < cfg->num_layers; ++i) {
         r = check_pf(cfg->pf_kind, cfg->layers[i].pf, buf, "layer", i);
         if (r) return r;
@@ -339,7 +349,9 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
-    if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI)
+    if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
+        cfg->source.kind == MCGB_SRC_UNIFORM_RECTANGULAR ||
+        cfg->source.kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR)
         return fail(MCGB_E_UNSUPPORTED, "source kind %d is implemented for layered media only",
                     cfg->source.kind);
     if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL) {

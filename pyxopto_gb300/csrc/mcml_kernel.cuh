@@ -163,6 +163,27 @@ static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c
         if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, R, 0.0f, accu);
         w = 1.0f - R;
         layer = src.layer_index;
+    } else if (src.kind >= MCGB_SRC_UNIFORM_RECTANGULAR) {
+        /* xopto/mcml/mcsource/rectangular.py:85-140 (uniform in the cosine up
+           to cos_min) and 363-413 (Lambertian up to NA); the emission angle in
+           air is refracted into the layer that holds the source */
+        pos.x = src.position[0] + (rng.next() - 0.5f) * src.sigma[0];
+        pos.y = src.position[1] + (rng.next() - 0.5f) * src.sigma[1];
+        pos.z = src.position[2];
+        float sin_fi, cos_fi, sin_theta, cos_theta;
+        mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
+        if (src.kind == MCGB_SRC_UNIFORM_RECTANGULAR) {
+            cos_theta = 1.0f - rng.next() * (1.0f - src.angular);
+            sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        } else {
+            sin_theta = mc_sqrt(rng.next()) * src.angular;
+        }
+        float n_layer = L[src.layer_index].g1.x;
+        sin_theta = mc_div(sin_theta, n_layer);
+        cos_theta = mc_sqrt(1.0f - sin_theta * sin_theta);
+        dir = f3{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
+        w = 1.0f - reflectance_cos2(src.clip, n_layer, cos_theta);
+        layer = src.layer_index;
     } else if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
         mcml_launch_fiber(c, L, rng, pos, dir, w, accu);
         layer = 1;

@@ -355,3 +355,83 @@ class IsotropicPoint(Source):
         return 'IsotropicPoint(position=({}, {}, {}))'.format(*self._position)
 
     __repr__ = __str__
+
+
+class UniformRectangular(Source):
+    """Rectangular source whose emission is uniform in the cosine of the
+    angle up to the numerical aperture in air, refracted into the layer that
+    holds the source; the Fresnel reflectance at the source face is taken
+    from the initial weight (xopto/mcml/mcsource/rectangular.py:32-316)."""
+    _kind = _abi.SRC_UNIFORM_RECTANGULAR
+
+    def __init__(self, width: float, height: float = None, n: float = 1.0, na: float = 0.0,
+                 position=(0.0, 0.0, 0.0)):
+        if isinstance(width, UniformRectangular):
+            o = width
+            width, height, n, na, position = o.width, o.height, o.n, o.na, o.position
+        self._width = float(width)
+        self._height = float(height)
+        self._n = max(1.0, float(n))
+        self._na = max(0.0, float(na))
+        self._position = np.zeros((3,))
+        self._position[:] = position
+
+    def _set_width(self, v):
+        self._width = float(v)
+
+    def _set_height(self, v):
+        self._height = float(v)
+
+    def _set_n(self, v):
+        self._n = max(1.0, float(v))
+
+    def _set_na(self, v):
+        self._na = max(0.0, float(v))
+
+    def _set_position(self, p):
+        self._position[:] = p
+
+    width = property(lambda self: self._width, _set_width, None, 'Source width (m).')
+    height = property(lambda self: self._height, _set_height, None, 'Source height (m).')
+    n = property(lambda self: self._n, _set_n, None, 'Source refractive index.')
+    na = property(lambda self: self._na, _set_na, None, 'Source numerical aperture.')
+    position = property(lambda self: self._position, _set_position)
+
+    def _angular(self) -> float:
+        return (1.0 - self._na ** 2) ** 0.5
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """rectangular.py:246-300: a source at z <= 0 sits on the surface in
+        layer 1, otherwise in the layer that contains its depth."""
+        if self._position[2] <= 0.0:
+            position = (self._position[0], self._position[1], 0.0)
+            layer_index = 1
+        else:
+            position = self._position
+            layer_index = mc.layer_index(self._position[2])
+        target.kind = self._kind
+        target.position[:] = [float(v) for v in position]
+        target.sigma[:] = [self._width, self._height]
+        target.clip = self._n
+        target.angular = self._angular()
+        target.layer_index = layer_index
+        return target
+
+    def todict(self):
+        return {'type': type(self).__name__, 'width': self._width, 'height': self._height,
+                'n': self._n, 'na': self._na, 'position': self._position.tolist()}
+
+    def __str__(self):
+        return '{}(width={}, height={}, n={}, na={}, position=({}, {}, {}))'.format(
+            type(self).__name__, self._width, self._height, self._n, self._na, *self._position)
+
+    __repr__ = __str__
+
+
+class LambertianRectangular(UniformRectangular):
+    """Rectangular source with Lambertian emission up to the numerical
+    aperture in air (xopto/mcml/mcsource/rectangular.py:317-529)."""
+    _kind = _abi.SRC_LAMBERTIAN_RECTANGULAR
+
+    def _angular(self) -> float:
+        return self._na

@@ -406,6 +406,29 @@ SCENARIOS = {
     # packet traces and their sampling volume (xopto/mcbase/mctrace.py,
     # xopto/mcbase/kernel/mcsv.template.c); the voxel grid reaches well past
     # rmax so no event sits less than a voxel below its lower corner
+    # rectangular sources (xopto/mcml/mcsource/rectangular.py): on the
+    # surface, and inside the second layer
+    'rect_uniform': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1e-3, n=1.4, mua=100.0, mus=1.2e4, pf=['Hg', 0.8]),
+                dict(d=INF, n=1.36, mua=30.0, mus=8e3, pf=['Hg', 0.9])],
+        source=dict(type='UniformRectangular', width=6e-4, height=3e-4, n=1.5, na=0.4,
+                    position=(1e-4, -2e-4, 0.0)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 2e-3, 20]),
+                       bottom=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=137),
+    'rect_lambertian_inside': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=5e-4, n=1.38, mua=80.0, mus=1.5e4, pf=['Hg', 0.85]),
+                dict(d=1.5e-3, n=1.45, mua=20.0, mus=1e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='LambertianRectangular', width=4e-4, height=8e-4, n=1.6, na=0.6,
+                    position=(0.0, 1e-4, 8e-4)),
+        detectors=dict(top=dict(type='Cartesian', x=[-1e-3, 1e-3, 8], y=[-1e-3, 1e-3, 6]),
+                       bottom=dict(type='Radial', axis=[0.0, 2e-3, 10])),
+        nphotons=3000, streams=32, rnginit=139),
     'trace_sampling_volume': dict(
         medium='mcml',
         layers=[_air(['Hg', 0.0]),
