@@ -111,14 +111,19 @@ enum {
     MCGB_SRC_ISOTROPIC_POINT = 7,
     MCGB_SRC_ISOTROPIC_VOXEL = 8,
     MCGB_SRC_UNIFORM_RECTANGULAR = 9,
-    MCGB_SRC_LAMBERTIAN_RECTANGULAR = 10
+    MCGB_SRC_LAMBERTIAN_RECTANGULAR = 10,
+    MCGB_SRC_UNIFORM_FIBER_LUT_NI = 11,
+    MCGB_SRC_UNIFORM_FIBER_LUT = 12,
+    MCGB_SRC_UNIFORM_RECTANGULAR_LUT = 13
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
        MCGB_DET_TOTAL_PL = 4, MCGB_DET_CARTESIAN = 5, MCGB_DET_CARTESIAN_PL = 6,
        MCGB_DET_SYMMETRIC_X = 7, MCGB_DET_LINEAR_ARRAY = 8, MCGB_DET_SIX_AROUND_ONE = 9,
        MCGB_DET_FIBER_ARRAY = 10, MCGB_DET_LINEAR_ARRAY_PL = 11, MCGB_DET_SIX_AROUND_ONE_PL = 12,
-       MCGB_DET_FIBER_ARRAY_PL = 13 };
+       MCGB_DET_FIBER_ARRAY_PL = 13, MCGB_DET_TOTAL_LUT = 14, MCGB_DET_TOTAL_LUT_PL = 15,
+       MCGB_DET_FIBER_LUT_ARRAY = 16 };
 #define MCGB_DET_FIBER_FLOATS 13            /* floats per FIBER_ARRAY fibre    */
+#define MCGB_DET_LUT_FIBER_FLOATS 16        /* floats per FIBER_LUT_ARRAY fibre */
 enum { MCGB_FLUENCE_NONE = 0, MCGB_FLUENCE_DEPOSITION = 1, MCGB_FLUENCE_RATE = 2 };
 /* Trace flags (xopto/mcbase/mctrace.py TRACE_START/END/ALL). */
 enum { MCGB_TRACE_NONE = 0, MCGB_TRACE_START = 1, MCGB_TRACE_END = 2, MCGB_TRACE_ALL = 7 };
@@ -207,7 +212,16 @@ typedef struct McgbMaterial {
      emission angle in air (uniform) or NA (Lambertian), layer_index = the
      layer that holds the source.  The reference's rectangular sources do not
      build with a specular detector (their launch reads a reflectance field
-     the source lacks), so that combination is rejected. */
+     the source lacks), so that combination is rejected.
+   Emission look-up-table sources, layered media only: the cosine of the
+     emission angle in air is drawn from lut_size floats of the float table
+     at lut_offset (EmissionLut, sampled by the reference's
+     fp_linear_lut_rel_sample, xopto/mcbase/kernel/mcbase.template.h:2507-2520).
+     UniformFiberLutNI (xopto/mcml/mcsource/fiberni.py:581-700) takes the
+     UniformFiberNI fields; UniformFiberLut (fiber.py:690-830) the
+     UniformFiber fields, and unlike UniformFiber it refracts the launch
+     direction into the sample; UniformRectangularLut (rectangular.py:530-700)
+     the rectangular fields without angular. */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];
@@ -219,7 +233,9 @@ typedef struct McgbSource {
     float clip;
     int32_t layer_index;                    /* IsotropicPoint, rectangular     */
     float angular;                          /* rectangular: cos_min or NA      */
-} McgbSource;                               /* 104 bytes */
+    uint32_t lut_offset;                    /* emission LUT sources            */
+    uint32_t lut_size;
+} McgbSource;                               /* 108 bytes */
 
 /* Surface detector (xopto/mcml/mcdetector/radial.py:66-75,117-150;
    total.py:52-56,86-108; radialpl.py:138-179,343-378; totalpl.py:107-135;
@@ -243,7 +259,17 @@ typedef struct McgbSource {
        cosine;
      FIBER_ARRAY (fiberarray.py:103-162,270-312): per fibre transformation
        (9), position (2), core r^2, acceptance cosine.  Top and bottom slots
-       only. */
+       only.
+   Collection look-up-table detectors: the deposit is the weight times a
+   sensitivity read from a CollectionLut at |cos| of the exit direction, by
+   the reference's fp_linear_lut_sample
+   (xopto/mcbase/kernel/mcbase.template.h:2522-2535; 0 outside the table):
+     TOTAL_LUT (total.py:240-330) and TOTAL_LUT_PL (totalpl.py, TotalLutPl):
+       direction, LUT first position in r_min, 1/span in inv_dr, size in n_y,
+       offset in table_offset; n = 1 (TOTAL_LUT_PL: n_pl bins);
+     FIBER_LUT_ARRAY (probe/fiberlutarray.py:30-200,290-324): n fibres, per
+       fibre transformation (9), position (2), core r^2, LUT first position,
+       1/span, and the LUT size and offset as uint32 bit patterns. */
 typedef struct McgbDetector {
     int32_t kind;
     float direction[3];

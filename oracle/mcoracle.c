@@ -255,12 +255,81 @@ static inline void xf_xy(const float *T, float x, float y, float *ox, float *oy)
     *oy = T[3] * x + T[4] * y + T[5] * 0.0f;
 }
 
+/* Linear look-up tables, the reference's fp_linear_lut_rel_sample and
+   fp_linear_lut_sample macros (xopto/mcbase/kernel/mcbase.template.h:
+   2507-2535): the lower entry is taken at the index rounded to the nearest
+   integer, the interpolation weight is the fractional part of the index. */
+static float lut_at(const float *t, uint32_t n, float fp_index) {
+    uint32_t i1 = cvt_uint(fp_index + 0.5f);
+    float w2 = fp_index - floorf(fp_index);
+    uint32_t i2 = i1 + 1u < n ? i1 + 1u : n - 1u;
+    return t[i1] * (1.0f - w2) + t[i2] * w2;
+}
+
+static float lut_rel(const float *t, uint32_t n, float where, float fallback) {
+    float fp_index = where * (float)(n - 1u);
+    return cvt_uint(fp_index + 0.5f) < n ? lut_at(t, n, fp_index) : fallback;
+}
+
+static float lut_abs(const float *t, uint32_t n, float first, float inv_span, float where,
+                     float fallback) {
+    float fp_index = (where - first) * inv_span * (float)(n - 1u);
+    return (fp_index >= 0.0f && fp_index <= (float)(n - 1u)) ? lut_at(t, n, fp_index) : fallback;
+}
+
+/* TotalLut (xopto/mcml/mcdetector/total.py:296-323), TotalLutPl (totalpl.py,
+   TotalLutPl) and FiberLutArray (probe/fiberlutarray.py:100-200): weight *
+   sensitivity, deposited as weight_to_int(weight*sensitivity)
+   (xopto/mcml/kernel/mcml.template.h:606). */
+static void lut_detector_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir, float weight,
+                                 float opl, uint64_t *accu, const float *lut) {
+    uint64_t index = 0;
+    float sensitivity = 0.0f;
+    if (det->kind == MCGB_DET_FIBER_LUT_ARRAY) {
+        const float *t = lut + det->table_offset;
+        uint32_t fiber = det->n;
+        float lx, ly;
+        for (uint32_t i = 0; i < det->n; ++i) {
+            const float *f = t + (size_t)i * MCGB_DET_LUT_FIBER_FLOATS;
+            xf_xy(f, pos.x - f[9], pos.y - f[10], &lx, &ly);
+            if (lx * lx + ly * ly <= f[11]) {
+                fiber = i;
+                break;
+            }
+        }
+        if (fiber >= det->n) return;
+        const float *f = t + (size_t)fiber * MCGB_DET_LUT_FIBER_FLOATS;
+        float pz = f[6] * dir.x + f[7] * dir.y + f[8] * dir.z;
+        uint32_t n, rel;
+        memcpy(&n, &f[14], 4);
+        memcpy(&rel, &f[15], 4);
+        if (n >= 1u && rel <= det->n_y && n <= det->n_y - rel)
+            sensitivity = lut_abs(t + rel, n, f[12], f[13], fabsf(pz), 0.0f);
+        index = fiber;
+    } else {
+        float c = fabsf(dir.x * det->direction[0] + dir.y * det->direction[1] +
+                        dir.z * det->direction[2]);
+        sensitivity = lut_abs(lut + det->table_offset, det->n_y, det->r_min, det->inv_dr, c, 0.0f);
+        if (det->kind == MCGB_DET_TOTAL_LUT_PL) {
+            float pl = opl;
+            if (det->pl_log_scale) pl = m_log(mm, fmaxf(pl, 1e-12f));
+            index = (uint64_t)clip_i(cvt_int((pl - det->pl_min) * det->inv_dpl), 0, (int32_t)det->n_pl - 1);
+        }
+    }
+    uint32_t w = cvt_uint(weight * sensitivity * (float)MCGB_ACCU_K + 0.5f);
+    if (w > 0) accu[det->offset + index] += w;
+}
+
 /* Fibre-probe detectors: LinearArray (xopto/mcml/mcdetector/probe/lineararray.py:103-162),
    SixAroundOne (sixaroundone.py:103-184; a later ring test overrides an earlier hit),
    FiberArray (fiberarray.py:103-162) and the path-length variants (lineararraypl.py,
    sixaroundonepl.py, fiberarraypl.py: bin pl_index*n + fibre). */
 static void probe_deposit(int mm, const McgbDetector *det, v3 pos, v3 dir, float weight,
                           float opl, uint64_t *accu, const float *lut) {
+    if (det->kind >= MCGB_DET_TOTAL_LUT) {
+        lut_detector_deposit(mm, det, pos, dir, weight, opl, accu, lut);
+        return;
+    }
     int base = det->kind >= MCGB_DET_LINEAR_ARRAY_PL ? det->kind - 3 : det->kind;
     const float *t = lut + det->table_offset;
     const float *T = t;
@@ -427,10 +496,12 @@ typedef struct {
    (fiber.py:576-640).  The tilted kinds test pt_mc.z (0 after the move to
    the surface) against the critical cosine before refracting, so their
    direction is never refracted. */
-static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x,
-                              uint32_t a, uint64_t *accu) {
+static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, const float *lut, MlState *s,
+                              uint64_t *x, uint32_t a, uint64_t *accu) {
     const McgbSource *src = &c->source;
-    int tilted = src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER;
+    int from_lut = src->kind == MCGB_SRC_UNIFORM_FIBER_LUT_NI || src->kind == MCGB_SRC_UNIFORM_FIBER_LUT;
+    int tilted = src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER ||
+                 src->kind == MCGB_SRC_UNIFORM_FIBER_LUT;
     int lambertian = src->kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
                      src->kind == MCGB_SRC_LAMBERTIAN_FIBER;
     float n_sample = c->layers[1].n, n_core = src->clip;
@@ -458,7 +529,10 @@ static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint6
     if (lambertian) {
         sin_theta = sqrtf(rnd(x, a)) * src->sigma[1];
     } else {
-        cos_theta = 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
+        /* UniformFiberLut(NI): fp_linear_lut_rel_sample of the emission LUT
+           (fiber.py:796-797, fiberni.py:625-626) */
+        cos_theta = from_lut ? lut_rel(lut + src->lut_offset, src->lut_size, rnd(x, a), 0.0f)
+                             : 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
         sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
     }
     sin_theta = sin_theta / (tilted ? n_core : n_sample);
@@ -471,6 +545,11 @@ static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint6
         d.z = T[6] * pt.x + T[7] * pt.y + T[8] * pt.z;
         float cc = cos_critical(n_core, n_sample);
         s->dir = d;
+        if (from_lut && d.z > cc) {
+            /* UniformFiberLut refracts into the sample, fiber.py:806-813 */
+            v3 normal = {0.0f, 0.0f, 1.0f};
+            s->dir = refract3(d, normal, n_core, n_sample);
+        }
         R = reflectance(n_core, n_sample, d.z, cc);
         if (c->specular.kind != MCGB_DET_NONE)
             detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu, NULL);
@@ -490,8 +569,8 @@ static void mcml_launch_fiber(int mm, const McgbMcmlConfig *c, MlState *s, uint6
 /* Line.mcsim_launch (xopto/mcml/mcsource/line.py:95-108),
    GaussianBeam.mcsim_launch (xopto/mcml/mcsource/gaussianbeam.py:119-170) and
    the fibre sources (mcml_launch_fiber). */
-static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x,
-                        uint32_t a, uint64_t *accu) {
+static void mcml_launch(int mm, const McgbMcmlConfig *c, const float *lut, MlState *s,
+                        uint64_t *x, uint32_t a, uint64_t *accu) {
     const McgbSource *src = &c->source;
     if (src->kind == MCGB_SRC_LINE) {
         s->w = 1.0f - src->reflectance;
@@ -559,9 +638,12 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
             detector_deposit(mm, &c->specular, s->pos, d, R, 0.0f, accu, NULL);
         s->w = 1.0f - R;
         s->layer = src->layer_index;
-    } else if (src->kind >= MCGB_SRC_UNIFORM_RECTANGULAR) {
-        /* UniformRectangular / LambertianRectangular.mcsim_launch,
-           xopto/mcml/mcsource/rectangular.py:85-140,363-413 */
+    } else if (src->kind == MCGB_SRC_UNIFORM_RECTANGULAR ||
+               src->kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR ||
+               src->kind == MCGB_SRC_UNIFORM_RECTANGULAR_LUT) {
+        /* UniformRectangular / LambertianRectangular / UniformRectangularLut
+           .mcsim_launch, xopto/mcml/mcsource/rectangular.py:85-140,363-413,
+           600-650 */
         float sin_fi, cos_fi, sin_theta, cos_theta;
         s->pos.x = src->position[0] + (rnd(x, a) - 0.5f) * src->sigma[0];
         s->pos.y = src->position[1] + (rnd(x, a) - 0.5f) * src->sigma[1];
@@ -569,6 +651,9 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
         m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
         if (src->kind == MCGB_SRC_UNIFORM_RECTANGULAR) {
             cos_theta = 1.0f - rnd(x, a) * (1.0f - src->angular);
+            sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+        } else if (src->kind == MCGB_SRC_UNIFORM_RECTANGULAR_LUT) {
+            cos_theta = lut_rel(lut + src->lut_offset, src->lut_size, rnd(x, a), 0.0f);
             sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
         } else {
             sin_theta = sqrtf(rnd(x, a)) * src->angular;
@@ -582,7 +667,7 @@ static void mcml_launch(int mm, const McgbMcmlConfig *c, MlState *s, uint64_t *x
         s->w = 1.0f - reflectance_cos2(src->clip, n_layer, cos_theta);
         s->layer = src->layer_index;
     } else if (src->kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
-        mcml_launch_fiber(mm, c, s, x, a, accu);
+        mcml_launch_fiber(mm, c, lut, s, x, a, accu);
         s->layer = 1;
     } else {
         float cos_fi, sin_fi, r;
@@ -800,7 +885,7 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
         TraceState ts;
         memset(&s, 0, sizeof(s));
         ts.photon_index = p; ts.trace_count = 0; ts.events = 0;
-        mcml_launch(mm, c, &s, &x, a, accu);
+        mcml_launch(mm, c, lut, &s, &x, a, accu);
         uint32_t events = EV_LAUNCH;
 #define MO_TRACE_SNAPSHOT() do { ts.pos = s.pos; ts.dir = s.dir; ts.w = s.w; ts.opl = s.opl; \
                                  ts.events = events; } while (0)

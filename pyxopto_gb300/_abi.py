@@ -23,11 +23,14 @@ SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI, SRC_LAMBERTIAN_FIBER_NI = 0, 
 SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT = 4, 5, 6, 7
 SRC_ISOTROPIC_VOXEL = 8
 SRC_UNIFORM_RECTANGULAR, SRC_LAMBERTIAN_RECTANGULAR = 9, 10
+SRC_UNIFORM_FIBER_LUT_NI, SRC_UNIFORM_FIBER_LUT, SRC_UNIFORM_RECTANGULAR_LUT = 11, 12, 13
 DET_NONE, DET_TOTAL, DET_RADIAL, DET_RADIAL_PL, DET_TOTAL_PL = 0, 1, 2, 3, 4
 DET_CARTESIAN, DET_CARTESIAN_PL, DET_SYMMETRIC_X = 5, 6, 7
 DET_LINEAR_ARRAY, DET_SIX_AROUND_ONE, DET_FIBER_ARRAY = 8, 9, 10
 DET_LINEAR_ARRAY_PL, DET_SIX_AROUND_ONE_PL, DET_FIBER_ARRAY_PL = 11, 12, 13
 DET_FIBER_FLOATS = 13
+DET_TOTAL_LUT, DET_TOTAL_LUT_PL, DET_FIBER_LUT_ARRAY = 14, 15, 16
+DET_LUT_FIBER_FLOATS = 16
 FLUENCE_NONE, FLUENCE_DEPOSITION, FLUENCE_RATE = 0, 1, 2
 TRACE_NONE, TRACE_START, TRACE_END, TRACE_ALL = 0, 1, 2, 7
 MATH_EXACT, MATH_FAST = 0, 1
@@ -58,7 +61,7 @@ class McgbSource(C.Structure):
     _fields_ = [('kind', i32), ('position', f32 * 3), ('direction', f32 * 3),
                 ('direction_reflected', f32 * 3), ('reflectance', f32),
                 ('transformation', f32 * 9), ('sigma', f32 * 2), ('clip', f32),
-                ('layer_index', i32), ('angular', f32)]
+                ('layer_index', i32), ('angular', f32), ('lut_offset', u32), ('lut_size', u32)]
 
 
 class McgbDetector(C.Structure):

@@ -104,8 +104,17 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
     if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
-    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_LAMBERTIAN_RECTANGULAR)
+    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_UNIFORM_RECTANGULAR_LUT)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
+    if (src.kind >= MCGB_SRC_UNIFORM_FIBER_LUT_NI) {
+        if (src.lut_size == 0 || !b->fp_lut || !range_ok(src.lut_offset, src.lut_size, b->fp_lut_size))
+            return fail(MCGB_E_SIZE, "source emission LUT [%u, +%u) beyond the float table (%llu)",
+                        src.lut_offset, src.lut_size, (unsigned long long)b->fp_lut_size);
+        if (src.kind != MCGB_SRC_UNIFORM_RECTANGULAR_LUT &&
+            !(src.sigma[0] >= 0.0f && src.clip > 0.0f))
+            return fail(MCGB_E_INVALID, "fiber source: core radius %g, core index %g",
+                        (double)src.sigma[0], (double)src.clip);
+    }
     if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI && src.kind <= MCGB_SRC_LAMBERTIAN_FIBER &&
         !(src.sigma[0] >= 0.0f && src.sigma[1] >= 0.0f && src.sigma[1] <= 1.0f && src.clip > 0.0f))
         return fail(MCGB_E_INVALID, "fiber source: core radius %g, angular parameter %g, core index %g",
@@ -121,13 +130,24 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     for (int i = 0; i < 3; ++i) {
         const McgbDetector &d = dets[i];
         if (d.kind == MCGB_DET_NONE) continue;
-        if (d.kind < MCGB_DET_TOTAL || d.kind > MCGB_DET_FIBER_ARRAY_PL)
+        if (d.kind < MCGB_DET_TOTAL || d.kind > MCGB_DET_FIBER_LUT_ARRAY)
             return fail(MCGB_E_INVALID, "%s detector: unknown kind %d", names[i], d.kind);
         const bool pl = d.kind == MCGB_DET_RADIAL_PL || d.kind == MCGB_DET_TOTAL_PL ||
                         d.kind == MCGB_DET_CARTESIAN_PL || d.kind == MCGB_DET_LINEAR_ARRAY_PL ||
-                        d.kind == MCGB_DET_SIX_AROUND_ONE_PL || d.kind == MCGB_DET_FIBER_ARRAY_PL;
-        if (d.kind >= MCGB_DET_LINEAR_ARRAY) {
-            if (i == 2) return fail(MCGB_E_INVALID, "the specular slot takes no fibre-probe detector");
+                        d.kind == MCGB_DET_SIX_AROUND_ONE_PL || d.kind == MCGB_DET_FIBER_ARRAY_PL ||
+                        d.kind == MCGB_DET_TOTAL_LUT_PL;
+        if (d.kind >= MCGB_DET_LINEAR_ARRAY && i == 2)
+            return fail(MCGB_E_INVALID, "the specular slot takes no fibre-probe or look-up-table detector");
+        if (d.kind >= MCGB_DET_TOTAL_LUT) {
+            const bool fibers = d.kind == MCGB_DET_FIBER_LUT_ARRAY;
+            if (fibers ? (d.n == 0 || d.n > 4096) : d.n != 1)
+                return fail(MCGB_E_INVALID, "%s look-up-table detector: n = %u", names[i], d.n);
+            if (d.n_y == 0 || (fibers && d.n_y < (uint64_t)MCGB_DET_LUT_FIBER_FLOATS * d.n))
+                return fail(MCGB_E_INVALID, "%s look-up-table detector: table of %u floats", names[i], d.n_y);
+            if (!b->fp_lut || !range_ok(d.table_offset, d.n_y, b->fp_lut_size))
+                return fail(MCGB_E_SIZE, "%s look-up-table detector table [%u, +%u) beyond the float table",
+                            names[i], d.table_offset, d.n_y);
+        } else if (d.kind >= MCGB_DET_LINEAR_ARRAY) {
             const int base = d.kind >= MCGB_DET_LINEAR_ARRAY_PL ? d.kind - 3 : d.kind;
             if (base == MCGB_DET_SIX_AROUND_ONE && d.n != 7)
                 return fail(MCGB_E_INVALID, "%s six-around-one detector needs n = 7", names[i]);
@@ -301,10 +321,12 @@ int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *strea
     if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL)
         return fail(MCGB_E_UNSUPPORTED, "the voxel source is implemented for voxelized media only");
     if ((cfg->source.kind == MCGB_SRC_UNIFORM_FIBER || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
-         cfg->source.kind == MCGB_SRC_UNIFORM_BEAM) && !(cfg->source.direction[2] > 0.0f))
+         cfg->source.kind == MCGB_SRC_UNIFORM_BEAM || cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_LUT) &&
+        !(cfg->source.direction[2] > 0.0f))
         return fail(MCGB_E_INVALID, "source: the z component of the direction must be positive");
     bool rectangular = cfg->source.kind == MCGB_SRC_UNIFORM_RECTANGULAR ||
-                       cfg->source.kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR;
+                       cfg->source.kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR ||
+                       cfg->source.kind == MCGB_SRC_UNIFORM_RECTANGULAR_LUT;
     if ((cfg->source.kind == MCGB_SRC_ISOTROPIC_POINT || rectangular) &&
         (cfg->source.layer_index < 1 || cfg->source.layer_index > (int32_t)cfg->num_layers - 2))
         return fail(MCGB_E_INVALID, "source layer index %d outside the sample layers [1, %u]",
@@ -349,9 +371,11 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
+    if (cfg->top.kind >= MCGB_DET_TOTAL_LUT || cfg->bottom.kind >= MCGB_DET_TOTAL_LUT)
+        return fail(MCGB_E_UNSUPPORTED, "look-up-table detectors are layered-media only (the reference's "
+                    "voxelized TotalLut reads a LUT accessor its kernel lacks and does not build)");
     if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
-        cfg->source.kind == MCGB_SRC_UNIFORM_RECTANGULAR ||
-        cfg->source.kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR)
+        cfg->source.kind >= MCGB_SRC_UNIFORM_RECTANGULAR)
         return fail(MCGB_E_UNSUPPORTED, "source kind %d is implemented for layered media only",
                     cfg->source.kind);
     if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL) {

@@ -287,6 +287,80 @@ MCGB_DEV int probe_pl_index(const McgbDetector &det, float opl) {
     return clip_i(cvt_int((pl - det.pl_min) * det.inv_dpl), 0, (int)det.n_pl - 1);
 }
 
+/* Linear look-up tables (mc_fp_lut_t, xopto/mcbase/kernel/mcbase.template.h:
+   2494-2535).  Both samplers take the lower table entry at the index rounded
+   to the nearest integer but interpolate with the fractional part of the
+   index, exactly as the reference's macros do.
+   lut_sample_rel: position `where` in [0, 1] over the n entries
+   (fp_linear_lut_rel_sample); lut_sample: position (where - first) *
+   inv_span over the table, `fallback` outside it (fp_linear_lut_sample). */
+MCGB_DEV float lut_interp(const float *t, uint32_t n, float fp_index) {
+    uint32_t i1 = cvt_uint(fp_index + 0.5f);
+    float w2 = fp_index - floorf(fp_index);
+    uint32_t i2 = i1 + 1u < n ? i1 + 1u : n - 1u;
+    return t[i1] * (1.0f - w2) + t[i2] * w2;
+}
+
+MCGB_DEV float lut_sample_rel(const float *t, uint32_t n, float where, float fallback) {
+    float fp_index = where * (float)(n - 1u);
+    if (cvt_uint(fp_index + 0.5f) < n) return lut_interp(t, n, fp_index);
+    return fallback;
+}
+
+MCGB_DEV float lut_sample(const float *t, uint32_t n, float first, float inv_span, float where,
+                          float fallback) {
+    float fp_index = (where - first) * inv_span * (float)(n - 1u);
+    if (fp_index >= 0.0f && fp_index <= (float)(n - 1u)) return lut_interp(t, n, fp_index);
+    return fallback;
+}
+
+/* weight_to_int(weight*sensitivity) of the look-up-table detectors
+   (xopto/mcml/kernel/mcml.template.h:606). */
+MCGB_DEV uint32_t lut_weight(float weight, float sensitivity) {
+    return cvt_uint(weight * sensitivity * (float)MCGB_ACCU_K + 0.5f);
+}
+
+/* Collection look-up-table detectors: TotalLut (xopto/mcml/mcdetector/
+   total.py:296-323), TotalLutPl (totalpl.py, TotalLutPl) and FiberLutArray
+   (probe/fiberlutarray.py:100-200): weight x sensitivity at the |cosine| of
+   the exit direction to the detector (fibre) axis; each fibre's table lives
+   inside the detector's float table, whose size (n_y) the C ABI checked. */
+MCGB_DEV void lut_detector_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir,
+                                   float weight, float opl, uint64_t *accu, const float *lut) {
+    uint64_t index = 0;
+    float sensitivity = 0.0f;
+    if (det.kind == MCGB_DET_FIBER_LUT_ARRAY) {
+        const float *t = lut + det.table_offset;
+        uint32_t fiber = det.n;
+        for (uint32_t i = 0; i < det.n; ++i) {
+            const float *f = t + (size_t)i * MCGB_DET_LUT_FIBER_FLOATS;
+            float2 lp = transform_xy(f, pos.x - f[9], pos.y - f[10]);
+            if (lp.x * lp.x + lp.y * lp.y <= f[11]) {
+                fiber = i;
+                break;
+            }
+        }
+        if (fiber >= det.n) return;
+        const float *f = t + (size_t)fiber * MCGB_DET_LUT_FIBER_FLOATS;
+        float pz = f[6] * dir.x + f[7] * dir.y + f[8] * dir.z;
+        uint32_t n = __float_as_uint(f[14]), rel = __float_as_uint(f[15]);
+        if (n >= 1u && rel <= det.n_y && n <= det.n_y - rel)
+            sensitivity = lut_sample(t + rel, n, f[12], f[13], fabsf(pz), 0.0f);
+        index = fiber;
+    } else {
+        f3 ddir{det.direction[0], det.direction[1], det.direction[2]};
+        sensitivity = lut_sample(lut + det.table_offset, det.n_y, det.r_min, det.inv_dr,
+                                 fabsf(dot3(dir, ddir)), 0.0f);
+        if (det.kind == MCGB_DET_TOTAL_LUT_PL) {
+            float pl = opl;
+            if (det.pl_log_scale) pl = mc_log(fmaxf(pl, 1e-12f));
+            index = (uint64_t)clip_i(cvt_int((pl - det.pl_min) * det.inv_dpl), 0, (int)det.n_pl - 1);
+        }
+    }
+    uint32_t w = lut_weight(weight, sensitivity);
+    if (w > 0) accu_add(accu, det.offset + index, w);
+}
+
 /* Fibre-probe detectors: LinearArray (xopto/mcml/mcdetector/probe/
    lineararray.py:103-162), SixAroundOne (sixaroundone.py:103-184; a later
    ring test overrides an earlier hit, as there), FiberArray
@@ -294,6 +368,10 @@ MCGB_DEV int probe_pl_index(const McgbDetector &det, float opl) {
    sixaroundonepl.py, fiberarraypl.py: bin pl_index*n + fibre). */
 MCGB_DEV void probe_deposit(const McgbDetector &det, const f3 &pos, const f3 &dir, float weight,
                             float opl, uint64_t *accu, const float *lut) {
+    if (det.kind >= MCGB_DET_TOTAL_LUT) {
+        lut_detector_deposit(det, pos, dir, weight, opl, accu, lut);
+        return;
+    }
     const int base = det.kind >= MCGB_DET_LINEAR_ARRAY_PL ? det.kind - 3 : det.kind;
     const float *t = lut + det.table_offset;
     const float *T = t;
@@ -338,7 +416,7 @@ MCGB_DEV void probe_deposit(const McgbDetector &det, const f3 &pos, const f3 &di
     float pz = T[6] * dir.x + T[7] * dir.y + T[8] * dir.z;
     float accept = (float)(cos_min <= fabsf(pz));
     uint64_t index = fiber;
-    if (det.kind >= MCGB_DET_LINEAR_ARRAY_PL) index += (uint64_t)probe_pl_index(det, opl) * det.n;
+    if (base != det.kind) index += (uint64_t)probe_pl_index(det, opl) * det.n;
     uint32_t w = weight_to_u32(weight, accept);
     if (w > 0) accu_add(accu, det.offset + index, w);
 }

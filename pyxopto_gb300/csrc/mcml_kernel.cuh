@@ -51,10 +51,13 @@ struct MlSmem {
    surface) with the critical cosine before refracting, so the reference
    never refracts their direction; that is restated as is. */
 static __device__ __forceinline__ void mcml_launch_fiber(const McgbMcmlConfig &c, const MlLayer *L,
-                                                         Rng &rng, f3 &pos, f3 &dir, float &w,
-                                                         uint64_t *accu) {
+                                                         const float *lut, Rng &rng, f3 &pos,
+                                                         f3 &dir, float &w, uint64_t *accu) {
     const McgbSource &src = c.source;
-    const bool tilted = src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER;
+    const bool from_lut = src.kind == MCGB_SRC_UNIFORM_FIBER_LUT_NI ||
+                          src.kind == MCGB_SRC_UNIFORM_FIBER_LUT;
+    const bool tilted = src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
+                        src.kind == MCGB_SRC_UNIFORM_FIBER_LUT;
     const bool lambertian = src.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
                             src.kind == MCGB_SRC_LAMBERTIAN_FIBER;
     const float n_sample = L[1].g1.x, n_core = src.clip;
@@ -77,7 +80,8 @@ static __device__ __forceinline__ void mcml_launch_fiber(const McgbMcmlConfig &c
     if (lambertian) {
         sin_theta = mc_sqrt(rng.next()) * src.sigma[1];
     } else {
-        cos_theta = 1.0f - rng.next() * (1.0f - src.sigma[1]);
+        cos_theta = from_lut ? lut_sample_rel(lut + src.lut_offset, src.lut_size, rng.next(), 0.0f)
+                             : 1.0f - rng.next() * (1.0f - src.sigma[1]);
         sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
     }
     sin_theta = mc_div(sin_theta, tilted ? n_core : n_sample);
@@ -89,6 +93,9 @@ static __device__ __forceinline__ void mcml_launch_fiber(const McgbMcmlConfig &c
              T[6] * pt.x + T[7] * pt.y + T[8] * pt.z};
         float cc = cos_critical(n_core, n_sample);
         dir = d;
+        /* UniformFiberLut refracts into the sample (fiber.py:806-813);
+           UniformFiber and LambertianFiber keep the direction in the core */
+        if (from_lut && d.z > cc) dir = refract3(d, f3{0.0f, 0.0f, 1.0f}, n_core, n_sample);
         R = reflectance(n_core, n_sample, d.z, cc);
         if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, R, 0.0f, accu);
     } else {
@@ -108,8 +115,9 @@ static __device__ __forceinline__ void mcml_launch_fiber(const McgbMcmlConfig &c
    (xopto/mcml/mcsource/gaussianbeam.py:119-170, uniformbeam.py:107-146,
    point.py:76-128, fiberni.py, fiber.py). */
 static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c, const MlLayer *L,
-                                                         Rng &rng, f3 &pos, f3 &dir, float &w,
-                                                         int &layer, uint64_t *accu) {
+                                                         const float *lut, Rng &rng, f3 &pos,
+                                                         f3 &dir, float &w, int &layer,
+                                                         uint64_t *accu) {
     const McgbSource &src = c.source;
     if (src.kind == MCGB_SRC_UNIFORM_BEAM) {
         /* xopto/mcml/mcsource/uniformbeam.py:107-146 */
@@ -163,10 +171,12 @@ static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c
         if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, R, 0.0f, accu);
         w = 1.0f - R;
         layer = src.layer_index;
-    } else if (src.kind >= MCGB_SRC_UNIFORM_RECTANGULAR) {
+    } else if (src.kind == MCGB_SRC_UNIFORM_RECTANGULAR || src.kind == MCGB_SRC_LAMBERTIAN_RECTANGULAR ||
+               src.kind == MCGB_SRC_UNIFORM_RECTANGULAR_LUT) {
         /* xopto/mcml/mcsource/rectangular.py:85-140 (uniform in the cosine up
-           to cos_min) and 363-413 (Lambertian up to NA); the emission angle in
-           air is refracted into the layer that holds the source */
+           to cos_min), 363-413 (Lambertian up to NA) and 600-650 (cosine from
+           the emission LUT); the emission angle in air is refracted into the
+           layer that holds the source */
         pos.x = src.position[0] + (rng.next() - 0.5f) * src.sigma[0];
         pos.y = src.position[1] + (rng.next() - 0.5f) * src.sigma[1];
         pos.z = src.position[2];
@@ -174,6 +184,9 @@ static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c
         mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
         if (src.kind == MCGB_SRC_UNIFORM_RECTANGULAR) {
             cos_theta = 1.0f - rng.next() * (1.0f - src.angular);
+            sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
+        } else if (src.kind == MCGB_SRC_UNIFORM_RECTANGULAR_LUT) {
+            cos_theta = lut_sample_rel(lut + src.lut_offset, src.lut_size, rng.next(), 0.0f);
             sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
         } else {
             sin_theta = mc_sqrt(rng.next()) * src.angular;
@@ -185,7 +198,7 @@ static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c
         w = 1.0f - reflectance_cos2(src.clip, n_layer, cos_theta);
         layer = src.layer_index;
     } else if (src.kind >= MCGB_SRC_UNIFORM_FIBER_NI) {
-        mcml_launch_fiber(c, L, rng, pos, dir, w, accu);
+        mcml_launch_fiber(c, L, lut, rng, pos, dir, w, accu);
         layer = 1;
     } else {
         float sin_fi, cos_fi;
@@ -219,8 +232,8 @@ static __device__ __forceinline__ void mcml_launch_other(const McgbMcmlConfig &c
    (an out-of-line call measured slower). */
 template <bool SIMPLE>
 static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, const MlLayer *L,
-                                                   Rng &rng, f3 &pos, f3 &dir, float &w,
-                                                   int &layer, uint64_t *accu) {
+                                                   const float *lut, Rng &rng, f3 &pos, f3 &dir,
+                                                   float &w, int &layer, uint64_t *accu) {
     const McgbSource &src = c.source;
     if (SIMPLE || src.kind == MCGB_SRC_LINE) {
         w = 1.0f - src.reflectance;
@@ -232,7 +245,7 @@ static __device__ __forceinline__ void mcml_launch(const McgbMcmlConfig &c, cons
         }
         layer = 1;
     } else {
-        mcml_launch_other(c, L, rng, pos, dir, w, layer, accu);
+        mcml_launch_other(c, L, lut, rng, pos, dir, w, layer, accu);
     }
 }
 
@@ -476,7 +489,7 @@ static __device__ __forceinline__ void mcml_begin(const McgbMcmlConfig &c, const
     s.trace_count = 0;
     s.steps = 0;
     s.events = MCGB_EV_LAUNCH;
-    mcml_launch<SIMPLE>(c, x.L, rng, s.pos, s.dir, s.w, s.layer, b.accumulator);
+    mcml_launch<SIMPLE>(c, x.L, x.lut, rng, s.pos, s.dir, s.w, s.layer, b.accumulator);
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }

@@ -457,6 +457,89 @@ class SymmetricX(_Directional):
         return 'SymmetricX(xaxis={}, cosmin={})'.format(self._x_axis, self._cosmin)
 
 
+class TotalLut(Detector):
+    """Total reflectance/transmittance weighted by a CollectionLut of the
+    |cosine| between the exit direction and ``direction``
+    (xopto/mcml/mcdetector/total.py:240-460); one bin."""
+    kind = _abi.DET_TOTAL_LUT
+
+    def __init__(self, lut, direction=(0.0, 0.0, 1.0)):
+        if isinstance(lut, TotalLut):
+            other = lut
+            super().__init__(np.copy(other.raw), other.nphotons)
+            lut, direction = other.lut, other.direction
+        else:
+            super().__init__(np.zeros((1,)), 0)
+        self._lut = lut
+        self._direction = np.zeros((3,))
+        self.direction = direction
+
+    def _set_direction(self, d):
+        self._direction[:] = d
+        n = np.linalg.norm(self._direction)
+        if n == 0.0:
+            raise ValueError('Direction vector norm/length must not be 0!')
+        self._direction *= 1.0 / n
+
+    lut = property(lambda self: self._lut, None, None, 'Collection look-up table.')
+    direction = property(lambda self: self._direction, _set_direction)
+
+    def _get_normalized(self):
+        return self.raw * (1.0 / max(self.nphotons, 1.0))
+
+    normalized = property(_get_normalized)
+    reflectance = property(_get_normalized)
+    transmittance = property(_get_normalized)
+
+    def pack(self, mc, target):
+        first, inv_span, n, offset = self._lut.pack(mc)
+        target.kind = self.kind
+        target.offset = mc.cl_allocate_rw_accumulator_buffer(self, self.shape)
+        target.direction[:] = [float(v) for v in self._direction]
+        target.r_min, target.inv_dr, target.n_y, target.table_offset = first, inv_span, n, offset
+        target.n = 1
+        return target
+
+    def copy(self):
+        return TotalLut(self)
+
+    def todict(self):
+        return {'type': 'TotalLut', 'lut': self._lut.todict(), 'direction': self._direction.tolist()}
+
+    def __str__(self):
+        return 'TotalLut(lut={}, direction=({}, {}, {}))'.format(self._lut, *self._direction)
+
+
+class TotalLutPl(TotalLut):
+    """TotalLut resolved by optical path length
+    (xopto/mcml/mcdetector/totalpl.py, TotalLutPl); raw has shape (n_pl, 1)."""
+    kind = _abi.DET_TOTAL_LUT_PL
+    tracks_pathlength = True
+
+    def __init__(self, lut, plaxis=None, direction=(0.0, 0.0, 1.0)):
+        if isinstance(lut, TotalLutPl):
+            other = lut
+            TotalLut.__init__(self, other.lut, other.direction)
+            self._pl_axis = type(other.plaxis)(other.plaxis)
+            self._raw_data = np.copy(other.raw)
+            self._nphotons = other.nphotons
+            return
+        TotalLut.__init__(self, lut, direction)
+        self._pl_axis = plaxis if plaxis is not None else Axis(0.0, 1.0, 1)
+        self._raw_data = np.zeros((self._pl_axis.n, 1))
+
+    plaxis = property(lambda self: self._pl_axis)
+    pl = property(lambda self: self._pl_axis.centers)
+
+    def pack(self, mc, target):
+        TotalLut.pack(self, mc, target)
+        _pack_pl_axis(self._pl_axis, target)
+        return target
+
+    def copy(self):
+        return TotalLutPl(self)
+
+
 class Detectors:
     """Top, bottom and specular detectors
     (xopto/mcml/mcdetector/base.py:295-568)."""
@@ -501,4 +584,5 @@ class Detectors:
 
 
 __all__ = ['Axis', 'RadialAxis', 'SymmetricAxis', 'Detector', 'DetectorDefault', 'Total', 'Radial',
-           'TotalPl', 'RadialPl', 'Cartesian', 'CartesianPl', 'SymmetricX', 'Detectors']
+           'TotalPl', 'RadialPl', 'Cartesian', 'CartesianPl', 'SymmetricX', 'TotalLut', 'TotalLutPl',
+           'Detectors']

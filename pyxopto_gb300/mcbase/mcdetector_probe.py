@@ -205,5 +205,56 @@ class FiberArrayPl(FiberArray):
         FiberArray.__init__(self, fibers, plaxis if plaxis is not None else Axis(0.0, 1.0, 1))
 
 
+class FiberLutArray(_Probe):
+    """Array of fibres (FiberLayout of MultimodeFiberLut) whose collection
+    is weighted by each fibre's CollectionLut at the |cosine| of the exit
+    direction to the fibre axis (xopto/mcml/mcdetector/probe/fiberlutarray.py:
+    30-366).  The float table holds, per fibre, transformation, position,
+    core r^2, LUT first position and 1/span, and the LUT size and offset
+    (relative to the table) as uint32 bit patterns, then the LUT data."""
+    kind = kind_pl = _abi.DET_FIBER_LUT_ARRAY
+
+    def __init__(self, fibers):
+        if isinstance(fibers, FiberLutArray):
+            fibers = fibers.fibers
+        self._fibers = [FiberLayout(f) for f in fibers]
+        super().__init__(np.zeros((len(self._fibers),)), 0)
+
+    fibers = property(lambda self: self._fibers)
+
+    def n_fibers(self):
+        return len(self._fibers)
+
+    def table(self):
+        """fiberlutarray.py:305-324."""
+        n = len(self._fibers)
+        head = np.zeros((n, _abi.DET_LUT_FIBER_FLOATS), dtype=np.float32)
+        data = []
+        rel = n * _abi.DET_LUT_FIBER_FLOATS
+        for i, fl in enumerate(self._fibers):
+            lut = fl.fiber.collection
+            head[i, :9] = _fiber_transform(fl.direction)
+            head[i, 9:11] = fl.position[:2]
+            head[i, 11] = 0.25 * fl.fiber.dcore ** 2
+            head[i, 12] = lut.first
+            head[i, 13] = 1.0 / (lut.last - lut.first)
+            head[i, 14:16] = np.array([lut.data.size, rel], dtype=np.uint32).view(np.float32)
+            data.append(np.asarray(lut.data, dtype=np.float32))
+            rel += lut.data.size
+        return np.concatenate([head.ravel()] + data)
+
+    def pack(self, mc, target: _abi.McgbDetector):
+        table = self.table()
+        target.kind = self.kind
+        target.offset = mc.cl_allocate_rw_accumulator_buffer(self, self.shape)
+        target.n = self.n_fibers()
+        target.n_y = table.size
+        target.table_offset = mc.append_r_lut(table)
+        return target
+
+    def copy(self):
+        return FiberLutArray(self)
+
+
 __all__ = ['LinearArray', 'LinearArrayPl', 'SixAroundOne', 'SixAroundOnePl', 'FiberArray',
-           'FiberArrayPl']
+           'FiberArrayPl', 'FiberLutArray']

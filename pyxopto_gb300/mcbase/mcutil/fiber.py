@@ -100,3 +100,59 @@ class FiberLayout:
             self._fiber, *self._position, *self._direction)
 
     __repr__ = __str__
+
+
+class MultimodeFiberLut:
+    """Multimode fibre whose emission and collection are given by look-up
+    tables (xopto/mcbase/mcutil/fiber.py:224-420)."""
+
+    def __init__(self, dcore: float, dcladding: float, ncore: float, ncladding: float = None,
+                 emission=None, collection=None):
+        from .lut import EmissionLut, CollectionLut
+        if isinstance(dcore, MultimodeFiberLut):
+            o = dcore
+            dcore, dcladding, ncore, ncladding = o.dcore, o.dcladding, o.ncore, o.ncladding
+            emission, collection = o.emission, o.collection
+        self._dcore = float(dcore)
+        self._dcladding = float(dcladding)
+        self._ncore = float(ncore)
+        self._ncladding = self._ncore if ncladding is None else float(ncladding)
+        if isinstance(emission, str):
+            emission = EmissionLut(emission)
+        elif isinstance(emission, np.ndarray):
+            emission = EmissionLut(emission)
+        if isinstance(collection, str):
+            collection = CollectionLut(collection)
+        self._emission = emission
+        self._collection = collection
+
+    def validate(self):
+        if self._dcore > self._dcladding:
+            raise ValueError('Fiber core diameter must be smaller than the fiber cladding diameter!')
+
+    def _set_dcore(self, v):
+        self._dcore = float(v)
+
+    def _set_dcladding(self, v):
+        self._dcladding = float(v)
+
+    def _set_ncore(self, v):
+        self._ncore = float(v)
+
+    dcore = property(lambda self: self._dcore, _set_dcore, None, 'Core diameter (m).')
+    dcladding = property(lambda self: self._dcladding, _set_dcladding, None, 'Cladding diameter (m).')
+    ncore = property(lambda self: self._ncore, _set_ncore, None, 'Core refractive index.')
+    ncladding = property(lambda self: self._ncladding, None, None, 'Cladding refractive index.')
+    emission = property(lambda self: self._emission, None, None, 'Emission look-up table.')
+    collection = property(lambda self: self._collection, None, None, 'Collection look-up table.')
+
+    def todict(self) -> dict:
+        return {'type': 'MultimodeFiberLut', 'dcore': self._dcore, 'dcladding': self._dcladding,
+                'ncore': self._ncore, 'emission': self._emission, 'collection': self._collection}
+
+    def __repr__(self):
+        return 'MultimodeFiberLut(dcore={:f}, dcladding={:f}, ncore={:f}, emission={}, ' \
+               'collection={})'.format(self._dcore, self._dcladding, self._ncore, self._emission,
+                                       self._collection)
+
+    __str__ = __repr__

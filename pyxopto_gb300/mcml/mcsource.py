@@ -435,3 +435,109 @@ class LambertianRectangular(UniformRectangular):
 
     def _angular(self) -> float:
         return self._na
+
+
+def _pack_emission(mc, target, emission):
+    """Appends an EmissionLut to the float table (LinearLut.cl_pack,
+    xopto/mcbase/mcutil/lut.py:164-193); the device samples it by a uniform
+    random number (fp_linear_lut_rel_sample)."""
+    if emission is None:
+        raise ValueError('The source needs an emission look-up table!')
+    _, _, n, offset = emission.pack(mc)
+    target.lut_offset = offset
+    target.lut_size = n
+
+
+class UniformFiberLutNI(UniformFiberNI):
+    """Fibre source with normal incidence whose emission-angle cosine in air
+    is drawn from the fibre's EmissionLut (a MultimodeFiberLut), refracted
+    into the sample (xopto/mcml/mcsource/fiberni.py:581-760)."""
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiberni.py:796-830: position, core radius, core index, LUT."""
+        target.kind = _abi.SRC_UNIFORM_FIBER_LUT_NI
+        target.position[:] = [float(v) for v in self._position]
+        target.sigma[0] = self._fiber.dcore * 0.5
+        target.sigma[1] = 0.0
+        target.clip = self._fiber.ncore
+        _pack_emission(mc, target, self._fiber.emission)
+        return target
+
+    def todict(self):
+        return {'type': 'UniformFiberLutNI', 'fiber': self._fiber.todict(),
+                'position': self._position.tolist()}
+
+    def __str__(self):
+        return 'UniformFiberLutNI(fiber={}, position=({}, {}, {}))'.format(self._fiber, *self._position)
+
+    __repr__ = __str__
+
+
+class UniformFiberLut(UniformFiber):
+    """Tilted fibre source whose emission-angle cosine in air is drawn from
+    the fibre's EmissionLut; unlike UniformFiber, the launch direction is
+    refracted into the sample (xopto/mcml/mcsource/fiber.py:690-1010)."""
+    _kind = _abi.SRC_UNIFORM_FIBER_LUT
+
+    def _angular(self):
+        return 0.0
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiber.py:970-990: rotation onto the fibre axis, position, axis,
+        core radius, core index, LUT."""
+        UniformFiber.pack(self, mc, target)
+        _pack_emission(mc, target, self._fiber.emission)
+        return target
+
+
+class UniformRectangularLut(Source):
+    """Rectangular source whose emission-angle cosine in air is drawn from
+    an EmissionLut (xopto/mcml/mcsource/rectangular.py:530-854)."""
+
+    def __init__(self, lut, width: float = None, height: float = None, n: float = 1.0,
+                 position=(0.0, 0.0, 0.0)):
+        if isinstance(lut, UniformRectangularLut):
+            o = lut
+            lut, width, height, n, position = o.lut, o.width, o.height, o.n, o.position
+        self._lut = lut
+        self._width = float(width)
+        self._height = float(height)
+        self._n = max(1.0, float(n))
+        self._position = np.zeros((3,))
+        self._position[:] = position
+
+    def _set_position(self, p):
+        self._position[:] = p
+
+    lut = property(lambda self: self._lut)
+    width = property(lambda self: self._width)
+    height = property(lambda self: self._height)
+    n = property(lambda self: self._n)
+    position = property(lambda self: self._position, _set_position)
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """rectangular.py:780-830, with the layer rule of UniformRectangular."""
+        if self._position[2] <= 0.0:
+            position = (self._position[0], self._position[1], 0.0)
+            layer_index = 1
+        else:
+            position = self._position
+            layer_index = mc.layer_index(self._position[2])
+        _pack_emission(mc, target, self._lut)
+        target.kind = _abi.SRC_UNIFORM_RECTANGULAR_LUT
+        target.position[:] = [float(v) for v in position]
+        target.sigma[:] = [self._width, self._height]
+        target.clip = self._n
+        target.angular = 0.0
+        target.layer_index = layer_index
+        return target
+
+    def todict(self):
+        return {'type': 'UniformRectangularLut', 'lut': self._lut.todict(), 'width': self._width,
+                'height': self._height, 'n': self._n, 'position': self._position.tolist()}
+
+    def __str__(self):
+        return 'UniformRectangularLut(lut={}, width={}, height={}, n={}, position=({}, {}, {}))'.format(
+            self._lut, self._width, self._height, self._n, *self._position)
+
+    __repr__ = __str__

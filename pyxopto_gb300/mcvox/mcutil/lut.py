@@ -1,0 +1,2 @@
+"""Look-up tables (xopto/mcvox/mcutil/lut.py re-exports xopto/mcbase/mcutil/lut.py)."""
+from ...mcbase.mcutil.lut import LinearLut, EmissionLut, CollectionLut  # noqa: F401

@@ -429,6 +429,50 @@ SCENARIOS = {
         detectors=dict(top=dict(type='Cartesian', x=[-1e-3, 1e-3, 8], y=[-1e-3, 1e-3, 6]),
                        bottom=dict(type='Radial', axis=[0.0, 2e-3, 10])),
         nphotons=3000, streams=32, rnginit=139),
+    # emission and collection look-up tables (xopto/mcbase/mcutil/lut.py):
+    # tilted and normal LUT fibres, a LUT rectangle, TotalLut(Pl), FiberLutArray
+    'lut_fiber_tilted': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1e-3, n=1.4, mua=80.0, mus=1.2e4, pf=['Hg', 0.8]),
+                dict(d=INF, n=1.36, mua=30.0, mus=8e3, pf=['Hg', 0.9])],
+        source=dict(type='UniformFiberLut', direction=(0.35, 0.1, 1.0), position=(1e-4, 0.0, 0.0),
+                    fiber_lut=dict(dcore=400e-6, dcladding=420e-6, ncore=1.46, ncladding=1.44,
+                                   emission=dict(cos_min=0.85, points=40, width=0.05))),
+        detectors=dict(top=dict(type='TotalLut', collection=dict(cos_min=0.6, points=30),
+                                direction=(0.0, 0.2, 1.0)),
+                       bottom=dict(type='TotalLutPl', collection=dict(cos_min=0.3, points=20, power=1.0),
+                                   plaxis=[0.0, 2e-2, 8]),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=32, rnginit=149),
+    'lut_fiber_ni_array': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=1.5e-3, n=1.38, mua=60.0, mus=1.5e4, pf=['Hg', 0.85]),
+                _air(['Hg', 0.0])],
+        source=dict(type='UniformFiberLutNI', position=(-2e-4, 1e-4, 0.0),
+                    fiber_lut=dict(dcore=200e-6, dcladding=220e-6, ncore=1.452, ncladding=1.44,
+                                   emission=dict(cos_min=0.9, points=30, width=0.03, n=400))),
+        detectors=dict(top=dict(type='FiberLutArray', fibers=[
+            dict(fiber_lut=dict(dcore=400e-6, dcladding=440e-6, ncore=1.46, ncladding=1.44,
+                                collection=dict(cos_min=0.5, points=25)),
+                 position=(3e-4, 0.0, 0.0), direction=(0.0, 0.0, 1.0)),
+            dict(fiber_lut=dict(dcore=600e-6, dcladding=630e-6, ncore=1.45, ncladding=1.43,
+                                collection=dict(cos_min=0.7, points=25, power=3.0)),
+                 position=(-6e-4, -2e-4, 0.0), direction=(0.2, -0.1, 1.0))]),
+            specular=dict(type='Total')),
+        nphotons=4000, streams=32, rnginit=151),
+    'lut_rectangular': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]),
+                dict(d=6e-4, n=1.38, mua=80.0, mus=1.5e4, pf=['Hg', 0.85]),
+                dict(d=1.5e-3, n=1.45, mua=20.0, mus=1e4, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='UniformRectangularLut', width=5e-4, height=3e-4, n=1.5,
+                    position=(1e-4, 0.0, 3e-4), emission=dict(cos_min=0.7, points=35, width=0.1)),
+        detectors=dict(top=dict(type='TotalLut', collection=dict(cos_min=0.4, points=30)),
+                       bottom=dict(type='Radial', axis=[0.0, 2e-3, 10])),
+        nphotons=3000, streams=32, rnginit=157),
     'trace_sampling_volume': dict(
         medium='mcml',
         layers=[_air(['Hg', 0.0]),
@@ -572,6 +616,19 @@ def _detectors(pkg, spec):
         elif d['type'] in ('LinearArray', 'LinearArrayPl', 'SixAroundOne', 'SixAroundOnePl',
                            'FiberArray', 'FiberArrayPl'):
             slots[slot] = _probe_detector(pkg, d)
+        elif d['type'] in ('TotalLut', 'TotalLutPl'):
+            pkg_name = pkg.__name__.rsplit('.', 1)[0]
+            lut = _collection(_luts(pkg_name)[1], d['collection'])
+            kw = dict(direction=d.get('direction', (0.0, 0.0, 1.0)))
+            if d['type'] == 'TotalLutPl':
+                kw['plaxis'] = _axis(pkg, {'axis': d['plaxis'], 'logscale': d.get('pllogscale', False)})
+            slots[slot] = getattr(pkg.mcdetector, d['type'])(lut, **kw)
+        elif d['type'] == 'FiberLutArray':
+            pkg_name = pkg.__name__.rsplit('.', 1)[0]
+            fibermod = _luts(pkg_name)[0]
+            slots[slot] = pkg.mcdetector.FiberLutArray(
+                [fibermod.FiberLayout(_fiber_lut(pkg_name, f['fiber_lut']), position=f['position'],
+                                      direction=f['direction']) for f in d['fibers']])
         else:
             slots[slot] = pkg.mcdetector.Radial(_axis(pkg, d), position=d.get('position', (0.0, 0.0)),
                                                 cosmin=d.get('cosmin', 0.0))
@@ -656,13 +713,46 @@ def _surface(pkg, spec):
     return sm.SurfaceLayouts(top=layout(spec.get('top')), bottom=layout(spec.get('bottom')))
 
 
+def _luts(pkg_name):
+    """(fiber module, lut module) of a package (xopto.mcml, xopto.mcvox or
+    the pyxopto_gb300 equivalents)."""
+    import importlib
+    return (importlib.import_module(pkg_name + '.mcutil.fiber'),
+            importlib.import_module(pkg_name + '.mcutil.lut'))
+
+
+def _emission(lutmod, spec):
+    ct = np.linspace(spec['cos_min'], 1.0, spec['points'])
+    radiance = np.exp(-(1.0 - ct) / spec['width']) + spec.get('floor', 0.05)
+    return lutmod.EmissionLut(radiance, ct, n=spec.get('n', 500))
+
+
+def _collection(lutmod, spec):
+    ct = np.linspace(spec['cos_min'], 1.0, spec['points'])
+    return lutmod.CollectionLut(ct ** spec.get('power', 2.0), ct, n=spec.get('n', 300))
+
+
+def _fiber_lut(pkg_name, spec):
+    fibermod, lutmod = _luts(pkg_name)
+    kw = dict(spec)
+    if 'emission' in kw:
+        kw['emission'] = _emission(lutmod, kw['emission'])
+    if 'collection' in kw:
+        kw['collection'] = _collection(lutmod, kw['collection'])
+    return fibermod.MultimodeFiberLut(**kw)
+
+
 def _source(src_mod, spec):
     import importlib
     kw = {k: v for k, v in spec.items() if k != 'type'}
+    medium_pkg = src_mod.__name__.rsplit('.', 1)[0]              # e.g. xopto.mcml
     if 'fiber' in kw:
-        medium_pkg = src_mod.__name__.rsplit('.', 1)[0]          # e.g. xopto.mcml
         fiber = importlib.import_module(medium_pkg + '.mcutil.fiber')
         kw['fiber'] = fiber.MultimodeFiber(**kw['fiber'])
+    if 'fiber_lut' in kw:
+        kw['fiber'] = _fiber_lut(medium_pkg, kw.pop('fiber_lut'))
+    if 'emission' in kw:
+        kw['lut'] = _emission(_luts(medium_pkg)[1], kw.pop('emission'))
     return getattr(src_mod, spec['type'])(**kw)
 
 

@@ -223,15 +223,16 @@ def test_linear_probe_sweep(cuda, lib, key):
     LinearArray detector.  The reference passes at |mean relative error| <
     0.5 % over its full sweep; on the subset the noise of the mean is about
     0.3 %, so the bound here is 1 %.  The ratio of the summed reflectances
-    of each fibre must agree within 2 %: both sides are Monte Carlo
-    estimates, and the farthest fibre's sum carries about 0.5 % noise."""
+    of each fibre must agree within 3 %: both sides are Monte Carlo
+    estimates, and on the 80-point Gegenbauer subset the farthest fibre's
+    sum carries about 1 % noise."""
     data = probe_sweep.load(key)
     sim = probe_sweep.build(data, fast=True)
     refl, ref, _ = probe_sweep.run(sim, data, 10_000_000, stride=5)
     err = probe_sweep.relative_error(refl, ref)
     assert abs(err.mean()) < 1.0, err.mean()
     ratio = refl.sum(axis=0) / ref.sum(axis=0)
-    assert np.all(np.abs(ratio - 1.0) < 0.02), ratio
+    assert np.all(np.abs(ratio - 1.0) < 0.03), ratio
 
 
 SV_SCENARIOS = sorted(n for n, s in scenarios.SCENARIOS.items() if s.get('sampling_volume'))
