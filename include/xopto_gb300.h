@@ -114,7 +114,8 @@ enum {
     MCGB_SRC_LAMBERTIAN_RECTANGULAR = 10,
     MCGB_SRC_UNIFORM_FIBER_LUT_NI = 11,
     MCGB_SRC_UNIFORM_FIBER_LUT = 12,
-    MCGB_SRC_UNIFORM_RECTANGULAR_LUT = 13
+    MCGB_SRC_UNIFORM_RECTANGULAR_LUT = 13,
+    MCGB_SRC_ISOTROPIC_VOXELS = 14
 };
 enum { MCGB_DET_NONE = 0, MCGB_DET_TOTAL = 1, MCGB_DET_RADIAL = 2, MCGB_DET_RADIAL_PL = 3,
        MCGB_DET_TOTAL_PL = 4, MCGB_DET_CARTESIAN = 5, MCGB_DET_CARTESIAN_PL = 6,
@@ -204,7 +205,8 @@ typedef struct McgbMaterial {
      surrounding medium), sigma (beam radii; fibre core radius and
      sqrt(1 - NA^2) or NA) and clip (fibre core index); IsotropicPoint
      (point.py:74-140) takes position; IsotropicVoxel (voxel.py:78-107) takes
-     the voxel index as floats in position.
+     the voxel index as floats in direction and the voxel centre in position
+     (the centre of the rmax sphere, mcvox.template.c:585,983).
    UniformRectangular / LambertianRectangular, layered media only
      (xopto/mcml/mcsource/rectangular.py:85-140,363-413): position = centre
      (z = 0 for a source on the surface), sigma = width (x) and height (y),
@@ -221,7 +223,11 @@ typedef struct McgbMaterial {
      UniformFiberNI fields; UniformFiberLut (fiber.py:690-830) the
      UniformFiber fields, and unlike UniformFiber it refracts the launch
      direction into the sample; UniformRectangularLut (rectangular.py:530-700)
-     the rectangular fields without angular. */
+     the rectangular fields without angular.
+   IsotropicVoxels, voxelized media only (xopto/mcvox/mcsource/voxel.py:
+     195-380): lut_size voxels of 4 floats (weight, x, y, z voxel index) in
+     the float table at lut_offset; a packet starts in one of them, chosen
+     uniformly, with that weight; position = centre of the mean voxel index. */
 typedef struct McgbSource {
     int32_t kind;
     float position[3];

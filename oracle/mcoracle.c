@@ -1151,8 +1151,8 @@ static inline v3 transform3(const float *T, v3 p) {
    (fiber.py:257-352,603-700), IsotropicVoxel (voxel.py:78-107); then the voxel
    of the launch position (xopto/mcvox/kernel/mcvox.template.c:240-262). */
 static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *mats,
-                         const uint8_t *vox, MvState *s, uint64_t *x, uint32_t a,
-                         uint64_t *accu, v3 prev_pos) {
+                         const uint8_t *vox, const float *lut, MvState *s, uint64_t *x,
+                         uint32_t a, uint64_t *accu, v3 prev_pos) {
     const McgbSource *src = &c->source;
     const float *T = src->transformation;
     if (src->kind == MCGB_SRC_LINE) {
@@ -1262,14 +1262,24 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
             detector_deposit(mm, &c->specular, s->pos, packet_dir, specular_r, 0.0f, accu, NULL);
         s->w = 1.0f - specular_r;
     } else {
-        /* IsotropicVoxel */
+        /* IsotropicVoxel; IsotropicVoxels picks its voxel first,
+           xopto/mcvox/mcsource/voxel.py:230-245 (mc_min of the int casts) */
+        float vx = src->direction[0], vy = src->direction[1], vz = src->direction[2];
+        s->w = 1.0f;
+        if (src->kind == MCGB_SRC_ISOTROPIC_VOXELS) {
+            int32_t n = (int32_t)src->lut_size;
+            int32_t k = cvt_int(rnd(x, a) * (float)src->lut_size);
+            if (k > n - 1) k = n - 1;
+            const float *e = lut + src->lut_offset + (size_t)k * 4u;
+            s->w = e[0];
+            vx = e[1];
+            vy = e[2];
+            vz = e[3];
+        }
         const float one_minus_eps = 1.0f - 1.1920929e-07f;
-        s->pos.x = (src->position[0] + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[0] +
-                   c->top_left[0];
-        s->pos.y = (src->position[1] + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[1] +
-                   c->top_left[1];
-        s->pos.z = (src->position[2] + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[2] +
-                   c->top_left[2];
+        s->pos.x = (vx + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[0] + c->top_left[0];
+        s->pos.y = (vy + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[1] + c->top_left[1];
+        s->pos.z = (vz + fminf(rnd(x, a), one_minus_eps)) * c->voxel_size[2] + c->top_left[2];
         float sin_fi, cos_fi;
         m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
         float cos_theta = 1.0f - 2.0f * rnd(x, a);
@@ -1277,7 +1287,6 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         s->dir.x = cos_fi * sin_theta;
         s->dir.y = sin_fi * sin_theta;
         s->dir.z = cos_theta;
-        s->w = 1.0f;
     }
     s->vox = mv_index(c, s->pos);
     s->mat = mv_valid(c, s->vox) ? mv_material_at(c, vox, s->vox) : 0;
@@ -1349,7 +1358,7 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
         TraceState ts;
         memset(&s, 0, sizeof(s));
         ts.photon_index = p; ts.trace_count = 0; ts.events = 0;
-        mcvox_launch(mm, c, mats, vox, &s, &x, a, accu, prev_pos);
+        mcvox_launch(mm, c, mats, vox, lut, &s, &x, a, accu, prev_pos);
         uint32_t events = EV_LAUNCH;
 #define MV_TRACE_SNAPSHOT() do { ts.pos = s.pos; ts.dir = s.dir; ts.w = s.w; ts.opl = s.opl; \
                                  ts.events = events; } while (0)

@@ -24,6 +24,7 @@ SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT =
 SRC_ISOTROPIC_VOXEL = 8
 SRC_UNIFORM_RECTANGULAR, SRC_LAMBERTIAN_RECTANGULAR = 9, 10
 SRC_UNIFORM_FIBER_LUT_NI, SRC_UNIFORM_FIBER_LUT, SRC_UNIFORM_RECTANGULAR_LUT = 11, 12, 13
+SRC_ISOTROPIC_VOXELS = 14
 DET_NONE, DET_TOTAL, DET_RADIAL, DET_RADIAL_PL, DET_TOTAL_PL = 0, 1, 2, 3, 4
 DET_CARTESIAN, DET_CARTESIAN_PL, DET_SYMMETRIC_X = 5, 6, 7
 DET_LINEAR_ARRAY, DET_SIX_AROUND_ONE, DET_FIBER_ARRAY = 8, 9, 10

@@ -104,13 +104,15 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
     if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
-    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_UNIFORM_RECTANGULAR_LUT)
+    if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_ISOTROPIC_VOXELS)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
     if (src.kind >= MCGB_SRC_UNIFORM_FIBER_LUT_NI) {
-        if (src.lut_size == 0 || !b->fp_lut || !range_ok(src.lut_offset, src.lut_size, b->fp_lut_size))
-            return fail(MCGB_E_SIZE, "source emission LUT [%u, +%u) beyond the float table (%llu)",
-                        src.lut_offset, src.lut_size, (unsigned long long)b->fp_lut_size);
-        if (src.kind != MCGB_SRC_UNIFORM_RECTANGULAR_LUT &&
+        const uint64_t floats = (uint64_t)src.lut_size * (src.kind == MCGB_SRC_ISOTROPIC_VOXELS ? 4u : 1u);
+        if (src.lut_size == 0 || src.lut_size > (1u << 24) || !b->fp_lut ||
+            !range_ok(src.lut_offset, floats, b->fp_lut_size))
+            return fail(MCGB_E_SIZE, "source table [%u, +%llu) beyond the float table (%llu)",
+                        src.lut_offset, (unsigned long long)floats, (unsigned long long)b->fp_lut_size);
+        if (src.kind != MCGB_SRC_UNIFORM_RECTANGULAR_LUT && src.kind != MCGB_SRC_ISOTROPIC_VOXELS &&
             !(src.sigma[0] >= 0.0f && src.clip > 0.0f))
             return fail(MCGB_E_INVALID, "fiber source: core radius %g, core index %g",
                         (double)src.sigma[0], (double)src.clip);
@@ -318,8 +320,8 @@ int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *strea
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
-    if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL)
-        return fail(MCGB_E_UNSUPPORTED, "the voxel source is implemented for voxelized media only");
+    if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL || cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXELS)
+        return fail(MCGB_E_UNSUPPORTED, "the voxel sources are implemented for voxelized media only");
     if ((cfg->source.kind == MCGB_SRC_UNIFORM_FIBER || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
          cfg->source.kind == MCGB_SRC_UNIFORM_BEAM || cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_LUT) &&
         !(cfg->source.direction[2] > 0.0f))
@@ -375,12 +377,12 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
         return fail(MCGB_E_UNSUPPORTED, "look-up-table detectors are layered-media only (the reference's "
                     "voxelized TotalLut reads a LUT accessor its kernel lacks and does not build)");
     if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
-        cfg->source.kind >= MCGB_SRC_UNIFORM_RECTANGULAR)
+        (cfg->source.kind >= MCGB_SRC_UNIFORM_RECTANGULAR && cfg->source.kind != MCGB_SRC_ISOTROPIC_VOXELS))
         return fail(MCGB_E_UNSUPPORTED, "source kind %d is implemented for layered media only",
                     cfg->source.kind);
     if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL) {
         for (int k = 0; k < 3; ++k) {
-            float v = cfg->source.position[k];
+            float v = cfg->source.direction[k];
             if (!(v >= 0.0f && v < (float)cfg->shape[k] && v == (float)(int)v))
                 return fail(MCGB_E_INVALID, "voxel source index %g outside the grid", (double)v);
         }

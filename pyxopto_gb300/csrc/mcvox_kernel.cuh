@@ -137,8 +137,9 @@ static __device__ __forceinline__ void mv_beam_enter(const McgbMcvoxConfig &c, c
 template <bool SIMPLE>
 static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, const MvGeom &g,
                                                     const MvMaterial *M, const uint8_t *vox,
-                                                    Rng &rng, f3 &pos, f3 &dir, float &w, i3 &vi,
-                                                    int &mat, uint64_t *accu, f3 prev_pos) {
+                                                    const float *lut, Rng &rng, f3 &pos, f3 &dir,
+                                                    float &w, i3 &vi, int &mat, uint64_t *accu,
+                                                    f3 prev_pos) {
     const McgbSource &src = c.source;
     const float *T = src.transformation;
     if (src.kind == MCGB_SRC_LINE) {
@@ -246,21 +247,32 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
             detector_deposit(c.specular, pos, packet_dir, specular_r, 0.0f, accu);
         w = 1.0f - specular_r;
     } else {
-        /* IsotropicVoxel: uniform in the voxel, isotropic direction */
+        /* IsotropicVoxel(s): uniform in the voxel, isotropic direction;
+           IsotropicVoxels first picks one of its voxels (voxel.py:230-245) */
+        float vx = src.direction[0], vy = src.direction[1], vz = src.direction[2];
+        w = 1.0f;
+        if (src.kind == MCGB_SRC_ISOTROPIC_VOXELS) {
+            int n = (int)src.lut_size;
+            int k = min(cvt_int(rng.next() * (float)src.lut_size), n - 1);
+            const float *e = lut + src.lut_offset + (size_t)k * 4u;
+            w = e[0];
+            vx = e[1];
+            vy = e[2];
+            vz = e[3];
+        }
         const float one_minus_eps = 1.0f - 1.1920929e-07f;
         float ux = fminf(rng.next(), one_minus_eps);
-        float px = (src.position[0] + ux) * g.vs[0] + g.tl[0];
+        float px = (vx + ux) * g.vs[0] + g.tl[0];
         float uy = fminf(rng.next(), one_minus_eps);
-        float py = (src.position[1] + uy) * g.vs[1] + g.tl[1];
+        float py = (vy + uy) * g.vs[1] + g.tl[1];
         float uz = fminf(rng.next(), one_minus_eps);
-        float pz = (src.position[2] + uz) * g.vs[2] + g.tl[2];
+        float pz = (vz + uz) * g.vs[2] + g.tl[2];
         pos = f3{px, py, pz};
         float sin_fi, cos_fi;
         mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
         float cos_theta = 1.0f - 2.0f * rng.next();
         float sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
         dir = f3{cos_fi * sin_theta, sin_fi * sin_theta, cos_theta};
-        w = 1.0f;
     }
     vi = mv_index(g, pos);
     mat = mv_valid(g, vi) ? mv_material_at(g, vox, vi) : 0;
@@ -357,8 +369,8 @@ static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, con
     s.trace_count = 0;
     s.steps = 0;
     s.events = MCGB_EV_LAUNCH;
-    mcvox_launch<SIMPLE>(c, x.g, x.M, x.vox, rng, s.pos, s.dir, s.w, s.vi, s.mat, b.accumulator,
-                         prev_pos);
+    mcvox_launch<SIMPLE>(c, x.g, x.M, x.vox, x.lut, rng, s.pos, s.dir, s.w, s.vi, s.mat,
+                         b.accumulator, prev_pos);
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }

@@ -246,7 +246,8 @@ class IsotropicVoxel:
         if not (0 <= x < nx and 0 <= y < ny and 0 <= z < nz):
             raise ValueError('Voxel index ({}, {}, {}) is not valid!'.format(x, y, z))
         target.kind = _abi.SRC_ISOTROPIC_VOXEL
-        target.position[:] = [float(x), float(y), float(z)]
+        target.direction[:] = [float(x), float(y), float(z)]
+        target.position[:] = [float(v) for v in mc.voxels.center(self._voxel)]
         return target
 
     def todict(self):
@@ -254,5 +255,50 @@ class IsotropicVoxel:
 
     def __str__(self):
         return 'IsotropicVoxel(voxel=({}, {}, {}))'.format(*self._voxel)
+
+    __repr__ = __str__
+
+
+class IsotropicVoxels:
+    """Isotropic source spread over a set of voxels, each with a weight in
+    [0, 1]; a packet starts uniformly within one voxel chosen uniformly
+    (xopto/mcvox/mcsource/voxel.py:195-380)."""
+
+    def __init__(self, voxels, weights=None):
+        if isinstance(voxels, IsotropicVoxels):
+            voxels, weights = voxels.voxels, voxels.weights
+        voxels = np.asarray(voxels)
+        if voxels.shape[-1] != 3 or voxels.ndim > 2:
+            raise ValueError('Shape of the voxel array must be (n, 3)!')
+        voxels = np.reshape(voxels, (-1, 3))
+        self._data = np.ones((voxels.shape[0], 4))
+        self._data[:, 1:] = voxels
+        if weights is not None:
+            weights = np.asarray(weights, dtype=np.float64)
+            if weights.size != self._data.shape[0]:
+                raise ValueError('The number of weights must equal the number of voxels!')
+            self._data[:, 0] = np.clip(weights, 0.0, 1.0)
+
+    voxels = property(lambda self: self._data[:, 1:])
+    weights = property(lambda self: self._data[:, 0])
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """voxel.py:340-380: the (weight, x, y, z) rows go to the float
+        table; position is the centre of the mean voxel index."""
+        for v in self._data[:, 1:]:
+            if not mc.voxels.isvalid([int(i) for i in v]):
+                raise ValueError('Voxel index ({}, {}, {}) is not valid!'.format(*v))
+        target.kind = _abi.SRC_ISOTROPIC_VOXELS
+        target.lut_offset = mc.append_r_lut(np.asarray(self._data, dtype=np.float32).ravel())
+        target.lut_size = self._data.shape[0]
+        target.position[:] = [float(v) for v in mc.voxels.center(np.mean(self._data[:, 1:], 0))]
+        return target
+
+    def todict(self):
+        return {'type': 'IsotropicVoxels', 'voxels': self._data[:, 1:].tolist(),
+                'weights': self._data[:, 0].tolist()}
+
+    def __str__(self):
+        return 'IsotropicVoxels(n={})'.format(self._data.shape[0])
 
     __repr__ = __str__

@@ -256,6 +256,29 @@ SCENARIOS = {
         detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), bottom=dict(type='Total')),
         fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='deposition'),
         nphotons=2000, streams=20, rnginit=71),
+    # voxel sources with a finite rmax: the rmax sphere is centred on the
+    # (mean) source voxel (xopto/mcvox/kernel/mcvox.template.c:585,983)
+    'vox_isotropic_voxel_rmax': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='IsotropicVoxel', voxel=(2, 9, 5)),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), bottom=dict(type='Total')),
+        fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='deposition'),
+        rmax=4e-4, nphotons=2000, streams=20, rnginit=167),
+    'vox_isotropic_voxels': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=100.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='IsotropicVoxels', voxels=[(1, 2, 0), (4, 6, 3), (8, 10, 7), (5, 5, 5), (0, 11, 2)],
+                    weights=[1.0, 0.5, 0.8, 0.25, 1.0]),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1e-3, 10]), bottom=dict(type='Total')),
+        fluence=dict(x=[-1e-3, 1e-3, 5], y=[-1e-3, 1e-3, 6], z=[0.0, 1.5e-3, 4], mode='deposition'),
+        rmax=1.2e-3, nphotons=2000, streams=20, rnginit=173),
     # Cartesian, CartesianPl and SymmetricX detectors (xopto/mcml/mcdetector/
     # cartesian.py, cartesianpl.py, symmetric.py), oblique beam
     'cartesian_detectors': dict(
@@ -753,6 +776,9 @@ def _source(src_mod, spec):
         kw['fiber'] = _fiber_lut(medium_pkg, kw.pop('fiber_lut'))
     if 'emission' in kw:
         kw['lut'] = _emission(_luts(medium_pkg)[1], kw.pop('emission'))
+    if 'voxels' in kw:
+        kw['voxels'] = np.asarray(kw['voxels'])
+        kw['weights'] = np.asarray(kw['weights'])
     return getattr(src_mod, spec['type'])(**kw)
 
 
