@@ -52,10 +52,10 @@ L2_FLUSH_BYTES = 256 << 20
 # fraction of issue slots in use (smsp__issue_active), the resource that
 # bounds this kernel.
 PROFILED_TRAFFIC = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (8.91e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (8.61e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
 }
 PROFILED_ISSUE_ACTIVE = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.889, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.895, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
 }
 METRIC = 'packets/s (1 GB300)'
 
