@@ -159,6 +159,19 @@ class McUseFluenceCache(McBoolOption):
         super().__init__('MC_USE_FLUENCE_CACHE', value)
 
 
+class McUseEvents(McBoolOption):
+    """Packet event tracking (xopto/mcbase/mcoptions.py:709-732).  The GPU
+    kernels always track events where a trace event mask needs them, so the
+    option is accepted and changes nothing; like the reference's constructor
+    (which names MC_USE_PACKED_STRUCTURES there), it is only recorded."""
+    on = McBoolOption('MC_USE_EVENTS', True)
+    off = McBoolOption('MC_USE_EVENTS', False)
+    default = off
+
+    def __init__(self, value: bool = False):
+        super().__init__('MC_USE_EVENTS', value)
+
+
 class McUseSoft64Atomics(McBoolOption):
     on = McBoolOption('MC_USE_SOFT_64_ATOMICS', True)
     off = McBoolOption('MC_USE_SOFT_64_ATOMICS', False)
