@@ -171,3 +171,56 @@ def test_sampling_volume_host_objects():
     assert mctrace.Trace(100).maxlen == 100
     with pytest.raises(TypeError):
         mctrace.Filter(x=0.5)
+
+
+def test_reference_unbuildable_combinations_rejected(lib):
+    """Combinations whose reference kernel does not build are refused before
+    any launch: a rectangular source with a specular detector
+    (xopto/mcml/mcsource/rectangular.py:141) and look-up-table detectors in
+    voxelized media (xopto/mcvox/mcdetector/total.py:313)."""
+    import scenarios
+    from pyxopto_gb300 import _abi
+    spec = dict(scenarios.SCENARIOS['rect_uniform'])
+    spec['detectors'] = dict(spec['detectors'], specular=dict(type='Total'))
+    mc = scenarios.build_mc(spec)
+    cfg = mc.pack(1000, 8)
+    b = _abi.McgbBuffers()
+    b.rng_x, b.rng_a, b.counters = 16, 16, 16
+    b.accumulator, b.accumulator_size = 16, mc._acc.size
+    assert lib.mcgb_mcml_run(C.byref(cfg), C.byref(b), None) == _abi.E_UNSUPPORTED
+    assert b'specular' in lib.mcgb_last_error()
+    vox = scenarios.build_mc('vox_cartesian')
+    vcfg, _ = vox.pack(1000, 8)
+    vcfg.top.kind = _abi.DET_TOTAL_LUT
+    vcfg.top.n, vcfg.top.n_y, vcfg.top.table_offset = 1, 4, 0
+    vcfg.top.offset = 0
+    vb = _abi.McgbBuffers()
+    vb.rng_x, vb.rng_a, vb.counters, vb.voxels, vb.materials = 16, 16, 16, 16, 16
+    vb.accumulator, vb.accumulator_size = 16, vox._acc.size
+    vb.fp_lut, vb.fp_lut_size = 16, 4
+    assert lib.mcgb_mcvox_run(C.byref(vcfg), C.byref(vb), None) == _abi.E_UNSUPPORTED
+    assert b'look-up-table' in lib.mcgb_last_error()
+
+
+def test_sampling_volume_needs_a_trace():
+    import scenarios
+    from pyxopto_gb300.mcml import mcsv
+    mc = scenarios.build_mc('c1_line_hg_radial')
+    sv = mcsv.SamplingVolume(mcsv.Axis(0, 1e-3, 2), mcsv.Axis(0, 1e-3, 2), mcsv.Axis(0, 1e-3, 2))
+    with pytest.raises(RuntimeError):
+        mc.sampling_volume(None, sv)
+
+
+def test_lut_classes():
+    """LinearLut interpolation and the CDF inversion of EmissionLut
+    (xopto/mcbase/mcutil/lut.py:155-325): an isotropic radiance over
+    cos(theta) in [0, 1] has the density sin(theta), so the table is
+    monotone and spans [0, 1]."""
+    from pyxopto_gb300.mcml.mcutil import lut
+    ll = lut.LinearLut([0.0, 1.0, 4.0], first=1.0, last=3.0)
+    assert np.allclose(ll([1.0, 1.5, 2.0, 2.5, 3.0]), [0.0, 0.5, 1.0, 2.5, 4.0])
+    em = lut.EmissionLut(np.ones(50), n=200)
+    assert em.data.size == 200 and abs(em.data[0]) < 1e-9 and abs(em.data[-1] - 1.0) < 1e-9
+    assert np.all(np.diff(em.data) >= 0.0)
+    col = lut.CollectionLut([0.0, 1.0], costheta=[0.5, 1.0], n=11)
+    assert col.first == 0.5 and col.last == 1.0 and np.allclose(col.data, np.linspace(0, 1, 11))
