@@ -168,6 +168,34 @@ def reference_cpu(workload, seconds=12.0, threads=None, max_packets=None):
 
 
 # --------------------------------------------------------------- GPU side
+def fp32_peak_tflops(torch, lib, dev):
+    """FP32 FMA throughput of this GPU, measured with the library's probe
+    kernel (16 independent FMA chains per thread, full occupancy): best of
+    three launches of about 30 ms, timed with CUDA events.  This is the
+    denominator of the transport kernels' roofline figure."""
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, threads = 2 * sms, 1024
+    out = torch.zeros((blocks,), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    def timed(iters):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        from pyxopto_gb300 import _lib
+        _lib.check(lib.mcgb_fp32_fma_rate(blocks, threads, iters, C.c_void_p(out.data_ptr()), sptr))
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    ms = timed(200)
+    iters = max(200, int(200 * 30.0 / max(ms, 1e-3)))
+    best = min(timed(iters) for _ in range(3))
+    flops = float(blocks) * threads * iters * 256
+    return flops / (best / 1e3) / 1e12, {'blocks': blocks, 'threads': threads, 'iters': iters,
+                                         'ms': best}
+
+
 def gpu_bench(args, rank, world, local_rank):
     import torch
     import scenarios
@@ -255,9 +283,11 @@ def gpu_bench(args, rank, world, local_rank):
         e2e = {'value': nphotons * args.e2e_steps * world / dt, 'unit': 'packets/s',
                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
                'path': 'pyxopto_gb300.mcml.mc.Mc.run'}
+    fp32_peak, fp32_probe = fp32_peak_tflops(torch, lib, dev)
     return dict(total_ms=total_ms, kernel_ms=kernel_ms, steps_per_launch=steps_per_launch,
                 clocks=clocks, e2e=e2e, nphotons=nphotons, streams=streams,
-                packets_done=int(host_counters[_abi.CNT_PACKETS]))
+                packets_done=int(host_counters[_abi.CNT_PACKETS]),
+                fp32_peak=fp32_peak, fp32_probe=fp32_probe)
 
 
 def batched_bench(args):
@@ -490,7 +520,8 @@ def main():
     kern_ms = float(np.mean(res['kernel_ms']))
     peaks = measured_peaks()
     sm_max = peaks.get('sm_max_mhz') or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_derived = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_peak = res['fp32_peak']
     achieved = res['steps_per_launch'] * OPS_PER_STEP / (kern_ms / 1e3) / 1e12
     traffic = PROFILED_TRAFFIC.get((args.workload, args.math, args.scheduling))
     roofline = {'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
@@ -498,8 +529,12 @@ def main():
                 'traffic_source': traffic[1] if traffic else None,
                 'issue_active': (PROFILED_ISSUE_ACTIVE.get((args.workload, args.math, args.scheduling))
                                  or (None,))[0],
-                'peak_source': 'derived: 152 SMs x 128 FP32 lanes x 2 x sm_max_mhz {} '
-                               '(MEASURED_PEAKS.json); no FP32 peak is measured there'.format(sm_max),
+                'peak_source': 'measured in this run: FP32 FMA throughput of the library probe kernel '
+                               '(mcgb_fp32_fma_rate, {blocks} blocks x {threads} threads, best of 3 '
+                               'launches of {ms:.1f} ms); MEASURED_PEAKS.json holds no FP32 '
+                               'peak'.format(**res['fp32_probe']),
+                'peak_derived': fp32_derived,
+                'peak_derived_source': '152 SMs x 128 FP32 lanes x 2 flops x sm_max_mhz {}'.format(sm_max),
                 'ops_per_step': OPS_PER_STEP, 'steps_per_launch': res['steps_per_launch'],
                 'kernel_ms': kern_ms, 'steps_per_s': res['steps_per_launch'] / (kern_ms / 1e3)}
     line = {'metric': METRIC, 'value': value, 'unit': 'packets/s', 'n_gpus': world,

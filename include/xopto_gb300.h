@@ -484,6 +484,15 @@ int mcgb_rng_init(uint64_t *host_x, uint32_t *host_a, uint32_t n, uint64_t xinit
    like RngKernel). */
 int mcgb_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *dev_out, void *stream);
 
+/* FP32 throughput probe: blocks x threads threads each run 16 independent
+   fused multiply-add chains for 8 * iters steps (2 flops each), so one launch
+   is blocks * threads * iters * 256 flops.  dev_out (blocks floats) receives
+   a value only in a case that does not occur, which keeps the chains live.
+   It measures the FP32 peak that the transport kernels are compared with;
+   it has no counterpart in the reference. */
+int mcgb_fp32_fma_rate(uint32_t blocks, uint32_t threads, uint32_t iters, float *dev_out,
+                       void *stream);
+
 /* Fill a device uint64 buffer with a value (ScalarFillMcAccu). */
 int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream);
 

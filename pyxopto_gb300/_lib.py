@@ -28,6 +28,7 @@ _SIGNATURES = {
     'mcgb_rng_init': (C.c_int, [_vp, _vp, C.c_uint32, C.c_uint64]),
     'mcgb_rng_dump': (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint64, _vp, _vp]),
     'mcgb_fill_u64': (C.c_int, [_vp, C.c_uint64, C.c_uint64, _vp]),
+    'mcgb_fp32_fma_rate': (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, _vp, _vp]),
     'mcgb_reduce_tallies': (C.c_int, [_vp, _vp, C.c_uint64]),
     'mcgb_sampling_volume': (C.c_int, [C.POINTER(_abi.McgbSamplingVolume), _vp, C.c_uint64, _vp,
                                        _vp, C.c_uint64, _vp, _vp, _vp]),

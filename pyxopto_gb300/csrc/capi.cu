@@ -252,6 +252,27 @@ __global__ void rng_dump_kernel(uint64_t x, uint32_t a, uint64_t n, float *out) 
 }
 
 /* ScalarFillMcAccu (xopto/mcbase/kernel/mcbase.template.c:1740-1748) */
+/* 16 independent FMA chains per thread, 8 unrolled steps per iteration;
+   x -> x * 0.9999999 + 1e-7 stays near 1, so no chain overflows or goes
+   subnormal. */
+__global__ void __launch_bounds__(1024) fma_rate_kernel(uint32_t iters, float *out) {
+    float a[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = 1.0f + (float)(threadIdx.x + k) * 1e-6f;
+    const float m = 0.9999999f, c = 1e-7f;
+    for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) a[k] = fmaf(a[k], m, c);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s += a[k];
+    if (s == -1.0f) out[blockIdx.x] = s;
+}
+
 __global__ void fill_u64_kernel(uint64_t *p, uint64_t n, uint64_t v) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -421,6 +442,16 @@ int mcgb_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *dev_out, void *stre
     rng_dump_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(x, a, n, dev_out);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? MCGB_OK : cuda_fail(e, "rng dump launch");
+}
+
+int mcgb_fp32_fma_rate(uint32_t blocks, uint32_t threads, uint32_t iters, float *dev_out,
+                       void *stream) {
+    if (!dev_out) return fail(MCGB_E_INVALID, "output buffer is NULL");
+    if (blocks == 0 || blocks > 65535u || threads == 0 || threads > 1024u || threads % 32u)
+        return fail(MCGB_E_INVALID, "fma probe: %u blocks of %u threads", blocks, threads);
+    fma_rate_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, dev_out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? MCGB_OK : cuda_fail(e, "fma probe launch");
 }
 
 int mcgb_fill_u64(uint64_t *dev, uint64_t n, uint64_t value, void *stream) {
