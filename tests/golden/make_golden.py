@@ -27,6 +27,9 @@ Writes
   cuda_mcml_fiber2.npz   the same for the two-layer sample, sweep on the
                          second layer (cuda_doublelayer_uniformfiber.pkl,
                          test validate.py:692-866).
+  sfdi_30deg_variable_na.npz  the SFDI amplitudes and phases of the 30 degree
+                         incidence test (validate.py:867-1050); written by
+                         `make_golden.py sfdi`.
   linear_probe_*.npz     the reflectances of the six- and nine-fibre
                          linear-probe tests (single_layer_*_linear_probe.pkl,
                          validate.py:1227-1758); written by
@@ -207,7 +210,32 @@ def make_linear_probe(key):
     print('linear_probe', key, refl.shape)
 
 
+def make_sfdi():
+    """Spatial-frequency amplitude and phase of the reference's SFDI test
+    (30 degree incidence, SymmetricX detector, 45 detector NAs;
+    xopto/mcml/test/validate.py:867-1050) with its geometry."""
+    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference',
+                        'single_layer_sfdi_30deg_incidence_variable_na.pkl')
+    with open(path, 'rb') as f:
+        d = pickle.load(f)
+    layers, ax = d['layers'], d['detector']['axis']
+    np.savez_compressed(
+        os.path.join(HERE, 'sfdi_30deg_variable_na.npz'),
+        n=np.array([l['basic']['n'] for l in layers]), d=np.array([l['basic']['d'] for l in layers]),
+        mua=np.array([l['basic']['mua'] for l in layers]), mus=np.array([l['basic']['mus'] for l in layers]),
+        g=np.array([l['pf']['pfparams'][0] for l in layers]),
+        direction=np.array(d['source']['direction'], dtype=np.float64),
+        axis=np.array([ax['center'], ax['range'], ax['n_half'], float(ax['logscale'])]),
+        frequencies=np.asarray(d['frequencies'], np.float64), na=np.asarray(d['lut']['na'], np.float64),
+        amplitude=np.asarray(d['amplitude'], np.float64), phase=np.asarray(d['phase'], np.float64),
+        rmax=np.array([d['mc']['rmax']]))
+    print('sfdi', np.asarray(d['amplitude']).shape)
+
+
 if __name__ == '__main__':
+    if sys.argv[1:2] == ['sfdi']:
+        make_sfdi()
+        sys.exit(0)
     if sys.argv[1:2] == ['linear_probe']:
         for k in PROBE_PICKLES:
             make_linear_probe(k)
