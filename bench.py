@@ -401,13 +401,18 @@ def fiber_sweep_bench(args):
     xopto/mcml/test/validate.py:348-511): 400 sequential Mc.run calls of
     1e7 packets each (a 20 x 20 mua/mus' sweep, UniformFiberNI source),
     timed through the public API; one step = one sweep.  The reference
-    prints 5.7 s per sweep for an RTX A6000 (OpenCL, fast relaxed math)."""
+    prints 5.7 s per sweep for an RTX A6000 (OpenCL, fast relaxed math).
+    Workload 'fiber_sweep_vox' is the voxelized version
+    (test/mcvox/performance.py running xopto/mcvox/test/validate.py:357-536:
+    the layer as one voxel, UniformFiber source), 8.3 s on an RTX A6000."""
     import torch
     import fiber_sweep
     from pyxopto_gb300 import _abi
+    vox = args.workload == 'fiber_sweep_vox'
     data = fiber_sweep.load()
     nphotons = int(args.packets or 10_000_000)
-    sim = fiber_sweep.build(data, fast=args.math == 'fast', scheduling=args.scheduling)
+    builder = fiber_sweep.build_vox if vox else fiber_sweep.build
+    sim = builder(data, fast=args.math == 'fast', scheduling=args.scheduling)
     for _ in range(args.warmup):
         fiber_sweep.run(sim, data, nphotons)
     torch.cuda.synchronize()
@@ -426,18 +431,21 @@ def fiber_sweep_bench(args):
     return {'metric': 'packets/s (fibre sweep through Mc.run, 400 x {:.0e} packets)'.format(nphotons),
             'value': npk / sweep_s, 'unit': 'packets/s', 'ms_per_step': sweep_s * 1e3,
             'seconds_per_sweep': sweep_s,
-            'reference_published_seconds_per_sweep': {'RTX A6000': 5.7, 'RTX 2080 Ti': 7.4,
-                                                      'source': 'test/performance.py:122-125'},
+            'reference_published_seconds_per_sweep': (
+                {'RTX A6000': 8.3, 'RTX 2080 Ti': 9.9, 'source': 'test/mcvox/performance.py:138-141'}
+                if vox else {'RTX A6000': 5.7, 'RTX 2080 Ti': 7.4, 'source': 'test/performance.py:122-125'}),
             'mean_rel_error_vs_cuda_mcml_pct': float(np.mean(errs)),
-            'config': {'workload': 'fiber_sweep', 'simulations': 400, 'packets_per_sim': nphotons,
-                       'source': 'UniformFiberNI 200 um, NA 0.22', 'layer_mm': 8, 'rmax_m': 5e-3,
+            'config': {'workload': args.workload, 'simulations': 400, 'packets_per_sim': nphotons,
+                       'medium': 'mcvox (one voxel)' if vox else 'mcml',
+                       'source': ('UniformFiber' if vox else 'UniformFiberNI') + ' 200 um, NA 0.22',
+                       'layer_mm': 8, 'rmax_m': 5e-3,
                        'detector': 'Radial 0-1.7 mm / 340 bins, fibre acceptance',
                        'math': args.math, 'scheduling': args.scheduling},
             'clocks': clocks, 'gpu_launches': 400 * args.steps,
             'e2e': {'value': npk / sweep_s, 'unit': 'packets/s',
-                    'h2d_bytes_per_step': 400 * C.sizeof(_abi.McgbMcmlConfig),
+                    'h2d_bytes_per_step': 400 * (C.sizeof(_abi.McgbMcvoxConfig) + 2 * C.sizeof(_abi.McgbMaterial) if vox else C.sizeof(_abi.McgbMcmlConfig)),
                     'd2h_bytes_per_step': 400 * (8 * 340 + 8 * _abi.NUM_COUNTERS),
-                    'path': 'pyxopto_gb300.mcml.mc.Mc.run, 400 calls'}}
+                    'path': 'pyxopto_gb300.{}.mc.Mc.run, 400 calls'.format('mcvox' if vox else 'mcml')}}
 
 
 def main():
@@ -463,11 +471,12 @@ def main():
                          'a headline number uses the workload size)')
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
-    if args.workload in ('batched_4096', 'surrogate', 'fiber_sweep') and args.impl == 'gb300':
+    if args.workload in ('batched_4096', 'surrogate', 'fiber_sweep', 'fiber_sweep_vox') and \
+            args.impl == 'gb300':
         import torch
         torch.cuda.set_device(local_rank)
         res = {'batched_4096': batched_bench, 'surrogate': surrogate_bench,
-               'fiber_sweep': fiber_sweep_bench}[args.workload](args)
+               'fiber_sweep': fiber_sweep_bench, 'fiber_sweep_vox': fiber_sweep_bench}[args.workload](args)
         line = dict({'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
                      'scaling': 'none', 'vs_baseline': None, 'dtype': 'f32',
                      'data': 'synthetic (seeded parameter draws and RNG streams)'}, **res)

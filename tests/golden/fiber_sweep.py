@@ -46,6 +46,34 @@ def build(data, fast=True, scheduling='dynamic', rnginit=1):
     return sim
 
 
+def build_vox(data, fast=True, scheduling='dynamic', rnginit=1):
+    """The voxelized-medium version of the test (xopto/mcvox/test/validate.py:
+    357-536): one voxel spanning +-2 rmax laterally and the layer thickness
+    in depth, material 1 = the layer, material 0 = the fibre-side medium
+    (also below the sample), the tilted-fibre source at normal incidence."""
+    from pyxopto_gb300.mcvox import mc
+    from pyxopto_gb300.mcvox.mcutil import fiber
+    g = data['g']
+    rmax = float(data['rmax'][0])
+    A = mc.mcgeometry.Axis
+    voxels = mc.mcgeometry.Voxels(A(-2.0 * rmax, 2.0 * rmax, 1), A(-2.0 * rmax, 2.0 * rmax, 1),
+                                  A(0.0, float(data['d'][1]), 1))
+    materials = [mc.mcmaterial.Material(n=float(data['n'][0]), mua=0.0, mus=0.0, pf=mc.mcpf.Hg(float(g[0]))),
+                 mc.mcmaterial.Material(n=float(data['n'][1]), mua=0.0, mus=0.0, pf=mc.mcpf.Hg(float(g[1])))]
+    dcore, dclad, ncore, na = (float(v) for v in data['fiber'])
+    source = mc.mcsource.UniformFiber(fiber.MultimodeFiber(dcore, dclad, ncore, na))
+    start, stop, n = data['axis']
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(
+        mc.mcdetector.RadialAxis(float(start), float(stop), int(n)), cosmin=float(data['cosmin'][0])))
+    opts = [mc.mcoptions.McScheduling(scheduling)]
+    if fast:
+        opts.append(mc.mcoptions.McUseNativeMath(True))
+    sim = mc.Mc(voxels, materials, source, det, options=opts, rnginit=rnginit)
+    sim.rmax = rmax
+    sim.voxels.material[...] = 1
+    return sim
+
+
 def run(sim, data, nphotons):
     """Runs the 400 simulations in sequence (as the reference does); returns
     (fibre reflectance [20, 20, 5], seconds spent in Mc.run)."""
@@ -55,9 +83,11 @@ def run(sim, data, nphotons):
     g = float(data['g'][k])
     profiles, r = [], None
     t = 0.0
+    target = sim.materials[1] if hasattr(sim, 'materials') else None
     for i in range(mua.size):
-        sim.layers[k].mua = float(mua.flat[i])
-        sim.layers[k].mus = float(musr.flat[i]) / (1.0 - g)
+        obj = target if target is not None else sim.layers[k]
+        obj.mua = float(mua.flat[i])
+        obj.mus = float(musr.flat[i]) / (1.0 - g)
         t0 = time.perf_counter()
         _, _, det = sim.run(nphotons)
         t += time.perf_counter() - t0

@@ -308,3 +308,42 @@ def test_sfdi_30deg_variable_na(cuda, lib):
     ea, ep = sfdi_sweep.errors(data, idx, amp, ph)
     assert ea.max() < 0.025, ea
     assert ep.max() < 0.025, ep
+
+
+@pytest.mark.parametrize('fast', [False, True])
+def test_cuda_mcml_golden_profile_voxelized(cuda, lib, fast):
+    """The voxelized simulator's version of SingleLayerLineSourceRadialProfile
+    (xopto/mcvox/test/validate.py:213-356): the layer as one voxel spanning
+    +-2 rmax, radial reflectance against the CUDA-MCML profile, pass if
+    |mean relative error| < 0.5 %."""
+    from pyxopto_gb300.mcvox import mc
+    g = np.load(os.path.join(GOLD, 'cuda_mcml_radial.npz'))
+    rmax = float(g['rmax'][0])
+    A = mc.mcgeometry.Axis
+    vox = mc.mcgeometry.Voxels(A(-2.0 * rmax, 2.0 * rmax, 1), A(-2.0 * rmax, 2.0 * rmax, 1),
+                               A(0.0, float(g['d'][1]), 1))
+    mats = [mc.mcmaterial.Material(n=float(g['n'][i]), mua=float(g['mua'][i]), mus=float(g['mus'][i]),
+                                   pf=mc.mcpf.Hg(float(g['g'][i]))) for i in range(2)]
+    start, stop, nb = g['axis']
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(
+        mc.mcdetector.RadialAxis(float(start), float(stop), int(nb)), cosmin=float(g['cosmin'][0])))
+    opts = [mc.mcoptions.McUseNativeMath(True)] if fast else []
+    sim = mc.Mc(vox, mats, mc.mcsource.Line(), det, options=opts, rnginit=7)
+    sim.rmax = rmax
+    sim.voxels.material[...] = 1
+    _, _, res = sim.run(10_000_000)
+    rel = (res.top.reflectance - g['reflectance']) / g['reflectance'] * 100.0
+    assert abs(np.mean(rel)) < 0.5, np.mean(rel)
+
+
+def test_cuda_mcml_fiber_sweep_voxelized(cuda, lib):
+    """The voxelized simulator's SingleLayerUniformFiberRadial
+    (xopto/mcvox/test/validate.py:357-536) against the CUDA-MCML fibre
+    reflectances, pass if |mean relative error| < 0.5 % (1e6 packets per
+    point here, 1e7 in the reference)."""
+    data = fiber_sweep.load()
+    sim = fiber_sweep.build_vox(data, fast=True)
+    refl, _ = fiber_sweep.run(sim, data, 1_000_000)
+    err = fiber_sweep.relative_error(data, refl)
+    assert abs(err.mean()) < 0.5, err.mean()
+    assert np.median(np.abs(err)) < 3.0, np.median(np.abs(err))
