@@ -27,6 +27,8 @@ Writes
   cuda_mcml_fiber2.npz   the same for the two-layer sample, sweep on the
                          second layer (cuda_doublelayer_uniformfiber.pkl,
                          test validate.py:692-866).
+  uniformfiber_trace.npz the geometry of the trace self-consistency test
+                         (validate.py:1059-1226); `make_golden.py trace_check`.
   sfdi_30deg_variable_na.npz  the SFDI amplitudes and phases of the 30 degree
                          incidence test (validate.py:867-1050); written by
                          `make_golden.py sfdi`.
@@ -232,7 +234,30 @@ def make_sfdi():
     print('sfdi', np.asarray(d['amplitude']).shape)
 
 
+def make_trace_check():
+    """Geometry of the reference's trace self-consistency test
+    (SingleLayerUniformFiberTrace, xopto/mcml/test/validate.py:1059-1226)."""
+    path = os.path.join(render_ref.REFERENCE, 'xopto', 'mcml', 'test', 'reference',
+                        'single_layer_uniformfiber_trace.pkl')
+    with open(path, 'rb') as f:
+        d = pickle.load(f)
+    layers, src, det = d['layers'], d['source'], d['detector']
+    np.savez_compressed(
+        os.path.join(HERE, 'uniformfiber_trace.npz'),
+        n=np.array([l['basic']['n'] for l in layers]), d=np.array([l['basic']['d'] for l in layers]),
+        g=np.array([l['pf']['pfparams'][0] for l in layers]),
+        fiber=np.array([src['dcore'], src['dcladding'], src['ncore'], src['na']]),
+        axis=np.array([det['axis']['start'], det['axis']['stop'], det['axis']['n']]),
+        cosmin=np.array([det['cosmin']]), maxlen=np.array([d['trace']['maxlen']]),
+        mua=np.asarray(d['lut']['mua'], np.float64), musr=np.asarray(d['lut']['musr'], np.float64),
+        rmax=np.array([d['mc']['rmax']]))
+    print('trace check', d['lut'])
+
+
 if __name__ == '__main__':
+    if sys.argv[1:2] == ['trace_check']:
+        make_trace_check()
+        sys.exit(0)
     if sys.argv[1:2] == ['sfdi']:
         make_sfdi()
         sys.exit(0)

@@ -347,3 +347,46 @@ def test_cuda_mcml_fiber_sweep_voxelized(cuda, lib):
     err = fiber_sweep.relative_error(data, refl)
     assert abs(err.mean()) < 0.5, err.mean()
     assert np.median(np.abs(err)) < 3.0, np.median(np.abs(err))
+
+
+def test_uniformfiber_trace_matches_radial_detector(cuda, lib):
+    """The reference's SingleLayerUniformFiberTrace test
+    (xopto/mcml/test/validate.py:1059-1226): 1e6 packets of a UniformFiber
+    source with a 100-event trace; the reflectance rebuilt from the terminal
+    trace events (z <= 0, |pz| >= cosmin) equals the Radial detector's in
+    every ring within 0.1 %, for five (mua, mus') points."""
+    from pyxopto_gb300.mcml import mc
+    from pyxopto_gb300.mcml.mcutil import fiber
+    d = np.load(os.path.join(GOLD, 'uniformfiber_trace.npz'))
+    layers = mc.mclayer.Layers([
+        mc.mclayer.Layer(d=float(d['d'][i]), n=float(d['n'][i]), mua=0.0, mus=0.0,
+                         pf=mc.mcpf.Hg(float(d['g'][i]))) for i in range(3)])
+    dcore, dclad, ncore, na = (float(v) for v in d['fiber'])
+    source = mc.mcsource.UniformFiber(fiber.MultimodeFiber(dcore, dclad, ncore, na))
+    start, stop, nb = d['axis']
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Radial(
+        mc.mcdetector.RadialAxis(float(start), float(stop), int(nb)), cosmin=float(d['cosmin'][0])))
+    sim = mc.Mc(layers, source, det, mc.mctrace.Trace(maxlen=int(d['maxlen'][0])),
+                options=[mc.mcoptions.McUseNativeMath(True)], rnginit=11)
+    sim.rmax = float(d['rmax'][0])
+    top = sim.detectors.top
+    edges, nr, cosmin = top.edges, top.n, top.cosmin
+    dr = edges[1] - edges[0]
+    rings = np.pi * (edges[1:] ** 2 - edges[:-1] ** 2)
+    nphotons = 1_000_000
+    g1 = float(d['g'][1])
+    for mua, musr in zip(d['mua'], d['musr']):
+        sim.layers[1].mua = float(mua)
+        sim.layers[1].mus = float(musr) / (1.0 - g1)
+        tr, _, res = sim.run(nphotons)
+        term = np.minimum(tr.n - 1, tr.maxlen - 1)
+        last = tr.data[np.arange(nphotons), term]
+        rind = np.minimum(np.floor(np.sqrt(last['x'] ** 2 + last['y'] ** 2) / dr), nr - 1).astype(int)
+        ok = (last['z'] <= 0.0) & (np.abs(last['pz']) >= cosmin)
+        refl_trace = np.bincount(rind[ok], weights=last['w'][ok].astype(np.float64), minlength=nr)
+        refl_trace = refl_trace / (nphotons * rings)
+        refl = res.top.reflectance
+        mask = refl != 0
+        assert not np.any((refl == 0) & (refl_trace != 0))
+        err = np.abs(refl_trace[mask] - refl[mask]) / refl[mask]
+        assert err.max() < 1e-3, (mua, musr, err.max())
