@@ -344,6 +344,26 @@ class Cartesian(_Directional):
     reflectance = property(_get_normalized)
     transmittance = property(_get_normalized)
 
+    def radial(self, raxis, order=2, nfi=360, center=(0.0, 0.0)) -> 'Radial':
+        """A Radial detector resampled from this one: the per-area data is
+        interpolated at nfi azimuths on every ring of ``raxis`` around
+        ``center`` and summed with the ring areas
+        (xopto/mcml/mcdetector/cartesian.py:289-327)."""
+        from .mcutil.interp import interp2
+        nfi = int(nfi)
+        dfi = 2.0 * np.pi / nfi
+        fi = np.linspace(0.5 * dfi, 2.0 * np.pi - 0.5 * dfi, nfi)
+        area = self._x_axis.step * self._y_axis.step
+        a = np.pi * (raxis.edges[1:] ** 2 - raxis.edges[:-1] ** 2)
+        w = np.reshape(a / (nfi * area), (1, raxis.n))
+        R, Fi = np.meshgrid(raxis.centers, fi)
+        Xi, Yi = R * np.cos(Fi) + center[0], R * np.sin(Fi) + center[1]
+        raw = interp2(Xi, Yi, self.x, self.y, self.raw, order=order)
+        raw = (raw * w).sum(0)
+        out = Radial(raxis, cosmin=self._cosmin)
+        out.set_raw_data(raw, self.nphotons)
+        return out
+
     def pack(self, mc, target):
         """cartesian.py:340-372."""
         target.kind = self.kind

@@ -46,6 +46,30 @@ def build(data, fast=True, scheduling='dynamic', rnginit=1):
     return sim
 
 
+def build_cartesian(data, fast=True, scheduling='dynamic', rnginit=1):
+    """SingleLayerUniformFiberCartesian (xopto/mcml/test/validate.py:514-690):
+    the same sample and source with a Cartesian detector of 1.1 x rmax by
+    1.05 x rmax half-widths at the radial step, resampled to the radial axis
+    by Cartesian.radial before the fibre integration.  Returns (simulator,
+    radial axis)."""
+    import numpy as np
+    sim = build(data, fast=fast, scheduling=scheduling, rnginit=rnginit)
+    from pyxopto_gb300.mcml import mc
+    start, stop, nr = (float(v) for v in data['axis'])
+    dr = stop / nr
+    nx = np.ceil(nr * 2.2 / 2.0) * 2.0
+    ny = np.ceil(nr * 2.1 / 2.0) * 2.0
+    det = mc.mcdetector.Detectors(top=mc.mcdetector.Cartesian(
+        mc.mcdetector.Axis(-dr * nx * 0.5, dr * nx * 0.5, int(nx)),
+        mc.mcdetector.Axis(-dr * ny * 0.5, dr * ny * 0.5, int(ny)), cosmin=float(data['cosmin'][0])))
+    opts = [mc.mcoptions.McScheduling(scheduling)]
+    if fast:
+        opts.append(mc.mcoptions.McUseNativeMath(True))
+    cart = mc.Mc(sim.layers, sim.source, det, options=opts, rnginit=rnginit)
+    cart.rmax = sim.rmax
+    return cart, mc.mcdetector.RadialAxis(start, stop, int(nr))
+
+
 def build_vox(data, fast=True, scheduling='dynamic', rnginit=1):
     """The voxelized-medium version of the test (xopto/mcvox/test/validate.py:
     357-536): one voxel spanning +-2 rmax laterally and the layer thickness
@@ -74,7 +98,7 @@ def build_vox(data, fast=True, scheduling='dynamic', rnginit=1):
     return sim
 
 
-def run(sim, data, nphotons):
+def run(sim, data, nphotons, raxis=None):
     """Runs the 400 simulations in sequence (as the reference does); returns
     (fibre reflectance [20, 20, 5], seconds spent in Mc.run)."""
     from pyxopto_gb300.util import convolve
@@ -91,8 +115,12 @@ def run(sim, data, nphotons):
         t0 = time.perf_counter()
         _, _, det = sim.run(nphotons)
         t += time.perf_counter() - t0
-        profiles.append(det.top.reflectance)
-        r = det.top.r
+        if raxis is not None:
+            profiles.append(det.top.radial(raxis).reflectance)
+            r = raxis.centers
+        else:
+            profiles.append(det.top.reflectance)
+            r = det.top.r
     refl = convolve.fiber_reflectance(r, np.asarray(profiles), sds=list(data['sds']),
                                       dcore=float(data['sds_dcore'][0]))
     return refl.reshape(data['reflectance'].shape), t

@@ -390,3 +390,16 @@ def test_uniformfiber_trace_matches_radial_detector(cuda, lib):
         assert not np.any((refl == 0) & (refl_trace != 0))
         err = np.abs(refl_trace[mask] - refl[mask]) / refl[mask]
         assert err.max() < 1e-3, (mua, musr, err.max())
+
+
+def test_cuda_mcml_fiber_sweep_cartesian(cuda, lib):
+    """The reference's SingleLayerUniformFiberCartesian test
+    (xopto/mcml/test/validate.py:514-690): the fibre sweep with a Cartesian
+    detector resampled by Cartesian.radial, against the CUDA-MCML fibre
+    reflectances; pass if |mean relative error| < 0.5 % (1e6 packets per
+    point here, 1e7 in the reference)."""
+    data = fiber_sweep.load()
+    sim, raxis = fiber_sweep.build_cartesian(data, fast=True)
+    refl, _ = fiber_sweep.run(sim, data, 1_000_000, raxis=raxis)
+    err = fiber_sweep.relative_error(data, refl)
+    assert abs(err.mean()) < 0.5, err.mean()
