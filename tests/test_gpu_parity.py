@@ -388,8 +388,9 @@ def test_uniformfiber_trace_matches_radial_detector(cuda, lib):
         refl = res.top.reflectance
         mask = refl != 0
         assert not np.any((refl == 0) & (refl_trace != 0))
-        err = np.abs(refl_trace[mask] - refl[mask]) / refl[mask]
-        assert err.max() < 1e-3, (mua, musr, err.max())
+        if mask.any():      # no reflectance at all for the purely absorbing point
+            err = np.abs(refl_trace[mask] - refl[mask]) / refl[mask]
+            assert err.max() < 1e-3, (mua, musr, err.max())
 
 
 def test_cuda_mcml_fiber_sweep_cartesian(cuda, lib):
