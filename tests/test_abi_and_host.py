@@ -224,3 +224,14 @@ def test_lut_classes():
     assert np.all(np.diff(em.data) >= 0.0)
     col = lut.CollectionLut([0.0, 1.0], costheta=[0.5, 1.0], n=11)
     assert col.first == 0.5 and col.last == 1.0 and np.allclose(col.data, np.linspace(0, 1, 11))
+
+
+def test_cartesian_to_radial_conversion():
+    """Cartesian.radial (xopto/mcml/mcdetector/cartesian.py:289-327): a
+    uniform Cartesian reflectance stays the same reflectance on every ring
+    that lies inside the grid."""
+    from pyxopto_gb300.mcml import mcdetector
+    cart = mcdetector.Cartesian(mcdetector.Axis(-1e-3, 1e-3, 40), mcdetector.Axis(-1e-3, 1e-3, 40))
+    cart.set_raw_data(np.full(cart.shape, 3.0), 1000)
+    rad = cart.radial(mcdetector.RadialAxis(0.0, 8e-4, 16))
+    assert np.allclose(rad.reflectance, cart.reflectance[0, 0], rtol=1e-6)
