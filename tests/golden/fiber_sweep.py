@@ -80,10 +80,21 @@ def build_vox(data, fast=True, scheduling='dynamic', rnginit=1):
     g = data['g']
     rmax = float(data['rmax'][0])
     A = mc.mcgeometry.Axis
-    voxels = mc.mcgeometry.Voxels(A(-2.0 * rmax, 2.0 * rmax, 1), A(-2.0 * rmax, 2.0 * rmax, 1),
-                                  A(0.0, float(data['d'][1]), 1))
-    materials = [mc.mcmaterial.Material(n=float(data['n'][0]), mua=0.0, mus=0.0, pf=mc.mcpf.Hg(float(g[0]))),
-                 mc.mcmaterial.Material(n=float(data['n'][1]), mua=0.0, mus=0.0, pf=mc.mcpf.Hg(float(g[1])))]
+    double = 'fixed_layer' in data.files
+    if double:
+        # DoubleLayerUniformFiberRadial (xopto/mcvox/test/validate.py:730-925):
+        # 0.1 mm voxels in depth, material 1 down to the first layer's depth
+        thickness = float(data['d'][1] + data['d'][2])
+        zaxis = A(0.0, thickness, int(round(thickness / 0.1e-3)))
+    else:
+        zaxis = A(0.0, float(data['d'][1]), 1)
+    voxels = mc.mcgeometry.Voxels(A(-2.0 * rmax, 2.0 * rmax, 1), A(-2.0 * rmax, 2.0 * rmax, 1), zaxis)
+    materials = [mc.mcmaterial.Material(n=float(data['n'][i]), mua=0.0, mus=0.0, pf=mc.mcpf.Hg(float(g[i])))
+                 for i in range(3 if double else 2)]
+    if double:
+        k = int(data['fixed_layer'][0])
+        materials[k].mua = float(data['fixed_mua'][0])
+        materials[k].mus = float(data['fixed_musr'][0]) / (1.0 - float(g[k]))
     dcore, dclad, ncore, na = (float(v) for v in data['fiber'])
     source = mc.mcsource.UniformFiber(fiber.MultimodeFiber(dcore, dclad, ncore, na))
     start, stop, n = data['axis']
@@ -95,6 +106,9 @@ def build_vox(data, fast=True, scheduling='dynamic', rnginit=1):
     sim = mc.Mc(voxels, materials, source, det, options=opts, rnginit=rnginit)
     sim.rmax = rmax
     sim.voxels.material[...] = 1
+    if double:
+        zc = zaxis.centers
+        sim.voxels.material[zc > float(data['d'][1]), :, :] = 2
     return sim
 
 
@@ -107,7 +121,7 @@ def run(sim, data, nphotons, raxis=None):
     g = float(data['g'][k])
     profiles, r = [], None
     t = 0.0
-    target = sim.materials[1] if hasattr(sim, 'materials') else None
+    target = sim.materials[k] if hasattr(sim, 'materials') else None
     for i in range(mua.size):
         obj = target if target is not None else sim.layers[k]
         obj.mua = float(mua.flat[i])

@@ -336,12 +336,14 @@ def test_cuda_mcml_golden_profile_voxelized(cuda, lib, fast):
     assert abs(np.mean(rel)) < 0.5, np.mean(rel)
 
 
-def test_cuda_mcml_fiber_sweep_voxelized(cuda, lib):
-    """The voxelized simulator's SingleLayerUniformFiberRadial
-    (xopto/mcvox/test/validate.py:357-536) against the CUDA-MCML fibre
-    reflectances, pass if |mean relative error| < 0.5 % (1e6 packets per
-    point here, 1e7 in the reference)."""
-    data = fiber_sweep.load()
+@pytest.mark.parametrize('double', [False, True])
+def test_cuda_mcml_fiber_sweep_voxelized(cuda, lib, double):
+    """The voxelized simulator's SingleLayerUniformFiberRadial and
+    DoubleLayerUniformFiberRadial (xopto/mcvox/test/validate.py:357-536,
+    730-925; the two-layer sample as 85 voxels of 0.1 mm in depth) against
+    the CUDA-MCML fibre reflectances, pass if |mean relative error| < 0.5 %
+    (1e6 packets per point here, 1e7 in the reference)."""
+    data = fiber_sweep.load(double)
     sim = fiber_sweep.build_vox(data, fast=True)
     refl, _ = fiber_sweep.run(sim, data, 1_000_000)
     err = fiber_sweep.relative_error(data, refl)
