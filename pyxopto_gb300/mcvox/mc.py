@@ -13,7 +13,7 @@ from .._engine import McEngine, torch_cuda
 from ..mcbase.mcmaterial import Material, Materials
 from ..mcbase.mcutil import Axis, RadialAxis
 from . import (mcgeometry, mcsource, mcdetector, mcpf, mcfluence, mctrace, mcoptions, mctypes,
-               mcmaterial, mcsv)
+               mcmaterial, mcsv, mcsurface)
 
 
 class Mc(McEngine):
@@ -23,8 +23,8 @@ class Mc(McEngine):
                  surface=None, types=mctypes.McDataTypesSingle, options=None, rnginit=None,
                  cl_devices=None, cl_build_options=None, cl_profiling=False):
         super().__init__(options=options, rnginit=rnginit, types=types)
-        if surface is not None:
-            raise ValueError('Surface layouts are not supported by the GB300 kernels.')
+        mcsurface.check_supported(surface)
+        self._surface = surface
         self._voxels = voxels
         self._materials = Materials(materials)
         self._pf_type = type(self._materials[0].pf)

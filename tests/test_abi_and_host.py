@@ -235,3 +235,16 @@ def test_cartesian_to_radial_conversion():
     cart.set_raw_data(np.full(cart.shape, 3.0), 1000)
     rad = cart.radial(mcdetector.RadialAxis(0.0, 8e-4, 16))
     assert np.allclose(rad.reflectance, cart.reflectance[0, 0], rtol=1e-6)
+
+
+def test_voxelized_surface_layouts_refused():
+    """None of the reference's voxelized surface layouts builds into its
+    kernel (xopto/mcvox/mcsurface), so mcvox.Mc takes only the default
+    layouts and refuses the others with an explanation."""
+    import scenarios
+    from pyxopto_gb300.mcvox import mc
+    m = scenarios.build_mc('vox_cartesian')
+    mc.Mc(m.voxels, m.materials, m.source, surface=mc.mcsurface.SurfaceLayouts())
+    with pytest.raises(ValueError, match='do not build'):
+        mc.Mc(m.voxels, m.materials, m.source,
+              surface=mc.mcsurface.SurfaceLayouts(bottom=mc.mcsurface.LambertianReflector(0.5)))
