@@ -596,6 +596,16 @@ class Detectors:
     def slots(self):
         return (('top', self._top), ('bottom', self._bottom), ('specular', self._specular))
 
+    def todict(self) -> dict:
+        """Configuration of the three slots (xopto/mcml/mcdetector/base.py:
+        Detectors.todict); an empty slot is None."""
+        def one(d):
+            if isinstance(d, DetectorDefault) or not hasattr(d, 'todict'):
+                return None
+            return d.todict()
+        return {'type': 'Detectors', 'top': one(self._top), 'bottom': one(self._bottom),
+                'specular': one(self._specular)}
+
     def __str__(self):
         return 'Detectors(top={}, bottom={}, specular={})'.format(
             self._top, self._bottom, self._specular)

@@ -248,3 +248,13 @@ def test_voxelized_surface_layouts_refused():
     with pytest.raises(ValueError, match='do not build'):
         mc.Mc(m.voxels, m.materials, m.source,
               surface=mc.mcsurface.SurfaceLayouts(bottom=mc.mcsurface.LambertianReflector(0.5)))
+
+
+def test_run_helper_configuration():
+    """McRunHelper builds its simulator from the create_* hooks in the
+    reference's order and reports the configuration (mcrun/helper.py)."""
+    from pyxopto_gb300.mcml import mcrun
+    h = mcrun.McRunHelper()
+    cfg = h.collect_mc_config()
+    assert cfg['detectors'] is not None and cfg['fluence'] is None and cfg['trace'] is None
+    assert h.collect_detectors(None) == {'reflectance': None, 'transmittance': None, 'specular': None}

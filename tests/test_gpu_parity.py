@@ -406,3 +406,34 @@ def test_cuda_mcml_fiber_sweep_cartesian(cuda, lib):
     refl, _ = fiber_sweep.run(sim, data, 1_000_000, raxis=raxis)
     err = fiber_sweep.relative_error(data, refl)
     assert abs(err.mean()) < 0.5, err.mean()
+
+
+def test_run_helpers(cuda, lib):
+    """RunMinWeightTop and McRunHelper (xopto/mcml/mcrun) drive Mc.run:
+    batches accumulate until the top detector holds the asked weight, and a
+    helper subclass updates the layers before each of its runs."""
+    from pyxopto_gb300.mcml import mc, mcrun
+    sim = scenarios.build_mc('c1_line_hg_radial', scheduling='dynamic')
+    runner = mcrun.RunMinWeightTop(min_weight=500.0, batch_size=20_000)
+    trace, fluence, det = runner.run(sim)
+    assert runner.weight >= 500.0 and runner.n % 20_000 == 0
+    assert det.top.nphotons == runner.n
+
+    class Helper(mcrun.McRunHelper):
+        def create_layers(self):
+            return mc.mclayer.Layers([
+                mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.8)),
+                mc.mclayer.Layer(d=float('inf'), n=1.4, mua=100.0, mus=1e4, pf=mc.mcpf.Hg(0.8)),
+                mc.mclayer.Layer(d=0.0, n=1.0, mua=0.0, mus=0.0, pf=mc.mcpf.Hg(0.8))])
+
+        def create_detectors(self):
+            return mc.mcdetector.Detectors(top=mc.mcdetector.Total())
+
+        def update_layers(self):
+            self.mc_obj.layers[1].mua *= 2.0
+
+    h = Helper(options=[mc.mcoptions.McUseNativeMath(True)])
+    res = h.run_batch(3, 100_000)
+    totals = [float(np.sum(r['detectors']['reflectance'])) for r in res]
+    assert [r['index'] for r in res] == [0, 1, 2]
+    assert totals[0] > totals[1] > totals[2] > 0.0     # more absorption, less reflectance
