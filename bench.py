@@ -53,9 +53,11 @@ L2_FLUSH_BYTES = 256 << 20
 # bounds this kernel.
 PROFILED_TRAFFIC = {
     ('c2_skin_gk_fluence', 'fast', 'dynamic'): (8.61e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (1.774e10, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 PROFILED_ISSUE_ACTIVE = {
     ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.895, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.870, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 METRIC = 'packets/s (1 GB300)'
 
@@ -487,7 +489,9 @@ def main():
     spec = scenarios.ALL[args.workload]
     config = {'workload': args.workload, 'packets_per_step': int(args.packets or spec['nphotons']),
               'medium': spec['medium'], 'math': args.math, 'scheduling': args.scheduling,
-              'l2': 'flushed between steps (256 MB write); fluence tally 8 MB fits L2'}
+              'l2': 'flushed between steps (256 MB write); fluence tally {:.0f} MB'.format(
+                  8.0 * np.prod([a[2] for a in (spec['fluence']['x'], spec['fluence']['y'],
+                                                spec['fluence']['z'])]) / 1e6 if spec.get('fluence') else 0.0)}
 
     if args.impl == 'reference':
         if rank != 0:
