@@ -437,3 +437,29 @@ def test_run_helpers(cuda, lib):
     totals = [float(np.sum(r['detectors']['reflectance'])) for r in res]
     assert [r['index'] for r in res] == [0, 1, 2]
     assert totals[0] > totals[1] > totals[2] > 0.0     # more absorption, less reflectance
+
+
+def test_fast_voxel_walk_statistically_equal_fluence(cuda, lib):
+    """FAST mode crosses same-material voxel walls with the rest of the
+    sampled step instead of a new one (the free path is memoryless).  The
+    fluence it deposits, per depth slice, and the top tally agree with EXACT
+    mode, which follows the reference's per-wall sampling bit for bit."""
+    spec = dict(scenarios.SCENARIOS['c3_vox_cylinder'])
+    fast = scenarios.build_mc(spec, fast=True)
+    exact = scenarios.build_mc(spec)
+    exact._rnginit = 515151
+
+    def batches(mc):
+        rows, tops = [], []
+        for _ in range(10):
+            _, flu, det = mc.run(100_000, maxthreads=4096)
+            raw = np.asarray(flu.raw, dtype=np.float64)
+            rows.append(raw.reshape(raw.shape[0], -1).sum(1) / 1e5)
+            tops.append(np.asarray(det.top.raw, dtype=np.float64).sum() / 1e5)
+        return np.array(rows), np.array(tops)
+    fa, ta = batches(fast)
+    ea, tb = batches(exact)
+    z = _z(fa, ea)
+    assert np.max(np.abs(z)) < 4.5, z
+    assert np.mean(z ** 2) < 2.0, z
+    assert abs(ta.mean() - tb.mean()) / tb.mean() < 1e-2
