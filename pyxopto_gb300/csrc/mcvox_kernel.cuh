@@ -404,46 +404,6 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     dist.y = (s.dir.y != 0.0f) ? mc_div(dist.y, s.dir.y) : __int_as_float(0x7f800000);
     dist.z = (s.dir.z != 0.0f) ? mc_div(dist.z, s.dir.z) : __int_as_float(0x7f800000);
     float d = fminf(dist.x, fminf(dist.y, dist.z));
-#if MCGB_FAST_MATH
-    if (!XTRA && METHOD != MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) {
-        /* FAST mode walks across walls into voxels of the same material
-           with the rest of the sampled step instead of ending the step at
-           each wall and sampling a new one.  The free path is exponential,
-           so the rest of a step beyond a wall has the distribution of a new
-           step: the physics is the reference's, with fewer random numbers,
-           and the lanes of a warp reach their next interaction together.
-           Every wall crossed still counts as an interaction step.  EXACT
-           mode keeps the reference's order of random numbers. */
-        for (int guard = 0; d < step && guard < 1 << 20; ++guard) {
-            i3 nv = s.vi;
-            int nx = (dist.x <= dist.y) && (dist.x <= dist.z);
-            int ny = nx ? 0 : ((dist.y <= dist.x) && (dist.y <= dist.z));
-            int nz = !(nx + ny);
-            nv.x += s.dir.x < 0.0f ? -nx : nx;
-            nv.y += s.dir.y < 0.0f ? -ny : ny;
-            nv.z += s.dir.z < 0.0f ? -nz : nz;
-            if (!mv_valid(g, nv) || mv_material_at(g, x.vox, nv) != s.mat) break;
-            s.pos.x = s.pos.x + d * s.dir.x;
-            s.pos.y = s.pos.y + d * s.dir.y;
-            s.pos.z = s.pos.z + d * s.dir.z;
-            step -= d;
-            s.vi = nv;
-            ++s.steps;
-            if (x.use_rmax) {
-                /* the reference ends the packet at the first wall past rmax */
-                f3 dd{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
-                if (dot3(dd, dd) > x.rmax2) return true;
-            }
-            dist.x = g.tl[0] + (float)((s.dir.x >= 0.0f) + s.vi.x) * g.vs[0] - s.pos.x;
-            dist.y = g.tl[1] + (float)((s.dir.y >= 0.0f) + s.vi.y) * g.vs[1] - s.pos.y;
-            dist.z = g.tl[2] + (float)((s.dir.z >= 0.0f) + s.vi.z) * g.vs[2] - s.pos.z;
-            dist.x = (s.dir.x != 0.0f) ? mc_div(dist.x, s.dir.x) : __int_as_float(0x7f800000);
-            dist.y = (s.dir.y != 0.0f) ? mc_div(dist.y, s.dir.y) : __int_as_float(0x7f800000);
-            dist.z = (s.dir.z != 0.0f) ? mc_div(dist.z, s.dir.z) : __int_as_float(0x7f800000);
-            d = fminf(dist.x, fminf(dist.y, dist.z));
-        }
-    }
-#endif
     float d_ok = fminf(d, step);
     s.pos.x = s.pos.x + d_ok * s.dir.x;
     s.pos.y = s.pos.y + d_ok * s.dir.y;

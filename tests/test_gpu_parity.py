@@ -439,11 +439,10 @@ def test_run_helpers(cuda, lib):
     assert totals[0] > totals[1] > totals[2] > 0.0     # more absorption, less reflectance
 
 
-def test_fast_voxel_walk_statistically_equal_fluence(cuda, lib):
-    """FAST mode crosses same-material voxel walls with the rest of the
-    sampled step instead of a new one (the free path is memoryless).  The
-    fluence it deposits, per depth slice, and the top tally agree with EXACT
-    mode, which follows the reference's per-wall sampling bit for bit."""
+def test_fast_voxel_fluence_statistically_equal_to_exact(cuda, lib):
+    """The fluence FAST mode deposits in a voxelized medium, per depth
+    slice, and its top tally agree with EXACT mode, which is bit-identical
+    to the reference kernel."""
     spec = dict(scenarios.SCENARIOS['c3_vox_cylinder'])
     fast = scenarios.build_mc(spec, fast=True)
     exact = scenarios.build_mc(spec)
