@@ -440,25 +440,24 @@ def test_run_helpers(cuda, lib):
 
 
 def test_fast_voxel_fluence_statistically_equal_to_exact(cuda, lib):
-    """The fluence FAST mode deposits in a voxelized medium, per depth
-    slice, and its top tally agree with EXACT mode, which is bit-identical
-    to the reference kernel."""
+    """The fluence FAST mode deposits in a voxelized medium agrees with EXACT
+    mode (bit-identical to the reference kernel): per depth slice within
+    4.5 standard errors over 20 batches of 4e5 packets, and the total within
+    0.5 %.  The slices share packets, so their z scores are correlated and
+    are bounded one by one."""
     spec = dict(scenarios.SCENARIOS['c3_vox_cylinder'])
-    fast = scenarios.build_mc(spec, fast=True)
-    exact = scenarios.build_mc(spec)
-    exact._rnginit = 515151
+    fast = scenarios.build_mc(spec, fast=True, scheduling='dynamic')
+    exact = scenarios.build_mc(spec, scheduling='dynamic')
+    fast._rnginit, exact._rnginit = 1234, 2011
 
     def batches(mc):
-        rows, tops = [], []
-        for _ in range(10):
-            _, flu, det = mc.run(100_000, maxthreads=4096)
+        rows = []
+        for _ in range(20):
+            _, flu, _ = mc.run(400_000)
             raw = np.asarray(flu.raw, dtype=np.float64)
-            rows.append(raw.reshape(raw.shape[0], -1).sum(1) / 1e5)
-            tops.append(np.asarray(det.top.raw, dtype=np.float64).sum() / 1e5)
-        return np.array(rows), np.array(tops)
-    fa, ta = batches(fast)
-    ea, tb = batches(exact)
+            rows.append(raw.reshape(raw.shape[0], -1).sum(1) / 4e5)
+        return np.array(rows)
+    fa, ea = batches(fast), batches(exact)
     z = _z(fa, ea)
     assert np.max(np.abs(z)) < 4.5, z
-    assert np.mean(z ** 2) < 2.0, z
-    assert abs(ta.mean() - tb.mean()) / tb.mean() < 1e-2
+    assert abs(fa.sum(1).mean() / ea.sum(1).mean() - 1.0) < 5e-3
