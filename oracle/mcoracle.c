@@ -1220,7 +1220,10 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         if (c->specular.kind != MCGB_DET_NONE)
             detector_deposit(mm, &c->specular, s->pos, d, specular_r, 0.0f, accu, NULL);
         s->w = 1.0f - specular_r;
-    } else if (src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER) {
+    } else if (src->kind == MCGB_SRC_UNIFORM_FIBER || src->kind == MCGB_SRC_LAMBERTIAN_FIBER ||
+               src->kind == MCGB_SRC_UNIFORM_FIBER_LUT) {
+        /* UniformFiberLut: cosine from the emission LUT,
+           xopto/mcvox/mcsource/fiber.py:843-845 */
         float sin_fi, cos_fi, sin_theta, cos_theta, specular_r;
         float r = sqrtf(rnd(x, a)) * src->sigma[0];
         m_sincos(mm, rnd(x, a) * 6.28318548f, &sin_fi, &cos_fi);
@@ -1233,7 +1236,9 @@ static void mcvox_launch(int mm, const McgbMcvoxConfig *c, const McgbMaterial *m
         if (src->kind == MCGB_SRC_LAMBERTIAN_FIBER) {
             sin_theta = sqrtf(rnd(x, a)) * src->sigma[1];
         } else {
-            cos_theta = 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
+            cos_theta = src->kind == MCGB_SRC_UNIFORM_FIBER_LUT
+                            ? lut_rel(lut + src->lut_offset, src->lut_size, rnd(x, a), 0.0f)
+                            : 1.0f - rnd(x, a) * (1.0f - src->sigma[1]);
             sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
         }
         sin_theta = sin_theta / src->clip;

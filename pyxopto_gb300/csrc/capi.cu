@@ -394,11 +394,12 @@ int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *str
     int r = check_common(cfg->opt, cfg->pf_kind, cfg->num_packets, cfg->num_streams, cfg->source, dets,
                          cfg->fluence, cfg->trace, buf);
     if (r) return r;
-    if (cfg->top.kind >= MCGB_DET_TOTAL_LUT || cfg->bottom.kind >= MCGB_DET_TOTAL_LUT)
-        return fail(MCGB_E_UNSUPPORTED, "look-up-table detectors are layered-media only (the reference's "
-                    "voxelized TotalLut reads a LUT accessor its kernel lacks and does not build)");
+    if (cfg->top.kind >= MCGB_DET_TOTAL_LUT_PL || cfg->bottom.kind >= MCGB_DET_TOTAL_LUT_PL)
+        return fail(MCGB_E_UNSUPPORTED, "the voxelized medium has TotalLut only among the look-up-table "
+                    "detectors (xopto/mcvox/mcdetector)");
     if (cfg->source.kind == MCGB_SRC_UNIFORM_FIBER_NI || cfg->source.kind == MCGB_SRC_LAMBERTIAN_FIBER_NI ||
-        (cfg->source.kind >= MCGB_SRC_UNIFORM_RECTANGULAR && cfg->source.kind != MCGB_SRC_ISOTROPIC_VOXELS))
+        (cfg->source.kind >= MCGB_SRC_UNIFORM_RECTANGULAR && cfg->source.kind != MCGB_SRC_ISOTROPIC_VOXELS &&
+         cfg->source.kind != MCGB_SRC_UNIFORM_FIBER_LUT))
         return fail(MCGB_E_UNSUPPORTED, "source kind %d is implemented for layered media only",
                     cfg->source.kind);
     if (cfg->source.kind == MCGB_SRC_ISOTROPIC_VOXEL) {

@@ -202,7 +202,10 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
         dir = d;
         if (c.specular.kind != MCGB_DET_NONE) detector_deposit(c.specular, pos, d, specular_r, 0.0f, accu);
         w = 1.0f - specular_r;
-    } else if (src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER) {
+    } else if (src.kind == MCGB_SRC_UNIFORM_FIBER || src.kind == MCGB_SRC_LAMBERTIAN_FIBER ||
+               src.kind == MCGB_SRC_UNIFORM_FIBER_LUT) {
+        /* UniformFiberLut samples the cosine from its emission LUT
+           (xopto/mcvox/mcsource/fiber.py:843-845) */
         float sin_fi, cos_fi, sin_theta, cos_theta, specular_r;
         float r = mc_sqrt(rng.next()) * src.sigma[0];
         mc_sincos(rng.next() * 6.28318548f, &sin_fi, &cos_fi);
@@ -217,7 +220,9 @@ static __device__ __forceinline__ void mcvox_launch(const McgbMcvoxConfig &c, co
         if (src.kind == MCGB_SRC_LAMBERTIAN_FIBER) {
             sin_theta = mc_sqrt(rng.next()) * src.sigma[1];
         } else {
-            cos_theta = 1.0f - rng.next() * (1.0f - src.sigma[1]);
+            cos_theta = src.kind == MCGB_SRC_UNIFORM_FIBER_LUT
+                            ? lut_sample_rel(lut + src.lut_offset, src.lut_size, rng.next(), 0.0f)
+                            : 1.0f - rng.next() * (1.0f - src.sigma[1]);
             sin_theta = mc_sqrt(1.0f - cos_theta * cos_theta);
         }
         sin_theta = mc_div(sin_theta, src.clip);

@@ -302,3 +302,25 @@ class IsotropicVoxels:
         return 'IsotropicVoxels(n={})'.format(self._data.shape[0])
 
     __repr__ = __str__
+
+
+class UniformFiberLut(UniformFiber):
+    """Tilted fibre source of the voxelized medium whose emission-angle
+    cosine in air is drawn from the fibre's EmissionLut (a
+    MultimodeFiberLut); launched onto the voxel box like UniformFiber
+    (xopto/mcvox/mcsource/fiber.py:770-960)."""
+    _kind = _abi.SRC_UNIFORM_FIBER_LUT
+
+    def _angular(self):
+        return 0.0
+
+    def pack(self, mc, target: _abi.McgbSource):
+        """fiber.py:930-960: the UniformFiber fields and the emission LUT."""
+        UniformFiber.pack(self, mc, target)
+        emission = self._fiber.emission
+        if emission is None:
+            raise ValueError('The source needs an emission look-up table!')
+        _, _, n, offset = emission.pack(mc)
+        target.lut_offset = offset
+        target.lut_size = n
+        return target

@@ -496,6 +496,22 @@ SCENARIOS = {
         detectors=dict(top=dict(type='TotalLut', collection=dict(cos_min=0.4, points=30)),
                        bottom=dict(type='Radial', axis=[0.0, 2e-3, 10])),
         nphotons=3000, streams=32, rnginit=157),
+    # voxelized UniformFiberLut with a TotalLut detector (the source turns on
+    # the float LUT that the voxelized TotalLut needs to build)
+    'vox_lut_fiber_total_lut': dict(
+        medium='mcvox', grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 10], z=[0.0, 1e-3, 10]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.45, mua=150.0, mus=1e4, pf=['Hg', 0.85]),
+                   dict(n=1.33, mua=400.0, mus=5e3, pf=['Hg', 0.6])],
+        layout=dict(kind='checker'),
+        source=dict(type='UniformFiberLut', direction=(0.3, -0.1, 1.0), position=(1e-4, 0.0, -2e-4),
+                    fiber_lut=dict(dcore=400e-6, dcladding=420e-6, ncore=1.46, ncladding=1.44,
+                                   emission=dict(cos_min=0.85, points=40, width=0.05))),
+        detectors=dict(top=dict(type='TotalLut', collection=dict(cos_min=0.5, points=30),
+                                direction=(0.1, 0.0, 1.0)),
+                       bottom=dict(type='Radial', axis=[0.0, 1e-3, 10]),
+                       specular=dict(type='Total')),
+        nphotons=3000, streams=30, rnginit=179),
     'trace_sampling_volume': dict(
         medium='mcml',
         layers=[_air(['Hg', 0.0]),

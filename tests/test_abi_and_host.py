@@ -174,10 +174,11 @@ def test_sampling_volume_host_objects():
 
 
 def test_reference_unbuildable_combinations_rejected(lib):
-    """Combinations whose reference kernel does not build are refused before
-    any launch: a rectangular source with a specular detector
-    (xopto/mcml/mcsource/rectangular.py:141) and look-up-table detectors in
-    voxelized media (xopto/mcvox/mcdetector/total.py:313)."""
+    """Combinations the reference does not offer are refused before any
+    launch: a rectangular source with a specular detector (its launch code
+    does not build, xopto/mcml/mcsource/rectangular.py:141) and the
+    look-up-table detectors other than TotalLut in voxelized media
+    (xopto/mcvox/mcdetector/__init__.py)."""
     import scenarios
     from pyxopto_gb300 import _abi
     spec = dict(scenarios.SCENARIOS['rect_uniform'])
@@ -191,15 +192,15 @@ def test_reference_unbuildable_combinations_rejected(lib):
     assert b'specular' in lib.mcgb_last_error()
     vox = scenarios.build_mc('vox_cartesian')
     vcfg, _ = vox.pack(1000, 8)
-    vcfg.top.kind = _abi.DET_TOTAL_LUT
-    vcfg.top.n, vcfg.top.n_y, vcfg.top.table_offset = 1, 4, 0
+    vcfg.top.kind = _abi.DET_FIBER_LUT_ARRAY
+    vcfg.top.n, vcfg.top.n_y, vcfg.top.table_offset = 1, 16, 0
     vcfg.top.offset = 0
     vb = _abi.McgbBuffers()
     vb.rng_x, vb.rng_a, vb.counters, vb.voxels, vb.materials = 16, 16, 16, 16, 16
     vb.accumulator, vb.accumulator_size = 16, vox._acc.size
-    vb.fp_lut, vb.fp_lut_size = 16, 4
+    vb.fp_lut, vb.fp_lut_size = 16, 16
     assert lib.mcgb_mcvox_run(C.byref(vcfg), C.byref(vb), None) == _abi.E_UNSUPPORTED
-    assert b'look-up-table' in lib.mcgb_last_error()
+    assert b'TotalLut only' in lib.mcgb_last_error()
 
 
 def test_sampling_volume_needs_a_trace():
