@@ -99,7 +99,13 @@ enum {
 enum { MCGB_METHOD_ALBEDO_WEIGHT = 0,       /* MC_METHOD 0 (default)      */
        MCGB_METHOD_ALBEDO_REJECTION = 1,    /* MC_METHOD 1                */
        MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT = 2 };
-enum { MCGB_PF_HG = 0, MCGB_PF_GK = 1, MCGB_PF_LUT = 2 };
+enum { MCGB_PF_HG = 0, MCGB_PF_GK = 1, MCGB_PF_LUT = 2,
+       MCGB_PF_EXT = 3 };                   /* the analytic samplers below */
+/* McgbPf.ext_kind of an MCGB_PF_EXT phase function */
+enum { MCGB_PF_EXT_HG2 = 0,                /* xopto/mcbase/mcpf/hg2.py:102-130 */
+       MCGB_PF_EXT_MHG = 1,                /* xopto/mcbase/mcpf/mhg.py:87-109  */
+       MCGB_PF_EXT_PC = 2,                 /* xopto/mcbase/mcpf/pc.py:80-92    */
+       MCGB_PF_EXT_MPC = 3 };              /* xopto/mcbase/mcpf/mpc.py:88-106  */
 enum {
     MCGB_SRC_LINE = 0,
     MCGB_SRC_GAUSSIAN_BEAM = 1,
@@ -148,12 +154,14 @@ enum { MCGB_SCHED_STATIC = 0, MCGB_SCHED_DYNAMIC = 1 };
 /* Scattering phase function of one layer/material.
    Hg:  p[0]=g                      (xopto/mcbase/mcpf/hg.py:80-95)
    Gk:  p[0..4]=g, a, inv_a, a1, a2 (xopto/mcbase/mcpf/gk.py:102-124,153-178)
-   Lut: p[0..2]=a, b, c; lut_offset, lut_size (xopto/mcbase/mcpf/lut.py:125-155) */
+   Lut: p[0..2]=a, b, c; lut_offset, lut_size (xopto/mcbase/mcpf/lut.py:125-155)
+   Ext: ext_kind selects the sampler;
+        Hg2 p[0..2]=g1, g2, b; MHg p[0..1]=g, beta; Pc p[0]=n; MPc p[0..1]=n, beta */
 typedef struct McgbPf {
     float p[5];
     uint32_t lut_offset;
     uint32_t lut_size;
-    uint32_t reserved;
+    uint32_t ext_kind;                      /* MCGB_PF_EXT_* (Ext only)         */
 } McgbPf;                                   /* 32 bytes */
 
 /* One layer (xopto/mcml/mclayer/layer.py:40-72 ClLayer). */

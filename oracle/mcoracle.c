@@ -48,6 +48,7 @@ typedef struct { int32_t x, y, z; } i3;
 static inline float m_log(int mm, float x) { return mm ? pm_logf(x) : logf(x); }
 static inline float m_exp(int mm, float x) { return mm ? pm_expf(x) : expf(x); }
 static inline float m_pow(int mm, float x, float y) { return mm ? pm_powrf(x, y) : powf(x, y); }
+static inline float m_cbrt(int mm, float x) { return mm ? pm_cbrtf(x) : cbrtf(x); }
 static inline void m_sincos(int mm, float x, float *s, float *c) {
     if (mm) pm_sincosf(x, s, c); else sincosf(x, s, c);
 }
@@ -200,7 +201,9 @@ static void scatter_direction(int mm, v3 *dir, float cos_theta, float fi) {
 /* Returns cos(theta) and the azimuth; draws in the reference's order.
    Hg: xopto/mcbase/mcpf/hg.py:80-95
    Gk: xopto/mcbase/mcpf/gk.py:102-124
-   Lut: xopto/mcbase/mcpf/lut.py:125-155 */
+   Lut: xopto/mcbase/mcpf/lut.py:125-155
+   Hg2: xopto/mcbase/mcpf/hg2.py:102-130    MHg: xopto/mcbase/mcpf/mhg.py:87-109
+   Pc:  xopto/mcbase/mcpf/pc.py:80-92       MPc: xopto/mcbase/mcpf/mpc.py:88-106 */
 static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
                        uint64_t *x, uint32_t a, float *azimuth) {
     float cos_theta;
@@ -225,6 +228,30 @@ static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
             cos_theta = tmp / (2.0f * g);
         }
         /* mc_fclip = clamp = min(max(x, lo), hi) */
+        return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
+    } else if (kind == MCGB_PF_EXT) {
+        *azimuth = 6.28318548f * rnd(x, a);
+        if (pf->ext_kind == MCGB_PF_EXT_HG2) {
+            float g = rnd(x, a) >= pf->p[2] ? pf->p[0] : pf->p[1];
+            float k = (1.0f - g * g) / (1.0f + g * (2.0f * rnd(x, a) - 1.0f));
+            cos_theta = (1.0f + g * g - k * k) / (2.0f * g);
+            if (g == 0.0f) cos_theta = 1.0f - 2.0f * rnd(x, a);
+            return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        }
+        if (pf->ext_kind == MCGB_PF_EXT_PC) {
+            cos_theta = 2.0f * m_pow(mm, rnd(x, a), 1.0f / (pf->p[0] + 1.0f)) - 1.0f;
+        } else if (rnd(x, a) <= pf->p[1]) {
+            if (pf->ext_kind == MCGB_PF_EXT_MHG) {
+                float g = pf->p[0];
+                float k = (1.0f - g * g) / (1.0f + g * (2.0f * rnd(x, a) - 1.0f));
+                cos_theta = (1.0f + g * g - k * k) / (2.0f * g);
+                if (g == 0.0f) cos_theta = 1.0f - 2.0f * rnd(x, a);
+            } else {
+                cos_theta = 2.0f * m_pow(mm, rnd(x, a), 1.0f / (pf->p[0] + 1.0f)) - 1.0f;
+            }
+        } else {
+            cos_theta = m_cbrt(mm, 2.0f * rnd(x, a) - 1.0f);
+        }
         return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
     } else {
         float la = pf->p[0], lb = pf->p[1], lc = pf->p[2];
@@ -1579,6 +1606,7 @@ void mco_rng_dump(uint64_t x, uint32_t a, uint64_t n, float *out) {
 float mco_pm_log(float x) { return pm_logf(x); }
 float mco_pm_exp(float x) { return pm_expf(x); }
 float mco_pm_pow(float x, float y) { return pm_powrf(x, y); }
+float mco_pm_cbrt(float x) { return pm_cbrtf(x); }
 void mco_pm_sincos(float x, float *s, float *c) { pm_sincosf(x, s, c); }
 
 /* ---------------------------------------------------------------------------

@@ -42,6 +42,8 @@ def load():
         lib.mco_pm_exp.argtypes = [C.c_float]
         lib.mco_pm_pow.restype = C.c_float
         lib.mco_pm_pow.argtypes = [C.c_float, C.c_float]
+        lib.mco_pm_cbrt.restype = C.c_float
+        lib.mco_pm_cbrt.argtypes = [C.c_float]
         lib.mco_pm_sincos.argtypes = [C.c_float, vp, vp]
         lib.mco_sizeof.argtypes = [C.c_int]
         lib.mco_sampling_volume.restype = C.c_uint64

@@ -18,7 +18,8 @@ CNT_PACKETS, CNT_STEPS, CNT_STATUS, CNT_THREADS, CNT_ABORT, CNT_QUEUE, NUM_COUNT
 SCHED_STATIC, SCHED_DYNAMIC = 0, 1
 
 METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT = 0, 1, 2
-PF_HG, PF_GK, PF_LUT = 0, 1, 2
+PF_HG, PF_GK, PF_LUT, PF_EXT = 0, 1, 2, 3
+PF_EXT_HG2, PF_EXT_MHG, PF_EXT_PC, PF_EXT_MPC = 0, 1, 2, 3
 SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI, SRC_LAMBERTIAN_FIBER_NI = 0, 1, 2, 3
 SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT = 4, 5, 6, 7
 SRC_ISOTROPIC_VOXEL = 8
@@ -43,7 +44,7 @@ u64 = C.c_uint64
 
 
 class McgbPf(C.Structure):
-    _fields_ = [('p', f32 * 5), ('lut_offset', u32), ('lut_size', u32), ('reserved', u32)]
+    _fields_ = [('p', f32 * 5), ('lut_offset', u32), ('lut_size', u32), ('ext_kind', u32)]
 
 
 class McgbLayer(C.Structure):

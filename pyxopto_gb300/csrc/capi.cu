@@ -48,6 +48,8 @@ bool range_ok(uint64_t offset, uint64_t count, uint64_t size) {
 }
 
 int check_pf(int kind, const McgbPf &pf, const McgbBuffers *b, const char *who, unsigned idx) {
+    if (kind == MCGB_PF_EXT && pf.ext_kind > MCGB_PF_EXT_MPC)
+        return fail(MCGB_E_INVALID, "%s %u: unknown analytic phase function %u", who, idx, pf.ext_kind);
     if (kind == MCGB_PF_LUT) {
         if (!b->fp_lut) return fail(MCGB_E_INVALID, "%s %u: Lut phase function without a LUT buffer", who, idx);
         if (pf.lut_size < 2) return fail(MCGB_E_INVALID, "%s %u: Lut size %u < 2", who, idx, pf.lut_size);
@@ -103,7 +105,7 @@ int check_common(const McgbRunOptions &o, int pf_kind, uint64_t num_packets, uin
     if (o.method < 0 || o.method > 2) return fail(MCGB_E_INVALID, "unknown method %d", o.method);
     if (o.math != MCGB_MATH_EXACT && o.math != MCGB_MATH_FAST)
         return fail(MCGB_E_INVALID, "unknown math mode %d", o.math);
-    if (pf_kind < 0 || pf_kind > 2) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
+    if (pf_kind < 0 || pf_kind > MCGB_PF_EXT) return fail(MCGB_E_INVALID, "unknown phase function %d", pf_kind);
     if (src.kind < MCGB_SRC_LINE || src.kind > MCGB_SRC_ISOTROPIC_VOXELS)
         return fail(MCGB_E_INVALID, "unknown source kind %d", src.kind);
     if (src.kind >= MCGB_SRC_UNIFORM_FIBER_LUT_NI) {

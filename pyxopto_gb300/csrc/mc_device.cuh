@@ -34,6 +34,7 @@
 MCGB_DEV float mc_log(float x) { return __logf(x); }
 MCGB_DEV float mc_exp(float x) { return __expf(x); }
 MCGB_DEV float mc_pow(float x, float y) { return __powf(x, y); }
+MCGB_DEV float mc_cbrt(float x) { return cbrtf(x); }
 MCGB_DEV void mc_sincos(float x, float *s, float *c) { __sincosf(x, s, c); }
 MCGB_DEV float mc_div(float a, float b) { return __fdividef(a, b); }
 MCGB_DEV float mc_sqrt(float x) { return sqrtf(x); }
@@ -42,6 +43,7 @@ MCGB_DEV float mc_rcp_length(float x2) { return rsqrtf(x2); }
 MCGB_DEV float mc_log(float x) { return pm_logf(x); }
 MCGB_DEV float mc_exp(float x) { return pm_expf(x); }
 MCGB_DEV float mc_pow(float x, float y) { return pm_powrf(x, y); }
+MCGB_DEV float mc_cbrt(float x) { return pm_cbrtf(x); }
 MCGB_DEV void mc_sincos(float x, float *s, float *c) { pm_sincosf(x, s, c); }
 MCGB_DEV float mc_div(float a, float b) { return a / b; }
 MCGB_DEV float mc_sqrt(float x) { return sqrtf(x); }
@@ -217,6 +219,9 @@ MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
         float g = pf.p[0];
         pf0 = make_float4(g, pf.p[1], -pf.p[2], pf.p[3]);
         pf1 = make_float4(pf.p[4], 1.0f + g * g, 2.0f * g, mc_div(1.0f - g, 1.0f + g));
+    } else if (kind == MCGB_PF_EXT) {
+        pf0 = make_float4(pf.p[0], pf.p[1], pf.p[2], pf.p[3]);
+        pf1 = make_float4(pf.p[4], 0.0f, 0.0f, __int_as_float((int)pf.ext_kind));
     } else {
         uint32_t n1 = pf.lut_size - 1u;
         pf0 = make_float4(pf.p[0], pf.p[1], pf.p[2], (float)n1);
@@ -228,7 +233,9 @@ MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
    as in the reference.
    Hg:  xopto/mcbase/mcpf/hg.py:80-95
    Gk:  xopto/mcbase/mcpf/gk.py:102-124
-   Lut: xopto/mcbase/mcpf/lut.py:125-155 */
+   Lut: xopto/mcbase/mcpf/lut.py:125-155
+   Ext: Hg2 xopto/mcbase/mcpf/hg2.py:102-130, MHg mhg.py:87-109,
+        Pc pc.py:80-92, MPc mpc.py:88-106 */
 template <int PF>
 MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut, Rng &rng,
                          float *azimuth) {
@@ -249,6 +256,33 @@ MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut,
             float tmp = pf0.w * rng.next() + pf1.x;
             tmp = pf1.y - mc_pow(tmp, pf0.z);
             cos_theta = mc_div(tmp, pf1.z);
+        }
+        return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
+    } else if (PF == MCGB_PF_EXT) {
+        int ext = __float_as_int(pf1.w);
+        float cos_theta;
+        if (ext == MCGB_PF_EXT_HG2) {
+            /* component 1 when u >= b, else component 2 */
+            float g = rng.next() >= pf0.z ? pf0.x : pf0.y;
+            float k = mc_div(1.0f - g * g, 1.0f + g * (2.0f * rng.next() - 1.0f));
+            cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
+            if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
+            return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        }
+        if (ext == MCGB_PF_EXT_PC) {
+            cos_theta = 2.0f * mc_pow(rng.next(), mc_div(1.0f, pf0.x + 1.0f)) - 1.0f;
+        } else if (rng.next() <= pf0.y) {
+            if (ext == MCGB_PF_EXT_MHG) {
+                float g = pf0.x;
+                float k = mc_div(1.0f - g * g, 1.0f + g * (2.0f * rng.next() - 1.0f));
+                cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
+                if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
+            } else {
+                cos_theta = 2.0f * mc_pow(rng.next(), mc_div(1.0f, pf0.x + 1.0f)) - 1.0f;
+            }
+        } else {
+            /* the (3/2) cos^2 component: cos = cbrt(2u - 1) */
+            cos_theta = mc_cbrt(2.0f * rng.next() - 1.0f);
         }
         return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
     } else {

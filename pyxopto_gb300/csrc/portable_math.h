@@ -153,4 +153,14 @@ PM_FN float pm_powrf(float x, float y) {
     return pm_expf(y * pm_logf(x));
 }
 
+/* cbrt: exp(log(|x|)/3) refined by one Newton step y -= (y^3 - |x|)/(3y^2),
+   with the sign of x; 0, inf and NaN are returned unchanged. */
+PM_FN float pm_cbrtf(float x) {
+    if (x == 0.0f || x != x || x - x != 0.0f) return x;
+    float s = x < 0.0f ? -x : x;
+    float y = pm_expf(pm_logf(s) * 0.333333343f);
+    y = y - (y * y * y - s) / (3.0f * y * y);
+    return x < 0.0f ? -y : y;
+}
+
 #endif /* XOPTO_GB300_PORTABLE_MATH_H */

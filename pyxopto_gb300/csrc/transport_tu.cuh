@@ -31,7 +31,8 @@
 namespace MCGB_NS {
 
 #define MCGB_METHODS(V, K, PF) {V(K, PF, 0), V(K, PF, 1), V(K, PF, 2)}
-#define MCGB_TABLE(V, K) {MCGB_METHODS(V, K, 0), MCGB_METHODS(V, K, 1), MCGB_METHODS(V, K, 2)}
+#define MCGB_TABLE(V, K) {MCGB_METHODS(V, K, 0), MCGB_METHODS(V, K, 1), MCGB_METHODS(V, K, 2), \
+                          MCGB_METHODS(V, K, 3)}
 
 /* Static scheduling kernels: phase function x method x fluence; they carry
    every optional feature and every source. */
@@ -40,10 +41,10 @@ const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence);
 #if MCGB_PART == 0
 
 #define MCGB_VS(K, PF, M) {(const void *)K<PF, M, false>, (const void *)K<PF, M, true>}
-static const void *const kStatic[3][3][2] = MCGB_TABLE(MCGB_VS, MCGB_STATIC_KERNEL);
+static const void *const kStatic[4][3][2] = MCGB_TABLE(MCGB_VS, MCGB_STATIC_KERNEL);
 
 const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence) {
-    if (pf < 0 || pf > 2 || method < 0 || method > 2) return nullptr;
+    if (pf < 0 || pf > 3 || method < 0 || method > 2) return nullptr;
     return kStatic[pf][method][fluence ? 1 : 0];
 }
 
@@ -56,10 +57,10 @@ const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence) {
 #define MCGB_VX(K, PF, M, F) {{(const void *)K<PF, M, F, false, false>, (const void *)K<PF, M, F, false, true>}, \
                               {(const void *)K<PF, M, F, true, false>, (const void *)K<PF, M, F, true, true>}}
 #define MCGB_VD(K, PF, M) {MCGB_VX(K, PF, M, false), MCGB_VX(K, PF, M, true)}
-static const void *const kDynamic[3][3][2][2][2] = MCGB_TABLE(MCGB_VD, MCGB_DYNAMIC_KERNEL);
+static const void *const kDynamic[4][3][2][2][2] = MCGB_TABLE(MCGB_VD, MCGB_DYNAMIC_KERNEL);
 
 static const void *select(int sched, int pf, int method, bool fluence, bool xtra, bool simple) {
-    if (pf < 0 || pf > 2 || method < 0 || method > 2 || sched < 0 || sched > 1) return nullptr;
+    if (pf < 0 || pf > 3 || method < 0 || method > 2 || sched < 0 || sched > 1) return nullptr;
     if (sched == MCGB_SCHED_STATIC) return MCGB_SELECT_STATIC(pf, method, fluence);
     return kDynamic[pf][method][fluence ? 1 : 0][xtra ? 1 : 0][simple ? 1 : 0];
 }

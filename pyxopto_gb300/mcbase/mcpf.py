@@ -1,6 +1,7 @@
-"""Scattering phase functions: Henyey-Greenstein, Gegenbauer kernel and
-lookup table, with the reference's names and parameters
-(xopto/mcbase/mcpf/hg.py, gk.py, lut.py).
+"""Scattering phase functions: Henyey-Greenstein, Gegenbauer kernel, lookup
+table and the analytic mixtures Hg2, MHg, Pc and MPc, with the reference's
+names and parameters (xopto/mcbase/mcpf/hg.py, gk.py, lut.py, hg2.py, mhg.py,
+pc.py, mpc.py).
 
 Each object packs itself into the ``McgbPf`` struct that the GB300 kernels
 read from their shared-memory layer/material table.
@@ -151,6 +152,96 @@ class Lut(PfBase):
         return 'Lut(params=({}, {}, {}), size={})'.format(*self._params, self._lut.size)
 
 
+def _clip_g(g):
+    return min(max(float(g), -1.0), 1.0)
+
+
+class _Ext(PfBase):
+    """Analytic samplers that share the MCGB_PF_EXT kernels; ``ext_kind``
+    selects the sampler and ``_params`` fills McgbPf.p in order."""
+    kind = _abi.PF_EXT
+    ext_kind = None
+    _names = ()
+
+    def _params(self):
+        return [getattr(self, name) for name in self._names]
+
+    def pack(self, mc, target):
+        for i, value in enumerate(self._params()):
+            target.p[i] = value
+        target.ext_kind = self.ext_kind
+        return target
+
+    def todict(self):
+        d = {name: getattr(self, name) for name in self._names}
+        d['type'] = type(self).__name__
+        return d
+
+    def __str__(self):
+        return '{}({})'.format(type(self).__name__, ', '.join(
+            '{}={}'.format(name, getattr(self, name)) for name in self._names))
+
+
+class Hg2(_Ext):
+    """Mixture of two Henyey-Greenstein phase functions,
+    (1 - b)*Hg(g1) + b*Hg(g2) (xopto/mcbase/mcpf/hg2.py:25-231)."""
+    ext_kind = _abi.PF_EXT_HG2
+    _names = ('g1', 'g2', 'b')
+
+    def __init__(self, g1: float, g2: float, b: float):
+        self.g1, self.g2, self.b = g1, g2, b
+
+    g1 = property(lambda self: self._g1, lambda self, g: setattr(self, '_g1', _clip_g(g)),
+                  None, 'Anisotropy factor of the first component.')
+    g2 = property(lambda self: self._g2, lambda self, g: setattr(self, '_g2', _clip_g(g)),
+                  None, 'Anisotropy factor of the second component.')
+    b = property(lambda self: self._b, lambda self, b: setattr(self, '_b', float(b)),
+                 None, 'Contribution of the second component.')
+
+
+class MHg(_Ext):
+    """Modified Henyey-Greenstein phase function,
+    b*Hg(g) + (1 - b)*(3/2)cos^2 (xopto/mcbase/mcpf/mhg.py:25-195)."""
+    ext_kind = _abi.PF_EXT_MHG
+    _names = ('g', 'b')
+
+    def __init__(self, g: float, b: float):
+        self.g, self.b = g, b
+
+    g = property(lambda self: self._g, lambda self, g: setattr(self, '_g', _clip_g(g)),
+                 None, 'Anisotropy factor of the Henyey-Greenstein component.')
+    b = property(lambda self: self._b, lambda self, b: setattr(self, '_b', float(b)),
+                 None, 'Contribution of the Henyey-Greenstein component.')
+
+
+class Pc(_Ext):
+    """Power of cosines phase function, cos(theta/2)^(2n)
+    (xopto/mcbase/mcpf/pc.py:25-186)."""
+    ext_kind = _abi.PF_EXT_PC
+    _names = ('n',)
+
+    def __init__(self, n: float):
+        self.n = n
+
+    n = property(lambda self: self._n, lambda self, n: setattr(self, '_n', float(n)),
+                 None, 'Power of the cosine.')
+
+
+class MPc(_Ext):
+    """Modified power of cosines phase function,
+    b*Pc(n) + (1 - b)*(3/2)cos^2 (xopto/mcbase/mcpf/mpc.py:25-196)."""
+    ext_kind = _abi.PF_EXT_MPC
+    _names = ('n', 'b')
+
+    def __init__(self, n: float, b: float):
+        self.n, self.b = n, b
+
+    n = property(lambda self: self._n, lambda self, n: setattr(self, '_n', float(n)),
+                 None, 'Power of the cosine.')
+    b = property(lambda self: self._b, lambda self, b: setattr(self, '_b', float(b)),
+                 None, 'Contribution of the power of cosines component.')
+
+
 def pf_fromdict(data: dict) -> PfBase:
-    kinds = {'Hg': Hg, 'Gk': Gk, 'Lut': Lut}
+    kinds = {'Hg': Hg, 'Gk': Gk, 'Lut': Lut, 'Hg2': Hg2, 'MHg': MHg, 'Pc': Pc, 'MPc': MPc}
     return kinds[data['type']].fromdict(data)

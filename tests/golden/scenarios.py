@@ -52,6 +52,34 @@ SCENARIOS = {
         fluence=dict(x=[-5e-3, 5e-3, 20], y=[-5e-3, 5e-3, 20], z=[0.0, 10e-3, 20],
                      mode='deposition'),
         nphotons=1500, streams=32, rnginit=7),
+    # the analytic mixture samplers (xopto/mcbase/mcpf/hg2.py, mhg.py, pc.py,
+    # mpc.py); a zero anisotropy component exercises the isotropic branch
+    'pf_hg2_radial': dict(
+        medium='mcml',
+        layers=[_air(['Hg2', 0.0, 0.0, 0.0]),
+                dict(d=1e-3, n=1.4, mua=200.0, mus=1.5e4, pf=['Hg2', 0.92, -0.3, 0.25]),
+                dict(d=INF, n=1.4, mua=50.0, mus=8e3, pf=['Hg2', 0.8, 0.0, 0.5]),
+                _air(['Hg2', 0.0, 0.0, 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 4e-3, 40]), specular=dict(type='Total')),
+        nphotons=3000, streams=40, rnginit=21),
+    'pf_mhg_fluence': dict(
+        medium='mcml',
+        layers=[_air(['MHg', 0.0, 1.0]),
+                dict(d=2e-3, n=1.37, mua=100.0, mus=1e4, pf=['MHg', 0.85, 0.9]),
+                dict(d=4e-3, n=1.45, mua=30.0, mus=1.2e4, pf=['MHg', 0.0, 0.6]),
+                _air(['MHg', 0.0, 1.0])],
+        source=dict(type='GaussianBeam', sigma=2e-4, clip=5.0), method=2,
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Total')),
+        fluence=dict(x=[-2e-3, 2e-3, 8], y=[-2e-3, 2e-3, 8], z=[0.0, 6e-3, 12], mode='deposition'),
+        nphotons=2000, streams=32, rnginit=22),
+    'pf_pc_rejection': dict(
+        medium='mcml',
+        layers=[_air(['Pc', 1.0]), dict(d=3e-3, n=1.33, mua=150.0, mus=1e4, pf=['Pc', 12.0]),
+                _air(['Pc', 1.0])],
+        source=dict(type='Line'), method=1,
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), bottom=dict(type='Total')),
+        nphotons=3000, streams=40, rnginit=23),
     'gk_alpha_1p2_rejection': dict(
         medium='mcml',
         layers=[_air(['Gk', 0.0, 1.2]), dict(d=2e-3, n=1.4, mua=300.0, mus=6e3, pf=['Gk', 0.7, 1.2]),
@@ -102,6 +130,19 @@ SCENARIOS = {
         fluence=dict(x=[-1.2e-3, 1.2e-3, 24], y=[-1.2e-3, 1.2e-3, 24], z=[0.0, 2.4e-3, 24],
                      mode='deposition'),
         nphotons=1500, streams=32, rnginit=9),
+    'pf_mpc_vox_cylinder': dict(
+        medium='mcvox',
+        grid=dict(x=[-1.2e-3, 1.2e-3, 16], y=[-1.2e-3, 1.2e-3, 16], z=[0.0, 2.4e-3, 16]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['MPc', 1.0, 1.0]),
+                   dict(n=1.40, mua=20.0, mus=1.5e4, pf=['MPc', 20.0, 0.85]),
+                   dict(n=1.40, mua=150.0, mus=2e4, pf=['MPc', 8.0, 0.5]),
+                   dict(n=1.33, mua=2000.0, mus=1.5e4, pf=['MPc', 30.0, 0.95])],
+        layout=dict(kind='skin_vessel', epidermis=1e-4, vessel_depth=1.0e-3, vessel_radius=4e-4),
+        source=dict(type='GaussianBeam', sigma=3e-4, clip=5.0),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1.2e-3, 12]), bottom=dict(type='Total')),
+        fluence=dict(x=[-1.2e-3, 1.2e-3, 16], y=[-1.2e-3, 1.2e-3, 16], z=[0.0, 2.4e-3, 16],
+                     mode='deposition'),
+        nphotons=1500, streams=32, rnginit=24),
     'vox_line_gk_oblique': dict(
         medium='mcvox',
         grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
@@ -607,11 +648,29 @@ def voxel_layout(grid, layout):
     return m
 
 
+_WRAPPED = {}
+
+
+def _ext_pf_class(pkg, name):
+    """The phase-function class; the reference's Pc.cl_type lacks
+    @staticmethod (xopto/mcbase/mcpf/pc.py:28), so a reference simulator with
+    Pc does not build.  For fixtures that class is wrapped once with the
+    method made static; its sampler code is used unchanged."""
+    cls = getattr(pkg.mcpf, name)
+    if 'cl_type' in cls.__dict__ and not isinstance(cls.__dict__['cl_type'], staticmethod):
+        if cls not in _WRAPPED:
+            _WRAPPED[cls] = type(name, (cls,), {'cl_type': staticmethod(cls.__dict__['cl_type'])})
+        cls = _WRAPPED[cls]
+    return cls
+
+
 def _pf(pkg, spec):
     if spec[0] == 'Hg':
         return pkg.mcpf.Hg(spec[1])
     if spec[0] == 'Gk':
         return pkg.mcpf.Gk(spec[1], spec[2])
+    if spec[0] in ('Hg2', 'MHg', 'Pc', 'MPc'):
+        return _ext_pf_class(pkg, spec[0])(*spec[1:])
     params, table = lut_table()
     return pkg.mcpf.Lut(params, table)
 

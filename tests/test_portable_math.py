@@ -1,4 +1,4 @@
-"""Accuracy of the portable single-precision log/exp/sincos/powr that the
+"""Accuracy of the portable single-precision log/exp/sincos/powr/cbrt that the
 EXACT math mode evaluates identically on the GPU and the CPU."""
 import numpy as np
 
@@ -59,3 +59,35 @@ def test_powr(oracle):
     want = np.power(x.astype(np.float64), y.astype(np.float64))
     assert np.max(np.abs(got - want) / want) < 2e-6
     assert lib.mco_pm_pow(0.0, 2.0) == 0.0 and lib.mco_pm_pow(1.0, 7.0) == 1.0
+
+
+def test_cbrt(oracle):
+    """cbrt(2u - 1) of the MHg/MPc samplers: within 2 ulp on [-1, 1] and
+    beyond, odd, and exact at 0, +-1 and +-8."""
+    lib = oracle.load()
+    rng = np.random.default_rng(2)
+    x = np.concatenate([rng.uniform(-1.0, 1.0, 20000),
+                        np.float32(2.0) ** rng.uniform(-120, 120, 4000)]).astype(np.float32)
+    got = np.array([lib.mco_pm_cbrt(float(v)) for v in x])
+    want = np.cbrt(x.astype(np.float64))
+    assert np.max(ulp_err(got, want)) <= 2.0
+    assert all(lib.mco_pm_cbrt(float(-v)) == -lib.mco_pm_cbrt(float(v)) for v in x[:200])
+    for v in (0.0, 1.0, -1.0, 8.0, -8.0):
+        assert lib.mco_pm_cbrt(v) == np.cbrt(v)
+
+
+def test_analytic_pf_pack():
+    """Hg2/MHg/Pc/MPc pack their parameters and sampler kind into McgbPf
+    and round-trip through todict."""
+    from pyxopto_gb300 import _abi
+    from pyxopto_gb300.mcml import mcpf
+    cases = [(mcpf.Hg2(0.9, -1.5, 0.25), _abi.PF_EXT_HG2, [0.9, -1.0, 0.25]),
+             (mcpf.MHg(0.8, 0.6), _abi.PF_EXT_MHG, [0.8, 0.6]),
+             (mcpf.Pc(12.0), _abi.PF_EXT_PC, [12.0]),
+             (mcpf.MPc(20.0, 0.85), _abi.PF_EXT_MPC, [20.0, 0.85])]
+    for pf, ext, params in cases:
+        t = pf.pack(None, _abi.McgbPf())
+        assert pf.kind == _abi.PF_EXT and t.ext_kind == ext
+        np.testing.assert_allclose(list(t.p)[:len(params)], params, rtol=1e-7)
+        again = mcpf.pf_fromdict(pf.todict())
+        assert type(again) is type(pf) and again.todict() == pf.todict()
