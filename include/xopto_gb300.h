@@ -105,7 +105,8 @@ enum { MCGB_PF_HG = 0, MCGB_PF_GK = 1, MCGB_PF_LUT = 2,
 enum { MCGB_PF_EXT_HG2 = 0,                /* xopto/mcbase/mcpf/hg2.py:102-130 */
        MCGB_PF_EXT_MHG = 1,                /* xopto/mcbase/mcpf/mhg.py:87-109  */
        MCGB_PF_EXT_PC = 2,                 /* xopto/mcbase/mcpf/pc.py:80-92    */
-       MCGB_PF_EXT_MPC = 3 };              /* xopto/mcbase/mcpf/mpc.py:88-106  */
+       MCGB_PF_EXT_MPC = 3,                /* xopto/mcbase/mcpf/mpc.py:88-106  */
+       MCGB_PF_EXT_MGK = 4 };              /* xopto/mcbase/mcpf/mgk.py:110-140 */
 enum {
     MCGB_SRC_LINE = 0,
     MCGB_SRC_GAUSSIAN_BEAM = 1,
@@ -156,7 +157,8 @@ enum { MCGB_SCHED_STATIC = 0, MCGB_SCHED_DYNAMIC = 1 };
    Gk:  p[0..4]=g, a, inv_a, a1, a2 (xopto/mcbase/mcpf/gk.py:102-124,153-178)
    Lut: p[0..2]=a, b, c; lut_offset, lut_size (xopto/mcbase/mcpf/lut.py:125-155)
    Ext: ext_kind selects the sampler;
-        Hg2 p[0..2]=g1, g2, b; MHg p[0..1]=g, beta; Pc p[0]=n; MPc p[0..1]=n, beta */
+        Hg2 p[0..2]=g1, g2, b; MHg p[0..1]=g, beta; Pc p[0]=n; MPc p[0..1]=n, beta;
+        MGk p[0..4]=g, beta, inv_a, a1, a2 (a == 0 is inv_a == 0 with g != 0) */
 typedef struct McgbPf {
     float p[5];
     uint32_t lut_offset;

@@ -203,7 +203,8 @@ static void scatter_direction(int mm, v3 *dir, float cos_theta, float fi) {
    Gk: xopto/mcbase/mcpf/gk.py:102-124
    Lut: xopto/mcbase/mcpf/lut.py:125-155
    Hg2: xopto/mcbase/mcpf/hg2.py:102-130    MHg: xopto/mcbase/mcpf/mhg.py:87-109
-   Pc:  xopto/mcbase/mcpf/pc.py:80-92       MPc: xopto/mcbase/mcpf/mpc.py:88-106 */
+   Pc:  xopto/mcbase/mcpf/pc.py:80-92       MPc: xopto/mcbase/mcpf/mpc.py:88-106
+   MGk: xopto/mcbase/mcpf/mgk.py:110-140 */
 static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
                        uint64_t *x, uint32_t a, float *azimuth) {
     float cos_theta;
@@ -237,6 +238,23 @@ static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
             cos_theta = (1.0f + g * g - k * k) / (2.0f * g);
             if (g == 0.0f) cos_theta = 1.0f - 2.0f * rnd(x, a);
             return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        }
+        if (pf->ext_kind == MCGB_PF_EXT_MGK) {
+            float g = pf->p[0], inv_a = pf->p[2], a1 = pf->p[3], a2 = pf->p[4];
+            if (rnd(x, a) <= pf->p[1]) {
+                if (g == 0.0f) {
+                    cos_theta = 1.0f - 2.0f * rnd(x, a);
+                } else if (inv_a == 0.0f) {
+                    cos_theta = a1 + m_pow(mm, (1.0f - g) / (1.0f + g), 2.0f * rnd(x, a)) * a2;
+                } else {
+                    float tmp = a1 * rnd(x, a) + a2;
+                    tmp = 1.0f + g * g - m_pow(mm, tmp, -inv_a);
+                    cos_theta = tmp / (2.0f * g);
+                }
+            } else {
+                cos_theta = m_cbrt(mm, 2.0f * rnd(x, a) - 1.0f);
+            }
+            return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
         }
         if (pf->ext_kind == MCGB_PF_EXT_PC) {
             cos_theta = 2.0f * m_pow(mm, rnd(x, a), 1.0f / (pf->p[0] + 1.0f)) - 1.0f;

@@ -48,7 +48,7 @@ bool range_ok(uint64_t offset, uint64_t count, uint64_t size) {
 }
 
 int check_pf(int kind, const McgbPf &pf, const McgbBuffers *b, const char *who, unsigned idx) {
-    if (kind == MCGB_PF_EXT && pf.ext_kind > MCGB_PF_EXT_MPC)
+    if (kind == MCGB_PF_EXT && pf.ext_kind > MCGB_PF_EXT_MGK)
         return fail(MCGB_E_INVALID, "%s %u: unknown analytic phase function %u", who, idx, pf.ext_kind);
     if (kind == MCGB_PF_LUT) {
         if (!b->fp_lut) return fail(MCGB_E_INVALID, "%s %u: Lut phase function without a LUT buffer", who, idx);

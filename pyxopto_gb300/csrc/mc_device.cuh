@@ -235,7 +235,7 @@ MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
    Gk:  xopto/mcbase/mcpf/gk.py:102-124
    Lut: xopto/mcbase/mcpf/lut.py:125-155
    Ext: Hg2 xopto/mcbase/mcpf/hg2.py:102-130, MHg mhg.py:87-109,
-        Pc pc.py:80-92, MPc mpc.py:88-106 */
+        Pc pc.py:80-92, MPc mpc.py:88-106, MGk mgk.py:110-140 */
 template <int PF>
 MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut, Rng &rng,
                          float *azimuth) {
@@ -268,6 +268,23 @@ MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut,
             cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
             if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
             return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        }
+        if (ext == MCGB_PF_EXT_MGK) {
+            if (rng.next() <= pf0.y) {
+                float g = pf0.x;
+                if (g == 0.0f) {
+                    cos_theta = 1.0f - 2.0f * rng.next();
+                } else if (pf0.z == 0.0f) {
+                    cos_theta = pf0.w + mc_pow(mc_div(1.0f - g, 1.0f + g), 2.0f * rng.next()) * pf1.x;
+                } else {
+                    float tmp = pf0.w * rng.next() + pf1.x;
+                    tmp = 1.0f + g * g - mc_pow(tmp, -pf0.z);
+                    cos_theta = mc_div(tmp, 2.0f * g);
+                }
+            } else {
+                cos_theta = mc_cbrt(2.0f * rng.next() - 1.0f);
+            }
+            return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
         }
         if (ext == MCGB_PF_EXT_PC) {
             cos_theta = 2.0f * mc_pow(rng.next(), mc_div(1.0f, pf0.x + 1.0f)) - 1.0f;

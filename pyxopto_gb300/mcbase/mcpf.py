@@ -242,6 +242,36 @@ class MPc(_Ext):
                  None, 'Contribution of the power of cosines component.')
 
 
+class MGk(Gk):
+    """Modified Gegenbauer kernel phase function,
+    b*Gk(g, a) + (1 - b)*(3/2)cos^2 (xopto/mcbase/mcpf/mgk.py:31-270).  The
+    constants inv_a, a1, a2 are the Gk ones (mgk.py:195-215).  The sampler
+    tells a == 0 by inv_a == 0, which is the same test for |a| >= 1.2e-38."""
+    kind = _abi.PF_EXT
+    ext_kind = _abi.PF_EXT_MGK
+
+    def __init__(self, g: float, a: float, b: float):
+        self._b = float(b)
+        super().__init__(g, a)
+
+    b = property(lambda self: self._b, lambda self, b: setattr(self, '_b', float(b)),
+                 None, 'Contribution of the Gegenbauer kernel component.')
+
+    def pack(self, mc, target):
+        inv_a, a1, a2 = self._precalculated
+        for i, value in enumerate((self.g, self._b, inv_a, a1, a2)):
+            target.p[i] = value
+        target.ext_kind = self.ext_kind
+        return target
+
+    def todict(self):
+        return {'g': self.g, 'a': self.a, 'b': self._b, 'type': 'MGk'}
+
+    def __str__(self):
+        return 'MGk(g={}, a={}, b={})'.format(self.g, self.a, self._b)
+
+
 def pf_fromdict(data: dict) -> PfBase:
-    kinds = {'Hg': Hg, 'Gk': Gk, 'Lut': Lut, 'Hg2': Hg2, 'MHg': MHg, 'Pc': Pc, 'MPc': MPc}
+    kinds = {'Hg': Hg, 'Gk': Gk, 'Lut': Lut, 'Hg2': Hg2, 'MHg': MHg, 'Pc': Pc, 'MPc': MPc,
+             'MGk': MGk}
     return kinds[data['type']].fromdict(data)

@@ -73,6 +73,16 @@ SCENARIOS = {
         detectors=dict(top=dict(type='Total'), bottom=dict(type='Total')),
         fluence=dict(x=[-2e-3, 2e-3, 8], y=[-2e-3, 2e-3, 8], z=[0.0, 6e-3, 12], mode='deposition'),
         nphotons=2000, streams=32, rnginit=22),
+    'pf_mgk_radial': dict(
+        medium='mcml',
+        layers=[_air(['MGk', 0.0, 0.5, 1.0]),
+                dict(d=1e-3, n=1.4, mua=150.0, mus=1.2e4, pf=['MGk', 0.9, 0.5, 0.8]),
+                dict(d=2e-3, n=1.4, mua=60.0, mus=1e4, pf=['MGk', 0.8, 0.0, 0.9]),
+                dict(d=INF, n=1.4, mua=40.0, mus=8e3, pf=['MGk', 0.0, 0.7, 0.5]),
+                _air(['MGk', 0.0, 0.5, 1.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 4e-3, 40]), specular=dict(type='Total')),
+        nphotons=3000, streams=40, rnginit=25),
     'pf_pc_rejection': dict(
         medium='mcml',
         layers=[_air(['Pc', 1.0]), dict(d=3e-3, n=1.33, mua=150.0, mus=1e4, pf=['Pc', 12.0]),
@@ -669,7 +679,7 @@ def _pf(pkg, spec):
         return pkg.mcpf.Hg(spec[1])
     if spec[0] == 'Gk':
         return pkg.mcpf.Gk(spec[1], spec[2])
-    if spec[0] in ('Hg2', 'MHg', 'Pc', 'MPc'):
+    if spec[0] in ('Hg2', 'MHg', 'Pc', 'MPc', 'MGk'):
         return _ext_pf_class(pkg, spec[0])(*spec[1:])
     params, table = lut_table()
     return pkg.mcpf.Lut(params, table)

@@ -84,7 +84,9 @@ def test_analytic_pf_pack():
     cases = [(mcpf.Hg2(0.9, -1.5, 0.25), _abi.PF_EXT_HG2, [0.9, -1.0, 0.25]),
              (mcpf.MHg(0.8, 0.6), _abi.PF_EXT_MHG, [0.8, 0.6]),
              (mcpf.Pc(12.0), _abi.PF_EXT_PC, [12.0]),
-             (mcpf.MPc(20.0, 0.85), _abi.PF_EXT_MPC, [20.0, 0.85])]
+             (mcpf.MPc(20.0, 0.85), _abi.PF_EXT_MPC, [20.0, 0.85]),
+             (mcpf.MGk(0.8, 0.0, 0.9), _abi.PF_EXT_MGK,
+              [0.8, 0.9, 0.0, (1 + 0.64) / 1.6, (1 + 1.6 + 0.64) / 1.6])]
     for pf, ext, params in cases:
         t = pf.pack(None, _abi.McgbPf())
         assert pf.kind == _abi.PF_EXT and t.ext_kind == ext
