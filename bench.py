@@ -130,19 +130,28 @@ def dist_env():
 
 
 # --------------------------------------------------------------- CPU side
+def reference_seeds():
+    """Stream seeds of the reference's own initialiser (clrng.Random().seeds
+    (4096, 1)), stored as a fixture so that the CPU arms load no library of
+    this package: tests/golden/ref_seeds.npz."""
+    d = np.load(os.path.join(ROOT, 'tests', 'golden', 'ref_seeds.npz'))
+    return d['x'].copy(), d['a'].copy()
+
+
 def reference_cpu(workload, seconds=12.0, threads=None, max_packets=None):
     """Times the reference CPU build (or the oracle port when the reference
     build is absent) on a bounded sample; returns (packets/s, meta)."""
-    import mcoracle
-    import scenarios
     import render_ref
-    from pyxopto_gb300.rng import Random
     threads = threads or os.cpu_count() or 1
     so = os.path.join(render_ref.REF_DIR, workload + '.so')
     kind = 'reference' if os.path.exists(so) else 'port'
-    streams = 4096
-    seeds = Random().seeds(streams, 1)
-    mc = scenarios.build_mc(workload) if kind == 'port' else None
+    seeds = reference_seeds()
+    streams = len(seeds[0])
+    mc = None
+    if kind == 'port':
+        import mcoracle
+        import scenarios
+        mc = scenarios.build_mc(workload)
 
     def run(n):
         t0 = time.perf_counter()

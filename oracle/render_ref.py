@@ -2,7 +2,7 @@
 for a parity scenario and compiles it for the host CPU into oracle/_ref/.
 
 TEST INFRASTRUCTURE ONLY.  Run in a container where the PyXOpto sources are
-importable (default /root/reference, override with XOPTO_REFERENCE):
+importable (REFERENCE below, override with XOPTO_REFERENCE):
 
     python oracle/render_ref.py c1_line_hg_radial c2_gk_fluence ...
 
@@ -34,6 +34,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 REF_DIR = os.path.join(HERE, '_ref')
+# This recipe reads the reference sources where the build container mounts
+# them; nothing else in the repository names that path.
 REFERENCE = os.environ.get('XOPTO_REFERENCE', '/root/reference')
 
 sys.path.insert(0, os.path.join(REPO, 'tests', 'golden'))

@@ -20,6 +20,7 @@
 #pragma once
 #include "mc_device.cuh"
 #include "batch_rng.h"
+#include "batch_launch.h"
 #include "mcml_kernel.cuh"
 
 namespace MCGB_NS {
@@ -30,6 +31,8 @@ struct __align__(16) BatchPrep {
     float reflectance;      /* specular reflectance of the Line source */
     float pad[3];
 };
+static_assert(sizeof(BatchPrep) <= MCGB_BATCH_PREP_BYTES,
+              "a per-simulation table must fit the scratch record of batch_launch.h");
 
 /* cos_critical / Fresnel at normal incidence in double precision, as the
    host-side packing of the layered simulator computes them

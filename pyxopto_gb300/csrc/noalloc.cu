@@ -15,8 +15,12 @@
  *
  * Host code cannot use the array's name as a device address, so the first
  * call on each device looks the address up with cudaGetSymbolAddress (with
- * that device current) and caches it; make that first call before any
- * stream capture.  All calls share the one array, so calls that overlap on
+ * that device current) and caches it together with the identity of the
+ * device's current context; make that first call before any stream capture.
+ * A device reset (cudaDeviceReset, or a release and re-creation of the
+ * primary context) reloads the library's module at a new address, so the
+ * next call sees a new context identity and looks the address up again; that
+ * call, too, belongs before any stream capture.  All calls share the one array, so calls that overlap on
  * the GPU (different streams, or different host threads on the same device)
  * race on it and must be serialized by the caller.  The array keeps the last
  * call's contents; everything the kernels need zeroed (the work-queue
@@ -39,6 +43,36 @@ constexpr int kMaxDevices = 64;
 
 std::mutex g_mu;
 void *g_scratch_ptr[kMaxDevices];
+unsigned long long g_scratch_ctx[kMaxDevices];   /* context identity of the cached address */
+
+/* Identity of the calling thread's current context (cuCtxGetCurrent +
+   cuCtxGetId, fetched through the runtime so that the library does not link
+   the driver library).  Returns false when it cannot be told; the caller then
+   looks the address up on every call. */
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+bool current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        resolved = true;
+        void *f = nullptr, *g = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q1) ==
+                cudaSuccess && q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &g, 12000, cudaEnableDefault, &q2) ==
+                cudaSuccess && q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+            get_id = reinterpret_cast<CtxGetIdFn>(g);
+        }
+    }
+    if (!get_current || !get_id) return false;
+    void *ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
+}
 
 }  // namespace
 
@@ -46,8 +80,8 @@ static __device__ __align__(256) unsigned char g_batch_scratch[kScratchBytes];
 
 namespace {
 
-/* Device address of g_batch_scratch on the current device (looked up once
-   per device). */
+/* Device address of g_batch_scratch on the current device: looked up once
+   per device and context, again after a device reset. */
 int scratch_address(void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -55,13 +89,23 @@ int scratch_address(void **out) {
     if (dev < 0 || dev >= kMaxDevices)
         return mcgb_internal::set_error(MCGB_E_UNSUPPORTED, "device ordinal beyond 63");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    unsigned long long ctx = 0;
+    bool known = current_context_id(&ctx);
+    if (!g_scratch_ptr[dev] || !known || g_scratch_ctx[dev] != ctx) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_batch_scratch);
         if (e != cudaSuccess || !p)
             return mcgb_internal::set_error(MCGB_E_CUDA,
                                             "cudaGetSymbolAddress of the batched scratch array failed");
+        /* the lookup may have created the context: take its identity now */
+        known = current_context_id(&ctx);
         g_scratch_ptr[dev] = p;
+        g_scratch_ctx[dev] = known ? ctx : 0ull;
+        if (!known) {
+            *out = p;
+            g_scratch_ptr[dev] = nullptr;
+            return MCGB_OK;
+        }
     }
     *out = g_scratch_ptr[dev];
     return MCGB_OK;

@@ -150,7 +150,7 @@ cudaError_t MCGB_OCCUPANCY(int block, size_t dyn_smem, int *blocks_per_sm) {
     /* the smallest residency over the static variants of the medium, so that
        one wave of the suggested stream count fits whichever variant runs */
     int best = 1 << 30;
-    for (int pf = 0; pf < 3; ++pf)
+    for (int pf = 0; pf <= MCGB_PF_EXT; ++pf)
         for (int m = 0; m < 3; ++m)
             for (int fl = 0; fl < 2; ++fl) {
                 int n = 0;

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run where the PyXOpto sources are importable (default /root/reference,
-override with XOPTO_REFERENCE):
+Run where the PyXOpto sources are importable (the reference tree that
+oracle/render_ref.py reads; override with XOPTO_REFERENCE):
 
     python tests/golden/make_golden.py
 
@@ -15,6 +15,10 @@ Writes
   rng_tables.npz         samples of the reference's safe-prime multiplier
                          table and of its seed expansion for several
                          initializers.
+  ref_seeds.npz          the reference's clrng.Random().seeds(4096, 1): the
+                         stream seeds that drive the reference CPU build in
+                         the benchmark's reference arm and in the
+                         reference-parity tests (`make_golden.py ref_seeds`).
   cuda_mcml_radial.npz   the CUDA-MCML radial reflectance profile that the
                          reference's validation suite compares against
                          (xopto/mcml/test/reference/cuda_singlelayer_linesource_radial.pkl,
@@ -96,6 +100,13 @@ def make_scenario(name):
         data['sv_total'] = total
     np.savez_compressed(os.path.join(HERE, 'golden_{}.npz'.format(name)), **data)
     print(name, {k: int(v.sum()) for k, v in data.items() if k.startswith('tally_')})
+
+
+def make_ref_seeds(n=4096, xinit=1):
+    x, a = reference_seeds(n, xinit)
+    np.savez_compressed(os.path.join(HERE, 'ref_seeds.npz'), x=np.asarray(x, np.uint64),
+                        a=np.asarray(a, np.uint32), xinit=np.array([xinit], np.uint64))
+    print('ref_seeds', n)
 
 
 def make_rng_tables():
@@ -255,6 +266,9 @@ def make_trace_check():
 
 
 if __name__ == '__main__':
+    if sys.argv[1:2] == ['ref_seeds']:
+        make_ref_seeds()
+        sys.exit(0)
     if sys.argv[1:2] == ['trace_check']:
         make_trace_check()
         sys.exit(0)
@@ -270,6 +284,7 @@ if __name__ == '__main__':
         make_scenario(n)
     if not sys.argv[1:]:
         make_rng_tables()
+        make_ref_seeds()
         make_cuda_mcml()
         make_cuda_fiber()
         make_cuda_fiber(double=True)

@@ -586,8 +586,10 @@ SCENARIOS = {
         nphotons=300, streams=30, rnginit=131),
 }
 
-# Bench workloads (not golden-tested at these sizes): the layered
-# configuration of the headline metric, and config 1 at full size.
+# Bench workloads at their full sizes: the layered configuration of the
+# headline metric, config 1, and the voxelized configuration.  Their
+# reference CPU builds (oracle/_ref/) are the CPU baseline and the other
+# side of tests/test_reference_parity.py.
 BENCH = {
     # 3-layer skin-like stack, Gegenbauer phase function (alpha 0.5), Line
     # source, Cartesian fluence 100x100x100 over 10x10x10 mm, 1e8 packets
