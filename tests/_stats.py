@@ -106,6 +106,19 @@ def gate(a, b, alpha=1e-3, draws=20000, seed=12345):
     return passed, report
 
 
+def record(what, report):
+    """Appends a gate report to the JSON-lines file named by the environment
+    variable MCGB_GATE_REPORT, when it is set (the numbers behind a passing
+    test)."""
+    import json
+    import os
+    path = os.environ.get('MCGB_GATE_REPORT')
+    if path:
+        test = os.environ.get('PYTEST_CURRENT_TEST', '').split(' ')[0]
+        with open(path, 'a') as f:
+            f.write(json.dumps(dict(report, test=test, what=what), default=float) + '\n')
+
+
 def per_packet(rows, packets, k=8388607.0):
     """Integer tallies of batches -> per-packet weights (float64)."""
     return np.asarray(rows, np.float64) / k / float(packets)

@@ -75,6 +75,7 @@ def gpu_batches(name, nphotons, keys):
 
 def _assert_gate(a, b, what):
     ok, rep = _stats.gate(a, b)
+    _stats.record(what, rep)
     assert ok, (what, rep)
     return rep
 
