@@ -41,7 +41,9 @@ def gelu_grad(x):
 
 def forward(weights, biases, x, acts):
     """weights: list of [N, K] float64 (already bf16-valued); x: [M, K0]
-    bf16-valued.  Returns (inputs, pres, y) with y bf16-rounded."""
+    bf16-valued.  Returns (inputs, pres, y): the hidden activations are
+    bf16-rounded as the GPU stores them; the output y is the last layer's
+    pre-activation, kept in full precision (the GPU keeps it in FP32)."""
     h = x
     inputs, pres = [], []
     for w, b, act in zip(weights, biases, acts):
@@ -49,7 +51,7 @@ def forward(weights, biases, x, acts):
         pre = h @ w.T + b
         pres.append(pre)
         h = bf16_round(gelu(pre) if act else pre)
-    return inputs, pres, h
+    return inputs, pres, pres[-1]
 
 
 def backward(weights, inputs, pres, dy, acts):
@@ -66,9 +68,20 @@ def backward(weights, inputs, pres, dy, acts):
     return dws, dbs
 
 
-def mse_grad(y, t, n_valid):
+def loss_grad(y, t, n_valid, mode=0, scale=1.0, weights=None, clip=4.0):
+    """Loss and bf16-rounded output gradient of mcgb_mlp_loss_grad: mode 0
+    squared error, mode 1 relative error of exp(scale*y) against a linear
+    target (the gradient clips the ratio at ``clip``)."""
     m, n = y.shape
-    d = np.zeros_like(y)
-    d[:, :n_valid] = y[:, :n_valid] - t[:, :n_valid]
-    loss = (d ** 2).sum() / (m * n_valid)
-    return bf16_round(2.0 * d / (m * n_valid)), loss
+    w = np.ones(n) if weights is None else np.asarray(weights, np.float64)
+    yv, tv = y[:, :n_valid], t[:, :n_valid]
+    g = np.zeros_like(y)
+    if mode == 0:
+        d = yv - tv
+        loss = (w[:n_valid] * d ** 2).sum() / (m * n_valid)
+        g[:, :n_valid] = 2.0 * w[:n_valid] * d / (m * n_valid)
+    else:
+        ratio = tv * np.exp(-scale * yv)
+        loss = (w[:n_valid] * (ratio - 1.0) ** 2).sum() / (m * n_valid)
+        g[:, :n_valid] = -2.0 * scale * w[:n_valid] * (np.minimum(ratio, clip) - 1.0) / (m * n_valid)
+    return bf16_round(g), loss

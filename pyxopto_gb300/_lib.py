@@ -32,6 +32,7 @@ _SIGNATURES = {
     'mcgb_reduce_tallies': (C.c_int, [_vp, _vp, C.c_uint64]),
     'mcgb_sampling_volume': (C.c_int, [C.POINTER(_abi.McgbSamplingVolume), _vp, C.c_uint64, _vp,
                                        _vp, C.c_uint64, _vp, _vp, _vp]),
+    'mcgb_voxel_radius': (C.c_int, [_vp, C.POINTER(C.c_int32), _vp, C.c_uint32, _vp]),
 }
 _OPTIONAL = {
     'mcgb_batched_run': (C.c_int, [C.POINTER(_abi.McgbBatchConfig), _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -44,7 +45,8 @@ _OPTIONAL = {
     'mcgb_mlp_linear_bwd_input': (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_linear_bwd_weight': (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_bwd_weight_scratch': (C.c_uint64, [C.c_int, C.c_int, C.c_int]),
-    'mcgb_mlp_mse_grad': (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    'mcgb_mlp_loss_grad': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     C.c_float, _vp]),
     'mcgb_mlp_adamw': (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_float,
                                  C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, _vp]),
 }

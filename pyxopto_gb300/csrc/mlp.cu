@@ -7,6 +7,8 @@
  *
  * GEMM: C[R, Cc] = sum_l A(r, l) B(c, l) on 64x64 output tiles, 4 warps of
  * 32x32, k-steps of 16 through mma.sync m16n8k16 (bf16 x bf16 -> f32).
+ * The forward epilogue also stores the FP32 pre-activation when asked; the
+ * last layer's FP32 pre-activation is the network output.
  * Operands are staged in shared memory with the reduction index contiguous;
  * transposed operands (activations in the weight gradient) are transposed
  * while staging.  The weight gradient splits the batch rows into fixed
@@ -183,10 +185,22 @@ __global__ void act_bwd_kernel(const bf16 *__restrict__ dy, const float *__restr
     }
 }
 
-__global__ void mse_grad_kernel(const bf16 *__restrict__ y, const float *__restrict__ tgt, bf16 *dy,
-                                float *loss, int M, int N, int nv) {
+/* Loss gradient of the network output Y [M, N] (FP32, the last layer's
+   pre-activation) against the target T [M, N], over the first nv columns,
+   with optional column weights W [N]:
+     mode 0 (squared error):  d = Y - T, loss W d^2, gradient 2 W d;
+     mode 1 (relative error of exp(scale Y)):  ratio = T exp(-scale Y),
+       loss W (ratio - 1)^2, gradient -2 scale W (min(ratio, clip) - 1) --
+       the derivative of (T - R)^2 / R^2 with R = exp(scale Y) and the
+       denominator held at the current prediction, so the fit converges to
+       the mean of T (unbiased in linear units), not to the mean of log T.
+   Loss and gradient are divided by M nv; the loss is reduced per block of
+   256 rows (fixed order).  Gradients are stored as bf16. */
+__global__ void loss_grad_kernel(const float *__restrict__ y, const float *__restrict__ tgt,
+                                 const float *__restrict__ wcol, bf16 *dy, float *loss, int M, int N,
+                                 int nv, int mode, float scale, float clip) {
     __shared__ float red[256];
-    const float scale = 1.0f / ((float)M * (float)nv);
+    const float inv = 1.0f / ((float)M * (float)nv);
     float s = 0.0f;
     size_t base = (size_t)blockIdx.x * 256;
     for (int i = threadIdx.x; i < 256 * N; i += blockDim.x) {
@@ -194,12 +208,21 @@ __global__ void mse_grad_kernel(const bf16 *__restrict__ y, const float *__restr
         int c = i % N;
         if (r >= (size_t)M) continue;
         size_t o = r * N + c;
-        float d = 0.0f;
+        float g = 0.0f;
         if (c < nv) {
-            d = __bfloat162float(y[o]) - tgt[o];
-            s += d * d * scale;
+            float w = wcol ? wcol[c] : 1.0f;
+            if (mode == 0) {
+                float d = y[o] - tgt[o];
+                s += w * d * d * inv;
+                g = 2.0f * w * d * inv;
+            } else {
+                float ratio = tgt[o] * expf(-scale * y[o]);
+                float d = ratio - 1.0f;
+                s += w * d * d * inv;
+                g = -2.0f * scale * w * (fminf(ratio, clip) - 1.0f) * inv;
+            }
         }
-        dy[o] = __float2bfloat16_rn(2.0f * d * scale);
+        dy[o] = __float2bfloat16_rn(g);
     }
     red[threadIdx.x] = s;
     __syncthreads();
@@ -253,9 +276,29 @@ int shape_ok(int m, int n, int k) {
     return MCGB_OK;
 }
 
-int weight_slices(int m) {
-    int s = (m + 2047) / 2048;
-    return s < 1 ? 1 : (s > 32 ? 32 : s);
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            n = v;
+        else
+            n = 152;
+    }
+    return n;
+}
+
+/* Reduction slices of the weight gradient: enough that the grid of
+   (n/64) x (k/64) tiles times slices covers every SM twice, each slice at
+   least one k-step of rows, at most 64 slices. */
+int weight_slices(int m, int n, int k) {
+    int tiles = ((n + BM - 1) / BM) * ((k + BN - 1) / BN);
+    int s = (2 * sm_count() + tiles - 1) / tiles;
+    int most = m / BK;
+    if (s > most) s = most;
+    if (s > 64) s = 64;
+    return s < 1 ? 1 : s;
 }
 
 }  // namespace
@@ -274,7 +317,8 @@ int mcgb_mlp_linear_fwd(const uint16_t *x, const uint16_t *w, const float *b, ui
 }
 
 uint64_t mcgb_mlp_bwd_weight_scratch(int m, int n, int k) {
-    return (uint64_t)weight_slices(m) * (uint64_t)n * (uint64_t)k;
+    if (m <= 0 || n <= 0 || k <= 0) return 0;
+    return (uint64_t)weight_slices(m, n, k) * (uint64_t)n * (uint64_t)k;
 }
 
 int mcgb_mlp_linear_bwd_input(const uint16_t *dpre, const uint16_t *wt, uint16_t *dx, int m, int n, int k,
@@ -295,7 +339,7 @@ int mcgb_mlp_linear_bwd_weight(const uint16_t *dpre, const uint16_t *x, float *d
     if (r) return r;
     if (!dpre || !x || !dw || !scratch) return fail(MCGB_E_INVALID, "NULL operand");
     /* dW[n,k] = sum_m dPre[m,n] X[m,k]: R = n, Cc = k, reduction over m */
-    int slices = weight_slices(m);
+    int slices = weight_slices(m, n, k);
     int per = ((m + slices - 1) / slices + BK - 1) / BK * BK;
     slices = (m + per - 1) / per;
     dim3 grid((k + BN - 1) / BN, (n + BM - 1) / BM, slices);
@@ -325,13 +369,13 @@ int mcgb_mlp_act_bwd(const uint16_t *dy, const float *pre, uint16_t *dpre, float
     return check_launch("mlp bias gradient");
 }
 
-int mcgb_mlp_mse_grad(const uint16_t *y, const float *t, uint16_t *dy, float *loss, int m, int n, int nv,
-                      void *stream) {
-    if (m <= 0 || n <= 0 || nv <= 0 || nv > n || !y || !t || !dy || !loss)
-        return fail(MCGB_E_INVALID, "bad mse_grad arguments");
-    mse_grad_kernel<<<(m + 255) / 256, 256, 0, (cudaStream_t)stream>>>((const bf16 *)y, t, (bf16 *)dy, loss,
-                                                                      m, n, nv);
-    return check_launch("mlp mse gradient");
+int mcgb_mlp_loss_grad(const float *y, const float *t, const float *w, uint16_t *dy, float *loss, int m,
+                       int n, int nv, int mode, float scale, void *stream) {
+    if (m <= 0 || n <= 0 || nv <= 0 || nv > n || !y || !t || !dy || !loss || mode < 0 || mode > 1)
+        return fail(MCGB_E_INVALID, "bad loss_grad arguments");
+    loss_grad_kernel<<<(m + 255) / 256, 256, 0, (cudaStream_t)stream>>>(y, t, w, (bf16 *)dy, loss, m, n, nv,
+                                                                       mode, scale, 4.0f);
+    return check_launch("mlp loss gradient");
 }
 
 int mcgb_mlp_adamw(float *w, uint16_t *wb, uint16_t *wt, const float *g, float *m, float *v, int rows,

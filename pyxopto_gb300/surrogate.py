@@ -3,8 +3,8 @@ the library's own BF16 kernels, with Monte Carlo kept as judge and
 fallback.
 
 Network: (log mua, log mus', g, n) -> 256 -> 256 -> 256 -> 30 bins of
-log10 radial reflectance, GELU activations, BF16 weights and activations,
-FP32 accumulation and FP32 master weights updated by AdamW.  The narrow input
+log radial reflectance, GELU activations, BF16 weights and activations,
+FP32 accumulation, FP32 output and FP32 master weights updated by AdamW.  The narrow input
 and output layers are zero-padded to 16 and 32 columns for the tensor-core
 tiles.  Training profiles come from the batched engine (BatchedMc).
 
@@ -19,9 +19,13 @@ The judge's own Monte Carlo noise is comparable to the 1 % tolerance at
 (a, b) and the noise is taken out of the measured error:
 err^2 = mean(((pred - m)/m)^2) - mean(((a - b)/(2 m))^2) with m = (a + b)/2,
 an unbiased estimate of the squared error against the exact profile, because
-E[(a - b)^2] / 4 is the variance of m.
+E[(a - b)^2] / 4 is the variance of m.  Where the judge's noise is large
+(far bins of strongly absorbing media) that estimate scatters widely, so a
+query fails only when it exceeds the tolerance by more than two of its own
+standard errors.
 """
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -29,6 +33,15 @@ import numpy as np
 from . import _lib
 from .batched import BatchedMc
 from .mcbase.mcutil import Axis
+
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'data')
+
+
+def default_weights():
+    """The network trained on 2^18 single-layer profiles of 1e6 packets each
+    (pyxopto_gb300.train_surrogate), shipped with the package."""
+    return os.path.join(DATA, 'surrogate_single_layer_radial.npz')
+
 
 RANGES = {'log_mua': (np.log(1.0), np.log(1000.0)), 'log_musr': (np.log(500.0), np.log(5000.0)),
           'g': (0.6, 0.95), 'n': (1.33, 1.5)}
@@ -109,18 +122,20 @@ class Mlp:
         return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
 
     def forward(self, x_bf16, store=True):
-        """x_bf16: [M, 16] bf16 tensor with M <= batch.  Returns the bf16
-        output view [M, 32]."""
+        """x_bf16: [M, 16] bf16 tensor with M <= batch.  Returns the FP32
+        network output view [M, 32] (the last layer's pre-activation)."""
         m = x_bf16.shape[0]
         if m > self.batch:
             self._alloc(m)
         self.h[0][:m].copy_(x_bf16)
+        last = len(self.w) - 1
         for i in range(len(self.w)):
             k, n = self.pads[i], self.pads[i + 1]
+            keep = store or i == last
             _lib.check(self.lib.mcgb_mlp_linear_fwd(
                 self._p(self.h[i]), self._p(self.wb[i]), self._p(self.b[i]), self._p(self.h[i + 1]),
-                self._p(self.pre[i]) if store else None, m, n, k, self.acts[i], self._stream()))
-        return self.h[-1][:m]
+                self._p(self.pre[i]) if keep else None, m, n, k, self.acts[i], self._stream()))
+        return self.pre[-1][:m]
 
     def backward(self, dy_bf16, m):
         """Gradients of every layer for the last forward pass of m rows."""
@@ -140,11 +155,18 @@ class Mlp:
                 g = self.grad_h[i]
         return self.dw, self.db
 
-    def mse_grad(self, y, t_f32, m, n_valid):
+    def loss_grad(self, y, t_f32, m, n_valid, mode=0, scale=1.0, weights=None):
+        """Gradient of the loss of the FP32 output y against t (mode 0:
+        squared error; mode 1: relative error of exp(scale*y) against a
+        linear target), into the bf16 output-gradient buffer."""
         dy = self.grad_h[-1]
-        _lib.check(self.lib.mcgb_mlp_mse_grad(self._p(y), self._p(t_f32), self._p(dy), self._p(self.loss_part),
-                                              m, self.pads[-1], n_valid, self._stream()))
+        _lib.check(self.lib.mcgb_mlp_loss_grad(self._p(y), self._p(t_f32), self._p(weights), self._p(dy),
+                                               self._p(self.loss_part), m, self.pads[-1], n_valid,
+                                               int(mode), float(scale), self._stream()))
         return dy
+
+    def mse_grad(self, y, t_f32, m, n_valid):
+        return self.loss_grad(y, t_f32, m, n_valid, mode=0)
 
     def adamw(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
         self.step_count += 1
@@ -157,24 +179,44 @@ class Mlp:
                                                self._p(self.db[i]), self._p(self.mb[i]), self._p(self.vb[i]),
                                                1, n, lr, b1, b2, eps, 0.0, self.step_count, self._stream()))
 
-    def train_step(self, x_bf16, t_f32, n_valid, lr):
+    def train_step(self, x_bf16, t_f32, n_valid, lr, mode=0, scale=1.0):
         m = x_bf16.shape[0]
         y = self.forward(x_bf16, store=True)
-        dy = self.mse_grad(y, t_f32, m, n_valid)
-        self.backward(dy, m)
+        self.loss_grad(y, t_f32, m, n_valid, mode=mode, scale=scale)
+        self.backward(self.grad_h[-1], m)
         self.adamw(lr=lr)
         return self.loss_part[:(m + 255) // 256]
 
+    def state(self):
+        """FP32 master weights and biases as numpy arrays."""
+        return ([w.cpu().numpy().copy() for w in self.w], [b.cpu().numpy().copy() for b in self.b])
+
+    def load_state(self, weights, biases):
+        for i in range(len(self.w)):
+            self.w[i].copy_(self.torch.from_numpy(np.asarray(weights[i], np.float32)))
+            self.b[i].copy_(self.torch.from_numpy(np.asarray(biases[i], np.float32)))
+        self.sync_copies()
+
 
 class Surrogate:
-    """Radial reflectance surrogate for the batched single-layer family."""
+    """Radial reflectance surrogate for the batched single-layer family.
 
-    def __init__(self, raxis: Axis = None, floor: float = 1e-2, seed: int = 0):
+    The network output z (FP32) gives the profile R_b = exp(mu_b + scale z_b)
+    per bin, with mu_b the training set's mean of ln R_b and scale the mean
+    over the bins of its standard deviation.  Training has two stages: the
+    squared error of z against the standardised ln R for ``warm_epochs``
+    epochs, then the relative error of R against the Monte Carlo profile in
+    linear units (loss mode 1 of mcgb_mlp_loss_grad), whose fit is the mean
+    profile itself -- a fit in log units would converge to the mean of the
+    log, biased low by half the squared relative noise of each label.  The
+    learning rate follows one cosine from ``lr`` to ``lr_min``."""
+
+    def __init__(self, raxis: Axis = None, seed: int = 0):
         self.raxis = raxis if raxis is not None else Axis(0.0, 3e-3, 30)
-        self.floor = float(floor)
         self.seed = seed
         self.mlp = None
-        self.mu = self.sd = None
+        self.mu = None
+        self.scale = None
         self.report = {}
 
     # -------------------------------------------------------- data
@@ -183,38 +225,53 @@ class Surrogate:
         b = BatchedMc(sims, raxis=self.raxis, fast=fast, seed=seed)
         return b.run()
 
-    def targets(self, refl):
-        return np.log10(np.maximum(refl, 0.0) + self.floor)
+    @staticmethod
+    def _musr(sims):
+        return np.asarray(sims['mus']) * (1.0 - np.asarray(sims['g']))
 
-    def fit(self, sims, refl, epochs=40, batch=4096, lr=2e-3, lr_min=5e-5, verbose=False):
-        """Trains the network on (sims, reflectance) for ``epochs`` passes."""
+    def fit(self, sims, refl, epochs=400, batch=4096, lr=2e-3, lr_min=2e-5, warm_epochs=10,
+            verbose=False):
+        """Trains the network on (sims, reflectance) for ``epochs`` passes;
+        returns the mean loss of every epoch."""
         import torch
-        x = features(sims['mua'], sims['mus'] * (1.0 - np.asarray(sims['g'])), sims['g'], sims['n'])
-        y = self.targets(refl)
-        self.mu, self.sd = y.mean(0), y.std(0) + 1e-6
-        t = np.zeros((len(x), OUT_PAD), np.float32)
-        t[:, :y.shape[1]] = (y - self.mu) / self.sd
+        refl = np.asarray(refl, np.float64)
         nb = self.raxis.n
+        x = features(sims['mua'], self._musr(sims), sims['g'], sims['n'])
+        pos = np.where(refl > 0, refl, np.nan)
+        tiny = 1e-6 * np.nanmedian(pos, axis=0)
+        lnr = np.log(np.maximum(refl, tiny[None, :]))
+        self.mu = lnr.mean(0)
+        self.scale = float(lnr.std(0).mean())
+        t_log = np.zeros((len(x), OUT_PAD), np.float32)
+        t_log[:, :nb] = (lnr - self.mu) / self.scale
+        t_lin = np.zeros((len(x), OUT_PAD), np.float32)
+        t_lin[:, :nb] = refl * np.exp(-self.mu)[None, :]
         if self.mlp is None:
             self.mlp = Mlp(sizes=(4, 256, 256, 256, nb), seed=self.seed, batch=batch)
         xd = torch.from_numpy(x).cuda().to(torch.bfloat16)
-        td = torch.from_numpy(t).cuda()
+        tl = torch.from_numpy(t_log).cuda()
+        tr = torch.from_numpy(t_lin).cuda()
         n = (len(x) // 8) * 8
         rng = np.random.default_rng(self.seed)
-        steps = epochs * max(1, n // batch)
+        per_epoch = max(1, n // batch)
+        steps = epochs * per_epoch
         hist = []
         t0 = time.perf_counter()
         k = 0
         for ep in range(epochs):
+            mode = 0 if ep < warm_epochs else 1
+            tgt = tl if mode == 0 else tr
             perm = torch.from_numpy(rng.permutation(len(x))[:n]).cuda()
+            total = torch.zeros((), dtype=torch.float32, device='cuda')
             for s in range(0, n - batch + 1, batch):
                 idx = perm[s:s + batch]
                 lr_k = lr_min + 0.5 * (lr - lr_min) * (1 + np.cos(np.pi * k / steps))
-                lp = self.mlp.train_step(xd[idx], td[idx], nb, lr_k)
+                lp = self.mlp.train_step(xd[idx], tgt[idx], nb, lr_k, mode=mode, scale=self.scale)
+                total += lp.sum()
                 k += 1
-            hist.append(float(lp.sum().item()))
+            hist.append(float(total.item()) / per_epoch)
             if verbose:
-                print('epoch', ep, hist[-1])
+                print('epoch', ep, 'mode', mode, hist[-1], flush=True)
         torch.cuda.synchronize()
         self.report['train_seconds'] = time.perf_counter() - t0
         self.report['train_steps'] = k
@@ -232,11 +289,34 @@ class Surrogate:
         xd = torch.from_numpy(xp).cuda().to(torch.bfloat16)
         out = []
         for s in range(0, mp, self.mlp.batch):
-            y = self.mlp.forward(xd[s:s + self.mlp.batch], store=False)
-            out.append(y[:, :self.raxis.n].float().cpu().numpy())
-        y = np.concatenate(out)[:m] * self.sd + self.mu
-        return np.maximum(10.0 ** y - self.floor, 0.0)
+            z = self.mlp.forward(xd[s:s + self.mlp.batch], store=False)
+            out.append(z[:, :self.raxis.n].cpu().numpy().astype(np.float64))
+        z = np.concatenate(out)[:m]
+        return np.exp(self.mu[None, :] + self.scale * z)
 
+    # ------------------------------------------------------ weights
+    def save(self, path):
+        """Writes the FP32 weights and the output normalisation (npz)."""
+        ws, bs = self.mlp.state()
+        arrays = {'w{}'.format(i): w for i, w in enumerate(ws)}
+        arrays.update({'b{}'.format(i): b for i, b in enumerate(bs)})
+        np.savez(path, sizes=np.array(self.mlp.sizes), mu=self.mu, scale=np.array([self.scale]),
+                 raxis=np.array([self.raxis.start, self.raxis.stop, self.raxis.n], np.float64), **arrays)
+
+    @classmethod
+    def load(cls, path, batch=4096):
+        d = np.load(path)
+        r = d['raxis']
+        sur = cls(raxis=Axis(float(r[0]), float(r[1]), int(r[2])))
+        sizes = [int(v) for v in d['sizes']]
+        sur.mlp = Mlp(sizes=sizes, batch=batch)
+        nl = len(sizes) - 1
+        sur.mlp.load_state([d['w{}'.format(i)] for i in range(nl)], [d['b{}'.format(i)] for i in range(nl)])
+        sur.mu = d['mu'].astype(np.float64)
+        sur.scale = float(d['scale'][0])
+        return sur
+
+    # -------------------------------------------------------- judge
     @staticmethod
     def rms_rel(pred, ref, mask=None):
         rel = (pred - ref) / np.where(ref > 0, ref, 1.0)
@@ -246,11 +326,15 @@ class Surrogate:
         return np.sqrt((rel ** 2).mean(1))
 
     @staticmethod
-    def judge_error(pred, a, b, mask=None):
+    def judge_error(pred, a, b, mask=None, with_se=False):
         """Noise-corrected relative RMS error of ``pred`` against the exact
         profile, from two independent Monte Carlo halves ``a`` and ``b``.
         Returns (corrected error, raw error against (a+b)/2, MC noise of
-        (a+b)/2), all per profile."""
+        (a+b)/2), all per profile; with ``with_se`` also the standard error
+        of the squared-error estimate.  Per bin, with e the relative error
+        against m = (a+b)/2 and q = (a-b)/(2m), d = e^2 - q^2 estimates the
+        squared bias without the noise; for Gaussian noise of variance s^2,
+        Var(d) = 4 s^4 + 4 bias^2 s^2, estimated with s^4 ~ q^4/3."""
         m = 0.5 * (a + b)
         den = np.where(m > 0, m, 1.0)
         e2 = ((pred - m) / den) ** 2
@@ -260,7 +344,13 @@ class Surrogate:
         cnt = np.maximum(mask.sum(1), 1)
         raw2 = np.where(mask, e2, 0.0).sum(1) / cnt
         noise2 = np.where(mask, n2, 0.0).sum(1) / cnt
-        return np.sqrt(np.maximum(raw2 - noise2, 0.0)), np.sqrt(raw2), np.sqrt(noise2)
+        err = np.sqrt(np.maximum(raw2 - noise2, 0.0))
+        if not with_se:
+            return err, np.sqrt(raw2), np.sqrt(noise2)
+        d = e2 - n2
+        var = (4.0 / 3.0) * n2 ** 2 + 4.0 * np.maximum(d, 0.0) * n2
+        se = np.sqrt(np.where(mask, var, 0.0).sum(1)) / cnt
+        return err, np.sqrt(raw2), np.sqrt(noise2), se
 
     def simulate_halves(self, sims, packets, seed=7):
         """Two independent Monte Carlo halves of ``packets``/2 packets each
@@ -272,16 +362,20 @@ class Surrogate:
         return r[:k], r[k:]
 
     def serve(self, sims, judge_fraction=0.01, judge_packets=1_000_000, tol=0.01, max_fail=0.1,
-              seed=7, rel_floor=None):
+              seed=7, rel_floor=None, confidence=2.0):
         """Answers a batch of queries: network prediction for all, Monte Carlo
-        judge on a fraction, MC fallback where the judge's noise-corrected
-        relative RMS error (over the bins above ``rel_floor`` of the profile
-        peak) exceeds ``tol``.  Returns (profiles, report)."""
+        judge on a fraction, MC fallback where the judge finds the relative
+        RMS error above ``tol``.  The judge's estimate of the squared error
+        (noise-corrected, over the bins above ``rel_floor`` of the profile
+        peak when given) is noisy itself; a query fails when the estimate
+        exceeds tol^2 by more than ``confidence`` standard errors (0: the
+        estimate alone decides).  Failed judged queries get their Monte
+        Carlo profile; when more than ``max_fail`` of the judged queries fail,
+        the whole batch is re-simulated.  Returns (profiles, report)."""
         import torch
         m = len(sims['mua'])
         t0 = time.perf_counter()
-        musr = np.asarray(sims['mus']) * (1.0 - np.asarray(sims['g']))
-        pred = self.predict(sims['mua'], musr, sims['g'], sims['n'])
+        pred = self.predict(sims['mua'], self._musr(sims), sims['g'], sims['n'])
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         rng = np.random.default_rng(seed)
@@ -294,8 +388,8 @@ class Surrogate:
         mask = None
         if rel_floor is not None:
             mask = mc >= rel_floor * mc.max(1, keepdims=True)
-        err, raw, noise = self.judge_error(pred[jidx], a, b, mask)
-        fail = err > tol
+        err, raw, noise, se = self.judge_error(pred[jidx], a, b, mask, with_se=True)
+        fail = err ** 2 - confidence * se > tol ** 2
         out = pred.copy()
         out[jidx[fail]] = mc[fail]
         fallback = bool(fail.mean() > max_fail)
@@ -310,7 +404,10 @@ class Surrogate:
                'judge_rms_rel_p90': float(np.percentile(err, 90)),
                'judge_raw_rms_rel_median': float(np.median(raw)),
                'judge_noise_rms_rel_median': float(np.median(noise)),
+               'judge_noise_rms_rel_p90': float(np.percentile(noise, 90)),
+               'judge_estimate_se_median': float(np.median(se)),
                'judge_fail_fraction': float(fail.mean()),
+               'judge_point_estimate_above_tol': float(np.mean(err > tol)),
                'fallback_all': fallback, 'infer_seconds': t1 - t0, 'judge_seconds': t2 - t1,
                'fallback_seconds': t3 - t2, 'seconds': (t3 if fallback else t2) - t0}
         rep['profiles_per_s'] = m / rep['seconds']

@@ -1,6 +1,8 @@
 """Surrogate MLP kernels: forward pass and gradients against the float64 CPU
-oracle (oracle/mlp_oracle.py), deterministic gradients, training
-convergence, and the end-to-end surrogate with its Monte Carlo judge."""
+oracle (oracle/mlp_oracle.py) at the served network's shape
+4-256-256-256-30, deterministic gradients, both loss modes, training
+convergence, and the served surrogate with its Monte Carlo judge and
+fallback."""
 import numpy as np
 import pytest
 
@@ -24,16 +26,16 @@ def _net(torch, sizes, seed=0, batch=512):
     return net
 
 
-def test_forward_and_gradients_match_oracle(cuda):
+@pytest.mark.parametrize('sizes', [(4, 256, 256, 256, 30), (4, 64, 64, 30)])
+def test_forward_and_gradients_match_oracle(cuda, sizes):
     torch = cuda
-    sizes = (4, 64, 64, 30)
     m = 512
     net = _net(torch, sizes, batch=m)
     rng = np.random.default_rng(5)
     x = np.zeros((m, 16), np.float32)
     x[:, :4] = rng.uniform(-1, 1, (m, 4))
     xb = torch.from_numpy(x).cuda().to(torch.bfloat16)
-    y = net.forward(xb).float().cpu().numpy()
+    y = net.forward(xb).cpu().numpy().astype(np.float64)
     dy = np.zeros((m, 32), np.float32)
     dy[:, :30] = rng.normal(0, 1e-2, (m, 30))
     dyb = torch.from_numpy(dy).cuda().to(torch.bfloat16)
@@ -46,7 +48,7 @@ def test_forward_and_gradients_match_oracle(cuda):
     xs = mo.from_bits(xb.view(torch.int16).cpu().numpy().view(np.uint16))
     acts = net.acts
     inputs, pres, yo = mo.forward(ws, bs, xs, acts)
-    assert np.max(np.abs(y - yo)) <= 2e-2 * max(1.0, np.max(np.abs(yo)))
+    assert np.max(np.abs(y[:, :30] - yo[:, :30])) <= 1e-3 * max(1.0, np.max(np.abs(yo)))
     dyo = mo.from_bits(dyb.view(torch.int16).cpu().numpy().view(np.uint16))
     dwo, dbo = mo.backward(ws, inputs, pres, dyo, acts)
     for i in range(len(ws)):
@@ -58,17 +60,20 @@ def test_forward_and_gradients_match_oracle(cuda):
     assert all(np.array_equal(a.cpu().numpy(), b_) for a, b_ in zip(net.dw, [d.astype(np.float32) for d in dw]))
 
 
-def test_mse_gradient_matches_oracle(cuda):
+@pytest.mark.parametrize('mode', [0, 1])
+def test_loss_gradient_matches_oracle(cuda, mode):
     torch = cuda
     from pyxopto_gb300.surrogate import Mlp
     net = Mlp(sizes=(4, 32, 30), batch=256)
     rng = np.random.default_rng(2)
     y = rng.normal(0, 1, (256, 32)).astype(np.float32)
     t = rng.normal(0, 1, (256, 32)).astype(np.float32)
-    yb = torch.from_numpy(y).cuda().to(torch.bfloat16)
-    dy = net.mse_grad(yb, torch.from_numpy(t).cuda(), 256, 30)
+    if mode == 1:
+        t = np.exp(rng.normal(0, 0.5, (256, 32))).astype(np.float32) * np.exp(0.7 * y)
+    dy = net.loss_grad(torch.from_numpy(y).cuda(), torch.from_numpy(t).cuda(), 256, 30, mode=mode,
+                       scale=0.7)
     got = dy.float().cpu().numpy()
-    ref, loss = mo.mse_grad(mo.from_bits(yb.view(torch.int16).cpu().numpy().view(np.uint16)), t, 30)
+    ref, loss = mo.loss_grad(y.astype(np.float64), t.astype(np.float64), 30, mode=mode, scale=0.7)
     assert np.max(np.abs(got - ref)) <= 1e-2 * np.max(np.abs(ref))
     assert abs(net.loss_part[:1].sum().item() - loss) < 1e-3 * loss
 
@@ -94,21 +99,37 @@ def test_training_reduces_loss(cuda):
     assert np.mean(losses[-20:]) < 0.05 * np.mean(losses[:5])
 
 
-def test_surrogate_end_to_end(cuda, lib):
+def test_surrogate_fit_reduces_loss(cuda, lib):
+    """Both training stages run on the library's kernels: a short fit on
+    low-packet profiles lowers the squared error of the first stage and
+    the relative error of the second."""
     from pyxopto_gb300.batched import BatchedMc
-    from pyxopto_gb300.surrogate import Surrogate, sequential_plain_mc
+    from pyxopto_gb300.surrogate import Surrogate
     sur = Surrogate()
     train = BatchedMc.sample_sims(8192, seed=21, packets=(20000, 20001))
     refl = sur.simulate(train)
-    hist = sur.fit(train, refl, epochs=25, batch=1024)
-    assert hist[-1] < 0.2 * hist[0]
-    test = BatchedMc.sample_sims(2048, seed=22, packets=(1, 2))
-    out, rep = sur.serve(test, judge_fraction=0.05, judge_packets=200000, tol=0.05, max_fail=1.0,
-                         rel_floor=1e-3)
-    assert out.shape == (2048, 30)
-    assert rep['judge_rms_rel_median'] < 0.1, rep
-    # what the network gains: the same 2048 profiles from sequential plain
-    # Monte Carlo at the judge's packet count
-    seq = BatchedMc.sample_sims(5, seed=23, packets=(1, 2))
-    plain = sequential_plain_mc(seq, 200000)
-    assert rep['profiles_per_s'] > 10.0 * plain, (rep['profiles_per_s'], plain)
+    hist = sur.fit(train, refl, epochs=30, batch=1024, warm_epochs=10)
+    assert hist[9] < 0.2 * hist[0]
+    assert hist[-1] < hist[10]
+
+
+def test_served_surrogate_meets_tolerance_with_fallback_live(cuda, lib):
+    """The trained network shipped with the package (trained on the GPU by
+    pyxopto_gb300.train_surrogate) served with its Monte Carlo judge at the
+    1 % tolerance and the library's default fallback (max_fail 0.1): the
+    batch is not re-simulated, the judged errors are low, and the service
+    runs at least 100x the profiles/s of sequential plain Mc.run calls at the
+    judge's packet count."""
+    from pyxopto_gb300.batched import BatchedMc
+    from pyxopto_gb300.surrogate import Surrogate, sequential_plain_mc, default_weights
+    sur = Surrogate.load(default_weights())
+    queries = BatchedMc.sample_sims(16384, seed=5, packets=(1, 2))
+    sur.serve(queries, seed=3)                        # warm-up
+    out, rep = sur.serve(queries, seed=7)
+    assert out.shape == (16384, 30) and np.all(np.isfinite(out))
+    assert not rep['fallback_all'], rep
+    assert rep['judge_fail_fraction'] <= 0.1, rep
+    assert rep['judge_rms_rel_median'] < 0.01, rep
+    seq = BatchedMc.sample_sims(9, seed=23, packets=(1, 2))
+    plain = sequential_plain_mc(seq, 1_000_000)
+    assert rep['profiles_per_s'] > 100.0 * plain, (rep['profiles_per_s'], plain)
