@@ -54,7 +54,7 @@
 extern "C" {
 #endif
 
-#define MCGB_ABI_VERSION 1
+#define MCGB_ABI_VERSION 3
 
 /* Fixed-point weight scale of the integer accumulators. */
 #define MCGB_ACCU_K 8388607
@@ -451,6 +451,9 @@ typedef struct McgbBuffers {
     const uint8_t *voxels;          /* mcvox: material index per voxel,
                                        flat index (z*ny + y)*nx + x          */
     const McgbMaterial *materials;  /* mcvox: [num_materials]                */
+    const uint8_t *voxel_radius;    /* mcvox, FAST math: homogeneous-cube
+                                       radius per voxel (mcgb_voxel_radius),
+                                       or NULL to stop at every voxel wall   */
     uint64_t *counters;             /* [MCGB_NUM_COUNTERS]                   */
 } McgbBuffers;
 
@@ -476,6 +479,21 @@ int mcgb_suggest_streams(int medium, int math, uint32_t block_size, uint32_t *st
    a check fails. */
 int mcgb_mcml_run(const McgbMcmlConfig *cfg, const McgbBuffers *buf, void *stream);
 int mcgb_mcvox_run(const McgbMcvoxConfig *cfg, const McgbBuffers *buf, void *stream);
+
+/* No counterpart in the reference.  Homogeneous-cube radius of every voxel
+   for the FAST-math voxelized kernels (McgbBuffers.voxel_radius):
+   dev_radius[v] (uint8, the voxels' layout) = the largest k <= max_radius
+   such that every voxel within Chebyshev distance k of v lies inside the
+   grid and holds v's material.  A packet in voxel v whose sampled free path
+   is shorter than k * min(voxel size) takes it in one move instead of
+   stopping at each same-material wall and drawing a new path length, as
+   the reference does (xopto/mcvox/kernel/mcvox.template.c:760-1038); the
+   free path is memoryless, so the interaction points have the same
+   distribution.  shape = (nx, ny, nz) on the host; max_radius in
+   [1, MCGB_VOXEL_RADIUS_MAX].  Launches only. */
+#define MCGB_VOXEL_RADIUS_MAX 64u
+int mcgb_voxel_radius(const uint8_t *dev_voxels, const int32_t shape[3], uint8_t *dev_radius,
+                      uint32_t max_radius, void *stream);
 
 /* Reads the device counter block (synchronizes the stream) and converts the
    status bits into a return code: MCGB_OK, MCGB_E_TIMEOUT or
@@ -607,7 +625,8 @@ int mcgb_batched_run_noalloc(const McgbBatchConfig *cfg, const McgbBatchSim *dev
    act: 0 = identity, 1 = GELU (tanh form). */
 
 /* Y[M,N] = act(X[M,K] W[N,K]^T + b[N]) stored as bf16; when pre != NULL the
-   FP32 pre-activation is stored as well (for the backward pass). */
+   FP32 pre-activation is stored as well (for the backward pass; for the
+   output layer it is the FP32 network output). */
 int mcgb_mlp_linear_fwd(const uint16_t *dev_x, const uint16_t *dev_w, const float *dev_b,
                         uint16_t *dev_y, float *dev_pre, int m, int n, int k, int act,
                         void *stream);
@@ -632,11 +651,19 @@ int mcgb_mlp_linear_bwd_weight(const uint16_t *dev_dpre, const uint16_t *dev_x, 
                                float *dev_scratch, int m, int n, int k, void *stream);
 uint64_t mcgb_mlp_bwd_weight_scratch(int m, int n, int k);
 
-/* Mean-squared-error gradient on the first n_valid of N columns:
-   dY = 2*(Y - T)/(M*n_valid) (bf16), other columns 0; the per-block loss
-   partial sums go to dev_loss[ceil(M/256)]. */
-int mcgb_mlp_mse_grad(const uint16_t *dev_y, const float *dev_t, uint16_t *dev_dy,
-                      float *dev_loss, int m, int n, int n_valid, void *stream);
+/* Loss gradient of the FP32 network output Y[M,N] (the last layer's
+   pre-activation) on the first n_valid of N columns, with optional column
+   weights W[N] (NULL = 1); other columns get 0.  Everything is divided by
+   M*n_valid; dY is stored as bf16 and the per-block loss partial sums go to
+   dev_loss[ceil(M/256)].
+     mode 0, squared error:  loss W (Y - T)^2, dY = 2 W (Y - T);
+     mode 1, relative error of R = exp(scale*Y) against a target T in the
+       same (linear) units:  loss W (T/R - 1)^2, dY = -2 scale W (min(T/R, 4) - 1),
+       the gradient with the denominator held at the current R, whose fit
+       is the mean of T (unbiased in linear units).  */
+int mcgb_mlp_loss_grad(const float *dev_y, const float *dev_t, const float *dev_w,
+                       uint16_t *dev_dy, float *dev_loss, int m, int n, int n_valid, int mode,
+                       float scale, void *stream);
 
 /* AdamW on FP32 master weights w[rows*cols] (decoupled weight decay); also
    writes the bf16 copy w_bf16[rows,cols] and, when wt_bf16 != NULL, the

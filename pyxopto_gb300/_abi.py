@@ -133,7 +133,7 @@ class McgbBuffers(C.Structure):
                 ('int_buffer', C.c_void_p), ('int_size', u64),
                 ('fp_lut', C.c_void_p), ('fp_lut_size', u64),
                 ('voxels', C.c_void_p), ('materials', C.c_void_p),
-                ('counters', C.c_void_p)]
+                ('voxel_radius', C.c_void_p), ('counters', C.c_void_p)]
 
 
 class McgbBatchSim(C.Structure):

@@ -35,6 +35,7 @@ UNITS = [
     ('mlp.cu', []),
     ('noalloc.cu', []),
     ('sampling_volume.cu', ['-fmad=false']),
+    ('voxel_radius.cu', []),
     ('rng_host.cpp', None),
 ]
 

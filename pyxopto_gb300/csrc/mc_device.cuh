@@ -209,16 +209,24 @@ MCGB_DEV void scatter_direction(f3 &dir, float cos_theta, float fi) {
    place:
      Hg:  pf0 = (g, 1 - g*g, 1 + g*g, 2*g)
      Gk:  pf0 = (g, a, -inv_a, a1), pf1 = (a2, 1 + g*g, 2*g, (1 - g)/(1 + g))
-     Lut: pf0 = (a, b, c, (float)(N - 1)), pf1 = (offset, N - 1) as int bits */
+     Lut: pf0 = (a, b, c, (float)(N - 1)), pf1 = (offset, N - 1) as int bits
+   FAST math stores 1/(2g) in place of 2g and multiplies (pf_div2g). */
+#if MCGB_FAST_MATH
+MCGB_DEV float pf_2g(float g) { return 1.0f / (2.0f * g); }
+MCGB_DEV float pf_div2g(float x, float c) { return x * c; }
+#else
+MCGB_DEV float pf_2g(float g) { return 2.0f * g; }
+MCGB_DEV float pf_div2g(float x, float c) { return mc_div(x, c); }
+#endif
 MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
     if (kind == MCGB_PF_HG) {
         float g = pf.p[0];
-        pf0 = make_float4(g, 1.0f - g * g, 1.0f + g * g, 2.0f * g);
+        pf0 = make_float4(g, 1.0f - g * g, 1.0f + g * g, pf_2g(g));
         pf1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     } else if (kind == MCGB_PF_GK) {
         float g = pf.p[0];
         pf0 = make_float4(g, pf.p[1], -pf.p[2], pf.p[3]);
-        pf1 = make_float4(pf.p[4], 1.0f + g * g, 2.0f * g, mc_div(1.0f - g, 1.0f + g));
+        pf1 = make_float4(pf.p[4], 1.0f + g * g, pf_2g(g), mc_div(1.0f - g, 1.0f + g));
     } else if (kind == MCGB_PF_EXT) {
         pf0 = make_float4(pf.p[0], pf.p[1], pf.p[2], pf.p[3]);
         pf1 = make_float4(pf.p[4], 0.0f, 0.0f, __int_as_float((int)pf.ext_kind));
@@ -243,7 +251,7 @@ MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut,
     if (PF == MCGB_PF_HG) {
         float g = pf0.x;
         float k = mc_div(pf0.y, 1.0f + g * (2.0f * rng.next() - 1.0f));
-        float cos_theta = mc_div(pf0.z - k * k, pf0.w);
+        float cos_theta = pf_div2g(pf0.z - k * k, pf0.w);
         if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
         return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
     } else if (PF == MCGB_PF_GK) {
@@ -255,7 +263,7 @@ MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut,
         } else {
             float tmp = pf0.w * rng.next() + pf1.x;
             tmp = pf1.y - mc_pow(tmp, pf0.z);
-            cos_theta = mc_div(tmp, pf1.z);
+            cos_theta = pf_div2g(tmp, pf1.z);
         }
         return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
     } else if (PF == MCGB_PF_EXT) {
@@ -551,9 +559,16 @@ MCGB_DEV FluenceCache fluence_cache(const McgbFluence &fl, uint64_t *accu) {
 
 MCGB_DEV void fluence_deposit(const McgbFluence &fl, const f3 &pos, float weight, float mua,
                               FluenceCache &cache) {
+#if MCGB_FAST_MATH
+    /* one multiply-add per axis; the offsets are loop invariants */
+    float ix = fmaf(pos.x, fl.inv_step[0], -fl.top_left[0] * fl.inv_step[0]);
+    float iy = fmaf(pos.y, fl.inv_step[1], -fl.top_left[1] * fl.inv_step[1]);
+    float iz = fmaf(pos.z, fl.inv_step[2], -fl.top_left[2] * fl.inv_step[2]);
+#else
     float ix = (pos.x - fl.top_left[0]) * fl.inv_step[0];
     float iy = (pos.y - fl.top_left[1]) * fl.inv_step[1];
     float iz = (pos.z - fl.top_left[2]) * fl.inv_step[2];
+#endif
     /* The reference accepts 0 <= indexf < shape and truncates.  With floor
        conversion (saturating), 0 <= indexf < shape  <=>  0 <= floor(indexf)
        < shape, and floor equals truncation there, so one unsigned compare

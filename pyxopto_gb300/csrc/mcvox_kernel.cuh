@@ -327,8 +327,11 @@ struct MvCtx {
     const MvMaterial *M;
     const float *lut;
     const uint8_t *vox;
+    const uint8_t *rad;   /* homogeneous-cube radii (FAST free flight), or NULL */
     MvGeom g;
-    float rmax2;
+    float rmax2, rmax;
+    float free_unit;      /* smallest voxel size, less a relative margin */
+    float free_eps;       /* absolute margin for the rounding of positions */
     bool use_rmax, use_trace, track_opl;
     uint32_t max_steps;   /* per-packet step limit, 0xFFFFFFFF when unlimited */
     f3 src_pos;
@@ -339,9 +342,37 @@ struct MvPacket {
     i3 vi;
     int mat;
     float w, opl;
+    float free;           /* FAST: radius around pos inside one material, 0 = none */
+    bool stale;           /* FAST: vi not updated since a free flight */
     uint32_t trace_count, events, steps;
     uint64_t p;
 };
+
+/* Radius of a ball around pos, inside voxel vi, that holds one material
+   and lies inside the grid (and inside rmax): the voxel's homogeneous-cube
+   radius k (mcgb_voxel_radius) times the smallest voxel size, less the
+   margins.  0 when free flight is off or vi lies outside the grid. */
+static __device__ __forceinline__ float mv_free_radius(const MvCtx &x, const i3 &vi, const f3 &pos) {
+    if (!x.rad || !mv_valid(x.g, vi)) return 0.0f;
+    uint64_t flat = ((uint64_t)vi.z * (uint64_t)x.g.sh[1] + (uint64_t)vi.y) * (uint64_t)x.g.sh[0] +
+                    (uint64_t)vi.x;
+    int k = __ldg(x.rad + flat);
+    if (k == 0) return 0.0f;
+    float f = (float)k * x.free_unit - x.free_eps;
+    if (x.use_rmax) {
+        f3 d{pos.x - x.src_pos.x, pos.y - x.src_pos.y, pos.z - x.src_pos.z};
+        f = fminf(f, x.rmax - mc_sqrt(dot3(d, d)));
+    }
+    return fmaxf(f, 0.0f);
+}
+
+/* Voxel of a position after free flights, clamped into the grid (the
+   position lies inside a homogeneous cube of the grid, so the clamp only
+   absorbs rounding at the cube's faces). */
+static __device__ __forceinline__ i3 mv_index_clamped(const MvGeom &g, const f3 &p) {
+    i3 i = mv_index(g, p);
+    return i3{clip_i(i.x, 0, g.sh[0] - 1), clip_i(i.y, 0, g.sh[1] - 1), clip_i(i.z, 0, g.sh[2] - 1)};
+}
 
 static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvMaterial *M, const float *lut) {
@@ -355,6 +386,7 @@ static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, cons
         x.g.vs[k] = c.voxel_size[k];
         x.g.sh[k] = c.shape[k];
     }
+    x.rmax = c.opt.rmax;
     x.rmax2 = c.opt.rmax * c.opt.rmax;
     x.use_rmax = x.rmax2 < __int_as_float(0x7f800000);
     x.use_trace = c.trace.flags != MCGB_TRACE_NONE;
@@ -362,6 +394,12 @@ static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, cons
     x.max_steps = (c.opt.max_steps_per_packet == 0 || c.opt.max_steps_per_packet > 0xFFFFFFFFull)
                       ? 0xFFFFFFFFu : (uint32_t)c.opt.max_steps_per_packet;
     x.src_pos = f3{c.source.position[0], c.source.position[1], c.source.position[2]};
+    /* Free flight (FAST math, no trace: a trace records every wall stop). */
+    x.rad = (MCGB_FAST_MATH && !x.use_trace) ? b.voxel_radius : nullptr;
+    x.free_unit = fminf(x.g.vs[0], fminf(x.g.vs[1], x.g.vs[2])) * 0.999f;
+    float ext = 0.0f;
+    for (int k = 0; k < 3; ++k) ext = fmaxf(ext, fmaxf(fabsf(x.g.tl[k]), fabsf(x.g.br[k])));
+    x.free_eps = ext * 1e-6f;
     return x;
 }
 
@@ -376,6 +414,8 @@ static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, con
     s.events = MCGB_EV_LAUNCH;
     mcvox_launch<SIMPLE>(c, x.g, x.M, x.vox, x.lut, rng, s.pos, s.dir, s.w, s.vi, s.mat,
                          b.accumulator, prev_pos);
+    s.stale = false;
+    s.free = MCGB_FAST_MATH ? mv_free_radius(x, s.vi, s.pos) : 0.0f;
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -385,11 +425,23 @@ static __device__ __forceinline__ void mcvox_end(const McgbMcvoxConfig &c, const
     if (x.use_trace) b.int_buffer[c.trace.count_offset + s.p] = (int32_t)s.trace_count;
 }
 
-/* One step of McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:760-1038. */
+/* One step of McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:760-1038.
+
+   FAST math adds free flight (albedo weight and albedo rejection): when the
+   sampled free path is shorter than s.free, the radius of a ball around the
+   packet that holds one material, the packet moves the whole path without
+   computing voxel walls and interacts there; s.free shrinks by the path and
+   the voxel index is recomputed from the position at the next step that
+   needs it.  The reference stops at every voxel wall and draws a new path
+   when the next voxel holds the same material; the exponential free path is
+   memoryless, so the interaction points have the same distribution.  Other
+   steps follow the reference exactly and reload s.free from the radius
+   table of the voxel they end in. */
 template <int PF, int METHOD, bool FLU, bool XTRA>
 static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
                                                   FluenceCache &fcache, uint32_t &status) {
+    constexpr bool FREE = MCGB_FAST_MATH && METHOD != MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT;
     const MvMaterial *M = x.M;
     const MvGeom &g = x.g;
     const McgbRunOptions &o = c.opt;
@@ -400,15 +452,26 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) ? mc_div(-mc_log(u), g0.x)
                                                                    : sample_step(u, g0.z);
     step = fminf(step, FLT_MAX);
-    /* mcsim_intersect, mcvox.template.c:173-196 */
+    const bool flight = FREE && step < s.free;
     f3 dist;
-    dist.x = g.tl[0] + (float)((s.dir.x >= 0.0f) + s.vi.x) * g.vs[0] - s.pos.x;
-    dist.y = g.tl[1] + (float)((s.dir.y >= 0.0f) + s.vi.y) * g.vs[1] - s.pos.y;
-    dist.z = g.tl[2] + (float)((s.dir.z >= 0.0f) + s.vi.z) * g.vs[2] - s.pos.z;
-    dist.x = (s.dir.x != 0.0f) ? mc_div(dist.x, s.dir.x) : __int_as_float(0x7f800000);
-    dist.y = (s.dir.y != 0.0f) ? mc_div(dist.y, s.dir.y) : __int_as_float(0x7f800000);
-    dist.z = (s.dir.z != 0.0f) ? mc_div(dist.z, s.dir.z) : __int_as_float(0x7f800000);
-    float d = fminf(dist.x, fminf(dist.y, dist.z));
+    float d;
+    if (flight) {
+        d = __int_as_float(0x7f800000);
+        dist = f3{d, d, d};
+    } else {
+        if (FREE && s.stale) {
+            s.vi = mv_index_clamped(g, s.pos);
+            s.stale = false;
+        }
+        /* mcsim_intersect, mcvox.template.c:173-196 */
+        dist.x = g.tl[0] + (float)((s.dir.x >= 0.0f) + s.vi.x) * g.vs[0] - s.pos.x;
+        dist.y = g.tl[1] + (float)((s.dir.y >= 0.0f) + s.vi.y) * g.vs[1] - s.pos.y;
+        dist.z = g.tl[2] + (float)((s.dir.z >= 0.0f) + s.vi.z) * g.vs[2] - s.pos.z;
+        dist.x = (s.dir.x != 0.0f) ? mc_div(dist.x, s.dir.x) : __int_as_float(0x7f800000);
+        dist.y = (s.dir.y != 0.0f) ? mc_div(dist.y, s.dir.y) : __int_as_float(0x7f800000);
+        dist.z = (s.dir.z != 0.0f) ? mc_div(dist.z, s.dir.z) : __int_as_float(0x7f800000);
+        d = fminf(dist.x, fminf(dist.y, dist.z));
+    }
     float d_ok = fminf(d, step);
     s.pos.x = s.pos.x + d_ok * s.dir.x;
     s.pos.y = s.pos.y + d_ok * s.dir.y;
@@ -457,6 +520,8 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             if (s.vi.z < 0) detector_deposit<XTRA>(c.top, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             else if (s.vi.z >= g.sh[2]) detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             done = true;
+        } else if (FREE) {
+            s.free = mv_free_radius(x, s.vi, s.pos);
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
         if (rng.next() < g0.w) {
@@ -470,6 +535,14 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
             scatter_direction(s.dir, ct, az);
             if (XTRA) s.events |= MCGB_EV_SCATTERING;
+        }
+        if (FREE) {
+            if (flight) {
+                s.free -= step;
+                s.stale = true;
+            } else {
+                s.free = mv_free_radius(x, s.vi, s.pos);
+            }
         }
     } else {
         float deposit = s.w * g0.w;
@@ -486,6 +559,14 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                 else s.w = mc_div(s.w, o.lottery_chance);
             } else {
                 done = true;
+            }
+        }
+        if (FREE) {
+            if (flight) {
+                s.free -= step;
+                s.stale = true;
+            } else {
+                s.free = mv_free_radius(x, s.vi, s.pos);
             }
         }
     }

@@ -102,6 +102,25 @@ McScheduling.dynamic = McScheduling('dynamic')
 McScheduling.default = McScheduling.dynamic
 
 
+class McVoxelFreeFlight(McBoolOption):
+    """Voxelized media with native math only (albedo weight and albedo
+    rejection, no trace): a packet whose sampled free path stays inside a
+    cube of voxels of its own material takes the whole path in one move
+    instead of stopping at every voxel wall and drawing a new path there, as
+    the reference does.  The free path is memoryless, so the interactions
+    have the same distribution; the tallies agree with the reference within
+    the Monte Carlo error.  On by default; off restores the wall-by-wall
+    walk."""
+    on = McBoolOption('MCGB_VOXEL_FREE_FLIGHT', True)
+    off = McBoolOption('MCGB_VOXEL_FREE_FLIGHT', False)
+
+    def __init__(self, value: bool = True):
+        super().__init__('MCGB_VOXEL_FREE_FLIGHT', value)
+
+
+McVoxelFreeFlight.default = McVoxelFreeFlight.on
+
+
 class McUseHalfMath(McBoolOption):
     """Mapped to McUseNativeMath: the GB300 fast path is the narrowest
     precision offered."""

@@ -4,6 +4,7 @@
 ``cl_devices``, ``cl_build_options`` and ``cl_profiling`` are accepted and
 ignored; voxels are uint8 material indices (at most 256 materials).
 """
+import ctypes as C
 import time
 
 import numpy as np
@@ -142,12 +143,35 @@ class Mc(McEngine):
         if self._dev.get('vox_key') != key:
             self._dev['vox'] = torch.from_numpy(vox.reshape(-1).copy()).to(device)
             self._dev['vox_key'] = key
+            self._dev.pop('vox_radius', None)
+        radius = None
+        if cfg.opt.math == _abi.MATH_FAST and self._free_flight():
+            radius = self._voxel_radius(torch, lib, cfg)
         mat_bytes = np.frombuffer(bytes(mats), dtype=np.uint8).copy()
         self._dev['mats'] = torch.from_numpy(mat_bytes).to(device)
         buffers = self._device_buffers(torch, device, self._lut_array(), {
             'voxels': self._dev['vox'].data_ptr(), 'materials': self._dev['mats'].data_ptr(),
-            '_dynamic': dynamic})
+            'voxel_radius': radius, '_dynamic': dynamic})
         return lib.mcgb_mcvox_run, cfg, buffers
+
+    # cap of the homogeneous-cube radius table: beyond about 30 voxels a
+    # longer radius saves few wall stops
+    VOXEL_RADIUS_CAP = 31
+
+    def _free_flight(self) -> bool:
+        return bool(self._resolved_options().get('MCGB_VOXEL_FREE_FLIGHT', True))
+
+    def _voxel_radius(self, torch, lib, cfg):
+        """Device address of the homogeneous-cube radius table of the current
+        voxels (mcgb_voxel_radius), computed once per voxel grid."""
+        if 'vox_radius' not in self._dev:
+            rad = torch.empty_like(self._dev['vox'])
+            shape = (C.c_int32 * 3)(*[int(v) for v in cfg.shape])
+            _lib.check(lib.mcgb_voxel_radius(C.c_void_p(self._dev['vox'].data_ptr()), shape,
+                                             C.c_void_p(rad.data_ptr()), self.VOXEL_RADIUS_CAP,
+                                             C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+            self._dev['vox_radius'] = rad
+        return self._dev['vox_radius'].data_ptr()
 
     def _download(self, nphotons, out):
         accu = self._dev['accu'].cpu().numpy().view(np.uint64)

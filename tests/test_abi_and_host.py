@@ -31,7 +31,7 @@ def test_struct_layouts(lib):
     from pyxopto_gb300 import _abi
     _abi.check_layout(lib.mcgb_sizeof)
     assert lib.mcgb_sizeof(0) == 72 and lib.mcgb_sizeof(5) == 64 and lib.mcgb_sizeof(99) == -1
-    assert lib.mcgb_abi_version() == 1
+    assert lib.mcgb_abi_version() == 3
 
 
 def _valid_cfg():

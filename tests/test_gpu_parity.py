@@ -441,3 +441,75 @@ def test_fast_voxel_fluence_statistically_equal_to_exact(cuda, lib):
     ok, rep = _stats.gate(fa, ea)
     assert ok, rep
     assert abs(fa.sum(1).mean() / ea.sum(1).mean() - 1.0) < 5e-3
+
+
+def _radius_reference(mat, cap):
+    """Largest k <= cap whose cube of voxels within Chebyshev distance k lies
+    inside the grid and holds one material (brute force over k)."""
+    from scipy import ndimage
+    nz, ny, nx = mat.shape
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing='ij')
+    edge = np.minimum.reduce([x, y, z, nx - 1 - x, ny - 1 - y, nz - 1 - z])
+    out = np.zeros(mat.shape, np.int64)
+    m = mat.astype(np.int64)
+    for k in range(1, cap + 1):
+        hi = ndimage.maximum_filter(m, size=2 * k + 1, mode='nearest')
+        lo = ndimage.minimum_filter(m, size=2 * k + 1, mode='nearest')
+        ok = (hi == m) & (lo == m) & (edge >= k)
+        out[ok] = k
+    return out
+
+
+def test_voxel_radius_table_matches_brute_force(cuda, lib):
+    """mcgb_voxel_radius (the free-flight table) against a brute-force
+    search on a grid with layers, a sphere and a thin plate."""
+    import ctypes as C
+    from pyxopto_gb300 import _lib
+    torch = cuda
+    nz, ny, nx = 24, 30, 40
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing='ij')
+    mat = np.ones((nz, ny, nx), np.uint8)
+    mat[z < 3] = 2
+    mat[(x - 20) ** 2 + (y - 14) ** 2 + (z - 12) ** 2 <= 36] = 3
+    mat[(x == 33) & (z > 5)] = 4
+    for cap in (3, 31):
+        dev = torch.from_numpy(mat.reshape(-1).copy()).cuda()
+        rad = torch.full_like(dev, 77)
+        shape = (C.c_int32 * 3)(nx, ny, nz)
+        _lib.check(lib.mcgb_voxel_radius(C.c_void_p(dev.data_ptr()), shape, C.c_void_p(rad.data_ptr()),
+                                         cap, None))
+        got = rad.cpu().numpy().reshape(mat.shape).astype(np.int64)
+        assert np.array_equal(got, _radius_reference(mat, cap)), cap
+
+
+def test_voxel_free_flight_statistically_equal_to_wall_walk(cuda, lib):
+    """Free flight (the FAST-math default in voxelized media) against the
+    reference's wall-by-wall walk in the same FAST kernels, on the 200^3
+    skin and vessel grid: depth profile, 1 mm^3 voxels and the detector
+    totals within the 3-sigma gate; free flight takes far fewer steps."""
+    from pyxopto_gb300.mcvox import mcoptions
+    name, nb, n = 'c3_vox_skin_vessel', 16, 1_000_000
+    fly = scenarios.build_mc(name, fast=True, scheduling='dynamic')
+    walk = scenarios.build_mc(name, fast=True, scheduling='dynamic')
+    walk._mc_options.append(mcoptions.McVoxelFreeFlight(False))
+    walk._rnginit = 4321
+
+    def batches(mc):
+        rows, tops, steps = [], [], 0
+        for _ in range(nb):
+            _, flu, det = mc.run(n)
+            raw = np.asarray(flu.raw, dtype=np.float64)
+            rows.append(raw)
+            tops.append([float(det.top.raw.sum()), float(det.bottom.raw.sum())])
+            steps += mc.run_report['steps']
+        return np.array(rows) / n, np.array(tops) / n, steps
+    fa, ta, sa = batches(fly)
+    wa, tw, sw = batches(walk)
+    depth = lambda f: f.reshape(nb, 200, -1).sum(2)
+    coarse = lambda f: f.reshape(nb, 10, 20, 10, 20, 10, 20).sum(axis=(2, 4, 6)).reshape(nb, -1)
+    for what, a, b in (('depth', depth(fa), depth(wa)), ('coarse', coarse(fa), coarse(wa)),
+                       ('totals', ta, tw)):
+        keep = (b.mean(0) > 0) & (b.std(0, ddof=1) / np.sqrt(nb) < 0.2 * b.mean(0))
+        ok, rep = _stats.gate(a[:, keep], b[:, keep])
+        assert ok, (what, rep)
+    assert sa < 0.8 * sw, (sa, sw)
