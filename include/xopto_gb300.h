@@ -106,7 +106,18 @@ enum { MCGB_PF_EXT_HG2 = 0,                /* xopto/mcbase/mcpf/hg2.py:102-130 *
        MCGB_PF_EXT_MHG = 1,                /* xopto/mcbase/mcpf/mhg.py:87-109  */
        MCGB_PF_EXT_PC = 2,                 /* xopto/mcbase/mcpf/pc.py:80-92    */
        MCGB_PF_EXT_MPC = 3,                /* xopto/mcbase/mcpf/mpc.py:88-106  */
-       MCGB_PF_EXT_MGK = 4 };              /* xopto/mcbase/mcpf/mgk.py:110-140 */
+       MCGB_PF_EXT_MGK = 4,                /* xopto/mcbase/mcpf/mgk.py:110-140 */
+       MCGB_PF_EXT_GK2 = 5,                /* xopto/mcbase/mcpf/gk2.py:119-159 */
+       MCGB_PF_EXT_HGA = 6,                /* xopto/mcbase/mcpf/hga.py:82-99   */
+       MCGB_PF_EXT_HGDIR = 7 };            /* xopto/mcbase/mcpf/hgdir.py:100-120 */
+/* Parameters of the analytic kinds: McgbPf.p holds them in the order of the
+   reference's packed struct (Hg2: g1, g2, b; MHg: g, b; Pc: n; MPc: n, b;
+   MGk: g, b, inv_a, a1, a2; HgDir: direction x, y, z, g, p).  Gk2 and Hga
+   keep theirs in the float LUT at McgbPf.lut_offset: Gk2 the 11 floats
+   (g, a, inv_a, a1, a2) of each term and b; Hga the 3x3 anisotropy tensor,
+   row major. */
+#define MCGB_PF_GK2_FLOATS 11u
+#define MCGB_PF_HGA_FLOATS 9u
 enum {
     MCGB_SRC_LINE = 0,
     MCGB_SRC_GAUSSIAN_BEAM = 1,

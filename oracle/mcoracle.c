@@ -204,10 +204,30 @@ static void scatter_direction(int mm, v3 *dir, float cos_theta, float fi) {
    Lut: xopto/mcbase/mcpf/lut.py:125-155
    Hg2: xopto/mcbase/mcpf/hg2.py:102-130    MHg: xopto/mcbase/mcpf/mhg.py:87-109
    Pc:  xopto/mcbase/mcpf/pc.py:80-92       MPc: xopto/mcbase/mcpf/mpc.py:88-106
-   MGk: xopto/mcbase/mcpf/mgk.py:110-140 */
+   MGk: xopto/mcbase/mcpf/mgk.py:110-140
+   Gk2: xopto/mcbase/mcpf/gk2.py:119-159   Hga: xopto/mcbase/mcpf/hga.py:82-99
+   HgDir: xopto/mcbase/mcpf/hgdir.py:100-120 (mcsim_pf_sample_dir: the
+   direction becomes the axis to rotate about, the azimuth is drawn last) */
 static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
-                       uint64_t *x, uint32_t a, float *azimuth) {
+                       uint64_t *x, uint32_t a, float *azimuth, v3 *dir) {
     float cos_theta;
+    if (kind == MCGB_PF_EXT && pf->ext_kind == MCGB_PF_EXT_HGDIR) {
+        float g = pf->p[3];
+        float k = (1.0f - g * g) / (1.0f + g * (2.0f * rnd(x, a) - 1.0f));
+        cos_theta = (1.0f + g * g - k * k) / (2.0f * g);
+        if (g == 0.0f) cos_theta = 1.0f - 2.0f * rnd(x, a);
+        cos_theta = fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        v3 axis = *dir;
+        if (rnd(x, a) < pf->p[4]) {
+            axis.x = pf->p[0];
+            axis.y = pf->p[1];
+            axis.z = pf->p[2];
+        }
+        if (dot3(*dir, axis) < 0.0f) cos_theta = -cos_theta;
+        *dir = axis;
+        *azimuth = 6.28318548f * rnd(x, a);
+        return cos_theta;
+    }
     if (kind == MCGB_PF_HG) {
         float g = pf->p[0];
         *azimuth = 6.28318548f * rnd(x, a);
@@ -232,6 +252,33 @@ static float pf_sample(int mm, int kind, const McgbPf *pf, const float *lut,
         return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
     } else if (kind == MCGB_PF_EXT) {
         *azimuth = 6.28318548f * rnd(x, a);
+        if (pf->ext_kind == MCGB_PF_EXT_HGA) {
+            /* tensor3f_project, xopto/mcbase/kernel/mcbase.template.h:2227-2230 */
+            const float *T = lut + pf->lut_offset;
+            v3 p = *dir;
+            float g = p.x * (T[0] * p.x + T[1] * p.y + T[2] * p.z) +
+                      p.y * (T[3] * p.x + T[4] * p.y + T[5] * p.z) +
+                      p.z * (T[6] * p.x + T[7] * p.y + T[8] * p.z);
+            float k = (1.0f - g * g) / (1.0f + g * (2.0f * rnd(x, a) - 1.0f));
+            cos_theta = (1.0f + g * g - k * k) / (2.0f * g);
+            if (g == 0.0f) cos_theta = 1.0f - 2.0f * rnd(x, a);
+            return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        }
+        if (pf->ext_kind == MCGB_PF_EXT_GK2) {
+            const float *q = lut + pf->lut_offset;
+            if (rnd(x, a) < q[10]) q += 5;
+            float g = q[0];
+            if (g == 0.0f) {
+                cos_theta = 1.0f - 2.0f * rnd(x, a);
+            } else if (q[1] == 0.0f) {
+                cos_theta = q[3] + m_pow(mm, (1.0f - g) / (1.0f + g), 2.0f * rnd(x, a)) * q[4];
+            } else {
+                float tmp = q[3] * rnd(x, a) + q[4];
+                tmp = 1.0f + g * g - m_pow(mm, tmp, -q[2]);
+                cos_theta = tmp / (2.0f * g);
+            }
+            return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
+        }
         if (pf->ext_kind == MCGB_PF_EXT_HG2) {
             float g = rnd(x, a) >= pf->p[2] ? pf->p[0] : pf->p[1];
             float k = (1.0f - g * g) / (1.0f + g * (2.0f * rnd(x, a) - 1.0f));
@@ -989,7 +1036,7 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                         done = 1;
                     }
                 } else {
-                    float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az);
+                    float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az, &s.dir);
                     scatter_direction(mm, &s.dir, ct, az);
                     events |= EV_SCATTERING;
                 }
@@ -1021,7 +1068,7 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                         if (c->fluence.kind != MCGB_FLUENCE_NONE)
                             fluence_deposit(&c->fluence, s.pos, deposit, L->mua, accu);
                     } else {
-                        float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az);
+                        float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az, &s.dir);
                         scatter_direction(mm, &s.dir, ct, az);
                         events |= EV_SCATTERING;
                     }
@@ -1032,7 +1079,7 @@ static uint64_t mcml_stream(int mm, const McgbMcmlConfig *c, const float *lut,
                     events |= EV_ABSORPTION;
                     if (c->fluence.kind != MCGB_FLUENCE_NONE)
                         fluence_deposit(&c->fluence, s.pos, deposit, L->mua, accu);
-                    float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az);
+                    float az, ct = pf_sample(mm, c->pf_kind, &L->pf, lut, &x, a, &az, &s.dir);
                     scatter_direction(mm, &s.dir, ct, az);
                     events |= EV_SCATTERING;
                     if (s.w < o->packet_weight_min) {
@@ -1457,7 +1504,7 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                         done = 1;
                     }
                 } else {
-                    float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az);
+                    float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az, &s.dir);
                     scatter_direction(mm, &s.dir, ct, az);
                     events |= EV_SCATTERING;
                 }
@@ -1488,7 +1535,7 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                         if (c->fluence.kind != MCGB_FLUENCE_NONE)
                             fluence_deposit(&c->fluence, s.pos, deposit, M->mua, accu);
                     } else {
-                        float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az);
+                        float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az, &s.dir);
                         scatter_direction(mm, &s.dir, ct, az);
                         events |= EV_SCATTERING;
                     }
@@ -1498,7 +1545,7 @@ static uint64_t mcvox_stream(int mm, const McgbMcvoxConfig *c, const McgbMateria
                     events |= EV_ABSORPTION;
                     if (c->fluence.kind != MCGB_FLUENCE_NONE)
                         fluence_deposit(&c->fluence, s.pos, deposit, M->mua, accu);
-                    float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az);
+                    float az, ct = pf_sample(mm, c->pf_kind, &M->pf, lut, &x, a, &az, &s.dir);
                     scatter_direction(mm, &s.dir, ct, az);
                     events |= EV_SCATTERING;
                     if (s.w < o->packet_weight_min) {

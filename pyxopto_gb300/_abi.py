@@ -20,6 +20,8 @@ SCHED_STATIC, SCHED_DYNAMIC = 0, 1
 METHOD_ALBEDO_WEIGHT, METHOD_ALBEDO_REJECTION, METHOD_MICROSCOPIC_BEER_LAMBERT = 0, 1, 2
 PF_HG, PF_GK, PF_LUT, PF_EXT = 0, 1, 2, 3
 PF_EXT_HG2, PF_EXT_MHG, PF_EXT_PC, PF_EXT_MPC, PF_EXT_MGK = 0, 1, 2, 3, 4
+PF_EXT_GK2, PF_EXT_HGA, PF_EXT_HGDIR = 5, 6, 7
+PF_GK2_FLOATS, PF_HGA_FLOATS = 11, 9
 SRC_LINE, SRC_GAUSSIAN_BEAM, SRC_UNIFORM_FIBER_NI, SRC_LAMBERTIAN_FIBER_NI = 0, 1, 2, 3
 SRC_UNIFORM_FIBER, SRC_LAMBERTIAN_FIBER, SRC_UNIFORM_BEAM, SRC_ISOTROPIC_POINT = 4, 5, 6, 7
 SRC_ISOTROPIC_VOXEL = 8

@@ -206,7 +206,7 @@ batched_kernel(const McgbBatchConfig cfg, const uint32_t *__restrict__ mult,
             } else {
                 float deposit = w * g0.w;
                 w -= deposit;
-                float az, ct = pf_sample<MCGB_PF_HG>(L[layer].pf0, L[layer].pf1, nullptr, rng, &az);
+                float az, ct = pf_sample<MCGB_PF_HG>(L[layer].pf0, L[layer].pf1, nullptr, rng, &az, dir);
                 scatter_direction(dir, ct, az);
                 if (w < 1e-4f) {
                     if (rng.next() > 0.1f) done = true;

@@ -48,8 +48,14 @@ bool range_ok(uint64_t offset, uint64_t count, uint64_t size) {
 }
 
 int check_pf(int kind, const McgbPf &pf, const McgbBuffers *b, const char *who, unsigned idx) {
-    if (kind == MCGB_PF_EXT && pf.ext_kind > MCGB_PF_EXT_MGK)
+    if (kind == MCGB_PF_EXT && pf.ext_kind > MCGB_PF_EXT_HGDIR)
         return fail(MCGB_E_INVALID, "%s %u: unknown analytic phase function %u", who, idx, pf.ext_kind);
+    if (kind == MCGB_PF_EXT && (pf.ext_kind == MCGB_PF_EXT_GK2 || pf.ext_kind == MCGB_PF_EXT_HGA)) {
+        uint32_t n = pf.ext_kind == MCGB_PF_EXT_GK2 ? MCGB_PF_GK2_FLOATS : MCGB_PF_HGA_FLOATS;
+        if (!b->fp_lut || !range_ok(pf.lut_offset, n, b->fp_lut_size))
+            return fail(MCGB_E_SIZE, "%s %u: phase-function parameters [%u, +%u) beyond the LUT buffer "
+                        "(%llu floats)", who, idx, pf.lut_offset, n, (unsigned long long)b->fp_lut_size);
+    }
     if (kind == MCGB_PF_LUT) {
         if (!b->fp_lut) return fail(MCGB_E_INVALID, "%s %u: Lut phase function without a LUT buffer", who, idx);
         if (pf.lut_size < 2) return fail(MCGB_E_INVALID, "%s %u: Lut size %u < 2", who, idx, pf.lut_size);

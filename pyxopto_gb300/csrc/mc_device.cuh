@@ -229,7 +229,8 @@ MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
         pf1 = make_float4(pf.p[4], 1.0f + g * g, pf_2g(g), mc_div(1.0f - g, 1.0f + g));
     } else if (kind == MCGB_PF_EXT) {
         pf0 = make_float4(pf.p[0], pf.p[1], pf.p[2], pf.p[3]);
-        pf1 = make_float4(pf.p[4], 0.0f, 0.0f, __int_as_float((int)pf.ext_kind));
+        pf1 = make_float4(pf.p[4], __int_as_float((int)pf.lut_offset), 0.0f,
+                          __int_as_float((int)pf.ext_kind));
     } else {
         uint32_t n1 = pf.lut_size - 1u;
         pf0 = make_float4(pf.p[0], pf.p[1], pf.p[2], (float)n1);
@@ -237,16 +238,33 @@ MCGB_DEV void pf_prepare(int kind, const McgbPf &pf, float4 &pf0, float4 &pf1) {
     }
 }
 
-/* Phase-function sampling.  Returns cos(theta); the azimuth is drawn first,
-   as in the reference.
+/* Phase-function sampling.  Returns cos(theta) of the new direction about
+   the axis ``dir`` and the azimuth, in the reference's order of draws (the
+   azimuth first, except for HgDir).  ``dir`` holds the packet's direction
+   on entry; HgDir replaces it with the axis it scatters about, the
+   phase function's own direction with probability p (the reference's
+   mcsim_pf_sample_dir, whose caller rotates that axis).
    Hg:  xopto/mcbase/mcpf/hg.py:80-95
    Gk:  xopto/mcbase/mcpf/gk.py:102-124
    Lut: xopto/mcbase/mcpf/lut.py:125-155
    Ext: Hg2 xopto/mcbase/mcpf/hg2.py:102-130, MHg mhg.py:87-109,
-        Pc pc.py:80-92, MPc mpc.py:88-106, MGk mgk.py:110-140 */
+        Pc pc.py:80-92, MPc mpc.py:88-106, MGk mgk.py:110-140,
+        Gk2 gk2.py:119-159, Hga hga.py:82-99, HgDir hgdir.py:100-120 */
 template <int PF>
 MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut, Rng &rng,
-                         float *azimuth) {
+                         float *azimuth, f3 &dir) {
+    if (PF == MCGB_PF_EXT && __float_as_int(pf1.w) == MCGB_PF_EXT_HGDIR) {
+        float g = pf0.w;
+        float k = mc_div(1.0f - g * g, 1.0f + g * (2.0f * rng.next() - 1.0f));
+        float cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
+        if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
+        cos_theta = fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        f3 axis = rng.next() < pf1.x ? f3{pf0.x, pf0.y, pf0.z} : dir;
+        if (dot3(dir, axis) < 0.0f) cos_theta = -cos_theta;
+        dir = axis;
+        *azimuth = 6.28318548f * rng.next();
+        return cos_theta;
+    }
     *azimuth = 6.28318548f * rng.next();
     if (PF == MCGB_PF_HG) {
         float g = pf0.x;
@@ -269,6 +287,34 @@ MCGB_DEV float pf_sample(const float4 &pf0, const float4 &pf1, const float *lut,
     } else if (PF == MCGB_PF_EXT) {
         int ext = __float_as_int(pf1.w);
         float cos_theta;
+        if (ext == MCGB_PF_EXT_HGA) {
+            /* Hg with g = dir^T G dir (tensor3f_project,
+               xopto/mcbase/kernel/mcbase.template.h:2227-2230) */
+            const float *T = lut + __float_as_int(pf1.y);
+            float g = dir.x * (T[0] * dir.x + T[1] * dir.y + T[2] * dir.z) +
+                      dir.y * (T[3] * dir.x + T[4] * dir.y + T[5] * dir.z) +
+                      dir.z * (T[6] * dir.x + T[7] * dir.y + T[8] * dir.z);
+            float k = mc_div(1.0f - g * g, 1.0f + g * (2.0f * rng.next() - 1.0f));
+            cos_theta = mc_div(1.0f + g * g - k * k, 2.0f * g);
+            if (g == 0.0f) cos_theta = 1.0f - 2.0f * rng.next();
+            return fmaxf(fminf(cos_theta, 1.0f), -1.0f);
+        }
+        if (ext == MCGB_PF_EXT_GK2) {
+            /* the first term when u >= b, else the second */
+            const float *q = lut + __float_as_int(pf1.y);
+            if (rng.next() < q[10]) q += 5;
+            float g = q[0];
+            if (g == 0.0f) {
+                cos_theta = 1.0f - 2.0f * rng.next();
+            } else if (q[1] == 0.0f) {
+                cos_theta = q[3] + mc_pow(mc_div(1.0f - g, 1.0f + g), 2.0f * rng.next()) * q[4];
+            } else {
+                float tmp = q[3] * rng.next() + q[4];
+                tmp = 1.0f + g * g - mc_pow(tmp, -q[2]);
+                cos_theta = mc_div(tmp, 2.0f * g);
+            }
+            return fminf(fmaxf(cos_theta, -1.0f), 1.0f);
+        }
         if (ext == MCGB_PF_EXT_HG2) {
             /* component 1 when u >= b, else component 2 */
             float g = rng.next() >= pf0.z ? pf0.x : pf0.y;

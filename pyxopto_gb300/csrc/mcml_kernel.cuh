@@ -559,7 +559,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             }
         } else {
             const MlLayer &cl = L[s.layer];
-            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
+            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az, s.dir);
             scatter_direction(s.dir, ct, az);
             if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
@@ -588,7 +588,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         } else {
             const MlLayer &cl = L[s.layer];
-            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
+            float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az, s.dir);
             scatter_direction(s.dir, ct, az);
             if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
@@ -599,7 +599,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         if (XTRA) s.events |= MCGB_EV_ABSORPTION;
         if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         const MlLayer &cl = L[s.layer];
-        float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az);
+        float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az, s.dir);
         scatter_direction(s.dir, ct, az);
         if (XTRA) s.events |= MCGB_EV_SCATTERING;
         if (s.w < o.packet_weight_min) {

@@ -502,7 +502,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             }
         } else {
             const MvMaterial &cm = M[s.mat];
-            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
+            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az, s.dir);
             scatter_direction(s.dir, ct, az);
             if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
@@ -532,7 +532,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
         } else {
             const MvMaterial &cm = M[s.mat];
-            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
+            float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az, s.dir);
             scatter_direction(s.dir, ct, az);
             if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
@@ -550,7 +550,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         if (XTRA) s.events |= MCGB_EV_ABSORPTION;
         if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
         const MvMaterial &cm = M[s.mat];
-        float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az);
+        float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az, s.dir);
         scatter_direction(s.dir, ct, az);
         if (XTRA) s.events |= MCGB_EV_SCATTERING;
         if (s.w < o.packet_weight_min) {

@@ -1,7 +1,8 @@
 """Scattering phase functions: Henyey-Greenstein, Gegenbauer kernel, lookup
-table and the analytic mixtures Hg2, MHg, Pc and MPc, with the reference's
-names and parameters (xopto/mcbase/mcpf/hg.py, gk.py, lut.py, hg2.py, mhg.py,
-pc.py, mpc.py).
+table, the analytic mixtures Hg2, MHg, Pc, MPc, MGk and Gk2, the
+anisotropic Hga and the directional HgDir, with the reference's names and
+parameters (xopto/mcbase/mcpf/hg.py, gk.py, lut.py, hg2.py, mhg.py, pc.py,
+mpc.py, mgk.py, gk2.py, hga.py, hgdir.py).
 
 Each object packs itself into the ``McgbPf`` struct that the GB300 kernels
 read from their shared-memory layer/material table.
@@ -271,7 +272,146 @@ class MGk(Gk):
         return 'MGk(g={}, a={}, b={})'.format(self.g, self.a, self._b)
 
 
+class Gk2(PfBase):
+    """Mixture of two Gegenbauer kernel phase functions,
+    (1 - b)*Gk(g1, a1) + b*Gk(g2, a2), the first forward (0 <= g1 <= 1), the
+    second backward (-1 <= g2 <= 0) (xopto/mcbase/mcpf/gk2.py:30-300).  The
+    eleven packed floats (each term's g, a and its Gk sampling constants,
+    then b) go to the simulator's float LUT."""
+    kind = _abi.PF_EXT
+    ext_kind = _abi.PF_EXT_GK2
+
+    def __init__(self, g1: float, a1: float, g2: float, a2: float, b: float):
+        self._gk1 = Gk(min(max(float(g1), 0.0), 1.0), a1)
+        self._gk2 = Gk(min(max(float(g2), -1.0), 0.0), a2)
+        self._b = min(max(float(b), 0.0), 1.0)
+
+    g1 = property(lambda self: self._gk1.g,
+                  lambda self, g: setattr(self._gk1, 'g', min(max(float(g), 0.0), 1.0)),
+                  None, 'Parameter g of the first (forward) term.')
+    a1 = property(lambda self: self._gk1.a, lambda self, a: setattr(self._gk1, 'a', a),
+                  None, 'Parameter alpha of the first term.')
+    g2 = property(lambda self: self._gk2.g,
+                  lambda self, g: setattr(self._gk2, 'g', min(max(float(g), -1.0), 0.0)),
+                  None, 'Parameter g of the second (backward) term.')
+    a2 = property(lambda self: self._gk2.a, lambda self, a: setattr(self._gk2, 'a', a),
+                  None, 'Parameter alpha of the second term.')
+    b = property(lambda self: self._b,
+                 lambda self, b: setattr(self, '_b', min(max(float(b), 0.0), 1.0)),
+                 None, 'Relative contribution of the second term.')
+
+    def params(self):
+        out = []
+        for gk in (self._gk1, self._gk2):
+            out += [gk.g, gk.a] + list(gk._precalculated)
+        return out + [self._b]
+
+    def pack(self, mc, target):
+        target.lut_offset = mc.append_r_lut(np.asarray(self.params(), dtype=np.float32))
+        target.lut_size = _abi.PF_GK2_FLOATS
+        target.ext_kind = self.ext_kind
+        return target
+
+    def todict(self):
+        return {'g1': self.g1, 'a1': self.a1, 'g2': self.g2, 'a2': self.a2, 'b': self._b,
+                'type': 'Gk2'}
+
+    def __str__(self):
+        return 'Gk2(g1={}, a1={}, g2={}, a2={}, b={})'.format(self.g1, self.a1, self.g2, self.a2,
+                                                            self._b)
+
+
+class Hga(PfBase):
+    """Anisotropic Henyey-Greenstein phase function: the anisotropy factor
+    is the projection p^T G p of the 3x3 tensor G on the propagation
+    direction p (xopto/mcbase/mcpf/hga.py:25-200).  A scalar g gives
+    G = g I; three values the diagonal.  The nine tensor floats go to the
+    simulator's float LUT."""
+    kind = _abi.PF_EXT
+    ext_kind = _abi.PF_EXT_HGA
+
+    def __init__(self, g):
+        self._g = np.zeros((3, 3))
+        self.g = g
+
+    def _get_g(self):
+        return self._g
+
+    def _set_g(self, g):
+        if isinstance(g, (float, int)):
+            v = min(max(float(g), -1.0), 1.0)
+            self._g[0, 0] = self._g[1, 1] = self._g[2, 2] = v
+        else:
+            g = np.asarray(g, dtype=float)
+            if g.size == 3:
+                g = np.clip(g, -1.0, 1.0)
+                self._g[0, 0], self._g[1, 1], self._g[2, 2] = g.ravel()
+            else:
+                self._g[:] = np.clip(g.reshape(3, 3), -1.0, 1.0)
+
+    g = property(_get_g, _set_g, None, 'Anisotropy tensor.')
+
+    def pack(self, mc, target):
+        target.lut_offset = mc.append_r_lut(np.asarray(self._g, dtype=np.float32).ravel())
+        target.lut_size = _abi.PF_HGA_FLOATS
+        target.ext_kind = self.ext_kind
+        return target
+
+    def todict(self):
+        return {'g': self._g.tolist(), 'type': 'Hga'}
+
+    def __str__(self):
+        return 'Hga(g={})'.format(self._g.tolist())
+
+
+class HgDir(PfBase):
+    """Directional Henyey-Greenstein phase function: with probability p the
+    packet scatters about the fixed unit ``direction`` (the polar angle
+    turned so that the new direction stays on the side of the packet's
+    current one), otherwise about its current direction
+    (xopto/mcbase/mcpf/hgdir.py:25-230)."""
+    kind = _abi.PF_EXT
+    ext_kind = _abi.PF_EXT_HGDIR
+
+    def __init__(self, g: float, direction=(0.0, 0.0, 1.0), p: float = 1.0):
+        self._direction = np.array((0.0, 0.0, 1.0))
+        self.direction = direction
+        self.g = g
+        self.p = p
+
+    g = property(lambda self: self._g,
+                 lambda self, g: setattr(self, '_g', min(max(float(g), -1.0), 1.0)),
+                 None, 'Anisotropy factor.')
+    p = property(lambda self: self._p,
+                 lambda self, p: setattr(self, '_p', min(max(float(p), 0.0), 1.0)),
+                 None, 'Probability of directional scattering.')
+
+    def _get_direction(self):
+        return self._direction
+
+    def _set_direction(self, direction):
+        d = np.asarray(direction, dtype=float).ravel()
+        norm = np.linalg.norm(d)
+        if norm == 0.0:
+            raise ValueError('The norm/length of the scattering direction vector must not be 0!')
+        self._direction[:] = d / norm
+
+    direction = property(_get_direction, _set_direction, None, 'Scattering direction.')
+
+    def pack(self, mc, target):
+        for i, value in enumerate(list(self._direction) + [self._g, self._p]):
+            target.p[i] = value
+        target.ext_kind = self.ext_kind
+        return target
+
+    def todict(self):
+        return {'g': self._g, 'direction': self._direction.tolist(), 'p': self._p, 'type': 'HgDir'}
+
+    def __str__(self):
+        return 'HgDir(g={}, direction={}, p={})'.format(self._g, self._direction.tolist(), self._p)
+
+
 def pf_fromdict(data: dict) -> PfBase:
     kinds = {'Hg': Hg, 'Gk': Gk, 'Lut': Lut, 'Hg2': Hg2, 'MHg': MHg, 'Pc': Pc, 'MPc': MPc,
-             'MGk': MGk}
+             'MGk': MGk, 'Gk2': Gk2, 'Hga': Hga, 'HgDir': HgDir}
     return kinds[data['type']].fromdict(data)

@@ -83,6 +83,40 @@ SCENARIOS = {
         source=dict(type='Line'),
         detectors=dict(top=dict(type='Radial', axis=[0.0, 4e-3, 40]), specular=dict(type='Total')),
         nphotons=3000, streams=40, rnginit=25),
+    # the two-term Gegenbauer kernel (xopto/mcbase/mcpf/gk2.py), with an
+    # isotropic first term and a zero alpha, the anisotropic Hga
+    # (xopto/mcbase/mcpf/hga.py) and the directional HgDir
+    # (xopto/mcbase/mcpf/hgdir.py)
+    'pf_gk2_radial': dict(
+        medium='mcml',
+        layers=[_air(['Gk2', 0.0, 0.5, 0.0, 0.5, 0.0]),
+                dict(d=1.5e-3, n=1.4, mua=120.0, mus=1.2e4, pf=['Gk2', 0.9, 0.5, -0.3, 0.8, 0.2]),
+                dict(d=1e-3, n=1.4, mua=80.0, mus=1e4, pf=['Gk2', 0.0, 0.5, -0.6, 0.0, 0.5]),
+                dict(d=INF, n=1.4, mua=40.0, mus=8e3, pf=['Gk2', 0.8, 0.0, -0.5, 1.2, 0.4]),
+                _air(['Gk2', 0.0, 0.5, 0.0, 0.5, 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 4e-3, 40]), specular=dict(type='Total')),
+        nphotons=3000, streams=40, rnginit=31),
+    'pf_hga_fluence': dict(
+        medium='mcml',
+        layers=[_air(['Hga', 0.0]),
+                dict(d=1e-3, n=1.37, mua=100.0, mus=1e4, pf=['Hga', [0.9, 0.7, 0.8]]),
+                dict(d=INF, n=1.4, mua=50.0, mus=1.2e4,
+                     pf=['Hga', [[0.8, 0.05, 0.0], [0.05, 0.6, 0.1], [0.0, 0.1, 0.9]]]),
+                _air(['Hga', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), specular=dict(type='Total')),
+        fluence=dict(x=[-2e-3, 2e-3, 8], y=[-2e-3, 2e-3, 8], z=[0.0, 4e-3, 8], mode='deposition'),
+        nphotons=2000, streams=32, rnginit=32),
+    'pf_hgdir_radial': dict(
+        medium='mcml',
+        layers=[_air(['HgDir', 0.0, [0.0, 0.0, 1.0], 1.0]),
+                dict(d=1e-3, n=1.4, mua=100.0, mus=1e4, pf=['HgDir', 0.8, [0.3, 0.0, 1.0], 0.5]),
+                dict(d=INF, n=1.4, mua=60.0, mus=9e3, pf=['HgDir', 0.0, [0.0, 0.5, -1.0], 0.7]),
+                _air(['HgDir', 0.0, [0.0, 0.0, 1.0], 1.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30]), specular=dict(type='Total')),
+        nphotons=3000, streams=40, rnginit=33),
     'pf_pc_rejection': dict(
         medium='mcml',
         layers=[_air(['Pc', 1.0]), dict(d=3e-3, n=1.33, mua=150.0, mus=1e4, pf=['Pc', 12.0]),
@@ -153,6 +187,19 @@ SCENARIOS = {
         fluence=dict(x=[-1.2e-3, 1.2e-3, 16], y=[-1.2e-3, 1.2e-3, 16], z=[0.0, 2.4e-3, 16],
                      mode='deposition'),
         nphotons=1500, streams=32, rnginit=24),
+    'pf_hgdir_vox_cylinder': dict(
+        medium='mcvox',
+        grid=dict(x=[-1.2e-3, 1.2e-3, 16], y=[-1.2e-3, 1.2e-3, 16], z=[0.0, 2.4e-3, 16]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['HgDir', 0.0, [0.0, 0.0, 1.0], 1.0]),
+                   dict(n=1.40, mua=20.0, mus=1.5e4, pf=['HgDir', 0.85, [0.0, 0.0, 1.0], 0.6]),
+                   dict(n=1.40, mua=150.0, mus=2e4, pf=['HgDir', 0.7, [1.0, 0.0, 0.2], 0.3]),
+                   dict(n=1.33, mua=2000.0, mus=1.5e4, pf=['HgDir', 0.9, [0.0, 1.0, 0.0], 0.9])],
+        layout=dict(kind='skin_vessel', epidermis=1e-4, vessel_depth=1.0e-3, vessel_radius=4e-4),
+        source=dict(type='GaussianBeam', sigma=3e-4, clip=5.0),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 1.2e-3, 12]), bottom=dict(type='Total')),
+        fluence=dict(x=[-1.2e-3, 1.2e-3, 16], y=[-1.2e-3, 1.2e-3, 16], z=[0.0, 2.4e-3, 16],
+                     mode='deposition'),
+        nphotons=1500, streams=32, rnginit=34),
     'vox_line_gk_oblique': dict(
         medium='mcvox',
         grid=dict(x=[-1e-3, 1e-3, 10], y=[-1e-3, 1e-3, 12], z=[0.0, 1.5e-3, 8]),
@@ -681,8 +728,20 @@ def _pf(pkg, spec):
         return pkg.mcpf.Hg(spec[1])
     if spec[0] == 'Gk':
         return pkg.mcpf.Gk(spec[1], spec[2])
-    if spec[0] in ('Hg2', 'MHg', 'Pc', 'MPc', 'MGk'):
+    if spec[0] in ('Hg2', 'MHg', 'Pc', 'MPc', 'MGk', 'Gk2'):
         return _ext_pf_class(pkg, spec[0])(*spec[1:])
+    if spec[0] == 'Hga':
+        g = np.asarray(spec[1], dtype=float)
+        if g.size != 9:
+            return pkg.mcpf.Hga(spec[1])
+        # the reference's Hga setter cannot take a full tensor
+        # (xopto/mcbase/mcpf/hga.py:131 compares an array with a float), so
+        # the tensor is written into its array after construction
+        pf = pkg.mcpf.Hga(0.0)
+        pf._g[:] = np.clip(g.reshape(3, 3), -1.0, 1.0)
+        return pf
+    if spec[0] == 'HgDir':
+        return pkg.mcpf.HgDir(spec[1], direction=tuple(spec[2]), p=spec[3])
     params, table = lut_table()
     return pkg.mcpf.Lut(params, table)
 
