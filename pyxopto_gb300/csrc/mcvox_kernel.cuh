@@ -427,16 +427,19 @@ static __device__ __forceinline__ void mcvox_end(const McgbMcvoxConfig &c, const
 
 /* One step of McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:760-1038.
 
-   FAST math adds free flight (albedo weight and albedo rejection): when the
-   sampled free path is shorter than s.free, the radius of a ball around the
-   packet that holds one material, the packet moves the whole path without
-   computing voxel walls and interacts there; s.free shrinks by the path and
-   the voxel index is recomputed from the position at the next step that
-   needs it.  The reference stops at every voxel wall and draws a new path
-   when the next voxel holds the same material; the exponential free path is
-   memoryless, so the interaction points have the same distribution.  Other
-   steps follow the reference exactly and reload s.free from the radius
-   table of the voxel they end in. */
+   FAST math adds free flight (albedo weight and albedo rejection).  s.free
+   is the radius of a ball around the packet that holds one material.  A
+   sampled free path shorter than s.free is taken in one move without
+   computing voxel walls, the packet interacts there, s.free shrinks by the
+   path, and the voxel index is recomputed from the position at the next
+   step that needs it.  A longer path first moves the packet through the
+   ball to its surface and continues with the remainder of the path, from
+   there exactly as the reference's walk; that step reloads s.free from the
+   radius table of the voxel it ends in.  The reference stops at every voxel
+   wall and draws a new path when the next voxel holds the same material;
+   the exponential free path is memoryless (the remainder of a path known to
+   exceed the radius is again exponential), so the interaction points have
+   the same distribution. */
 template <int PF, int METHOD, bool FLU, bool XTRA>
 static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
@@ -453,6 +456,18 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                                                                    : sample_step(u, g0.z);
     step = fminf(step, FLT_MAX);
     const bool flight = FREE && step < s.free;
+    if (FREE && !flight && s.free > 0.0f) {
+        /* The path reaches beyond the ball: move through it without an
+           interaction and go on with the remainder, which is again
+           exponential; the reference's walk then continues from there. */
+        s.pos.x = s.pos.x + s.free * s.dir.x;
+        s.pos.y = s.pos.y + s.free * s.dir.y;
+        s.pos.z = s.pos.z + s.free * s.dir.z;
+        if (XTRA && x.track_opl) s.opl += M[s.mat].g1.x * s.free;
+        step -= s.free;
+        s.free = 0.0f;
+        s.stale = true;
+    }
     f3 dist;
     float d;
     if (flight) {
