@@ -676,6 +676,13 @@ int mcgb_mlp_loss_grad(const float *dev_y, const float *dev_t, const float *dev_
                        uint16_t *dev_dy, float *dev_loss, int m, int n, int n_valid, int mode,
                        float scale, void *stream);
 
+/* Weight gradient of an input fed as two columns (the high and the low bf16
+   part of one FP32 value, so that the FP32-accumulating GEMM sees the input
+   at about 16 bits instead of bf16's 8): for j < count, dW[r, j] and
+   dW[r, j + shift] both become their sum (rows x cols row-major, FP32).
+   AdamW then moves the two copies of each weight alike. */
+int mcgb_mlp_tie_columns(float *dev_dw, int rows, int cols, int count, int shift, void *stream);
+
 /* AdamW on FP32 master weights w[rows*cols] (decoupled weight decay); also
    writes the bf16 copy w_bf16[rows,cols] and, when wt_bf16 != NULL, the
    transposed bf16 copy wt_bf16[cols,rows].  step counts from 1. */

@@ -255,6 +255,19 @@ __global__ void adamw_kernel(float *w, bf16 *wb, bf16 *wt, const float *__restri
     }
 }
 
+/* dW[:, j] = dW[:, j + shift] = dW[:, j] + dW[:, j + shift] for j < count:
+   the gradient of a weight shared by two input columns (the high and low
+   bf16 parts of one input), so that AdamW moves both copies alike. */
+__global__ void tie_columns_kernel(float *dw, int rows, int cols, int count, int shift) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * count) return;
+    int r = i / count, j = i % count;
+    float *row = dw + (size_t)r * cols;
+    float s = row[j] + row[j + shift];
+    row[j] = s;
+    row[j + shift] = s;
+}
+
 int fail(int code, const char *fmt, ...) {
     char buf[256];
     va_list ap;
@@ -376,6 +389,14 @@ int mcgb_mlp_loss_grad(const float *y, const float *t, const float *w, uint16_t 
     loss_grad_kernel<<<(m + 255) / 256, 256, 0, (cudaStream_t)stream>>>(y, t, w, (bf16 *)dy, loss, m, n, nv,
                                                                        mode, scale, 4.0f);
     return check_launch("mlp loss gradient");
+}
+
+int mcgb_mlp_tie_columns(float *dw, int rows, int cols, int count, int shift, void *stream) {
+    if (!dw || rows <= 0 || cols <= 0 || count <= 0 || shift < count || count + shift > cols)
+        return fail(MCGB_E_INVALID, "bad tie_columns arguments");
+    int n = rows * count;
+    tie_columns_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(dw, rows, cols, count, shift);
+    return check_launch("mlp tie columns");
 }
 
 int mcgb_mlp_adamw(float *w, uint16_t *wb, uint16_t *wt, const float *g, float *m, float *v, int rows,

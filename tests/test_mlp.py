@@ -133,3 +133,25 @@ def test_served_surrogate_meets_tolerance_with_fallback_live(cuda, lib):
     seq = BatchedMc.sample_sims(9, seed=23, packets=(1, 2))
     plain = sequential_plain_mc(seq, 1_000_000)
     assert rep['profiles_per_s'] > 100.0 * plain, (rep['profiles_per_s'], plain)
+
+
+def test_split_inputs_keep_16_bits_and_tied_weights_stay_equal(cuda, lib):
+    """The network input as high + low bf16 parts reproduces the FP32
+    features to about 16 bits, and training keeps the first layer's two
+    weight copies identical (mcgb_mlp_tie_columns + AdamW)."""
+    torch = cuda
+    from pyxopto_gb300.surrogate import Mlp, split_bf16, features
+    rng = np.random.default_rng(3)
+    x = features(np.exp(rng.uniform(0, 6.9, 512)), np.exp(rng.uniform(6.2, 8.5, 512)),
+                 rng.uniform(0.6, 0.95, 512), rng.uniform(1.33, 1.5, 512))
+    xs = split_bf16(x).float().cpu().numpy()
+    rec = xs[:, :4] + xs[:, 4:8]
+    assert np.max(np.abs(rec - x[:, :4])) < 2.0 ** -15
+    assert np.max(np.abs(xs[:, :4] - x[:, :4])) > 2.0 ** -12      # bf16 alone is coarser
+    net = Mlp(sizes=(4, 64, 30), batch=512)
+    t = torch.from_numpy(rng.normal(0, 1, (512, 32)).astype(np.float32)).cuda()
+    xd = split_bf16(x)
+    for _ in range(5):
+        net.train_step(xd, t, 30, 1e-2)
+    w = net.w[0].cpu().numpy()
+    assert np.array_equal(w[:, :4], w[:, 4:8])
