@@ -52,22 +52,36 @@ L2_FLUSH_BYTES = 256 << 20
 # fraction of issue slots in use (smsp__issue_active), the resource that
 # bounds this kernel.
 PROFILED_TRAFFIC = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (8.61e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
-    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (1.774e10, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (7.75e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (1.80e10, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 PROFILED_ISSUE_ACTIVE = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.895, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
-    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.870, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.892, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.825, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # L2 atomic-unit use of the transport kernel's 64-bit tally atomics, from a
-# small-case ncu capture (one kernel, one launch, 2e6 packets): the share of
+# medium-case ncu capture (one kernel, one launch, 2e7 packets): the share of
 # L2 cycles in which the atomic unit's input was active
-# (lts__d_atomic_input_cycles_active), and the reduction requests per
-# packet (lts__t_requests_op_red).
-PROFILED_L2_ATOMICS = {}
-# DRAM traffic of the voxel fluence (small-case ncu capture): GB/s of
-# dram__bytes_read + dram__bytes_write over the kernel's duration.
-PROFILED_HBM = {}
+# (lts__d_atomic_input_cycles_active), the reduction requests per packet and
+# per interaction step (lts__t_requests_op_red), and the L2 throughput.
+PROFILED_L2_ATOMICS = {
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (
+        {'atomic_unit_active_pct': 13.65, 'red_requests_per_packet': 436.8,
+         'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 20.47},
+        'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
+        {'atomic_unit_active_pct': 10.52, 'red_requests_per_packet': 300.0,
+         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 22.80},
+        'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+}
+# DRAM traffic of the voxel fluence (same capture): dram__bytes_read +
+# dram__bytes_write over the kernel's duration (L2 evictions of the 64 MB
+# fluence tally's atomics; the tally itself is read once).
+PROFILED_HBM = {
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
+        {'gbs': 35.9, 'bytes_per_packet': 180.2},
+        'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+}
 HBM_FALLBACK_GBS = 6800.0
 METRIC = 'packets/s (1 GB300)'
 

@@ -759,7 +759,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
         }
         if (!__any_sync(MCGB_FULL_MASK, active)) break;
 #pragma unroll 1
-        for (int k = 0; k < 8; ++k) {
+        for (int k = 0; k < 16; ++k) {
             if (active && mcml_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
@@ -768,7 +768,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
                 active = false;
             }
         }
-        iter += 8;
+        iter += 16;
         if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {

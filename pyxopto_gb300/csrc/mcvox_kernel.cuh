@@ -343,27 +343,32 @@ struct MvPacket {
     int mat;
     float w, opl;
     float free;           /* FAST: radius around pos inside one material, 0 = none */
+    float cube;           /* FAST: that radius for any point of voxel vi (its table entry) */
     bool stale;           /* FAST: vi not updated since a free flight */
     uint32_t trace_count, events, steps;
     uint64_t p;
 };
 
-/* Radius of a ball around pos, inside voxel vi, that holds one material
-   and lies inside the grid (and inside rmax): the voxel's homogeneous-cube
-   radius k (mcgb_voxel_radius) times the smallest voxel size, less the
-   margins.  0 when free flight is off or vi lies outside the grid. */
-static __device__ __forceinline__ float mv_free_radius(const MvCtx &x, const i3 &vi, const f3 &pos) {
+/* Radius of a ball around any point of voxel vi that holds one material
+   and lies inside the grid: the voxel's homogeneous-cube radius k
+   (mcgb_voxel_radius) times the smallest voxel size, less the margins.  0
+   when free flight is off or vi lies outside the grid.  Loaded when the
+   packet enters a voxel and kept in MvPacket.cube. */
+static __device__ __forceinline__ float mv_cube_radius(const MvCtx &x, const i3 &vi) {
     if (!x.rad || !mv_valid(x.g, vi)) return 0.0f;
     uint64_t flat = ((uint64_t)vi.z * (uint64_t)x.g.sh[1] + (uint64_t)vi.y) * (uint64_t)x.g.sh[0] +
                     (uint64_t)vi.x;
     int k = __ldg(x.rad + flat);
-    if (k == 0) return 0.0f;
-    float f = (float)k * x.free_unit - x.free_eps;
-    if (x.use_rmax) {
+    return k ? fmaxf((float)k * x.free_unit - x.free_eps, 0.0f) : 0.0f;
+}
+
+/* The free radius at pos from the voxel's cube radius, inside rmax too. */
+static __device__ __forceinline__ float mv_free_radius(const MvCtx &x, float cube, const f3 &pos) {
+    if (x.use_rmax && cube > 0.0f) {
         f3 d{pos.x - x.src_pos.x, pos.y - x.src_pos.y, pos.z - x.src_pos.z};
-        f = fminf(f, x.rmax - mc_sqrt(dot3(d, d)));
+        cube = fmaxf(fminf(cube, x.rmax - mc_sqrt(dot3(d, d))), 0.0f);
     }
-    return fmaxf(f, 0.0f);
+    return cube;
 }
 
 /* Voxel of a position after free flights, clamped into the grid (the
@@ -415,7 +420,8 @@ static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, con
     mcvox_launch<SIMPLE>(c, x.g, x.M, x.vox, x.lut, rng, s.pos, s.dir, s.w, s.vi, s.mat,
                          b.accumulator, prev_pos);
     s.stale = false;
-    s.free = MCGB_FAST_MATH ? mv_free_radius(x, s.vi, s.pos) : 0.0f;
+    s.cube = MCGB_FAST_MATH ? mv_cube_radius(x, s.vi) : 0.0f;
+    s.free = MCGB_FAST_MATH ? mv_free_radius(x, s.cube, s.pos) : 0.0f;
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -476,6 +482,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     } else {
         if (FREE && s.stale) {
             s.vi = mv_index_clamped(g, s.pos);
+            s.cube = mv_cube_radius(x, s.vi);
             s.stale = false;
         }
         /* mcsim_intersect, mcvox.template.c:173-196 */
@@ -530,13 +537,16 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             }
         }
     } else if (d < step) {
-        s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
+        uint32_t ev = mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng);
+        s.events |= ev | MCGB_EV_BOUNDARY_HIT;
         if (!mv_valid(g, s.vi)) {
             if (s.vi.z < 0) detector_deposit<XTRA>(c.top, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             else if (s.vi.z >= g.sh[2]) detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             done = true;
         } else if (FREE) {
-            s.free = mv_free_radius(x, s.vi, s.pos);
+            /* a refracted (or passing) packet entered the next voxel */
+            if (ev == MCGB_EV_REFRACTION) s.cube = mv_cube_radius(x, s.vi);
+            s.free = mv_free_radius(x, s.cube, s.pos);
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
         if (rng.next() < g0.w) {
@@ -556,7 +566,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                 s.free -= step;
                 s.stale = true;
             } else {
-                s.free = mv_free_radius(x, s.vi, s.pos);
+                s.free = mv_free_radius(x, s.cube, s.pos);
             }
         }
     } else {
@@ -581,7 +591,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                 s.free -= step;
                 s.stale = true;
             } else {
-                s.free = mv_free_radius(x, s.vi, s.pos);
+                s.free = mv_free_radius(x, s.cube, s.pos);
             }
         }
     }
@@ -730,7 +740,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
         }
         if (!__any_sync(0xffffffffu, active)) break;
 #pragma unroll 1
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 8; ++k) {
             if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
@@ -739,7 +749,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                 active = false;
             }
         }
-        iter += 4;
+        iter += 8;
         if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {

@@ -170,8 +170,11 @@ class Mc(McEngine):
             _lib.check(lib.mcgb_voxel_radius(C.c_void_p(self._dev['vox'].data_ptr()), shape,
                                              C.c_void_p(rad.data_ptr()), self.VOXEL_RADIUS_CAP,
                                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
-            self._dev['vox_radius'] = rad
-        return self._dev['vox_radius'].data_ptr()
+            # a grid without any homogeneous cube (one voxel thick, or a
+            # checkerboard) gains nothing from free flight: leave it off
+            self._dev['vox_radius'] = rad if int(rad.max().item()) > 0 else None
+        rad = self._dev['vox_radius']
+        return rad.data_ptr() if rad is not None else None
 
     def _download(self, nphotons, out):
         accu = self._dev['accu'].cpu().numpy().view(np.uint64)
