@@ -466,6 +466,41 @@ def surrogate_bench(args):
                     'path': 'pyxopto_gb300.surrogate.Surrogate.serve'}}
 
 
+def mlp_train_bench(args):
+    """One training step of the surrogate network 4-256-256-256-30 at batch
+    4096 on the library's kernels (forward, loss gradient, backward, tied
+    input columns, AdamW), timed with CUDA events over 50 steps per step of
+    the bench; metric training profiles/s."""
+    import torch
+    from pyxopto_gb300.surrogate import Mlp, split_bf16, features
+    rng = np.random.default_rng(0)
+    m = 4096
+    x = features(np.exp(rng.uniform(0, 6.9, m)), np.exp(rng.uniform(6.2, 8.5, m)),
+                 rng.uniform(0.6, 0.95, m), rng.uniform(1.33, 1.5, m))
+    t = np.zeros((m, 32), np.float32)
+    t[:, :30] = rng.normal(0, 1, (m, 30))
+    net = Mlp(sizes=(4, 256, 256, 256, 30), batch=m)
+    xd = split_bf16(x)
+    td = torch.from_numpy(t).cuda()
+    inner = 50
+    for _ in range(args.warmup * inner):
+        net.train_step(xd, td, 30, 1e-4)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps * inner):
+        net.train_step(xd, td, 30, 1e-4)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / (args.steps * inner)
+    flops = 3 * 2 * m * (16 * 256 + 256 * 256 * 2 + 256 * 32)
+    return {'metric': 'training profiles/s (MLP 4-256-256-256-30, batch 4096)', 'value': m / (ms / 1e3),
+            'unit': 'profiles/s', 'ms_per_step': ms, 'tflops_dense': flops / (ms / 1e3) / 1e12,
+            'config': {'workload': 'mlp_train_step', 'batch': m, 'layers': '4-256-256-256-30 (16/32 padded)',
+                       'steps_per_bench_step': inner},
+            'gpu_launches': args.steps * inner * 33}
+
+
 def fiber_sweep_bench(args):
     """The reference's own performance workload (test/performance.py running
     xopto/mcml/test/validate.py:348-511): 400 sequential Mc.run calls of
@@ -538,12 +573,13 @@ def main():
                          'a headline number uses the workload size)')
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
-    if args.workload in ('batched_4096', 'surrogate', 'fiber_sweep', 'fiber_sweep_vox') and \
-            args.impl == 'gb300':
+    if args.workload in ('batched_4096', 'surrogate', 'fiber_sweep', 'fiber_sweep_vox',
+                         'mlp_train_step') and args.impl == 'gb300':
         import torch
         torch.cuda.set_device(local_rank)
         res = {'batched_4096': batched_bench, 'surrogate': surrogate_bench,
-               'fiber_sweep': fiber_sweep_bench, 'fiber_sweep_vox': fiber_sweep_bench}[args.workload](args)
+               'fiber_sweep': fiber_sweep_bench, 'fiber_sweep_vox': fiber_sweep_bench,
+               'mlp_train_step': mlp_train_bench}[args.workload](args)
         line = dict({'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
                      'scaling': 'none', 'vs_baseline': None, 'dtype': 'f32',
                      'data': 'synthetic (seeded parameter draws and RNG streams)'}, **res)
