@@ -171,6 +171,10 @@ batched_kernel(const McgbBatchConfig cfg, const uint32_t *__restrict__ mult,
         }
         if (!__any_sync(MCGB_FULL, active)) break;
 
+        /* eight steps between refills: the refill's ballots and queue reads
+           cost more than the idle lanes of a packet that ends early */
+#pragma unroll 1
+        for (int k = 0; k < 8; ++k) {
         if (active) {
             const float4 g0 = L[layer].g0;
             ++steps;
@@ -219,7 +223,9 @@ batched_kernel(const McgbBatchConfig cfg, const uint32_t *__restrict__ mult,
                 ++packets;
             }
         }
-        if (((++iter) & 1023u) == 0) {
+        }
+        iter += 8;
+        if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {
                 if (globaltimer_ns() > t_deadline) stop = MCGB_STATUS_TIMEOUT;
