@@ -175,54 +175,54 @@ batched_kernel(const McgbBatchConfig cfg, const uint32_t *__restrict__ mult,
            cost more than the idle lanes of a packet that ends early */
 #pragma unroll 1
         for (int k = 0; k < 8; ++k) {
-        if (active) {
-            const float4 g0 = L[layer].g0;
-            ++steps;
-            float step = sample_step(rng.next(), g0.z);
-            step = fminf(step, FLT_MAX);
-            int next = layer;
-            if (pos.z + step * dir.z < g0.x) {
-                --next;
-                if (fabsf(dir.z) != 0.0f) step = mc_div(g0.x - pos.z, dir.z);
-            }
-            if (pos.z + step * dir.z >= g0.y) {
-                ++next;
-                if (fabsf(dir.z) != 0.0f) step = mc_div(g0.y - pos.z, dir.z);
-            }
-            pos.x = pos.x + dir.x * step;
-            pos.y = pos.y + dir.y * step;
-            pos.z = pos.z + dir.z * step;
-            if (layer < next) pos.z = g0.y;
-            if (layer > next) pos.z = g0.x;
-            bool done = false;
-            if (next != layer) {
-                mcml_boundary(L, layer, next, dir, rng);
-                if (!(layer > 0 && layer < 2)) {
-                    if (layer <= 0) {
-                        /* Radial detector, xopto/mcml/mcdetector/radial.py:117-150 */
-                        float r = mc_sqrt(pos.x * pos.x + pos.y * pos.y);
-                        int idx = clip_i(cvt_int(r * inv_dr), 0, last_bin);
-                        uint32_t wi = weight_to_u32(w, 1.0f);
-                        if (wi > 0) accu_add(tally, (uint64_t)sim * cfg.num_bins + idx, wi);
+            if (active) {
+                const float4 g0 = L[layer].g0;
+                ++steps;
+                float step = sample_step(rng.next(), g0.z);
+                step = fminf(step, FLT_MAX);
+                int next = layer;
+                if (pos.z + step * dir.z < g0.x) {
+                    --next;
+                    if (fabsf(dir.z) != 0.0f) step = mc_div(g0.x - pos.z, dir.z);
+                }
+                if (pos.z + step * dir.z >= g0.y) {
+                    ++next;
+                    if (fabsf(dir.z) != 0.0f) step = mc_div(g0.y - pos.z, dir.z);
+                }
+                pos.x = pos.x + dir.x * step;
+                pos.y = pos.y + dir.y * step;
+                pos.z = pos.z + dir.z * step;
+                if (layer < next) pos.z = g0.y;
+                if (layer > next) pos.z = g0.x;
+                bool done = false;
+                if (next != layer) {
+                    mcml_boundary(L, layer, next, dir, rng);
+                    if (!(layer > 0 && layer < 2)) {
+                        if (layer <= 0) {
+                            /* Radial detector, xopto/mcml/mcdetector/radial.py:117-150 */
+                            float r = mc_sqrt(pos.x * pos.x + pos.y * pos.y);
+                            int idx = clip_i(cvt_int(r * inv_dr), 0, last_bin);
+                            uint32_t wi = weight_to_u32(w, 1.0f);
+                            if (wi > 0) accu_add(tally, (uint64_t)sim * cfg.num_bins + idx, wi);
+                        }
+                        done = true;
                     }
-                    done = true;
+                } else {
+                    float deposit = w * g0.w;
+                    w -= deposit;
+                    float az, ct = pf_sample<MCGB_PF_HG>(L[layer].pf0, L[layer].pf1, nullptr, rng, &az, dir);
+                    scatter_direction(dir, ct, az);
+                    if (w < 1e-4f) {
+                        if (rng.next() > 0.1f) done = true;
+                        else w = mc_div(w, 0.1f);
+                    }
                 }
-            } else {
-                float deposit = w * g0.w;
-                w -= deposit;
-                float az, ct = pf_sample<MCGB_PF_HG>(L[layer].pf0, L[layer].pf1, nullptr, rng, &az, dir);
-                scatter_direction(dir, ct, az);
-                if (w < 1e-4f) {
-                    if (rng.next() > 0.1f) done = true;
-                    else w = mc_div(w, 0.1f);
+                if (RMAX && dot3(pos, pos) > rmax2) done = true;
+                if (done) {
+                    active = false;
+                    ++packets;
                 }
             }
-            if (RMAX && dot3(pos, pos) > rmax2) done = true;
-            if (done) {
-                active = false;
-                ++packets;
-            }
-        }
         }
         iter += 8;
         if ((iter & 1023u) == 0) {
