@@ -661,6 +661,16 @@ BENCH = {
         source=dict(type='Line'),
         detectors=dict(top=dict(type='Radial', axis=[0.0, 5e-3, 50]), specular=dict(type='Total')),
         nphotons=1_000_000, streams=0, rnginit=1),
+    # one simulation of the batched family: a semi-infinite layer in air,
+    # mua 0.1/mm, mus' 1.5/mm, g 0.8, n 1.4, radial 0-3 mm / 30 bins (the
+    # batched engine's detector), 1e6 packets
+    'c4_semiinf_radial': dict(
+        medium='mcml',
+        layers=[_air(['Hg', 0.0]), dict(d=INF, n=1.4, mua=100.0, mus=7500.0, pf=['Hg', 0.8]),
+                _air(['Hg', 0.0])],
+        source=dict(type='Line'),
+        detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30])),
+        nphotons=1_000_000, streams=0, rnginit=1),
     # 200^3 uint8 voxels of 0.05 mm: epidermis (0.1 mm) over a dermis-like
     # background (mua 0.02/mm, mus 15/mm, g 0.9) with a blood vessel
     # (radius 0.5 mm, mua 2/mm, n 1.33) along y at 1 mm depth; Gaussian beam
