@@ -1,7 +1,9 @@
 """Throughput benchmark of the GB300 photon-packet transport engine.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload c2_skin_gk_fluence|c1_slab_hg_radial] [--math fast|exact]
+                    [--workload c2_skin_gk_fluence|c1_slab_hg_radial|c3_vox_skin_vessel|
+                                batched_4096|surrogate|mlp_train_step|fiber_sweep|fiber_sweep_vox]
+                    [--math fast|exact] [--no-others]
 
 Workload (default): the 3-layer skin-like stack with the Gegenbauer phase
 function (alpha 0.5), a normal Line source and a 100x100x100 Cartesian
@@ -13,7 +15,10 @@ flushed by writing a 256 MB buffer between steps.
 Reported on one JSON line: the device-timed value, the end-to-end value
 through Mc.run (host packing, host<->device copies, tally download), the
 roofline of the transport kernel, the reference CPU build timed on this
-host's cores, and the SM clocks sampled during the timed region.
+host's cores, and the SM clocks sampled during the timed region.  The
+default run also measures the other configurations (the 10 mm slab, the
+200^3 voxel grid, the batched engine, the surrogate) and reports them under
+"other_workloads" in the same line.
 
 --impl reference times the reference's own McKernel (rendered by PyXOpto's
 plugins and compiled for the CPU, oracle/_ref/) on all host cores, on
@@ -553,18 +558,83 @@ def fiber_sweep_bench(args):
                     'path': 'pyxopto_gb300.{}.mc.Mc.run, 400 calls'.format('mcvox' if vox else 'mcml')}}
 
 
+DEFAULT_WORKLOAD = 'c2_skin_gk_fluence'
+
+
+def _transport_summary(args, workload):
+    """Config 1 or config 3 measured like the default workload, compactly."""
+    import copy
+    a = copy.copy(args)
+    a.workload, a.steps, a.warmup, a.e2e_steps = workload, 3, 2, 2
+    res = gpu_bench(a, 0, 1, 0)
+    n = res['nphotons']
+    kern_s = float(np.mean(res['kernel_ms'])) / 1e3
+    achieved = res['ref_spp'] * n * OPS_PER_STEP / kern_s / 1e12
+    out = {'value': n * a.steps / (res['total_ms'] / 1e3), 'unit': 'packets/s',
+           'e2e': res['e2e']['value'] if res['e2e'] else None, 'kernel_ms': kern_s * 1e3,
+           'roofline_frac': achieved / res['fp32_peak'], 'achieved_tflops': achieved,
+           'ref_steps_per_packet': res['ref_spp'],
+           'executed_steps_per_packet': res['steps_per_launch'] / float(n),
+           'clocks': res['clocks']}
+    if not args.no_cpu_baseline:
+        rate, meta = reference_cpu(workload, seconds=args.cpu_seconds / 2)
+        out['cpu_baseline'] = dict(meta, value=rate, unit='packets/s')
+    return out
+
+
+def other_workloads(args, fp32_peak):
+    """The other benchmark configurations, measured in the same run as the
+    headline line: config 1 (10 mm slab, 1e6 packets), config 3 (200^3
+    voxels, 1e8 packets), the batched engine (4096 simulations) and the
+    surrogate with its Monte Carlo judge (65536 queries).  Each entry has its
+    own timing (CUDA events for the device values); failures are recorded,
+    not raised."""
+    import copy
+    out = {}
+    for name in ('c1_slab_hg_radial', 'c3_vox_skin_vessel'):
+        try:
+            out[name] = _transport_summary(args, name)
+        except Exception as e:          # keep the headline line
+            out[name] = {'error': repr(e)}
+    try:
+        a = copy.copy(args)
+        a.steps, a.warmup, a.e2e_steps, a.sims = 2, 1, 1, 4096
+        r = batched_bench(a)
+        out['batched_4096'] = {k: r[k] for k in ('value', 'unit', 'ms_per_step', 'packets_per_s',
+                                                 'steps_per_s', 'sequential_plain_mc', 'clocks')}
+        out['batched_4096']['e2e'] = r['e2e']['value']
+        out['batched_4096']['roofline_frac'] = r['steps_per_s'] * OPS_PER_STEP / 1e12 / fp32_peak
+    except Exception as e:
+        out['batched_4096'] = {'error': repr(e)}
+    try:
+        a = copy.copy(args)
+        a.steps, a.warmup, a.seq_profiles = 2, 1, 8
+        r = surrogate_bench(a)
+        out['surrogate'] = {k: r[k] for k in ('value', 'unit', 'ms_per_step', 'gain_vs_sequential_plain_mc',
+                                              'sequential_plain_mc_profiles_per_s', 'fallback_all',
+                                              'surrogate_rms_rel_vs_mc', 'clocks')}
+        out['surrogate']['judge'] = {k: r['judge'][k] for k in (
+            'judge_fail_fraction', 'judge_rms_rel_median', 'judge_rms_rel_p90', 'judge_noise_rms_rel_median')}
+        out['surrogate']['held_out_at_training'] = (r['held_out_at_training'] or {}).get('error')
+    except Exception as e:
+        out['surrogate'] = {'error': repr(e)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--workload', default='c2_skin_gk_fluence')
+    ap.add_argument('--workload', default=DEFAULT_WORKLOAD)
     ap.add_argument('--math', default='fast', choices=['fast', 'exact'])
     ap.add_argument('--scheduling', default='dynamic', choices=['dynamic', 'static'])
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-others', action='store_true',
+                    help='default workload only: skip the other configurations in the same line')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--sims', type=int, default=4096, help='batched workload: simulations')
     ap.add_argument('--seq-profiles', type=int, default=16)
@@ -676,6 +746,8 @@ def main():
     if not args.no_cpu_baseline and world == 1:
         rate, meta = reference_cpu(args.workload, seconds=args.cpu_seconds)
         line['cpu_baseline'] = dict(meta, value=rate, unit='packets/s')
+    if world == 1 and args.workload == DEFAULT_WORKLOAD and not args.packets and not args.no_others:
+        line['other_workloads'] = other_workloads(args, fp32_peak)
     print(json.dumps(line))
     if world > 1:
         import torch
