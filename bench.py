@@ -608,7 +608,7 @@ def other_workloads(args, fp32_peak):
         out['batched_4096'] = {'error': repr(e)}
     try:
         a = copy.copy(args)
-        a.steps, a.warmup, a.seq_profiles = 2, 1, 8
+        a.steps, a.warmup, a.seq_profiles = 2, 1, 16
         r = surrogate_bench(a)
         out['surrogate'] = {k: r[k] for k in ('value', 'unit', 'ms_per_step', 'gain_vs_sequential_plain_mc',
                                               'sequential_plain_mc_profiles_per_s', 'fallback_all',
