@@ -62,7 +62,7 @@ PROFILED_TRAFFIC = {
 }
 PROFILED_ISSUE_ACTIVE = {
     ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.892, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
-    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.825, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.844, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # L2 atomic-unit use of the transport kernel's 64-bit tally atomics, from a
 # medium-case ncu capture (one kernel, one launch, 2e7 packets): the share of
@@ -75,8 +75,8 @@ PROFILED_L2_ATOMICS = {
          'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 20.47},
         'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
-        {'atomic_unit_active_pct': 10.52, 'red_requests_per_packet': 300.0,
-         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 22.80},
+        {'atomic_unit_active_pct': 11.22, 'red_requests_per_packet': 300.1,
+         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 21.96},
         'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # DRAM traffic of the voxel fluence (same capture): dram__bytes_read +
@@ -84,7 +84,7 @@ PROFILED_L2_ATOMICS = {
 # fluence tally's atomics; the tally itself is read once).
 PROFILED_HBM = {
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
-        {'gbs': 35.9, 'bytes_per_packet': 180.2},
+        {'gbs': 38.3, 'bytes_per_packet': 180.1},
         'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 HBM_FALLBACK_GBS = 6800.0
@@ -322,7 +322,7 @@ def gpu_bench(args, rank, world, local_rank):
             8 * _abi.NUM_COUNTERS
         e2e = {'value': nphotons * args.e2e_steps * world / dt, 'unit': 'packets/s',
                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
-               'path': 'pyxopto_gb300.mcml.mc.Mc.run'}
+               'path': 'pyxopto_gb300.{}.mc.Mc.run'.format(spec['medium'])}
     # reference steps per packet: the reference's loop iterations for this
     # workload, the unit of the algorithmic work.  The layered kernels run
     # the reference's loop step for step; voxelized FAST runs take free

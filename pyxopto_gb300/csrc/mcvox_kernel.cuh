@@ -339,44 +339,65 @@ struct MvCtx {
 
 struct MvPacket {
     f3 pos, dir;
-    i3 vi;
+    i3 vi;                /* the voxel; with free flight, the centre of the packet's cube */
     int mat;
     float w, opl;
-    float free;           /* FAST: radius around pos inside one material, 0 = none */
-    float cube;           /* FAST: that radius for any point of voxel vi (its table entry) */
-    bool stale;           /* FAST: vi not updated since a free flight */
+    float free;           /* FAST: radius around pos inside the cube, 0 = none */
+    int k;                /* FAST: half width of the cube around vi in voxels, 0 = the voxel */
     uint32_t trace_count, events, steps;
     uint64_t p;
 };
 
-/* Radius of a ball around any point of voxel vi that holds one material
-   and lies inside the grid: the voxel's homogeneous-cube radius k
-   (mcgb_voxel_radius) times the smallest voxel size, less the margins.  0
-   when free flight is off or vi lies outside the grid.  Loaded when the
-   packet enters a voxel and kept in MvPacket.cube. */
-static __device__ __forceinline__ float mv_cube_radius(const MvCtx &x, const i3 &vi) {
-    if (!x.rad || !mv_valid(x.g, vi)) return 0.0f;
+/* True when the cube of half width k around vi lies inside the rmax sphere
+   (with a relative margin): no position inside it ends a packet. */
+static __device__ __forceinline__ bool mv_cube_in_rmax(const MvCtx &x, const i3 &vi, int k) {
+    const MvGeom &g = x.g;
+    const int v[3] = {vi.x, vi.y, vi.z};
+    const float src[3] = {x.src_pos.x, x.src_pos.y, x.src_pos.z};
+    float r2 = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float lo = g.tl[a] + (float)(v[a] - k) * g.vs[a] - src[a];
+        float hi = g.tl[a] + (float)(v[a] + k + 1) * g.vs[a] - src[a];
+        float m = fmaxf(fabsf(lo), fabsf(hi));
+        r2 = fmaf(m, m, r2);
+    }
+    return r2 < x.rmax2 * 0.9999f;
+}
+
+/* Homogeneous-cube half width k of voxel vi (mcgb_voxel_radius): every
+   voxel within Chebyshev distance k of vi lies inside the grid and holds
+   vi's material.  With a finite rmax the cube also shrinks until it lies
+   inside the rmax sphere.  0 when free flight is off or vi lies outside the
+   grid. */
+static __device__ __forceinline__ int mv_cube_k(const MvCtx &x, const i3 &vi) {
+    if (!x.rad || !mv_valid(x.g, vi)) return 0;
     uint64_t flat = ((uint64_t)vi.z * (uint64_t)x.g.sh[1] + (uint64_t)vi.y) * (uint64_t)x.g.sh[0] +
                     (uint64_t)vi.x;
     int k = __ldg(x.rad + flat);
-    return k ? fmaxf((float)k * x.free_unit - x.free_eps, 0.0f) : 0.0f;
+    if (x.use_rmax)
+        while (k > 0 && !mv_cube_in_rmax(x, vi, k)) --k;
+    return k;
 }
 
-/* The free radius at pos from the voxel's cube radius, inside rmax too. */
-static __device__ __forceinline__ float mv_free_radius(const MvCtx &x, float cube, const f3 &pos) {
-    if (x.use_rmax && cube > 0.0f) {
-        f3 d{pos.x - x.src_pos.x, pos.y - x.src_pos.y, pos.z - x.src_pos.z};
-        cube = fmaxf(fminf(cube, x.rmax - mc_sqrt(dot3(d, d))), 0.0f);
-    }
-    return cube;
+/* Radius of a ball around any point of voxel vi inside its cube of half
+   width k: k times the smallest voxel size, less the margins. */
+static __device__ __forceinline__ float mv_ball(const MvCtx &x, int k) {
+    return k == 0 ? 0.0f : fmaxf((float)k * x.free_unit - x.free_eps, 0.0f);
 }
 
-/* Voxel of a position after free flights, clamped into the grid (the
-   position lies inside a homogeneous cube of the grid, so the clamp only
-   absorbs rounding at the cube's faces). */
-static __device__ __forceinline__ i3 mv_index_clamped(const MvGeom &g, const f3 &p) {
-    i3 i = mv_index(g, p);
-    return i3{clip_i(i.x, 0, g.sh[0] - 1), clip_i(i.y, 0, g.sh[1] - 1), clip_i(i.z, 0, g.sh[2] - 1)};
+/* Radius of a ball around pos, a point of the cube of half width k around
+   vi: its distance to the cube's faces, less the margins. */
+static __device__ __forceinline__ float mv_clearance(const MvCtx &x, const i3 &vi, int k, const f3 &pos) {
+    if (k == 0) return 0.0f;
+    const MvGeom &g = x.g;
+    float c = pos.x - (g.tl[0] + (float)(vi.x - k) * g.vs[0]);
+    c = fminf(c, g.tl[0] + (float)(vi.x + k + 1) * g.vs[0] - pos.x);
+    c = fminf(c, pos.y - (g.tl[1] + (float)(vi.y - k) * g.vs[1]));
+    c = fminf(c, g.tl[1] + (float)(vi.y + k + 1) * g.vs[1] - pos.y);
+    c = fminf(c, pos.z - (g.tl[2] + (float)(vi.z - k) * g.vs[2]));
+    c = fminf(c, g.tl[2] + (float)(vi.z + k + 1) * g.vs[2] - pos.z);
+    return fmaxf(c * 0.999f - x.free_eps, 0.0f);
 }
 
 static __device__ __forceinline__ MvCtx mcvox_ctx(const McgbMcvoxConfig &c, const McgbBuffers &b,
@@ -419,9 +440,8 @@ static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, con
     s.events = MCGB_EV_LAUNCH;
     mcvox_launch<SIMPLE>(c, x.g, x.M, x.vox, x.lut, rng, s.pos, s.dir, s.w, s.vi, s.mat,
                          b.accumulator, prev_pos);
-    s.stale = false;
-    s.cube = MCGB_FAST_MATH ? mv_cube_radius(x, s.vi) : 0.0f;
-    s.free = MCGB_FAST_MATH ? mv_free_radius(x, s.cube, s.pos) : 0.0f;
+    s.k = MCGB_FAST_MATH ? mv_cube_k(x, s.vi) : 0;
+    s.free = MCGB_FAST_MATH ? mv_ball(x, s.k) : 0.0f;
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -433,19 +453,23 @@ static __device__ __forceinline__ void mcvox_end(const McgbMcvoxConfig &c, const
 
 /* One step of McKernel (mcvox), xopto/mcvox/kernel/mcvox.template.c:760-1038.
 
-   FAST math adds free flight (albedo weight and albedo rejection).  s.free
-   is the radius of a ball around the packet that holds one material.  A
-   sampled free path shorter than s.free is taken in one move without
-   computing voxel walls, the packet interacts there, s.free shrinks by the
-   path, and the voxel index is recomputed from the position at the next
-   step that needs it.  A longer path first moves the packet through the
-   ball to its surface and continues with the remainder of the path, from
-   there exactly as the reference's walk; that step reloads s.free from the
-   radius table of the voxel it ends in.  The reference stops at every voxel
-   wall and draws a new path when the next voxel holds the same material;
-   the exponential free path is memoryless (the remainder of a path known to
-   exceed the radius is again exponential), so the interaction points have
-   the same distribution. */
+   FAST math adds free flight (albedo weight and albedo rejection).  A packet
+   keeps the centre vi and half width k of a cube of voxels that all hold its
+   material (the radius table; k = 0 is the packet's own voxel), and s.free,
+   the radius of a ball around it inside that cube.  A sampled free path
+   shorter than s.free is taken in one move without computing walls, the
+   packet interacts there and s.free shrinks by the path.  A longer path
+   first moves the packet through the ball to its surface and continues with
+   the remainder of the path; that step intersects the walls of the cube
+   rather than of one voxel.  An interaction inside the cube sets s.free to
+   the distance to the cube's faces.  At a face, the voxel inside the face
+   takes the place of vi and the reference's boundary logic follows; the
+   voxel the packet then lies in gives the next cube.  The reference stops at
+   every voxel wall and draws a new path when the next voxel holds the same
+   material; the exponential free path is memoryless (the remainder of a
+   path known to exceed a distance is again exponential), so the interaction
+   points have the same distribution.  With a finite rmax, cubes lie inside
+   the rmax sphere, so the packets end at the same steps as the reference's. */
 template <int PF, int METHOD, bool FLU, bool XTRA>
 static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
@@ -472,19 +496,23 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         if (XTRA && x.track_opl) s.opl += M[s.mat].g1.x * s.free;
         step -= s.free;
         s.free = 0.0f;
-        s.stale = true;
     }
     f3 dist;
     float d;
     if (flight) {
         d = __int_as_float(0x7f800000);
         dist = f3{d, d, d};
+    } else if (FREE) {
+        /* the walls of the packet's cube (its voxel's walls when k = 0) */
+        const int k = s.k;
+        dist.x = g.tl[0] + (float)(s.dir.x >= 0.0f ? s.vi.x + k + 1 : s.vi.x - k) * g.vs[0] - s.pos.x;
+        dist.y = g.tl[1] + (float)(s.dir.y >= 0.0f ? s.vi.y + k + 1 : s.vi.y - k) * g.vs[1] - s.pos.y;
+        dist.z = g.tl[2] + (float)(s.dir.z >= 0.0f ? s.vi.z + k + 1 : s.vi.z - k) * g.vs[2] - s.pos.z;
+        dist.x = (s.dir.x != 0.0f) ? mc_div(dist.x, s.dir.x) : __int_as_float(0x7f800000);
+        dist.y = (s.dir.y != 0.0f) ? mc_div(dist.y, s.dir.y) : __int_as_float(0x7f800000);
+        dist.z = (s.dir.z != 0.0f) ? mc_div(dist.z, s.dir.z) : __int_as_float(0x7f800000);
+        d = fminf(dist.x, fminf(dist.y, dist.z));
     } else {
-        if (FREE && s.stale) {
-            s.vi = mv_index_clamped(g, s.pos);
-            s.cube = mv_cube_radius(x, s.vi);
-            s.stale = false;
-        }
         /* mcsim_intersect, mcvox.template.c:173-196 */
         dist.x = g.tl[0] + (float)((s.dir.x >= 0.0f) + s.vi.x) * g.vs[0] - s.pos.x;
         dist.y = g.tl[1] + (float)((s.dir.y >= 0.0f) + s.vi.y) * g.vs[1] - s.pos.y;
@@ -537,6 +565,20 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             }
         }
     } else if (d < step) {
+        if (FREE && s.k > 0) {
+            /* at a face of the cube: the voxel inside that face (the
+               crossing axis as mv_boundary picks it, the other axes from the
+               position, kept inside the cube) */
+            const int k = s.k;
+            i3 f = mv_index(g, s.pos);
+            f.x = clip_i(f.x, s.vi.x - k, s.vi.x + k);
+            f.y = clip_i(f.y, s.vi.y - k, s.vi.y + k);
+            f.z = clip_i(f.z, s.vi.z - k, s.vi.z + k);
+            if (dist.x <= dist.y && dist.x <= dist.z) f.x = s.dir.x < 0.0f ? s.vi.x - k : s.vi.x + k;
+            else if (dist.y <= dist.z) f.y = s.dir.y < 0.0f ? s.vi.y - k : s.vi.y + k;
+            else f.z = s.dir.z < 0.0f ? s.vi.z - k : s.vi.z + k;
+            s.vi = f;
+        }
         uint32_t ev = mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng);
         s.events |= ev | MCGB_EV_BOUNDARY_HIT;
         if (!mv_valid(g, s.vi)) {
@@ -544,9 +586,9 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             else if (s.vi.z >= g.sh[2]) detector_deposit<XTRA>(c.bottom, s.pos, s.dir, s.w, s.opl, accu, x.lut);
             done = true;
         } else if (FREE) {
-            /* a refracted (or passing) packet entered the next voxel */
-            if (ev == MCGB_EV_REFRACTION) s.cube = mv_cube_radius(x, s.vi);
-            s.free = mv_free_radius(x, s.cube, s.pos);
+            /* the packet's new voxel, refracted into or reflected back to */
+            s.k = mv_cube_k(x, s.vi);
+            s.free = mv_ball(x, s.k);
         }
     } else if (METHOD == MCGB_METHOD_ALBEDO_REJECTION) {
         if (rng.next() < g0.w) {
@@ -561,14 +603,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             scatter_direction(s.dir, ct, az);
             if (XTRA) s.events |= MCGB_EV_SCATTERING;
         }
-        if (FREE) {
-            if (flight) {
-                s.free -= step;
-                s.stale = true;
-            } else {
-                s.free = mv_free_radius(x, s.cube, s.pos);
-            }
-        }
+        if (FREE) s.free = flight ? s.free - step : mv_clearance(x, s.vi, s.k, s.pos);
     } else {
         float deposit = s.w * g0.w;
         s.w -= deposit;
@@ -586,14 +621,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                 done = true;
             }
         }
-        if (FREE) {
-            if (flight) {
-                s.free -= step;
-                s.stale = true;
-            } else {
-                s.free = mv_free_radius(x, s.cube, s.pos);
-            }
-        }
+        if (FREE) s.free = flight ? s.free - step : mv_clearance(x, s.vi, s.k, s.pos);
     }
     /* mcvox.template.c:1004-1008 */
     bool escaped = s.w <= 0.0f;

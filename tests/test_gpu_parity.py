@@ -482,17 +482,22 @@ def test_voxel_radius_table_matches_brute_force(cuda, lib):
         assert np.array_equal(got, _radius_reference(mat, cap)), cap
 
 
-def test_voxel_free_flight_statistically_equal_to_wall_walk(cuda, lib):
+@pytest.mark.parametrize('rmax', [None, 1.5e-3])
+def test_voxel_free_flight_statistically_equal_to_wall_walk(cuda, lib, rmax):
     """Free flight (the FAST-math default in voxelized media) against the
     reference's wall-by-wall walk in the same FAST kernels, on the 200^3
     skin and vessel grid: depth profile, 1 mm^3 voxels and the detector
-    totals within the 3-sigma gate; free flight takes far fewer steps."""
+    totals within the 3-sigma gate; free flight takes far fewer steps.  With
+    a finite rmax the packets must end where the walk ends them (no fluence
+    beyond the voxel that crosses the rmax sphere)."""
     from pyxopto_gb300.mcvox import mcoptions
     name, nb, n = 'c3_vox_skin_vessel', 16, 1_000_000
     fly = scenarios.build_mc(name, fast=True, scheduling='dynamic')
     walk = scenarios.build_mc(name, fast=True, scheduling='dynamic')
     walk._mc_options.append(mcoptions.McVoxelFreeFlight(False))
     walk._rnginit = 4321
+    if rmax is not None:
+        fly.rmax = walk.rmax = rmax
 
     def batches(mc):
         rows, tops, steps = [], [], 0
@@ -512,4 +517,11 @@ def test_voxel_free_flight_statistically_equal_to_wall_walk(cuda, lib):
         keep = (b.mean(0) > 0) & (b.std(0, ddof=1) / np.sqrt(nb) < 0.2 * b.mean(0))
         ok, rep = _stats.gate(a[:, keep], b[:, keep])
         assert ok, (what, rep)
-    assert sa < 0.8 * sw, (sa, sw)
+    if rmax is not None:
+        # no deposit beyond the voxel that crosses the rmax sphere (centred
+        # on the beam's origin): beyond rmax + 1.5 voxel diagonals all is 0
+        c = (np.arange(200) + 0.5) * 5e-5
+        zc, yc, xc = np.meshgrid(c, c - 5e-3, c - 5e-3, indexing='ij')
+        far = np.sqrt(xc ** 2 + yc ** 2 + zc ** 2).reshape(-1) > rmax + 1.5 * np.sqrt(3) * 5e-5
+        assert not fa.reshape(nb, -1)[:, far].any() and not wa.reshape(nb, -1)[:, far].any()
+    assert sa < (0.8 if rmax is None else 0.95) * sw, (sa, sw)
