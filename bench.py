@@ -405,8 +405,10 @@ def surrogate_bench(args):
     Carlo judge and the library's default fallback (max_fail 0.1), against
     sequential plain Mc.run calls at the judge's packet count (1e6 packets,
     whose own Monte Carlo noise is about 1 % RMS relative); metric profiles/s."""
+    from pyxopto_gb300 import _lib
     from pyxopto_gb300.batched import BatchedMc
     from pyxopto_gb300.surrogate import Surrogate, default_weights, sequential_plain_mc
+    _lib.load().mcgb_mlp_gemm_path(0 if args.mlp_gemm == 'tcgen05' else 1)
     path = default_weights()
     sur = Surrogate.load(path)
     train_log = None
@@ -477,7 +479,9 @@ def mlp_train_bench(args):
     input columns, AdamW), timed with CUDA events over 50 steps per step of
     the bench; metric training profiles/s."""
     import torch
+    from pyxopto_gb300 import _lib
     from pyxopto_gb300.surrogate import Mlp, split_bf16, features
+    _lib.load().mcgb_mlp_gemm_path(0 if args.mlp_gemm == 'tcgen05' else 1)
     rng = np.random.default_rng(0)
     m = 4096
     x = features(np.exp(rng.uniform(0, 6.9, m)), np.exp(rng.uniform(6.2, 8.5, m)),
@@ -502,7 +506,7 @@ def mlp_train_bench(args):
     return {'metric': 'training profiles/s (MLP 4-256-256-256-30, batch 4096)', 'value': m / (ms / 1e3),
             'unit': 'profiles/s', 'ms_per_step': ms, 'tflops_dense': flops / (ms / 1e3) / 1e12,
             'config': {'workload': 'mlp_train_step', 'batch': m, 'layers': '4-256-256-256-30 (16/32 padded)',
-                       'steps_per_bench_step': inner},
+                       'steps_per_bench_step': inner, 'gemm': args.mlp_gemm},
             'gpu_launches': args.steps * inner * 33}
 
 
@@ -638,6 +642,8 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--sims', type=int, default=4096, help='batched workload: simulations')
     ap.add_argument('--seq-profiles', type=int, default=16)
+    ap.add_argument('--mlp-gemm', choices=['tcgen05', 'mma_sync'], default='tcgen05',
+                    help='GEMM implementation of the surrogate kernels (mlp_train_step, surrogate)')
     ap.add_argument('--packets', type=int, default=None,
                     help='override the packets per step (small profiling cases only; '
                          'a headline number uses the workload size)')

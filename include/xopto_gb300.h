@@ -476,7 +476,8 @@ int mcgb_abi_version(void);
    1 McgbSource, 2 McgbDetector, 3 McgbFluence, 4 McgbTrace, 5 McgbMaterial,
    6 McgbMcmlConfig, 7 McgbMcvoxConfig, 8 McgbBuffers, 9 McgbRunOptions,
    10 McgbPf, 11 McgbBatchSim, 12 McgbBatchConfig, 13 McgbSurface,
-   14 McgbSamplingVolume.  Returns -1 for an unknown kind. */
+   14 McgbSamplingVolume, 15 McgbAdamwTensor.  Returns -1 for an unknown
+   kind. */
 int mcgb_sizeof(int kind);
 
 /* Number of streams (device threads) that fills every SM of the current
@@ -682,6 +683,38 @@ int mcgb_mlp_loss_grad(const float *dev_y, const float *dev_t, const float *dev_
    dW[r, j + shift] both become their sum (rows x cols row-major, FP32).
    AdamW then moves the two copies of each weight alike. */
 int mcgb_mlp_tie_columns(float *dev_dw, int rows, int cols, int count, int shift, void *stream);
+
+/* One tensor of a multi-tensor AdamW step (mcgb_mlp_adamw_multi): FP32
+   master weights w[rows*cols], their bf16 copy, optionally the transposed
+   bf16 copy wt_bf16[cols,rows] (NULL = none), the FP32 gradient, the two
+   FP32 moments, and the tensor's decoupled weight decay. */
+typedef struct McgbAdamwTensor {
+    float *w;
+    uint16_t *w_bf16;
+    uint16_t *wt_bf16;
+    const float *grad;
+    float *m;
+    float *v;
+    int32_t rows, cols;
+    float weight_decay;
+    int32_t reserved;
+} McgbAdamwTensor;                       /* 64 bytes */
+
+#define MCGB_ADAMW_MAX_TENSORS 16
+
+/* mcgb_mlp_adamw on 1..MCGB_ADAMW_MAX_TENSORS tensors in one launch, with
+   the same arithmetic per element; `tensors` is a host array, read before
+   the call returns. */
+int mcgb_mlp_adamw_multi(const McgbAdamwTensor *tensors, int count, float lr, float beta1, float beta2,
+                         float eps, int step, void *stream);
+
+/* GEMM implementation behind the mcgb_mlp_* calls: 0 = tcgen05.mma on
+   128 x 64 tiles with the FP32 accumulator in tensor memory (the default),
+   1 = the warp-level mma.sync kernel on 64 x 64 tiles.  path = -1 only
+   queries.  Returns the path in effect before the call, or -1 for an
+   invalid path.  Process-wide; do not switch while MLP calls are queued on
+   another thread. */
+int mcgb_mlp_gemm_path(int path);
 
 /* AdamW on FP32 master weights w[rows*cols] (decoupled weight decay); also
    writes the bf16 copy w_bf16[rows,cols] and, when wt_bf16 != NULL, the

@@ -151,10 +151,18 @@ class McgbBatchConfig(C.Structure):
                 ('num_multipliers', u32), ('reserved', u32)]
 
 
+class McgbAdamwTensor(C.Structure):
+    _fields_ = [('w', C.c_void_p), ('w_bf16', C.c_void_p), ('wt_bf16', C.c_void_p),
+                ('grad', C.c_void_p), ('m', C.c_void_p), ('v', C.c_void_p),
+                ('rows', i32), ('cols', i32), ('weight_decay', f32), ('reserved', i32)]
+
+
+ADAMW_MAX_TENSORS = 16
+
 SIZEOF_KINDS = [McgbLayer, McgbSource, McgbDetector, McgbFluence, McgbTrace,
                 McgbMaterial, McgbMcmlConfig, McgbMcvoxConfig, McgbBuffers,
                 McgbRunOptions, McgbPf, McgbBatchSim, McgbBatchConfig, McgbSurface,
-                McgbSamplingVolume]
+                McgbSamplingVolume, McgbAdamwTensor]
 
 
 def check_layout(sizeof_fn):

@@ -46,6 +46,9 @@ _OPTIONAL = {
     'mcgb_mlp_linear_bwd_weight': (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     'mcgb_mlp_bwd_weight_scratch': (C.c_uint64, [C.c_int, C.c_int, C.c_int]),
     'mcgb_mlp_tie_columns': (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
+    'mcgb_mlp_gemm_path': (C.c_int, [C.c_int]),
+    'mcgb_mlp_adamw_multi': (C.c_int, [_vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                       _vp]),
     'mcgb_mlp_loss_grad': (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int,
                                      C.c_float, _vp]),
     'mcgb_mlp_adamw': (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_float,

@@ -319,6 +319,7 @@ int mcgb_sizeof(int kind) {
         case 12: return (int)sizeof(McgbBatchConfig);
         case 13: return (int)sizeof(McgbSurface);
         case 14: return (int)sizeof(McgbSamplingVolume);
+        case 15: return (int)sizeof(McgbAdamwTensor);
         default: return -1;
     }
 }

@@ -590,12 +590,20 @@ struct FluenceCache {
         if (sum) atomicAdd((unsigned long long *)(base + index), (unsigned long long)sum);
         sum = 0;
     }
+    /* Branch-free: the reduction of the previous voxel's sum is predicated
+       on a change of voxel, so lanes of a warp do not diverge around it. */
     __device__ __forceinline__ void add(uint32_t i, uint32_t w) {
-        if (i != index) {
-            flush();
-            index = i;
-        }
-        sum += w;
+        const bool miss = i != index;
+        const int fire = (miss && sum != 0ull) ? 1 : 0;
+        unsigned long long *addr = (unsigned long long *)(base + index);
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.s32 p, %2, 0;\n\t"
+            "@p red.global.add.u64 [%0], %1;\n\t}\n" ::"l"(addr),
+            "l"((unsigned long long)sum), "r"(fire)
+            : "memory");
+        index = miss ? i : index;
+        sum = (miss ? 0ull : sum) + w;
     }
 };
 

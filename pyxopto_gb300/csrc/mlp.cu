@@ -5,23 +5,24 @@
  * backward with a deterministic bias-gradient reduction, the MSE gradient
  * and AdamW.
  *
- * GEMM: C[R, Cc] = sum_l A(r, l) B(c, l) on 64x64 output tiles, 4 warps of
- * 32x32, k-steps of 16 through mma.sync m16n8k16 (bf16 x bf16 -> f32).
+ * GEMM: C[R, Cc] = sum_l A(r, l) B(c, l) with a fused epilogue.  Two
+ * implementations of the same contract:
+ *   - gemm_tc (mlp_tc.cuh, the default): tcgen05.mma on 128x64 tiles with
+ *     the FP32 accumulator in tensor memory;
+ *   - gemm_bf16 (below, selectable with mcgb_mlp_gemm_path(1)): 64x64 tiles,
+ *     4 warps of 32x32, k-steps of 16 through mma.sync m16n8k16.
  * The forward epilogue also stores the FP32 pre-activation when asked; the
  * last layer's FP32 pre-activation is the network output.
  * Operands are staged in shared memory with the reduction index contiguous;
  * transposed operands (activations in the weight gradient) are transposed
  * while staging.  The weight gradient splits the batch rows into fixed
  * slices and adds the slice results in a fixed order (deterministic).
- *
- * The layers of the surrogate are 256 wide and its batches 64k rows, small
- * GEMMs whose time is dominated by launch and epilogue work; the warp-level
- * mma.sync path keeps them simple.
  */
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <cstdarg>
 #include <string>
 #include "../../include/xopto_gb300.h"
@@ -47,6 +48,11 @@ __device__ __forceinline__ float gelu_grad(float x) {
     float t = tanhf(u);
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * 0.044715f * x * x);
 }
+
+#include "mlp_tc.cuh"
+
+/* 0 = tcgen05 (gemm_tc), 1 = mma.sync (gemm_bf16) */
+int g_gemm_path = 0;
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
     asm volatile(
@@ -159,12 +165,16 @@ __global__ void sum_slices(const float *__restrict__ part, float *out, int slice
     }
 }
 
-/* dPre = dY * act'(pre); column partial sums of dPre over row chunks of 256. */
+/* Rows per block of the activation backward: one column partial sum per
+   chunk of this many rows (the bias gradient adds them in chunk order). */
+constexpr int ACT_ROWS = 64;
+
+/* dPre = dY * act'(pre); column partial sums of dPre over row chunks of ACT_ROWS. */
 __global__ void act_bwd_kernel(const bf16 *__restrict__ dy, const float *__restrict__ pre, bf16 *dpre,
                                float *part, int M, int N, int act) {
     const int c = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int rbeg = blockIdx.y * 256;
-    const int rend = min(M, rbeg + 256);
+    const int rbeg = blockIdx.y * ACT_ROWS;
+    const int rend = min(M, rbeg + ACT_ROWS);
     __shared__ float red[8][33];
     float s = 0.0f;
     if (c < N) {
@@ -196,10 +206,12 @@ __global__ void act_bwd_kernel(const bf16 *__restrict__ dy, const float *__restr
        the mean of T (unbiased in linear units), not to the mean of log T.
    Loss and gradient are divided by M nv; the loss is reduced per block of
    256 rows (fixed order).  Gradients are stored as bf16. */
-__global__ void loss_grad_kernel(const float *__restrict__ y, const float *__restrict__ tgt,
-                                 const float *__restrict__ wcol, bf16 *dy, float *loss, int M, int N,
-                                 int nv, int mode, float scale, float clip) {
-    __shared__ float red[256];
+constexpr int LOSS_THREADS = 1024;
+
+__global__ void __launch_bounds__(LOSS_THREADS)
+loss_grad_kernel(const float *__restrict__ y, const float *__restrict__ tgt, const float *__restrict__ wcol,
+                 bf16 *dy, float *loss, int M, int N, int nv, int mode, float scale, float clip) {
+    __shared__ float red[LOSS_THREADS];
     const float inv = 1.0f / ((float)M * (float)nv);
     float s = 0.0f;
     size_t base = (size_t)blockIdx.x * 256;
@@ -226,32 +238,60 @@ __global__ void loss_grad_kernel(const float *__restrict__ y, const float *__res
     }
     red[threadIdx.x] = s;
     __syncthreads();
-    for (int k = 128; k > 0; k >>= 1) {
+    for (int k = LOSS_THREADS / 2; k > 0; k >>= 1) {
         if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
         __syncthreads();
     }
     if (threadIdx.x == 0) loss[blockIdx.x] = red[0];
 }
 
+/* One AdamW element: FP32 master weight, bf16 copy and (when wt) the
+   transposed bf16 copy of a rows x cols tensor. */
+__device__ __forceinline__ void adamw_element(size_t i, float *w, bf16 *wb, bf16 *wt, const float *gr, float *m,
+                                              float *v, int rows, int cols, float lr, float b1, float b2,
+                                              float eps, float wd, float c1, float c2) {
+    float g = gr[i];
+    float mi = b1 * m[i] + (1.0f - b1) * g;
+    float vi = b2 * v[i] + (1.0f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    float upd = (mi / c1) / (sqrtf(vi / c2) + eps);
+    float wi = w[i] - lr * (upd + wd * w[i]);
+    w[i] = wi;
+    bf16 h = __float2bfloat16_rn(wi);
+    wb[i] = h;
+    if (wt) {
+        size_t r = i / cols, c = i % cols;
+        wt[c * rows + r] = h;
+    }
+}
+
 __global__ void adamw_kernel(float *w, bf16 *wb, bf16 *wt, const float *__restrict__ gr, float *m, float *v,
                              int rows, int cols, float lr, float b1, float b2, float eps, float wd,
                              float c1, float c2) {
     size_t n = (size_t)rows * cols;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float g = gr[i];
-        float mi = b1 * m[i] + (1.0f - b1) * g;
-        float vi = b2 * v[i] + (1.0f - b2) * g * g;
-        m[i] = mi;
-        v[i] = vi;
-        float upd = (mi / c1) / (sqrtf(vi / c2) + eps);
-        float wi = w[i] - lr * (upd + wd * w[i]);
-        w[i] = wi;
-        bf16 h = __float2bfloat16_rn(wi);
-        wb[i] = h;
-        if (wt) {
-            size_t r = i / cols, c = i % cols;
-            wt[c * rows + r] = h;
-        }
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        adamw_element(i, w, wb, wt, gr, m, v, rows, cols, lr, b1, b2, eps, wd, c1, c2);
+}
+
+/* Several tensors in one launch: element i of the concatenation belongs to
+   the tensor k with start[k] <= i < start[k + 1]. */
+struct AdamwMulti {
+    McgbAdamwTensor t[MCGB_ADAMW_MAX_TENSORS];
+    uint64_t start[MCGB_ADAMW_MAX_TENSORS + 1];
+    int count;
+    float lr, b1, b2, eps, c1, c2;
+};
+
+__global__ void adamw_multi_kernel(const __grid_constant__ AdamwMulti p) {
+    const uint64_t total = p.start[p.count];
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        int k = 0;
+        while (k + 1 < p.count && i >= p.start[k + 1]) ++k;
+        const McgbAdamwTensor &T = p.t[k];
+        adamw_element((size_t)(i - p.start[k]), T.w, (bf16 *)T.w_bf16, (bf16 *)T.wt_bf16, T.grad, T.m, T.v, T.rows,
+                      T.cols, p.lr, p.b1, p.b2, p.eps, T.weight_decay, p.c1, p.c2);
     }
 }
 
@@ -302,16 +342,55 @@ int sm_count() {
     return n;
 }
 
-/* Reduction slices of the weight gradient: enough that the grid of
-   (n/64) x (k/64) tiles times slices covers every SM twice, each slice at
+/* Reduction slices of the weight gradient for a GEMM path: enough that the
+   grid of output tiles times slices covers every SM twice, each slice at
    least one k-step of rows, at most 64 slices. */
-int weight_slices(int m, int n, int k) {
-    int tiles = ((n + BM - 1) / BM) * ((k + BN - 1) / BN);
+int weight_slices(int m, int n, int k, int path) {
+    const int tm = path == 0 ? TBM : BM, tn = 64, tk = path == 0 ? TBK : BK;
+    int tiles = ((n + tm - 1) / tm) * ((k + tn - 1) / tn);
     int s = (2 * sm_count() + tiles - 1) / tiles;
-    int most = m / BK;
+    int most = m / tk;
     if (s > most) s = most;
     if (s > 64) s = 64;
     return s < 1 ? 1 : s;
+}
+
+template <int TBN_, bool TA, bool TB, int EPI>
+int launch_tc(const bf16 *A, int lda, const bf16 *B, int ldb, int R, int Cc, int L, int l_slice, int slices,
+              const float *bias, int act, bf16 *Cb, float *Cf, float *pre, int ldc, cudaStream_t st,
+              const char *what) {
+    typedef TcShape<TBN_> Sh;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(gemm_tc<TBN_, TA, TB, EPI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
+        if (e != cudaSuccess) return fail(MCGB_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+        attr = true;
+    }
+    dim3 grid((Cc + TBN_ - 1) / TBN_, (R + TBM - 1) / TBM, slices);
+    gemm_tc<TBN_, TA, TB, EPI><<<grid, TNT, Sh::SMEM, st>>>(A, lda, B, ldb, R, Cc, L, l_slice, bias, act, Cb, Cf,
+                                                            pre, ldc);
+    return check_launch(what);
+}
+
+/* One GEMM launch on the selected path; `slices` reduction slices of
+   l_slice each along blockIdx.z.  The tcgen05 path takes 128 x 64 tiles,
+   or 128 x 32 when 64-wide tiles would leave SMs without a CTA. */
+template <bool TA, bool TB, int EPI>
+int launch_gemm(const bf16 *A, int lda, const bf16 *B, int ldb, int R, int Cc, int L, int l_slice, int slices,
+                const float *bias, int act, bf16 *Cb, float *Cf, float *pre, int ldc, cudaStream_t st,
+                const char *what) {
+    if (g_gemm_path == 0) {
+        const long tiles64 = (long)((Cc + 63) / 64) * ((R + TBM - 1) / TBM) * slices;
+        if (tiles64 >= sm_count())
+            return launch_tc<64, TA, TB, EPI>(A, lda, B, ldb, R, Cc, L, l_slice, slices, bias, act, Cb, Cf, pre,
+                                              ldc, st, what);
+        return launch_tc<32, TA, TB, EPI>(A, lda, B, ldb, R, Cc, L, l_slice, slices, bias, act, Cb, Cf, pre, ldc,
+                                          st, what);
+    }
+    dim3 grid((Cc + BN - 1) / BN, (R + BM - 1) / BM, slices);
+    gemm_bf16<TA, TB, EPI><<<grid, NT, 0, st>>>(A, lda, B, ldb, R, Cc, L, l_slice, bias, act, Cb, Cf, pre, ldc);
+    return check_launch(what);
 }
 
 }  // namespace
@@ -323,15 +402,25 @@ int mcgb_mlp_linear_fwd(const uint16_t *x, const uint16_t *w, const float *b, ui
     int r = shape_ok(m, n, k);
     if (r) return r;
     if (!x || !w || !y) return fail(MCGB_E_INVALID, "NULL operand");
-    dim3 grid((n + BN - 1) / BN, (m + BM - 1) / BM, 1);
-    gemm_bf16<false, false, EPI_FWD><<<grid, NT, 0, (cudaStream_t)stream>>>(
-        (const bf16 *)x, k, (const bf16 *)w, k, m, n, k, k, b, act, (bf16 *)y, nullptr, pre, n);
-    return check_launch("mlp forward");
+    return launch_gemm<false, false, EPI_FWD>((const bf16 *)x, k, (const bf16 *)w, k, m, n, k, k, 1, b, act,
+                                              (bf16 *)y, nullptr, pre, n, (cudaStream_t)stream, "mlp forward");
 }
 
 uint64_t mcgb_mlp_bwd_weight_scratch(int m, int n, int k) {
     if (m <= 0 || n <= 0 || k <= 0) return 0;
-    return (uint64_t)weight_slices(m, n, k) * (uint64_t)n * (uint64_t)k;
+    int s0 = weight_slices(m, n, k, 0), s1 = weight_slices(m, n, k, 1);
+    return (uint64_t)(s0 > s1 ? s0 : s1) * (uint64_t)n * (uint64_t)k;
+}
+
+int mcgb_mlp_gemm_path(int path) {
+    int prev = g_gemm_path;
+    if (path == -1) return prev;
+    if (path != 0 && path != 1) {
+        fail(MCGB_E_INVALID, "GEMM path must be 0 (tcgen05) or 1 (mma.sync)");
+        return -1;
+    }
+    g_gemm_path = path;
+    return prev;
 }
 
 int mcgb_mlp_linear_bwd_input(const uint16_t *dpre, const uint16_t *wt, uint16_t *dx, int m, int n, int k,
@@ -340,10 +429,9 @@ int mcgb_mlp_linear_bwd_input(const uint16_t *dpre, const uint16_t *wt, uint16_t
     if (r) return r;
     if (!dpre || !wt || !dx) return fail(MCGB_E_INVALID, "NULL operand");
     /* dX[m,k] = sum_n dPre[m,n] Wt[k,n] */
-    dim3 grid((k + BN - 1) / BN, (m + BM - 1) / BM, 1);
-    gemm_bf16<false, false, EPI_BF16><<<grid, NT, 0, (cudaStream_t)stream>>>(
-        (const bf16 *)dpre, n, (const bf16 *)wt, n, m, k, n, n, nullptr, 0, (bf16 *)dx, nullptr, nullptr, k);
-    return check_launch("mlp backward input");
+    return launch_gemm<false, false, EPI_BF16>((const bf16 *)dpre, n, (const bf16 *)wt, n, m, k, n, n, 1, nullptr,
+                                               0, (bf16 *)dx, nullptr, nullptr, k, (cudaStream_t)stream,
+                                               "mlp backward input");
 }
 
 int mcgb_mlp_linear_bwd_weight(const uint16_t *dpre, const uint16_t *x, float *dw, float *scratch,
@@ -352,13 +440,13 @@ int mcgb_mlp_linear_bwd_weight(const uint16_t *dpre, const uint16_t *x, float *d
     if (r) return r;
     if (!dpre || !x || !dw || !scratch) return fail(MCGB_E_INVALID, "NULL operand");
     /* dW[n,k] = sum_m dPre[m,n] X[m,k]: R = n, Cc = k, reduction over m */
-    int slices = weight_slices(m, n, k);
-    int per = ((m + slices - 1) / slices + BK - 1) / BK * BK;
+    const int path = g_gemm_path, tk = path == 0 ? TBK : BK;
+    int slices = weight_slices(m, n, k, path);
+    int per = ((m + slices - 1) / slices + tk - 1) / tk * tk;
     slices = (m + per - 1) / per;
-    dim3 grid((k + BN - 1) / BN, (n + BM - 1) / BM, slices);
-    gemm_bf16<true, true, EPI_F32><<<grid, NT, 0, (cudaStream_t)stream>>>(
-        (const bf16 *)dpre, n, (const bf16 *)x, k, n, k, m, per, nullptr, 0, nullptr, scratch, nullptr, k);
-    r = check_launch("mlp backward weight");
+    r = launch_gemm<true, true, EPI_F32>((const bf16 *)dpre, n, (const bf16 *)x, k, n, k, m, per, slices, nullptr,
+                                         0, nullptr, scratch, nullptr, k, (cudaStream_t)stream,
+                                         "mlp backward weight");
     if (r) return r;
     size_t total = (size_t)n * k;
     unsigned blocks = (unsigned)((total + 255) / 256);
@@ -366,18 +454,21 @@ int mcgb_mlp_linear_bwd_weight(const uint16_t *dpre, const uint16_t *x, float *d
     return check_launch("mlp weight slice sum");
 }
 
-uint64_t mcgb_mlp_act_bwd_scratch(int m, int n) { return (uint64_t)((m + 255) / 256) * (uint64_t)n; }
+uint64_t mcgb_mlp_act_bwd_scratch(int m, int n) {
+    if (m <= 0 || n <= 0) return 0;
+    return (uint64_t)((m + ACT_ROWS - 1) / ACT_ROWS) * (uint64_t)n;
+}
 
 int mcgb_mlp_act_bwd(const uint16_t *dy, const float *pre, uint16_t *dpre, float *db, float *scratch,
                       int m, int n, int act, void *stream) {
     if (m <= 0 || n <= 0 || !dy || !dpre || !db || !scratch || (act && !pre))
         return fail(MCGB_E_INVALID, "bad act_bwd arguments");
-    dim3 grid((n + 31) / 32, (m + 255) / 256);
+    dim3 grid((n + 31) / 32, (m + ACT_ROWS - 1) / ACT_ROWS);
     act_bwd_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const bf16 *)dy, pre, (bf16 *)dpre, scratch,
                                                           m, n, act);
     int r = check_launch("mlp activation backward");
     if (r) return r;
-    int chunks = (m + 255) / 256;
+    int chunks = (m + ACT_ROWS - 1) / ACT_ROWS;
     sum_slices<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(scratch, db, chunks, (size_t)n);
     return check_launch("mlp bias gradient");
 }
@@ -386,8 +477,8 @@ int mcgb_mlp_loss_grad(const float *y, const float *t, const float *w, uint16_t 
                        int n, int nv, int mode, float scale, void *stream) {
     if (m <= 0 || n <= 0 || nv <= 0 || nv > n || !y || !t || !dy || !loss || mode < 0 || mode > 1)
         return fail(MCGB_E_INVALID, "bad loss_grad arguments");
-    loss_grad_kernel<<<(m + 255) / 256, 256, 0, (cudaStream_t)stream>>>(y, t, w, (bf16 *)dy, loss, m, n, nv,
-                                                                       mode, scale, 4.0f);
+    loss_grad_kernel<<<(m + 255) / 256, LOSS_THREADS, 0, (cudaStream_t)stream>>>(y, t, w, (bf16 *)dy, loss, m, n,
+                                                                                nv, mode, scale, 4.0f);
     return check_launch("mlp loss gradient");
 }
 
@@ -410,6 +501,34 @@ int mcgb_mlp_adamw(float *w, uint16_t *wb, uint16_t *wt, const float *g, float *
     adamw_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(w, (bf16 *)wb, (bf16 *)wt, g, m, v, rows, cols, lr,
                                                            b1, b2, eps, wd, c1, c2);
     return check_launch("mlp adamw");
+}
+
+int mcgb_mlp_adamw_multi(const McgbAdamwTensor *tensors, int count, float lr, float b1, float b2, float eps,
+                         int step, void *stream) {
+    if (!tensors || count < 1 || count > MCGB_ADAMW_MAX_TENSORS || step < 1)
+        return fail(MCGB_E_INVALID, "bad adamw_multi arguments");
+    AdamwMulti p;
+    memset(&p, 0, sizeof(p));
+    p.count = count;
+    p.start[0] = 0;
+    for (int k = 0; k < count; ++k) {
+        const McgbAdamwTensor &t = tensors[k];
+        if (!t.w || !t.w_bf16 || !t.grad || !t.m || !t.v || t.rows <= 0 || t.cols <= 0)
+            return fail(MCGB_E_INVALID, "bad adamw_multi tensor %d", k);
+        p.t[k] = t;
+        p.start[k + 1] = p.start[k] + (uint64_t)t.rows * (uint64_t)t.cols;
+    }
+    p.lr = lr;
+    p.b1 = b1;
+    p.b2 = b2;
+    p.eps = eps;
+    p.c1 = 1.0f - powf(b1, (float)step);
+    p.c2 = 1.0f - powf(b2, (float)step);
+    uint64_t blocks = (p.start[count] + 255) / 256;
+    uint64_t most = 4ull * (uint64_t)sm_count();
+    if (blocks > most) blocks = most;
+    adamw_multi_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(p);
+    return check_launch("mlp adamw multi");
 }
 
 }  // extern "C"

@@ -32,7 +32,7 @@ import time
 
 import numpy as np
 
-from . import _lib
+from . import _abi, _lib
 from .batched import BatchedMc
 from .mcbase.mcutil import Axis
 
@@ -130,6 +130,7 @@ class Mlp:
         self.dpre = [torch.empty((batch, p), dtype=torch.bfloat16, device='cuda') for p in self.pads[1:]]
         self.dw = [torch.empty_like(w) for w in self.w]
         self.db = [torch.empty_like(b) for b in self.b]
+        self._adamw_tab = None          # holds the gradient pointers
         nscr = 0
         for i in range(len(self.w)):
             nscr = max(nscr, int(self.lib.mcgb_mlp_bwd_weight_scratch(batch, self.pads[i + 1], self.pads[i])),
@@ -191,7 +192,36 @@ class Mlp:
     def mse_grad(self, y, t_f32, m, n_valid):
         return self.loss_grad(y, t_f32, m, n_valid, mode=0)
 
+    def _adamw_table(self):
+        """The multi-tensor AdamW table of the network: the weights (with
+        their transposed bf16 copies) and the biases of every layer."""
+        if getattr(self, '_adamw_tab', None) is None:
+            tab = (_abi.McgbAdamwTensor * (2 * len(self.w)))()
+            for i in range(len(self.w)):
+                n, k = self.w[i].shape
+                for j, (w, wb, wt, g, m, v, rows, cols) in enumerate((
+                        (self.w[i], self.wb[i], self.wt[i], self.dw[i], self.m[i], self.v[i], n, k),
+                        (self.b[i], self.bb[i], None, self.db[i], self.mb[i], self.vb[i], 1, n))):
+                    t = tab[2 * i + j]
+                    t.w, t.w_bf16 = w.data_ptr(), wb.data_ptr()
+                    t.wt_bf16 = wt.data_ptr() if wt is not None else None
+                    t.grad, t.m, t.v = g.data_ptr(), m.data_ptr(), v.data_ptr()
+                    t.rows, t.cols = rows, cols
+            self._adamw_tab = tab
+        return self._adamw_tab
+
     def adamw(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        """One AdamW step of every weight and bias (weight decay on the
+        weights only), in one launch."""
+        self.step_count += 1
+        tab = self._adamw_table()
+        for i in range(len(tab)):
+            tab[i].weight_decay = wd if i % 2 == 0 else 0.0
+        _lib.check(self.lib.mcgb_mlp_adamw_multi(tab, len(tab), lr, b1, b2, eps, self.step_count,
+                                                 self._stream()))
+
+    def adamw_per_tensor(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        """The same step as adamw(), one launch per tensor."""
         self.step_count += 1
         for i in range(len(self.w)):
             n, k = self.w[i].shape

@@ -26,8 +26,17 @@ def _net(torch, sizes, seed=0, batch=512):
     return net
 
 
+@pytest.fixture(params=[0, 1], ids=['tcgen05', 'mma_sync'])
+def gemm_path(request, lib):
+    """Run a test on each GEMM implementation, restoring the default."""
+    prev = lib.mcgb_mlp_gemm_path(request.param)
+    assert prev in (0, 1)
+    yield request.param
+    lib.mcgb_mlp_gemm_path(prev)
+
+
 @pytest.mark.parametrize('sizes', [(4, 256, 256, 256, 30), (4, 64, 64, 30)])
-def test_forward_and_gradients_match_oracle(cuda, sizes):
+def test_forward_and_gradients_match_oracle(cuda, sizes, gemm_path):
     torch = cuda
     m = 512
     net = _net(torch, sizes, batch=m)
@@ -58,6 +67,75 @@ def test_forward_and_gradients_match_oracle(cuda, sizes):
     net.forward(xb)
     net.backward(dyb, m)
     assert all(np.array_equal(a.cpu().numpy(), b_) for a, b_ in zip(net.dw, [d.astype(np.float32) for d in dw]))
+
+
+@pytest.mark.parametrize('m,n,k', [(4096, 256, 256), (4096, 32, 256), (4096, 256, 16), (136, 48, 32),
+                                   (520, 256, 256)])
+def test_gemm_paths_agree_with_float64(cuda, lib, m, n, k):
+    """The three GEMM entry points on the tcgen05 path and on the mma.sync
+    path against float64 products of the same bf16 operands: partial tiles
+    in every dimension (136 rows, 48 and 32 columns, a 16-wide reduction)."""
+    import ctypes as C
+    from pyxopto_gb300 import _lib
+    torch = cuda
+    rng = np.random.default_rng(m + 3 * n + 7 * k)
+    bf = lambda a: torch.from_numpy(a.astype(np.float32)).cuda().to(torch.bfloat16)
+    x = bf(rng.normal(0, 1, (m, k)))
+    w = bf(rng.normal(0, 1 / np.sqrt(k), (n, k)))
+    wt = w.t().contiguous()
+    b = torch.from_numpy(rng.normal(0, 0.1, n).astype(np.float32)).cuda()
+    dpre = bf(rng.normal(0, 1e-2, (m, n)))
+    X, W, DP = (t.float().cpu().numpy().astype(np.float64) for t in (x, w, dpre))
+    ref = {'pre': X @ W.T + b.cpu().numpy().astype(np.float64), 'dx': DP @ W, 'dw': DP.T @ X}
+    P = lambda t: C.c_void_p(t.data_ptr())
+    out = {}
+    for path in (0, 1):
+        prev = lib.mcgb_mlp_gemm_path(path)
+        try:
+            y = torch.full((m, n), float('nan'), dtype=torch.bfloat16, device='cuda')
+            pre = torch.full((m, n), float('nan'), device='cuda')
+            _lib.check(lib.mcgb_mlp_linear_fwd(P(x), P(w), P(b), P(y), P(pre), m, n, k, 1, None))
+            dx = torch.full((m, k), float('nan'), dtype=torch.bfloat16, device='cuda')
+            _lib.check(lib.mcgb_mlp_linear_bwd_input(P(dpre), P(wt), P(dx), m, n, k, None))
+            scratch = torch.empty(int(lib.mcgb_mlp_bwd_weight_scratch(m, n, k)), device='cuda')
+            dw = torch.full((n, k), float('nan'), device='cuda')
+            _lib.check(lib.mcgb_mlp_linear_bwd_weight(P(dpre), P(x), P(dw), P(scratch), m, n, k, None))
+            torch.cuda.synchronize()
+            out[path] = {'pre': pre, 'y': y, 'dx': dx, 'dw': dw}
+            out[path] = {key: v.float().cpu().numpy().astype(np.float64) for key, v in out[path].items()}
+        finally:
+            lib.mcgb_mlp_gemm_path(prev)
+    gelu = lambda v: 0.5 * v * (1 + np.tanh(0.7978845608028654 * (v + 0.044715 * v ** 3)))
+    for path, o in out.items():
+        for key in ('pre', 'dw'):             # FP32 results: accumulation order only
+            assert np.max(np.abs(o[key] - ref[key])) <= 1e-4 * np.max(np.abs(ref[key])), (path, key)
+        for key, r in (('y', gelu(ref['pre'])), ('dx', ref['dx'])):   # rounded to bf16
+            assert np.all(np.abs(o[key] - r) <= 2.0 ** -8 * np.abs(r) + 1e-3 * np.max(np.abs(r))), (path, key)
+    assert np.max(np.abs(out[0]['pre'] - out[1]['pre'])) <= 1e-5 * np.max(np.abs(ref['pre']))
+    assert lib.mcgb_mlp_gemm_path(-1) == 0
+    assert lib.mcgb_mlp_gemm_path(7) == -1
+
+
+def test_adamw_multi_equals_per_tensor(cuda, lib):
+    """The one-launch AdamW of every weight and bias gives the same bits as
+    one launch per tensor (weights with weight decay and their transposed
+    bf16 copies, biases without), over three steps."""
+    from pyxopto_gb300.surrogate import Mlp
+    torch = cuda
+    a = Mlp(sizes=(4, 64, 64, 30), seed=3, batch=256)
+    b = Mlp(sizes=(4, 64, 64, 30), seed=3, batch=256)
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        for ga, gb in zip(a.dw + a.db, b.dw + b.db):
+            g = torch.from_numpy(rng.normal(0, 1e-2, tuple(ga.shape)).astype(np.float32)).cuda()
+            ga.copy_(g)
+            gb.copy_(g)
+        a.adamw(lr=1e-3, wd=1e-2)
+        b.adamw_per_tensor(lr=1e-3, wd=1e-2)
+    torch.cuda.synchronize()
+    for name in ('w', 'b', 'wb', 'wt', 'm', 'v', 'bb', 'mb', 'vb'):
+        for x, y in zip(getattr(a, name), getattr(b, name)):
+            assert torch.equal(x, y), name
 
 
 @pytest.mark.parametrize('mode', [0, 1])
