@@ -502,12 +502,18 @@ def mlp_train_bench(args):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / (args.steps * inner)
+    # launches per step: the layers' forward GEMMs, the loss gradient, per
+    # layer the activation backward + bias sum and the weight gradient + slice
+    # sum, the input gradients below the top layer, the tied input columns and
+    # one AdamW over every tensor
+    nl = len(net.w)
+    launches = nl + 1 + 4 * nl + (nl - 1) + (1 if net.split else 0) + 1
     flops = 3 * 2 * m * (16 * 256 + 256 * 256 * 2 + 256 * 32)
     return {'metric': 'training profiles/s (MLP 4-256-256-256-30, batch 4096)', 'value': m / (ms / 1e3),
             'unit': 'profiles/s', 'ms_per_step': ms, 'tflops_dense': flops / (ms / 1e3) / 1e12,
             'config': {'workload': 'mlp_train_step', 'batch': m, 'layers': '4-256-256-256-30 (16/32 padded)',
                        'steps_per_bench_step': inner, 'gemm': args.mlp_gemm},
-            'gpu_launches': args.steps * inner * 33}
+            'gpu_launches': args.steps * inner * launches}
 
 
 def fiber_sweep_bench(args):

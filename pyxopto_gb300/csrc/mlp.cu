@@ -156,13 +156,31 @@ gemm_bf16(const bf16 *__restrict__ A, int lda, const bf16 *__restrict__ B, int l
             }
 }
 
-/* dW = sum of the slice partials in slice order. */
-__global__ void sum_slices(const float *__restrict__ part, float *out, int slices, size_t n) {
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float s = 0.0f;
-        for (int z = 0; z < slices; ++z) s += part[(size_t)z * n + i];
-        out[i] = s;
+/* out[i] = sum over z of part[z*n + i] in a fixed order: warp w of a block
+   adds slices w, w + 8, w + 16, ... of 32 consecutive entries, then the
+   eight warp sums are added in warp order.  One block per 32 entries. */
+constexpr int SUM_THREADS = 256;
+
+__global__ void __launch_bounds__(SUM_THREADS)
+sum_slices(const float *__restrict__ part, float *out, int slices, size_t n) {
+    __shared__ float red[SUM_THREADS / 32][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t i = (size_t)blockIdx.x * 32 + lane;
+    float s = 0.0f;
+    if (i < n)
+        for (int z = w; z < slices; z += SUM_THREADS / 32) s += part[(size_t)z * n + i];
+    red[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && i < n) {
+        float t = 0.0f;
+#pragma unroll
+        for (int k = 0; k < SUM_THREADS / 32; ++k) t += red[k][lane];
+        out[i] = t;
     }
+}
+
+void launch_sum_slices(const float *part, float *out, int slices, size_t n, cudaStream_t st) {
+    sum_slices<<<(unsigned)((n + 31) / 32), SUM_THREADS, 0, st>>>(part, out, slices, n);
 }
 
 /* Rows per block of the activation backward: one column partial sum per
@@ -448,9 +466,7 @@ int mcgb_mlp_linear_bwd_weight(const uint16_t *dpre, const uint16_t *x, float *d
                                          0, nullptr, scratch, nullptr, k, (cudaStream_t)stream,
                                          "mlp backward weight");
     if (r) return r;
-    size_t total = (size_t)n * k;
-    unsigned blocks = (unsigned)((total + 255) / 256);
-    sum_slices<<<blocks, 256, 0, (cudaStream_t)stream>>>(scratch, dw, slices, total);
+    launch_sum_slices(scratch, dw, slices, (size_t)n * k, (cudaStream_t)stream);
     return check_launch("mlp weight slice sum");
 }
 
@@ -469,7 +485,7 @@ int mcgb_mlp_act_bwd(const uint16_t *dy, const float *pre, uint16_t *dpre, float
     int r = check_launch("mlp activation backward");
     if (r) return r;
     int chunks = (m + ACT_ROWS - 1) / ACT_ROWS;
-    sum_slices<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(scratch, db, chunks, (size_t)n);
+    launch_sum_slices(scratch, db, chunks, (size_t)n, (cudaStream_t)stream);
     return check_launch("mlp bias gradient");
 }
 

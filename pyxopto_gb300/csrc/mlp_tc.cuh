@@ -20,10 +20,11 @@
  * 128 and between row groups 1024.  One MMA of K = 16 covers two reduction
  * groups, so MMA kk of a chunk starts 256 * kk bytes into each tile.
  *
- * Pipeline: two shared-memory stages; the next chunk's global loads go to
- * registers while one thread issues the current chunk's four MMAs and
- * commits them to the stage's mbarrier, which frees the stage two chunks
- * later.
+ * Pipeline: four shared-memory stages filled by cp.async (16 bytes per
+ * copy, zero-filled outside the matrix), so a 256-deep reduction has all its
+ * operands in flight at once; one thread issues each chunk's four MMAs and
+ * commits them to the stage's mbarrier, which frees the stage for the chunk
+ * four later.
  *
  * Epilogue: tcgen05.ld of 32 lanes x 16 columns per warp (warp w owns TMEM
  * lanes 32w..32w+31, one output row per thread), then the same fused
@@ -38,11 +39,15 @@ constexpr int TBM = 128, TBK = 64, TNT = 128;
 constexpr uint32_t TC_A_BYTES = TBM * TBK * 2;                 /* 16 KB */
 constexpr uint64_t TC_WAIT_NS = 1000000000ull;
 
+constexpr int TC_STAGES = 4;                                   /* K = 256 fits in flight at once */
+
 template <int BN>
 struct TcShape {
     static constexpr uint32_t B_BYTES = BN * TBK * 2;
     static constexpr uint32_t STAGE = TC_A_BYTES + B_BYTES;
-    static constexpr uint32_t SMEM = 2 * STAGE + 32;           /* two stages, 2 mbarriers, TMEM address */
+    static constexpr uint32_t BARS = TC_STAGES * STAGE;         /* one mbarrier per stage */
+    static constexpr uint32_t TADDR = BARS + 8 * TC_STAGES;     /* the TMEM address */
+    static constexpr uint32_t SMEM = TADDR + 16;
 };
 
 /* kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A
@@ -132,19 +137,34 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-/* Operand staging in two halves, so that the global loads of the next
-   chunk are in flight while the tensor cores work on the current one.
-   X(r, l) = TR ? X[l*ld + r] : X[r*ld + l]; rows >= R and reduction
-   indices >= L are zero (R, L, r0, l0 are multiples of 8).  Vector j of
-   thread t is v = t + 128 j:
+__device__ __forceinline__ void tc_cp16(uint32_t dst, const void *src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+/* Wait until at most n (0..TC_STAGES-1) of this thread's copy groups are pending. */
+__device__ __forceinline__ void tc_cp_wait(int n) {
+    switch (n) {
+        case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+        case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+        case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+        default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+    }
+}
+
+/* Operand staging with cp.async, 16 bytes per copy, zero-filled outside the
+   matrix.  X(r, l) = TR ? X[l*ld + r] : X[r*ld + l]; rows >= R and
+   reduction indices >= L are zero (R, L, r0, l0 are multiples of 8).
+   Vector j of thread t is v = t + 128 j:
      K-major (!TR): row-in-group v & 7, reduction group (v >> 3) & 7, row
        group v >> 6; 16 bytes of 8 reduction indices of one row, stored as
        row (v & 7) of core matrix (row group, reduction group);
      MN-major (TR): reduction index l from v & 15 and (v >> 5), row group
        from (v >> 4) & 1 and (v >> 5); 16 bytes of 8 rows at one reduction
        index, stored as row (l & 7) of core matrix (row group, l >> 3).
-   Every 8-lane phase of a warp's 16-byte stores covers 128 contiguous
-   bytes (no bank conflicts). */
+   Every 8-lane phase of a warp's 16-byte copies covers 128 contiguous
+   bytes of shared memory (no bank conflicts). */
 template <bool TR, int ROWS>
 struct TcStage {
     static constexpr int N = ROWS * TBK / 8 / TNT;
@@ -158,26 +178,18 @@ struct TcStage {
             row = ((hi / (TBK / 16)) * 2 + ((v >> 4) & 1)) * 8;
         }
     }
-    __device__ __forceinline__ static void load(uint4 (&reg)[N], const bf16 *__restrict__ X, int ld, int R,
-                                                int L, int r0, int l0) {
+    __device__ __forceinline__ static void issue(uint32_t S, const bf16 *__restrict__ X, int ld, int R, int L,
+                                                 int r0, int l0) {
 #pragma unroll
         for (int j = 0; j < N; ++j) {
             int row, l;
             map(threadIdx.x + TNT * j, row, l);
             const int r = r0 + row, ll = l0 + l;
-            reg[j] = make_uint4(0u, 0u, 0u, 0u);
-            if (r < R && ll < L)
-                reg[j] = __ldg(reinterpret_cast<const uint4 *>(TR ? X + (size_t)ll * ld + r : X + (size_t)r * ld + ll));
-        }
-    }
-    __device__ __forceinline__ static void store(uint8_t *S, const uint4 (&reg)[N]) {
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-            int row, l;
-            map(threadIdx.x + TNT * j, row, l);
+            const bool valid = r < R && ll < L;
+            const bf16 *src = valid ? (TR ? X + (size_t)ll * ld + r : X + (size_t)r * ld + ll) : X;
             const uint32_t off = TR ? (uint32_t)(((row >> 3) * (TBK / 8) + (l >> 3)) * 128 + (l & 7) * 16)
                                     : (uint32_t)(((row >> 3) * (TBK / 8) + (l >> 3)) * 128 + (row & 7) * 16);
-            *reinterpret_cast<uint4 *>(S + off) = reg[j];
+            tc_cp16(S + off, src, valid);
         }
     }
 };
@@ -191,7 +203,7 @@ gemm_tc(const bf16 *__restrict__ A, int lda, const bf16 *__restrict__ B, int ldb
     typedef TcStage<TB, BN> StB;
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tc_smem);
-    const uint32_t bar0 = sbase + 2 * Sh::STAGE, bar1 = bar0 + 8, taddr_slot = bar0 + 16;
+    const uint32_t bar0 = sbase + Sh::BARS, taddr_slot = sbase + Sh::TADDR;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int r0 = blockIdx.y * TBM, c0 = blockIdx.x * BN;
     const int lb = blockIdx.z * l_slice;
@@ -199,8 +211,8 @@ gemm_tc(const bf16 *__restrict__ A, int lda, const bf16 *__restrict__ B, int ldb
     const int nch = le > lb ? (le - lb + TBK - 1) / TBK : 0;
 
     if (tid == 0) {
-        tc_mbar_init(bar0);
-        tc_mbar_init(bar1);
+#pragma unroll
+        for (int s = 0; s < TC_STAGES; ++s) tc_mbar_init(bar0 + 8 * s);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -209,33 +221,27 @@ gemm_tc(const bf16 *__restrict__ A, int lda, const bf16 *__restrict__ B, int ldb
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    uint4 ra[StA::N], rb[StB::N];
-    if (nch > 0) {
-        StA::load(ra, A, lda, R, le, r0, lb);
-        StB::load(rb, B, ldb, Cc, le, c0, lb);
+    /* the first TC_STAGES chunks go in flight at once */
+    for (int i = 0; i < nch && i < TC_STAGES; ++i) {
+        const uint32_t st = sbase + i * Sh::STAGE;
+        StA::issue(st, A, lda, R, le, r0, lb + i * TBK);
+        StB::issue(st + TC_A_BYTES, B, ldb, Cc, le, c0, lb + i * TBK);
+        tc_cp_commit();
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(tc_smem + 2 * Sh::STAGE + 16);
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(tc_smem + Sh::TADDR);
     const uint64_t t_end = tc_clock_ns() + TC_WAIT_NS;
 
     bool ok = true;
     for (int i = 0; i < nch; ++i) {
-        const int s = i & 1;
-        const uint32_t bar = s ? bar1 : bar0;
-        /* the stage's previous chunk (i - 2) must have been consumed */
-        if (i >= 2 && ok) ok = tc_mbar_wait(bar, (uint32_t)((i - 2) >> 1) & 1u, t_end);
-        uint8_t *SA = tc_smem + s * Sh::STAGE;
-        StA::store(SA, ra);
-        StB::store(SA + TC_A_BYTES, rb);
+        const int s = i % TC_STAGES;
+        const uint32_t bar = bar0 + 8 * s;
+        /* chunk i has landed once no more than the later committed groups are pending */
+        tc_cp_wait(min(nch, i + TC_STAGES) - i - 1);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        if (i + 1 < nch) {
-            const int l0 = lb + (i + 1) * TBK;
-            StA::load(ra, A, lda, R, le, r0, l0);
-            StB::load(rb, B, ldb, Cc, le, c0, l0);
-        }
         if (tid == 0) {
             tc_fence_after();
             const uint32_t a = sbase + s * Sh::STAGE, b = a + TC_A_BYTES;
@@ -245,10 +251,19 @@ gemm_tc(const bf16 *__restrict__ A, int lda, const bf16 *__restrict__ B, int ldb
                        (i | kk) ? 1u : 0u);
             tc_commit(bar);
         }
+        if (i + TC_STAGES < nch) {
+            /* refill the stage once its MMAs have read it */
+            if (ok) ok = tc_mbar_wait(bar, (uint32_t)(i / TC_STAGES) & 1u, t_end);
+            const uint32_t st = sbase + s * Sh::STAGE;
+            const int l0 = lb + (i + TC_STAGES) * TBK;
+            StA::issue(st, A, lda, R, le, r0, l0);
+            StB::issue(st + TC_A_BYTES, B, ldb, Cc, le, c0, l0);
+            tc_cp_commit();
+        }
     }
     if (nch > 0 && ok) {
         const int i = nch - 1;
-        ok = tc_mbar_wait((i & 1) ? bar1 : bar0, (uint32_t)(i >> 1) & 1u, t_end);
+        ok = tc_mbar_wait(bar0 + 8 * (i % TC_STAGES), (uint32_t)(i / TC_STAGES) & 1u, t_end);
     }
     tc_fence_after();
 
