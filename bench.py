@@ -61,8 +61,8 @@ PROFILED_TRAFFIC = {
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (1.80e10, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 PROFILED_ISSUE_ACTIVE = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.892, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
-    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.844, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.897, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.845, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # L2 atomic-unit use of the transport kernel's 64-bit tally atomics, from a
 # medium-case ncu capture (one kernel, one launch, 2e7 packets): the share of
@@ -71,12 +71,12 @@ PROFILED_ISSUE_ACTIVE = {
 # per interaction step (lts__t_requests_op_red), and the L2 throughput.
 PROFILED_L2_ATOMICS = {
     ('c2_skin_gk_fluence', 'fast', 'dynamic'): (
-        {'atomic_unit_active_pct': 13.65, 'red_requests_per_packet': 436.8,
-         'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 20.47},
+        {'atomic_unit_active_pct': 14.20, 'red_requests_per_packet': 436.7,
+         'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 21.30},
         'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
-        {'atomic_unit_active_pct': 11.22, 'red_requests_per_packet': 300.1,
-         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 21.96},
+        {'atomic_unit_active_pct': 11.27, 'red_requests_per_packet': 300.0,
+         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 22.06},
         'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # DRAM traffic of the voxel fluence (same capture): dram__bytes_read +
@@ -84,7 +84,7 @@ PROFILED_L2_ATOMICS = {
 # fluence tally's atomics; the tally itself is read once).
 PROFILED_HBM = {
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
-        {'gbs': 38.3, 'bytes_per_packet': 180.1},
+        {'gbs': 38.5, 'bytes_per_packet': 180.1},
         'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 HBM_FALLBACK_GBS = 6800.0

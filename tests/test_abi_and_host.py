@@ -77,6 +77,26 @@ def test_validation_rejects_bad_configs(lib):
     assert _run(lib, cfg, b) == _abi.E_SIZE     # no trace buffers
 
 
+def test_mlp_entry_points_validate_arguments(lib):
+    """The surrogate's GEMM-path switch and multi-tensor AdamW reject bad
+    arguments before touching the device; scratch sizes follow the row
+    chunking."""
+    from pyxopto_gb300 import _abi
+    assert lib.mcgb_mlp_gemm_path(-1) in (0, 1)
+    assert lib.mcgb_mlp_gemm_path(5) == -1
+    assert b'GEMM path' in lib.mcgb_last_error()
+    tab = (_abi.McgbAdamwTensor * (_abi.ADAMW_MAX_TENSORS + 1))()
+    for count in (0, _abi.ADAMW_MAX_TENSORS + 1):
+        assert lib.mcgb_mlp_adamw_multi(tab, count, 1e-3, 0.9, 0.999, 1e-8, 1, None) == _abi.E_INVALID
+    assert lib.mcgb_mlp_adamw_multi(tab, 1, 1e-3, 0.9, 0.999, 1e-8, 1, None) == _abi.E_INVALID
+    assert b'tensor 0' in lib.mcgb_last_error()
+    assert lib.mcgb_mlp_adamw_multi(tab, 1, 1e-3, 0.9, 0.999, 1e-8, 0, None) == _abi.E_INVALID
+    assert lib.mcgb_mlp_act_bwd_scratch(4096, 256) == 64 * 256
+    assert lib.mcgb_mlp_act_bwd_scratch(0, 256) == 0
+    assert lib.mcgb_mlp_bwd_weight_scratch(0, 256, 256) == 0
+    assert lib.mcgb_mlp_bwd_weight_scratch(4096, 256, 256) % (256 * 256) == 0
+
+
 def test_zero_packets_is_a_no_op(lib):
     mc, cfg, b = _valid_cfg()
     cfg.num_packets = 0
