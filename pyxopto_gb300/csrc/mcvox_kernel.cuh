@@ -767,8 +767,9 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
             need &= ~taken;
         }
         if (!__any_sync(0xffffffffu, active)) break;
+        /* sixteen steps between refills, as in the layered kernel */
 #pragma unroll 1
-        for (int k = 0; k < 8; ++k) {
+        for (int k = 0; k < 16; ++k) {
             if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
@@ -777,7 +778,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                 active = false;
             }
         }
-        iter += 8;
+        iter += 16;
         if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {

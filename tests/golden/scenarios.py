@@ -692,7 +692,24 @@ BENCH = {
                      mode='deposition'),
         nphotons=100_000_000, streams=0, rnginit=1),
 }
-ALL = dict(SCENARIOS, **BENCH)
+# Statistical-only cases (no golden fixture): geometries that exercise the
+# FAST-math free flight against the wall walk.
+STAT = {
+    # a sphere of higher refractive index in a homogeneous cube: packets
+    # reflect and refract at the faces of large homogeneous cubes
+    'vox_sphere_mismatch': dict(
+        medium='mcvox', grid=dict(x=[-1.6e-3, 1.6e-3, 64], y=[-1.6e-3, 1.6e-3, 64], z=[0.0, 3.2e-3, 64]),
+        materials=[dict(n=1.0, mua=0.0, mus=0.0, pf=['Hg', 0.0]),
+                   dict(n=1.33, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
+                   dict(n=1.6, mua=200.0, mus=2e4, pf=['Hg', 0.9])],
+        layout=dict(kind='sphere', center=(0.0, 0.0, 1.2e-3), radius=8e-4),
+        source=dict(type='GaussianBeam', sigma=2e-4, clip=5.0),
+        detectors=dict(top=dict(type='Total'), bottom=dict(type='Total'), specular=dict(type='Total')),
+        fluence=dict(x=[-1.6e-3, 1.6e-3, 64], y=[-1.6e-3, 1.6e-3, 64], z=[0.0, 3.2e-3, 64],
+                     mode='deposition'),
+        nphotons=200_000, streams=0, rnginit=5),
+}
+ALL = dict(SCENARIOS, **BENCH, **STAT)
 
 
 def voxel_layout(grid, layout):
@@ -708,6 +725,9 @@ def voxel_layout(grid, layout):
         m[Z < layout['epidermis']] = 2
         r2 = X ** 2 + (Z - layout['vessel_depth']) ** 2
         m[r2 <= layout['vessel_radius'] ** 2] = 3
+    elif layout['kind'] == 'sphere':
+        cx, cy, cz = layout['center']
+        m[(X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2 <= layout['radius'] ** 2] = 2
     elif layout['kind'] == 'checker':
         ix = np.arange(nx)[None, None, :]
         iy = np.arange(ny)[None, :, None]

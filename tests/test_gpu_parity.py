@@ -443,6 +443,43 @@ def test_fast_voxel_fluence_statistically_equal_to_exact(cuda, lib):
     assert abs(fa.sum(1).mean() / ea.sum(1).mean() - 1.0) < 5e-3
 
 
+def test_box_stepping_reflects_and_refracts_like_the_wall_walk(cuda, lib):
+    """Free flight and box stepping where the faces of large homogeneous
+    cubes meet a refractive-index step (a sphere of n 1.6 in a cube of
+    n 1.33 under air), against the wall-by-wall walk in the same FAST
+    kernels: depth profile, 0.4 mm voxels, the deposits inside and outside
+    the sphere and the detector totals within the 3-sigma gate."""
+    from pyxopto_gb300.mcvox import mcoptions
+    name, nb, n = 'vox_sphere_mismatch', 16, 400_000
+    spec = scenarios.ALL[name]
+    inside = scenarios.voxel_layout(spec['grid'], spec['layout']).reshape(-1) == 2
+    fly = scenarios.build_mc(name, fast=True, scheduling='dynamic')
+    walk = scenarios.build_mc(name, fast=True, scheduling='dynamic')
+    walk._mc_options.append(mcoptions.McVoxelFreeFlight(False))
+    walk._rnginit = 977
+
+    def batches(mc):
+        rows, tots, steps = [], [], 0
+        for _ in range(nb):
+            _, flu, det = mc.run(n)
+            raw = np.asarray(flu.raw, dtype=np.float64).reshape(-1)
+            rows.append(raw)
+            tots.append([float(det.top.raw.sum()), float(det.bottom.raw.sum()),
+                         raw[inside].sum(), raw[~inside].sum()])
+            steps += mc.run_report['steps']
+        return np.array(rows) / n, np.array(tots) / n, steps
+    fa, ta, sa = batches(fly)
+    wa, tw, sw = batches(walk)
+    depth = lambda f: f.reshape(nb, 64, -1).sum(2)
+    coarse = lambda f: f.reshape(nb, 8, 8, 8, 8, 8, 8).sum(axis=(2, 4, 6)).reshape(nb, -1)
+    for what, a, b in (('depth', depth(fa), depth(wa)), ('coarse', coarse(fa), coarse(wa)),
+                       ('totals', ta, tw)):
+        keep = (b.mean(0) > 0) & (b.std(0, ddof=1) / np.sqrt(nb) < 0.2 * b.mean(0))
+        ok, rep = _stats.gate(a[:, keep], b[:, keep])
+        assert ok, (what, rep)
+    assert sa < 0.8 * sw, (sa, sw)
+
+
 def _radius_reference(mat, cap):
     """Largest k <= cap whose cube of voxels within Chebyshev distance k lies
     inside the grid and holds one material (brute force over k)."""
