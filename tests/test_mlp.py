@@ -70,11 +70,13 @@ def test_forward_and_gradients_match_oracle(cuda, sizes, gemm_path):
 
 
 @pytest.mark.parametrize('m,n,k', [(4096, 256, 256), (4096, 32, 256), (4096, 256, 16), (136, 48, 32),
-                                   (520, 256, 256)])
+                                   (520, 256, 256), (264, 64, 80), (256, 64, 1024)])
 def test_gemm_paths_agree_with_float64(cuda, lib, m, n, k):
     """The three GEMM entry points on the tcgen05 path and on the mma.sync
     path against float64 products of the same bf16 operands: partial tiles
-    in every dimension (136 rows, 48 and 32 columns, a 16-wide reduction)."""
+    in every dimension (136 and 264 rows, 48 and 32 columns, 16- and 80-wide
+    reductions) and a 1024-deep reduction that refills every shared-memory
+    stage of the tcgen05 pipeline four times."""
     import ctypes as C
     from pyxopto_gb300 import _lib
     torch = cuda
