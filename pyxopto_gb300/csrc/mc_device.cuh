@@ -611,6 +611,9 @@ MCGB_DEV FluenceCache fluence_cache(const McgbFluence &fl, uint64_t *accu) {
     return FluenceCache{accu + fl.offset, 0xFFFFFFFFu, 0ull};
 }
 
+/* RATE = false compiles out the fluence-rate scaling: the launcher sends
+   rate-mode tallies to the kernels with the optional features (XTRA). */
+template <bool RATE = true>
 MCGB_DEV void fluence_deposit(const McgbFluence &fl, const f3 &pos, float weight, float mua,
                               FluenceCache &cache) {
 #if MCGB_FAST_MATH
@@ -632,7 +635,7 @@ MCGB_DEV void fluence_deposit(const McgbFluence &fl, const f3 &pos, float weight
     uint32_t jz = (uint32_t)__float2int_rd(iz);
     if (jx < fl.shape[0] && jy < fl.shape[1] && jz < fl.shape[2]) {
         uint32_t index = (jz * fl.shape[1] + jy) * fl.shape[0] + jx;
-        if (fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
+        if (RATE && fl.kind == MCGB_FLUENCE_RATE) weight *= (mua != 0.0f) ? mc_div(1.0f, mua) : 0.0f;
         uint32_t w = (uint32_t)(weight * (float)fl.k + 0.5f);
         cache.add(index, w);
     }

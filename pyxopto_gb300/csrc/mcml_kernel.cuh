@@ -501,7 +501,10 @@ static __device__ __forceinline__ void mcml_end(const McgbMcmlConfig &c, const M
 
 /* One interaction step of a packet (the body of McKernel's while(!done)
    loop, xopto/mcml/kernel/mcml.template.c:525-814).  Returns true when the
-   packet terminated. */
+   packet terminated.  XTRA = false compiles out the optional features the
+   launcher routes to the XTRA kernels: trace, optical path length, step
+   limit, surface layouts, fibre-probe detectors, a finite rmax and the
+   fluence-rate scaling. */
 template <int PF, int METHOD, bool FLU, bool XTRA>
 static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const McgbBuffers &b,
                                                  const MlCtx &x, MlPacket &s, Rng &rng,
@@ -548,7 +551,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
                                   : 0.0f;
             f3 dp{s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
                   s.pos.z - step_back * s.dir.z};
-            fluence_deposit(c.fluence, dp, deposit, mua, fcache);
+            fluence_deposit<XTRA>(c.fluence, dp, deposit, mua, fcache);
         }
         if (next != s.layer) {
             { uint32_t ev = mcml_boundary<XTRA>(c, x.lut, L, s.layer, next, x.last_layer, s.pos, s.dir, s.w, rng); if (XTRA) s.events |= ev | MCGB_EV_BOUNDARY_HIT; }
@@ -585,7 +588,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
             done = true;
             s.w -= deposit;
             if (XTRA) s.events |= MCGB_EV_ABSORPTION;
-            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
+            if (FLU) fluence_deposit<XTRA>(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         } else {
             const MlLayer &cl = L[s.layer];
             float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az, s.dir);
@@ -597,7 +600,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         float deposit = s.w * g0.w;
         s.w -= deposit;
         if (XTRA) s.events |= MCGB_EV_ABSORPTION;
-        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
+        if (FLU) fluence_deposit<XTRA>(c.fluence, s.pos, deposit, L[s.layer].g1.y, fcache);
         const MlLayer &cl = L[s.layer];
         float az, ct = pf_sample<PF>(cl.pf0, cl.pf1, x.lut, rng, &az, s.dir);
         scatter_direction(s.dir, ct, az);
@@ -612,7 +615,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         }
     }
     /* rmax, mcml.template.c:759-763 */
-    if (x.use_rmax) {
+    if (XTRA && x.use_rmax) {
         f3 d{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
         if (dot3(d, d) > x.rmax2) {
             done = true;

@@ -541,7 +541,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
                                   : 0.0f;
             f3 dp{s.pos.x - step_back * s.dir.x, s.pos.y - step_back * s.dir.y,
                   s.pos.z - step_back * s.dir.z};
-            fluence_deposit(c.fluence, dp, deposit, mua, fcache);
+            fluence_deposit<XTRA>(c.fluence, dp, deposit, mua, fcache);
         }
         if (d < step) {
             s.events |= mv_boundary(g, M, x.vox, s.dir, s.vi, s.mat, dist, rng) | MCGB_EV_BOUNDARY_HIT;
@@ -596,7 +596,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
             s.w -= deposit;
             if (XTRA) s.events |= MCGB_EV_ABSORPTION;
             done = true;
-            if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
+            if (FLU) fluence_deposit<XTRA>(c.fluence, s.pos, deposit, g0.y, fcache);
         } else {
             const MvMaterial &cm = M[s.mat];
             float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az, s.dir);
@@ -608,7 +608,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
         float deposit = s.w * g0.w;
         s.w -= deposit;
         if (XTRA) s.events |= MCGB_EV_ABSORPTION;
-        if (FLU) fluence_deposit(c.fluence, s.pos, deposit, g0.y, fcache);
+        if (FLU) fluence_deposit<XTRA>(c.fluence, s.pos, deposit, g0.y, fcache);
         const MvMaterial &cm = M[s.mat];
         float az, ct = pf_sample<PF>(cm.pf0, cm.pf1, x.lut, rng, &az, s.dir);
         scatter_direction(s.dir, ct, az);
@@ -625,7 +625,7 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     }
     /* mcvox.template.c:1004-1008 */
     bool escaped = s.w <= 0.0f;
-    if (x.use_rmax) {
+    if (XTRA && x.use_rmax) {
         f3 dd{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
         escaped = escaped || dot3(dd, dd) > x.rmax2;
     }

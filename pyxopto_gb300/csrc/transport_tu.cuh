@@ -8,6 +8,7 @@
  */
 #pragma once
 #include <cuda_runtime.h>
+#include <limits>
 #include <mutex>
 #include "launch.h"
 #if MCGB_MEDIUM == 0
@@ -51,7 +52,8 @@ const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence) {
 #else
 
 /* Dynamic scheduling kernels: phase function x method x fluence x optional
-   features (trace, optical path length, per-packet step limit) x simple
+   features (trace, optical path length, per-packet step limit, fibre-probe
+   detectors, surface layouts, finite rmax, fluence rate) x simple
    source (the common sources only: Line in layered media, Line and
    GaussianBeam in voxelized media). */
 #define MCGB_VX(K, PF, M, F) {{(const void *)K<PF, M, F, false, false>, (const void *)K<PF, M, F, false, true>}, \
@@ -102,8 +104,12 @@ static cudaError_t resident_blocks(const void *k, int block, size_t dyn_smem, in
 cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_t stream,
                         const LaunchShape &shape) {
     const int sched = cfg.opt.scheduling;
+    /* the plain dynamic kernels (XTRA = false) also leave out the rmax test
+       and the fluence-rate scaling */
+    const float rmax2 = cfg.opt.rmax * cfg.opt.rmax;
     bool xtra = cfg.trace.flags != MCGB_TRACE_NONE || cfg.opt.track_optical_pathlength != 0 ||
-                cfg.opt.max_steps_per_packet != 0;
+                cfg.opt.max_steps_per_packet != 0 || rmax2 < std::numeric_limits<float>::infinity() ||
+                cfg.fluence.kind == MCGB_FLUENCE_RATE;
     xtra = xtra || cfg.top.kind >= MCGB_DET_LINEAR_ARRAY || cfg.bottom.kind >= MCGB_DET_LINEAR_ARRAY;
 #if MCGB_MEDIUM == 0
     xtra = xtra || cfg.surface_top.kind != MCGB_SURFACE_NONE ||
