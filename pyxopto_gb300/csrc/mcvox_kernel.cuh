@@ -767,9 +767,11 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
             need &= ~taken;
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        /* sixteen steps between refills, as in the layered kernel */
+        /* 32 steps between refills (+0.6 % against 16 on the skin and
+           vessel grid); the step body is not unrolled (two bodies per
+           iteration cost 10 % here) */
 #pragma unroll 1
-        for (int k = 0; k < 16; ++k) {
+        for (int k = 0; k < 32; ++k) {
             if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
@@ -778,7 +780,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                 active = false;
             }
         }
-        iter += 16;
+        iter += 32;
         if ((iter & 1023u) == 0) {
             uint32_t stop = 0;
             if (lane == 0) {
