@@ -308,11 +308,18 @@ def gpu_bench(args, rank, world, local_rank):
         api._rnginit = 2 + 7919 * rank
         api.run(nphotons, maxthreads=streams)        # warm-up (seeds, buffers)
         torch.cuda.synchronize()
+        barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             api.run(nphotons, maxthreads=streams)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        barrier()
+        if world > 1:
+            # the slowest rank's wall time, as for the device-timed value
+            t = torch.tensor([dt], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            dt = float(t.item())
         h2d = C.sizeof(cfg) + 4 * int(api._lut_size)
         if spec['medium'] == 'mcvox':
             # the voxel grid stays on the device between runs; the material
