@@ -57,11 +57,11 @@ L2_FLUSH_BYTES = 256 << 20
 # fraction of issue slots in use (smsp__issue_active), the resource that
 # bounds this kernel.
 PROFILED_TRAFFIC = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (7.75e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (7.74e6, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (1.80e10, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 PROFILED_ISSUE_ACTIVE = {
-    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.897, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
+    ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.875, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.845, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # L2 atomic-unit use of the transport kernel's 64-bit tally atomics, from a
@@ -71,8 +71,8 @@ PROFILED_ISSUE_ACTIVE = {
 # per interaction step (lts__t_requests_op_red), and the L2 throughput.
 PROFILED_L2_ATOMICS = {
     ('c2_skin_gk_fluence', 'fast', 'dynamic'): (
-        {'atomic_unit_active_pct': 14.20, 'red_requests_per_packet': 436.7,
-         'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 21.30},
+        {'atomic_unit_active_pct': 14.66, 'red_requests_per_packet': 436.6,
+         'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 21.98},
         'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
         {'atomic_unit_active_pct': 11.47, 'red_requests_per_packet': 300.1,

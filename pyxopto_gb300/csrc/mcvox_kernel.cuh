@@ -344,6 +344,7 @@ struct MvPacket {
     float w, opl;
     float free;           /* FAST: radius around pos inside the cube, 0 = none */
     int k;                /* FAST: half width of the cube around vi in voxels, 0 = the voxel */
+    float pend;           /* phased loop: the sampled path not yet taken, < 0 = none */
     uint32_t trace_count, events, steps;
     uint64_t p;
 };
@@ -442,6 +443,7 @@ static __device__ __forceinline__ void mcvox_begin(const McgbMcvoxConfig &c, con
                          b.accumulator, prev_pos);
     s.k = MCGB_FAST_MATH ? mv_cube_k(x, s.vi) : 0;
     s.free = MCGB_FAST_MATH ? mv_ball(x, s.k) : 0.0f;
+    s.pend = -1.0f;
     if (x.use_trace && (c.trace.flags & MCGB_TRACE_START))
         trace_event(c.trace, s.p, s.trace_count, s.events, s.pos, s.dir, s.w, s.opl, b.float_buffer);
 }
@@ -470,21 +472,27 @@ static __device__ __forceinline__ void mcvox_end(const McgbMcvoxConfig &c, const
    path known to exceed a distance is again exponential), so the interaction
    points have the same distribution.  With a finite rmax, cubes lie inside
    the rmax sphere, so the packets end at the same steps as the reference's. */
+template <int METHOD>
+static __device__ __forceinline__ float mcvox_sample(const MvCtx &x, MvPacket &s, Rng &rng) {
+    const float4 g0 = x.M[s.mat].g0;   /* mus, mua, step factor, mua_inv_mut */
+    ++s.steps;
+    float u = rng.next();
+    float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) ? mc_div(-mc_log(u), g0.x)
+                                                                   : sample_step(u, g0.z);
+    return fminf(step, FLT_MAX);
+}
+
+/* The rest of a step after its free path is drawn (mcvox_sample). */
 template <int PF, int METHOD, bool FLU, bool XTRA>
-static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
+static __device__ __forceinline__ bool mcvox_move(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
-                                                  FluenceCache &fcache, uint32_t &status) {
+                                                  FluenceCache &fcache, uint32_t &status, float step) {
     constexpr bool FREE = MCGB_FAST_MATH && METHOD != MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT;
     const MvMaterial *M = x.M;
     const MvGeom &g = x.g;
     const McgbRunOptions &o = c.opt;
     uint64_t *accu = b.accumulator;
     const float4 g0 = M[s.mat].g0;   /* mus, mua, step factor, mua_inv_mut */
-    ++s.steps;
-    float u = rng.next();
-    float step = (METHOD == MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT) ? mc_div(-mc_log(u), g0.x)
-                                                                   : sample_step(u, g0.z);
-    step = fminf(step, FLT_MAX);
     const bool flight = FREE && step < s.free;
     if (FREE && !flight && s.free > 0.0f) {
         /* The path reaches beyond the ball: move through it without an
@@ -646,6 +654,14 @@ static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, cons
     return done;
 }
 
+template <int PF, int METHOD, bool FLU, bool XTRA>
+static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
+                                                  const MvCtx &x, MvPacket &s, Rng &rng,
+                                                  FluenceCache &fcache, uint32_t &status) {
+    const float step = mcvox_sample<METHOD>(x, s, rng);
+    return mcvox_move<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status, step);
+}
+
 template <int PF>
 static __device__ __forceinline__ const float *mcvox_stage(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                            MvSmem &sm, float *s_lut, int lut_in_smem) {
@@ -722,6 +738,8 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
     __shared__ MvSmem sm;
     extern __shared__ float s_lut[];
     const float *lut = mcvox_stage<PF>(c, b, sm, s_lut, lut_in_smem);
+    /* the phased loop: FAST free flight in the plain kernels */
+    constexpr bool PHASED = MCGB_FAST_MATH && METHOD != MCGB_METHOD_MICROSCOPIC_BEER_LAMBERT && !XTRA;
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t t_deadline = globaltimer_ns() + deadline_ns;
     const MvCtx x = mcvox_ctx(c, b, sm.materials, lut);
@@ -772,7 +790,29 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
            iteration cost 10 % here) */
 #pragma unroll 1
         for (int k = 0; k < 32; ++k) {
-            if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
+            if (PHASED) {
+                /* Phased steps: every lane draws its path; lanes whose path
+                   leaves their ball (wall steps) wait until they are at
+                   least half of the active lanes, so that the wall code
+                   runs for many lanes at once while the others fly.  A
+                   lane's own sequence of operations is that of mcvox_step. */
+                if (active && s.pend < 0.0f) s.pend = mcvox_sample<METHOD>(x, s, rng);
+                const bool wall = active && !(s.pend < s.free);
+                const uint32_t act_m = __ballot_sync(0xffffffffu, active);
+                const uint32_t wall_m = __ballot_sync(0xffffffffu, wall);
+                const bool run_walls = 2 * __popc(wall_m) >= __popc(act_m);
+                if (active && (run_walls || !wall)) {
+                    const float step = s.pend;
+                    s.pend = -1.0f;
+                    if (mcvox_move<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status, step)) {
+                        ++packets;
+                        steps += s.steps;
+                        s.steps = 0;
+                        mcvox_end(c, b, x, s);
+                        active = false;
+                    }
+                }
+            } else if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
                 s.steps = 0;

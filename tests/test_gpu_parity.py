@@ -443,6 +443,28 @@ def test_fast_voxel_fluence_statistically_equal_to_exact(cuda, lib):
     assert abs(fa.sum(1).mean() / ea.sum(1).mean() - 1.0) < 5e-3
 
 
+@pytest.mark.parametrize('name', ['c3_vox_skin_vessel', 'vox_sphere_mismatch'])
+def test_phased_voxel_loop_keeps_every_packet_unchanged(cuda, lib, name):
+    """The plain FAST voxel kernel defers a lane's wall steps until half of
+    the warp's lanes wait for one (phased loop); each packet still runs the
+    same operations in the same order as in the unphased loop, which the
+    feature kernel keeps (chosen here by a step limit that is never reached):
+    fluence and detector tallies and the step count are the same integers."""
+    n = 2_000_000 if name == 'c3_vox_skin_vessel' else 500_000
+    out = []
+    for limit in (0, 1 << 40):
+        mc = scenarios.build_mc(name, fast=True, scheduling='dynamic')
+        mc._rnginit = 31
+        mc.max_steps_per_packet = limit
+        _, flu, det = mc.run(n)
+        out.append((np.asarray(flu.raw).copy(), np.asarray(det.top.raw).copy(),
+                    np.asarray(det.bottom.raw).copy(), mc.run_report['steps']))
+    (fa, ta, ba, sa), (fb, tb, bb, sb) = out
+    assert sa == sb
+    assert np.array_equal(ta, tb) and np.array_equal(ba, bb)
+    assert np.array_equal(fa, fb)
+
+
 def test_box_stepping_reflects_and_refracts_like_the_wall_walk(cuda, lib):
     """Free flight and box stepping where the faces of large homogeneous
     cubes meet a refractive-index step (a sphere of n 1.6 in a cube of
