@@ -62,7 +62,7 @@ PROFILED_TRAFFIC = {
 }
 PROFILED_ISSUE_ACTIVE = {
     ('c2_skin_gk_fluence', 'fast', 'dynamic'): (0.875, 'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
-    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.845, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
+    ('c3_vox_skin_vessel', 'fast', 'dynamic'): (0.867, 'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # L2 atomic-unit use of the transport kernel's 64-bit tally atomics, from a
 # medium-case ncu capture (one kernel, one launch, 2e7 packets): the share of
@@ -75,8 +75,8 @@ PROFILED_L2_ATOMICS = {
          'red_requests_per_ref_step': 0.484, 'lts_throughput_pct': 21.98},
         'profiles/mcml_dynamic_kernel_c2_skin_gk_fluence.md'),
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
-        {'atomic_unit_active_pct': 11.47, 'red_requests_per_packet': 300.1,
-         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 22.45},
+        {'atomic_unit_active_pct': 12.22, 'red_requests_per_packet': 300.1,
+         'red_requests_per_ref_step': 0.370, 'lts_throughput_pct': 24.04},
         'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 # DRAM traffic of the voxel fluence (same capture): dram__bytes_read +
@@ -84,7 +84,7 @@ PROFILED_L2_ATOMICS = {
 # fluence tally's atomics; the tally itself is read once).
 PROFILED_HBM = {
     ('c3_vox_skin_vessel', 'fast', 'dynamic'): (
-        {'gbs': 39.2, 'bytes_per_packet': 180.1},
+        {'gbs': 41.7, 'bytes_per_packet': 180.2},
         'profiles/mcvox_dynamic_kernel_c3_skin_vessel_200cubed.md'),
 }
 HBM_FALLBACK_GBS = 6800.0
