@@ -47,7 +47,7 @@ unsigned long long g_scratch_ctx[kMaxDevices];   /* context identity of the cach
 
 /* Identity of the calling thread's current context (cuCtxGetCurrent +
    cuCtxGetId, fetched through the runtime so that the library does not link
-   the driver library).  Returns false when it cannot be told; the caller then
+   libcuda).  Returns false when it cannot be told; the caller then
    looks the address up on every call. */
 typedef int (*CtxGetCurrentFn)(void **);
 typedef int (*CtxGetIdFn)(void *, unsigned long long *);

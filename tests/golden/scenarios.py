@@ -30,7 +30,7 @@ def lut_table(n=256, g=0.8):
 
 
 SCENARIOS = {
-    # BASELINE config 1 (10 mm slab, HG 0.8, Line, radial 0-5 mm / 50 bins)
+    # the benchmark slab at golden size (10 mm, HG 0.8, Line, radial 0-5 mm / 50 bins)
     'c1_line_hg_radial': dict(
         medium='mcml',
         layers=[_air(['Hg', 0.0]), dict(d=0.010, n=1.33, mua=100.0, mus=1e4, pf=['Hg', 0.8]),
@@ -38,7 +38,7 @@ SCENARIOS = {
         source=dict(type='Line'),
         detectors=dict(top=dict(type='Radial', axis=[0.0, 5e-3, 50]), specular=dict(type='Total')),
         nphotons=6000, streams=48, rnginit=1),
-    # BASELINE config 2 stack (Gk, three layers) with a Cartesian fluence grid
+    # the benchmark's three-layer Gk skin stack with a small Cartesian fluence grid
     'c2_gk_fluence': dict(
         medium='mcml',
         layers=[_air(['Gk', 0.0, 0.5]),
@@ -151,7 +151,7 @@ SCENARIOS = {
                        bottom=dict(type='Radial', axis=[0.0, 4e-3, 40]),
                        specular=dict(type='Total', cosmin=0.5)),
         nphotons=3000, streams=24, rnginit=5),
-    # BASELINE config 4 sample: semi-infinite, one draw of the batched ranges
+    # semi-infinite layer, one draw of the batched engine's parameter ranges
     'semiinf_hg': dict(
         medium='mcml',
         layers=[_air(['Hg', 0.0]), dict(d=INF, n=1.42, mua=30.0, mus=8000.0, pf=['Hg', 0.8]),
@@ -159,7 +159,7 @@ SCENARIOS = {
         source=dict(type='Line'),
         detectors=dict(top=dict(type='Radial', axis=[0.0, 3e-3, 30])),
         nphotons=1500, streams=16, rnginit=2, no_lottery=False),
-    # BASELINE config 3 shape (two layers + absorbing cylinder) on a 24^3 grid
+    # the skin and vessel shape (two layers + absorbing cylinder) on a 24^3 grid
     'c3_vox_cylinder': dict(
         medium='mcvox',
         grid=dict(x=[-1.2e-3, 1.2e-3, 24], y=[-1.2e-3, 1.2e-3, 24], z=[0.0, 2.4e-3, 24]),
