@@ -579,7 +579,8 @@ DEFAULT_WORKLOAD = 'c2_skin_gk_fluence'
 
 
 def _transport_summary(args, workload):
-    """Config 1 or config 3 measured like the default workload, compactly."""
+    """The 10 mm slab or the 200^3 skin and vessel voxels, measured like the
+    default workload, compactly."""
     import copy
     a = copy.copy(args)
     a.workload, a.steps, a.warmup, a.e2e_steps = workload, 3, 2, 2
@@ -601,8 +602,8 @@ def _transport_summary(args, workload):
 
 def other_workloads(args, fp32_peak):
     """The other benchmark configurations, measured in the same run as the
-    headline line: config 1 (10 mm slab, 1e6 packets), config 3 (200^3
-    voxels, 1e8 packets), the batched engine (4096 simulations) and the
+    headline line: the 10 mm slab (1e6 packets), the 200^3 skin and vessel
+    voxels (1e8 packets), the batched engine (4096 simulations) and the
     surrogate with its Monte Carlo judge (65536 queries).  Each entry has its
     own timing (CUDA events for the device values); failures are recorded,
     not raised."""

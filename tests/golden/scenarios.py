@@ -633,8 +633,8 @@ SCENARIOS = {
         nphotons=300, streams=30, rnginit=131),
 }
 
-# Bench workloads at their full sizes: the layered configuration of the
-# headline metric, config 1, and the voxelized configuration.  Their
+# Bench workloads at their full sizes: the three-layer skin stack of the
+# headline metric, the 10 mm slab, and the 200^3 skin and vessel voxels.  Their
 # reference CPU builds (oracle/_ref/) are the CPU baseline and the other
 # side of tests/test_reference_parity.py.
 BENCH = {

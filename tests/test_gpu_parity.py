@@ -80,7 +80,7 @@ def test_dynamic_tallies_independent_of_packets_per_item(cuda, lib, oracle, name
 
 
 def test_exact_mode_many_streams_bit_identical(cuda, lib, oracle):
-    """Full-occupancy launch (many blocks) on config 2's stack."""
+    """Full-occupancy launch (many blocks) on the three-layer skin stack."""
     mc = scenarios.build_mc('c2_gk_fluence')
     n, t = 20000, 4096
     ref = oracle.run(mc, n, t, oracle.PORTABLE, nthreads=8)

@@ -81,8 +81,8 @@ def _assert_gate(a, b, what):
 
 
 def test_c1_radial_profile_per_bin_3sigma(cuda, lib):
-    """Config 1 at its full 1e6 packets: the 50 radial bins, the total and
-    the specular reflectance."""
+    """The 10 mm slab at its full 1e6 packets: the 50 radial bins, the total
+    and the specular reflectance."""
     keys = ['top', 'specular']
     ref = reference_batches('c1_slab_hg_radial', 1_000_000, keys)
     gpu = gpu_batches('c1_slab_hg_radial', 1_000_000, keys)
@@ -149,17 +149,17 @@ def _fluence_checks(name, n_ref, n_gpu, shape, extra=None):
 
 
 def test_c2_fluence_grid_against_reference(cuda, lib):
-    """Config 2 on its 100^3 fluence grid: the GPU at 1e8 packets against the
-    reference build at 1e7, per depth slice, per 1 mm^3 coarse voxel, and the
-    top, bottom and specular totals."""
+    """The three-layer skin stack on its 100^3 fluence grid: the GPU at 1e8
+    packets against the reference build at 1e7, per depth slice, per 1 mm^3
+    coarse voxel, and the top, bottom and specular totals."""
     _fluence_checks('c2_skin_gk_fluence', 10_000_000, 100_000_000, (100, 100, 100))
 
 
 def test_c3_voxel_fluence_against_reference(cuda, lib):
-    """Config 3 on its 200^3 voxel grid: the GPU at 1e8 packets against the
-    reference build at 1e7, per depth slice, per 1 mm^3 coarse voxel, on the
-    x-z plane through the vessel (summed over y, 0.25 mm cells), and the
-    totals."""
+    """The skin and vessel voxels on their 200^3 grid: the GPU at 1e8 packets
+    against the reference build at 1e7, per depth slice, per 1 mm^3 coarse
+    voxel, on the x-z plane through the vessel (summed over y, 0.25 mm
+    cells), and the totals."""
     shape = (200, 200, 200)
 
     def xz_plane(fr, fg):
