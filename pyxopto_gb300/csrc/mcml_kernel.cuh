@@ -503,9 +503,10 @@ static __device__ __forceinline__ void mcml_end(const McgbMcmlConfig &c, const M
    loop, xopto/mcml/kernel/mcml.template.c:525-814).  Returns true when the
    packet terminated.  XTRA = false compiles out the optional features the
    launcher routes to the XTRA kernels: trace, optical path length, step
-   limit, surface layouts, fibre-probe detectors, a finite rmax and the
-   fluence-rate scaling. */
-template <int PF, int METHOD, bool FLU, bool XTRA>
+   limit, surface layouts, fibre-probe detectors and the fluence-rate
+   scaling.  RMAX = false compiles out the rmax test (the launcher takes the
+   SIMPLE kernels only without rmax). */
+template <int PF, int METHOD, bool FLU, bool XTRA, bool RMAX = true>
 static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const McgbBuffers &b,
                                                  const MlCtx &x, MlPacket &s, Rng &rng,
                                                  FluenceCache &fcache, uint32_t &status) {
@@ -615,7 +616,7 @@ static __device__ __forceinline__ bool mcml_step(const McgbMcmlConfig &c, const 
         }
     }
     /* rmax, mcml.template.c:759-763 */
-    if (XTRA && x.use_rmax) {
+    if (RMAX && x.use_rmax) {
         f3 d{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
         if (dot3(d, d) > x.rmax2) {
             done = true;
@@ -765,7 +766,7 @@ mcml_dynamic_kernel(const __grid_constant__ McgbMcmlConfig c, const McgbBuffers 
            the scheduler both bodies (+0.9 % on the layered stack) */
 #pragma unroll 2
         for (int k = 0; k < 16; ++k) {
-            if (active && mcml_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
+            if (active && mcml_step<PF, METHOD, FLU, XTRA, XTRA || !SIMPLE>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
                 s.steps = 0;

@@ -482,8 +482,10 @@ static __device__ __forceinline__ float mcvox_sample(const MvCtx &x, MvPacket &s
     return fminf(step, FLT_MAX);
 }
 
-/* The rest of a step after its free path is drawn (mcvox_sample). */
-template <int PF, int METHOD, bool FLU, bool XTRA>
+/* The rest of a step after its free path is drawn (mcvox_sample).  RMAX =
+   false compiles out the rmax test (the launcher takes the SIMPLE kernels
+   only without rmax). */
+template <int PF, int METHOD, bool FLU, bool XTRA, bool RMAX = true>
 static __device__ __forceinline__ bool mcvox_move(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
                                                   FluenceCache &fcache, uint32_t &status, float step) {
@@ -633,7 +635,7 @@ static __device__ __forceinline__ bool mcvox_move(const McgbMcvoxConfig &c, cons
     }
     /* mcvox.template.c:1004-1008 */
     bool escaped = s.w <= 0.0f;
-    if (XTRA && x.use_rmax) {
+    if (RMAX && x.use_rmax) {
         f3 dd{s.pos.x - x.src_pos.x, s.pos.y - x.src_pos.y, s.pos.z - x.src_pos.z};
         escaped = escaped || dot3(dd, dd) > x.rmax2;
     }
@@ -654,12 +656,12 @@ static __device__ __forceinline__ bool mcvox_move(const McgbMcvoxConfig &c, cons
     return done;
 }
 
-template <int PF, int METHOD, bool FLU, bool XTRA>
+template <int PF, int METHOD, bool FLU, bool XTRA, bool RMAX = true>
 static __device__ __forceinline__ bool mcvox_step(const McgbMcvoxConfig &c, const McgbBuffers &b,
                                                   const MvCtx &x, MvPacket &s, Rng &rng,
                                                   FluenceCache &fcache, uint32_t &status) {
     const float step = mcvox_sample<METHOD>(x, s, rng);
-    return mcvox_move<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status, step);
+    return mcvox_move<PF, METHOD, FLU, XTRA, RMAX>(c, b, x, s, rng, fcache, status, step);
 }
 
 template <int PF>
@@ -804,7 +806,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                 if (active && (run_walls || !wall)) {
                     const float step = s.pend;
                     s.pend = -1.0f;
-                    if (mcvox_move<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status, step)) {
+                    if (mcvox_move<PF, METHOD, FLU, XTRA, XTRA || !SIMPLE>(c, b, x, s, rng, fcache, status, step)) {
                         ++packets;
                         steps += s.steps;
                         s.steps = 0;
@@ -812,7 +814,7 @@ mcvox_dynamic_kernel(const __grid_constant__ McgbMcvoxConfig c, const McgbBuffer
                         active = false;
                     }
                 }
-            } else if (active && mcvox_step<PF, METHOD, FLU, XTRA>(c, b, x, s, rng, fcache, status)) {
+            } else if (active && mcvox_step<PF, METHOD, FLU, XTRA, XTRA || !SIMPLE>(c, b, x, s, rng, fcache, status)) {
                 ++packets;
                 steps += s.steps;
                 s.steps = 0;

@@ -53,9 +53,9 @@ const void *MCGB_SELECT_STATIC(int pf, int method, bool fluence) {
 
 /* Dynamic scheduling kernels: phase function x method x fluence x optional
    features (trace, optical path length, per-packet step limit, fibre-probe
-   detectors, surface layouts, finite rmax, fluence rate) x simple
-   source (the common sources only: Line in layered media, Line and
-   GaussianBeam in voxelized media). */
+   detectors, surface layouts, fluence rate) x simple launch (the common
+   sources only: Line in layered media, Line and GaussianBeam in voxelized
+   media; no rmax). */
 #define MCGB_VX(K, PF, M, F) {{(const void *)K<PF, M, F, false, false>, (const void *)K<PF, M, F, false, true>}, \
                               {(const void *)K<PF, M, F, true, false>, (const void *)K<PF, M, F, true, true>}}
 #define MCGB_VD(K, PF, M) {MCGB_VX(K, PF, M, false), MCGB_VX(K, PF, M, true)}
@@ -104,19 +104,19 @@ static cudaError_t resident_blocks(const void *k, int block, size_t dyn_smem, in
 cudaError_t MCGB_LAUNCH(const MCGB_CFG &cfg, const McgbBuffers &buf, cudaStream_t stream,
                         const LaunchShape &shape) {
     const int sched = cfg.opt.scheduling;
-    /* the plain dynamic kernels (XTRA = false) also leave out the rmax test
-       and the fluence-rate scaling */
+    /* the plain dynamic kernels (XTRA = false) also leave out the
+       fluence-rate scaling, and the SIMPLE ones the rmax test */
     const float rmax2 = cfg.opt.rmax * cfg.opt.rmax;
+    const bool rmax = rmax2 < std::numeric_limits<float>::infinity();
     bool xtra = cfg.trace.flags != MCGB_TRACE_NONE || cfg.opt.track_optical_pathlength != 0 ||
-                cfg.opt.max_steps_per_packet != 0 || rmax2 < std::numeric_limits<float>::infinity() ||
-                cfg.fluence.kind == MCGB_FLUENCE_RATE;
+                cfg.opt.max_steps_per_packet != 0 || cfg.fluence.kind == MCGB_FLUENCE_RATE;
     xtra = xtra || cfg.top.kind >= MCGB_DET_LINEAR_ARRAY || cfg.bottom.kind >= MCGB_DET_LINEAR_ARRAY;
 #if MCGB_MEDIUM == 0
     xtra = xtra || cfg.surface_top.kind != MCGB_SURFACE_NONE ||
            cfg.surface_bottom.kind != MCGB_SURFACE_NONE;
 #endif
     const void *k = select(sched, cfg.pf_kind, cfg.opt.method, cfg.fluence.kind != MCGB_FLUENCE_NONE,
-                           xtra, simple_source(cfg.source.kind));
+                           xtra, simple_source(cfg.source.kind) && !rmax);
     if (!k) return cudaErrorInvalidValue;
     if (shape.dyn_smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
